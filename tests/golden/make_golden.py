@@ -1,0 +1,257 @@
+"""Generate golden vectors from the reference LoopStructural implementation.
+
+Run in a container where the reference source tree is available:
+
+    python tests/golden/make_golden.py /path/to/LoopStructural
+
+It imports the reference's ``loop_interpolation`` / ``loop_common`` packages
+(``pyvista`` and ``yaml`` are stubbed: they are only used for VTK/YAML export)
+and writes small ``.npz`` fixtures next to this script.  The fixtures are
+committed; tests read them without the reference being present.
+
+What is recorded per case:
+  * every constraint family the reference adds (name, the raw column indices
+    passed to ``add_constraints_to_least_squares`` and the stored CSC matrix,
+    b and w after row normalisation),
+  * the assembled weighted system's FP64 direct solution of
+    (AᵀWA + 1e-16 I) x = AᵀWb,
+  * the reference's own ``solve_system('cg')`` solution at a tight tolerance,
+  * ``evaluate_value`` / ``evaluate_gradient`` of that solution at query
+    points (inside, on faces/corners, outside, NaN rows).
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _import_reference(root):
+    for name in ("pyvista", "yaml"):
+        if name not in sys.modules:
+            try:
+                __import__(name)
+            except Exception:
+                sys.modules[name] = types.ModuleType(name)
+    sys.path.insert(0, os.path.join(root, "packages", "loop_common", "src"))
+    sys.path.insert(0, os.path.join(root, "packages", "loop_interpolation", "src"))
+    import loop_interpolation as li  # noqa: F401
+    from loop_common.supports import StructuredGrid, TetMesh
+
+    return li, StructuredGrid, TetMesh
+
+
+def _field(p, fault=False):
+    f = p[:, 2] + 0.1 * np.sin(2 * np.pi * p[:, 0]) + 0.05 * np.cos(2 * np.pi * p[:, 1])
+    if fault:
+        f = f + 0.2 * (p[:, 0] > 0.5)
+    return f
+
+
+def _grad(p):
+    g = np.zeros_like(p)
+    g[:, 0] = 0.1 * 2 * np.pi * np.cos(2 * np.pi * p[:, 0])
+    g[:, 1] = -0.05 * 2 * np.pi * np.sin(2 * np.pi * p[:, 1])
+    g[:, 2] = 1.0
+    return g
+
+
+def _hook(li):
+    """Record every add_constraints_to_least_squares call's raw idc."""
+    from loop_interpolation._discrete_interpolator import DiscreteInterpolator
+
+    calls = []
+    orig = DiscreteInterpolator.add_constraints_to_least_squares
+
+    def wrapped(self, A, B, idc, w=1.0, name="undefined"):
+        before = set(self.constraints.keys())
+        orig(self, A, B, idc, w=w, name=name)
+        after = [k for k in self.constraints.keys() if k not in before]
+        if after:
+            idc_arr = np.array(idc)
+            if idc_arr.ndim > 2:
+                idc_arr = idc_arr.reshape(-1, idc_arr.shape[-1])
+            calls.append((after[0], idc_arr.astype(np.int64)))
+
+    DiscreteInterpolator.add_constraints_to_least_squares = wrapped
+    return calls, (DiscreteInterpolator, orig)
+
+
+def _families_to_arrays(interp, calls, prefix, out):
+    names = []
+    for name, idc in calls:
+        c = interp.constraints[name]
+        m = c["matrix"].tocsr()
+        m.sort_indices()
+        names.append(name)
+        out[f"{prefix}fam_{name}_idc"] = idc
+        out[f"{prefix}fam_{name}_indptr"] = m.indptr.astype(np.int64)
+        out[f"{prefix}fam_{name}_indices"] = m.indices.astype(np.int64)
+        out[f"{prefix}fam_{name}_data"] = m.data
+        out[f"{prefix}fam_{name}_b"] = np.asarray(c["b"], dtype=float)
+        out[f"{prefix}fam_{name}_w"] = np.asarray(c["w"], dtype=float)
+    out[f"{prefix}family_names"] = np.array(names)
+
+
+def _solve_direct(interp):
+    from scipy import sparse
+    from scipy.sparse.linalg import spsolve
+
+    A, b = interp.build_matrix()
+    A = A.tocsr()
+    N = (A.T @ A).tocsc() + sparse.eye(A.shape[1], format="csc") * (interp.ridge_factor**2)
+    return spsolve(N, A.T @ b)
+
+
+def _queries(rng, lo, hi, n=64):
+    q = rng.uniform(lo, hi, size=(n, 3))
+    extra = np.array(
+        [
+            [lo, lo, lo], [hi, hi, hi], [hi, lo, lo], [lo, hi, hi],
+            [hi, 0.5 * (lo + hi), 0.25 * (lo + hi)],
+            [hi + 1e-3, 0.5, 0.5], [lo - 1e-3, 0.5, 0.5], [0.5, hi + 0.5, 0.5],
+            [np.nan, 0.5, 0.5],
+        ]
+    )
+    return np.vstack([q, extra])
+
+
+def fd_case(li, StructuredGrid, name, cells, n_val, n_norm, n_grad, n_tan, n_iface, seed, setup_kwargs, out):
+    calls, (cls, orig) = _hook(li)
+    try:
+        rng = np.random.default_rng(seed)
+        grid = StructuredGrid(origin=np.zeros(3), nsteps=np.array(cells), step_vector=1.0 / np.array(cells, dtype=float))
+        interp = li.FiniteDifferenceInterpolator(grid)
+        vp = rng.uniform(0, 1, size=(n_val, 3))
+        vp[:4] = [[0, 0, 0], [1, 1, 1], [1, 0.5, 0.25], [0.5, 1.0, 0.0]]
+        vp[4] = [1.05, 0.5, 0.5]  # outside
+        vp[5] = [1.0 + 1e-17, 0.3, 0.3]  # inside by tolerance
+        val = np.column_stack([vp, _field(vp), rng.uniform(0.5, 2.0, n_val)])
+        val = np.vstack([val, [[0.3, np.nan, 0.2, 1.0, 1.0]]])  # dropped by validation
+        interp.set_value_constraints(val)
+        data = {"value_in": val}
+        if n_norm:
+            npnt = rng.uniform(0, 1, size=(n_norm, 3))
+            g = _grad(npnt)
+            g /= np.linalg.norm(g, axis=1)[:, None]
+            g += rng.normal(0, 0.02, size=g.shape)
+            nrm = np.column_stack([npnt, g, rng.uniform(0.5, 2.0, n_norm)])
+            interp.set_normal_constraints(nrm)
+            data["normal_in"] = nrm
+        if n_grad:
+            gp = rng.uniform(0, 1, size=(n_grad, 3))
+            gv = _grad(gp)
+            gv[0] = [0.0, 0.0, 2.0]  # vertical: strike from atan2(0, 0)
+            grd = np.column_stack([gp, gv, np.ones(n_grad)])
+            interp.set_gradient_constraints(grd)
+            data["gradient_in"] = grd
+        if n_tan:
+            tp = rng.uniform(0, 1, size=(n_tan, 3))
+            tv = rng.normal(size=(n_tan, 3))
+            tan = np.column_stack([tp, tv, np.ones(n_tan)])
+            interp.set_tangent_constraints(tan)
+            data["tangent_in"] = tan
+        if n_iface:
+            ip = rng.uniform(0, 1, size=(n_iface, 3))
+            ids = np.array([0.0, 1.0] * (n_iface // 2) + [0.0] * (n_iface % 2))
+            ifc = np.column_stack([ip, ids, np.ones(n_iface)])
+            interp.set_interface_constraints(ifc)
+            data["interface_in"] = ifc
+        for k in ("value", "normal", "gradient", "tangent", "interface"):
+            out[f"{name}_data_{k}"] = np.asarray(interp.data[k], dtype=float)
+        for k, v in data.items():
+            out[f"{name}_{k}"] = v
+        interp.setup_interpolator(**setup_kwargs)
+        _families_to_arrays(interp, calls, f"{name}_", out)
+        out[f"{name}_cells"] = np.array(cells)
+        out[f"{name}_weights_keys"] = np.array(list(interp.interpolation_weights.keys()))
+        out[f"{name}_weights_vals"] = np.array([float(v) if np.isscalar(v) else np.nan for v in interp.interpolation_weights.values()])
+        out[f"{name}_c_direct"] = _solve_direct(interp)
+        interp.solve_system("cg", solver_kwargs={"rtol": 1e-13, "atol": 0.0, "maxiter": 200000})
+        out[f"{name}_c_cg_tight"] = np.array(interp.c)
+        q = _queries(rng, 0.0, 1.0)
+        out[f"{name}_query"] = q
+        interp.c = out[f"{name}_c_direct"].copy()
+        out[f"{name}_eval_value"] = interp.evaluate_value(q)
+        out[f"{name}_eval_gradient"] = interp.evaluate_gradient(q)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
+def reg_index_case(li, StructuredGrid, cells, out):
+    """All twelve regularisation families' raw idc at a tiny grid."""
+    calls, (cls, orig) = _hook(li)
+    try:
+        grid = StructuredGrid(origin=np.zeros(3), nsteps=np.array(cells), step_vector=np.ones(3))
+        interp = li.FiniteDifferenceInterpolator(grid)
+        kw = dict(dxy=1.0, dyz=0.8, dxz=1.3, dxx=0.5, dyy=0.4, dzz=0.6, dx=0.7, dy=0.9, dz=1.1,
+                  cpw=0.0, gpw=0.0, npw=0.0, tpw=0.0, ipw=0.0)
+        interp.setup_interpolator(**kw)
+        tag = "reg_" + "x".join(str(c) for c in cells) + "_"
+        _families_to_arrays(interp, calls, tag, out)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
+def p1_case(li, TetMesh, name, cells, n_val, n_norm, seed, setup_kwargs, out):
+    calls, (cls, orig) = _hook(li)
+    try:
+        rng = np.random.default_rng(seed)
+        mesh = TetMesh(origin=np.zeros(3), nsteps_cells=np.array(cells), step_vector=1.0 / np.array(cells, dtype=float))
+        interp = li.P1Interpolator(mesh)
+        vp = rng.uniform(0, 1, size=(n_val, 3))
+        vp[0] = [0.0, 0.5, 0.5]  # on the boundary: outside for the strict TetMesh.inside
+        val = np.column_stack([vp, _field(vp, fault=True) + rng.normal(0, 0.01, n_val), np.ones(n_val)])
+        interp.set_value_constraints(val)
+        npnt = rng.uniform(0, 1, size=(n_norm, 3))
+        g = _grad(npnt)
+        nrm = np.column_stack([npnt, g, np.ones(n_norm)])
+        interp.set_normal_constraints(nrm)
+        out[f"{name}_value_in"] = val
+        out[f"{name}_normal_in"] = nrm
+        interp.setup_interpolator(**setup_kwargs)
+        _families_to_arrays(interp, calls, f"{name}_", out)
+        out[f"{name}_cells"] = np.array(cells)
+        out[f"{name}_shared_rel"] = np.asarray(mesh.shared_element_relationships, dtype=np.int64)
+        out[f"{name}_shared_nodes"] = np.asarray(mesh.shared_elements, dtype=np.int64)
+        out[f"{name}_elements"] = np.asarray(mesh.elements, dtype=np.int64)
+        out[f"{name}_neighbours"] = np.asarray(mesh.get_neighbours(), dtype=np.int64)
+        out[f"{name}_c_direct"] = _solve_direct(interp)
+        # solve once so that evaluate_* (which calls update()) does not re-solve
+        interp.solve_system("cg", solver_kwargs={"rtol": 1e-13, "atol": 0.0, "maxiter": 200000})
+        out[f"{name}_c_cg_tight"] = np.array(interp.c)
+        q = _queries(rng, 0.0, 1.0)
+        out[f"{name}_query"] = q
+        interp.c = out[f"{name}_c_direct"].copy()
+        out[f"{name}_eval_value"] = interp.evaluate_value(q)
+        out[f"{name}_eval_gradient"] = interp.evaluate_gradient(q)
+        vtx, bc, tet, inside = mesh.get_element_for_location(q[:-1])
+        out[f"{name}_loc_bc"] = bc
+        out[f"{name}_loc_tet"] = tet.astype(np.int64)
+        out[f"{name}_loc_inside"] = inside
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
+def main(root):
+    li, StructuredGrid, TetMesh = _import_reference(root)
+    out = {}
+    fd_case(li, StructuredGrid, "fd_small", (8, 6, 12), 40, 12, 6, 4, 6, seed=0,
+            setup_kwargs=dict(regularisation=0.1, cpw=1.0, npw=1.0, gpw=1.0, tpw=1.0, ipw=1.0), out=out)
+    fd_case(li, StructuredGrid, "fd_cfg1_20", (20, 20, 20), 200, 50, 0, 0, 0, seed=0,
+            setup_kwargs=dict(regularisation=0.1, cpw=1.0, npw=1.0), out=out)
+    for cells in ((5, 5, 5), (3, 4, 2), (2, 5, 6)):
+        reg_index_case(li, StructuredGrid, cells, out)
+    p1_case(li, TetMesh, "p1_small", (4, 3, 5), 30, 8, seed=1,
+            setup_kwargs=dict(cgw=0.1, cpw=1.0, npw=1.0), out=out)
+    path = os.path.join(HERE, "reference_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
