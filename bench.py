@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Benchmark: FD solve + evaluate at 200^3 nodes on one GB300.
+
+Workload (one "step"): the mixed-precision (FP32 CG + FP64 reliable updates)
+Jacobi-CG solve of the FD normal equations of a 200x200x200-node
+StructuredGrid (8,000,000 DOF) constrained by 20,000 value points and 5,000
+noisy normals of a faulted layered field, followed by value + gradient
+evaluation on a 256^3 lattice.  Synthetic, seeded inputs (no dataset).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints ONE JSON line (rank 0).  `value` is device time per step with inputs
+resident in HBM; `e2e` is the same step through the public Python API from
+host arrays (constraints set, assembled, solved, evaluated at host points,
+results copied back).  `--impl reference` times the CPU oracle port of the
+reference's default path (explicit assembly + column-scaled scipy CG) on a
+bounded sample and extrapolates to the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FD solve+eval s & HBM GB/s at 200³, mixed vs FP64 GPU at 1e-8 rel error"
+N_NODES = 200
+N_VALUE = 20_000
+N_NORMAL = 5_000
+NORMAL_SIGMA = 0.02
+LATTICE = 256
+REGULARISATION = 0.1
+
+
+# ---------------------------------------------------------------------------
+# synthetic workload (seeded)
+# ---------------------------------------------------------------------------
+def field(p, fault=True):
+    f = p[:, 2] + 0.1 * np.sin(2 * np.pi * p[:, 0]) + 0.05 * np.cos(2 * np.pi * p[:, 1])
+    if fault:
+        f = f + 0.2 * (p[:, 0] > 0.5)
+    return f
+
+
+def field_gradient(p):
+    g = np.zeros_like(p)
+    g[:, 0] = 0.2 * np.pi * np.cos(2 * np.pi * p[:, 0])
+    g[:, 1] = -0.1 * np.pi * np.sin(2 * np.pi * p[:, 1])
+    g[:, 2] = 1.0
+    return g
+
+
+def make_workload(n_nodes=N_NODES, n_value=N_VALUE, n_normal=N_NORMAL, sigma=NORMAL_SIGMA, seed=0):
+    rng = np.random.default_rng(seed)
+    noise = np.random.default_rng(seed + 1)
+    vp = rng.uniform(0, 1, size=(n_value, 3))
+    val = np.column_stack([vp, field(vp), np.ones(n_value)])
+    npnt = rng.uniform(0, 1, size=(n_normal, 3))
+    g = field_gradient(npnt)
+    g /= np.linalg.norm(g, axis=1)[:, None]
+    g += noise.normal(0, sigma, size=g.shape)
+    nrm = np.column_stack([npnt, g, np.ones(n_normal)])
+    cells = np.array([n_nodes - 1] * 3)
+    return cells, val, nrm
+
+
+def lattice_points(n=LATTICE):
+    """The 256^3 evaluation lattice over the unit box, i fastest."""
+    ax = np.linspace(0.0, 1.0, n)
+    return (0.0, 0.0, 0.0), (ax[1] - ax[0],) * 3, (n, n, n)
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def gpu_arm(args, rank, world):
+    import torch
+
+    import loopstructural_gb300 as L
+    from loopstructural_gb300 import fd
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    L.build()
+    cells, val, nrm = make_workload()
+    grid = L.StructuredGrid(origin=np.zeros(3), nsteps=cells, step_vector=1.0 / cells)
+    interp = L.FiniteDifferenceInterpolator(grid)
+    interp.set_value_constraints(val)
+    interp.set_normal_constraints(nrm)
+    interp.setup_interpolator(regularisation=REGULARISATION, cpw=1.0, npw=1.0)
+    system = interp._build_system()
+    lo, hs, ln = lattice_points()
+    solve_kw = dict(atol=0.0, rtol=args.rtol, precision="mixed", maxiter=args.maxiter)
+
+    def step():
+        x, st = system.solve(**solve_kw)
+        v, g = fd.eval_lattice(grid, x, lo, hs, ln)
+        return st
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    stats = []
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            stats.append(step())
+        e1.record()
+        torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    iters = int(np.mean([s["iterations"] for s in stats]))
+
+    # dominant-kernel roofline from CUDA-event timings of each kernel class
+    prof = fd.profile_iteration(system, "mixed", reps=50)
+    peak, peak_kind = measured_peaks()
+    dom = "stencil" if prof["stencil_ms"] >= prof["update_ms"] else "update"
+    if dom == "stencil":
+        dom_bytes, dom_ms = prof["stencil_bytes"], prof["stencil_ms"]
+    else:
+        dom_bytes, dom_ms = 7 * 4.0 * system.n + 4 * 4.0 * system.n, prof["update_ms"]
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    it_gbs = prof["iteration_bytes"] / (prof["iteration_ms"] * 1e-3) / 1e9
+
+    # e2e: the public API from host arrays
+    e2e_steps = max(1, min(args.steps, 2))
+    q_host = None
+    h2d = d2h = 0
+    t_e2e = []
+    ax = np.linspace(0.0, 1.0, LATTICE)
+    zz, yy, xx = np.meshgrid(ax, ax, ax, indexing="ij")
+    q_host = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], axis=1)
+    del xx, yy, zz
+    for _ in range(e2e_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it = L.FiniteDifferenceInterpolator(grid)
+        it.set_value_constraints(val)
+        it.set_normal_constraints(nrm)
+        it.setup_interpolator(regularisation=REGULARISATION, cpw=1.0, npw=1.0)
+        it.solve_system("cg", solver_kwargs=dict(rtol=args.rtol, atol=0.0, precision="mixed",
+                                                 maxiter=args.maxiter))
+        vv = it.evaluate_value(q_host)
+        gg = it.evaluate_gradient(q_host)
+        torch.cuda.synchronize()
+        t_e2e.append(time.perf_counter() - t0)
+        h2d = val.nbytes + nrm.nbytes + 2 * q_host.nbytes
+        d2h = it.c.nbytes + vv.nbytes + gg.nbytes
+        del it
+    e2e_s = float(np.mean(t_e2e))
+
+    out = {
+        "metric": METRIC,
+        "value": round(ms / 1e3, 6),
+        "unit": "s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms, 3),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+f64",
+        "data": "synthetic (seeded faulted layered field; no dataset)",
+        "config": {
+            "workload": "FD 200^3 nodes (8M DOF), 20000 value + 5000 normal pts, reg 0.1; mixed FP32 CG + FP64 "
+                        "reliable updates to rtol %g; value+gradient on a 256^3 lattice" % args.rtol,
+            "dof": system.n, "data_rows": system.nrows, "rtol": args.rtol,
+            "cache": "inputs larger than L2 (working set ~0.6 GB of 8M-DOF vectors)",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+        },
+        "solve": {"iterations": iters, "reliable_updates": int(np.mean([s["reliable_updates"] for s in stats])),
+                  "residual": stats[-1]["residual"], "threshold": stats[-1]["threshold"],
+                  "iteration_ms": prof["iteration_ms"], "iteration_GBps": round(it_gbs, 1),
+                  "dof_iterations_per_s": system.n * iters / (ms / 1e3)},
+        "kernels_ms": {k: prof[k] for k in ("stencil_ms", "data_ms", "update_ms", "iteration_ms")},
+        "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "traffic": None},
+        "e2e": {"value": round(e2e_s, 4), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+    # kernel launches per step: setup-free solve = per iteration 5 (stencil, data rows, data nodes,
+    # update x/r, update p) + per reliable update 5; eval 1
+    upd = out["solve"]["reliable_updates"]
+    out["gpu_launches"] = int(args.steps * (5 * iters + 6 * upd + 8 + 1))
+    if args.cpu_baseline and rank == 0:
+        out["cpu_baseline"] = cpu_baseline(iters, args.rtol)
+    system.close()
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU reference (oracle port of the reference's default path)
+# ---------------------------------------------------------------------------
+def cpu_reference_sample(rtol, sample_nodes=60, iters_for_rate=30):
+    """Time the reference default path (explicit assembly + column-scaled
+    scipy CG + evaluation) on a bounded sample and extrapolate to 200^3."""
+    from oracle import fd_oracle as fdo
+
+    cells, val, nrm = make_workload(n_nodes=sample_nodes,
+                                    n_value=int(N_VALUE * (sample_nodes / N_NODES) ** 3) + 1,
+                                    n_normal=int(N_NORMAL * (sample_nodes / N_NODES) ** 3) + 1)
+    grid = fdo.Grid(np.zeros(3), cells, 1.0 / cells)
+    w = fdo.resolve_weights(regularisation=REGULARISATION, cpw=1.0, npw=1.0)
+    t0 = time.perf_counter()
+    cs = fdo.assemble(grid, {"value": val, "normal": nrm}, w)
+    A, b = cs.matrix()
+    t_asm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    _, _, it = fdo.solve_reference_cg(A, b, tol=0.0, rtol=1e-30, maxiter=iters_for_rate)
+    t_it = (time.perf_counter() - t0) / max(it, 1)
+    c = np.random.default_rng(0).normal(size=grid.n_nodes)
+    q = np.random.default_rng(1).uniform(0, 1, size=(200_000, 3))
+    t0 = time.perf_counter()
+    grid.evaluate_value(q, c)
+    grid.evaluate_gradient(q, c)
+    t_eval_pt = (time.perf_counter() - t0) / q.shape[0]
+    scale = (N_NODES / sample_nodes) ** 3
+    return {"assembly_s": t_asm * scale, "s_per_iteration": t_it * scale, "eval_s": t_eval_pt * LATTICE ** 3,
+            "sample": f"{sample_nodes}^3 nodes: assembly + {iters_for_rate} scipy-cg iterations of the "
+                      f"column-scaled explicit system, eval of 200k points; scaled x{scale:.1f} (DOF) and x"
+                      f"{LATTICE ** 3 / 2e5:.1f} (points)"}
+
+
+def cpu_baseline(gpu_iters, rtol):
+    r = cpu_reference_sample(rtol)
+    total = r["s_per_iteration"] * gpu_iters + r["eval_s"]
+    return {"value": round(total, 3), "unit": "s", "cores": 1, "kind": "port",
+            "sample": r["sample"] + f"; x {gpu_iters} iterations (the GPU solve's count at rtol {rtol:g})"}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return None
+    # iteration count of the reference path at this tolerance: CG iterations grow
+    # ~linearly in n (column-scaled, measured); calibrate at n = 24 and scale to 200
+    from oracle import fd_oracle as fdo
+
+    n_cal = 24
+    cells, val, nrm = make_workload(n_nodes=n_cal, n_value=max(2, int(N_VALUE * (n_cal / N_NODES) ** 3)),
+                                    n_normal=max(2, int(N_NORMAL * (n_cal / N_NODES) ** 3)))
+    grid = fdo.Grid(np.zeros(3), cells, 1.0 / cells)
+    cs = fdo.assemble(grid, {"value": val, "normal": nrm}, fdo.resolve_weights(regularisation=REGULARISATION,
+                                                                                 cpw=1.0, npw=1.0))
+    A, b = cs.matrix()
+    _, _, it_cal = fdo.solve_reference_cg(A, b, tol=0.0, rtol=args.rtol, maxiter=200000)
+    iters = int(it_cal * N_NODES / n_cal)
+    times = []
+    r = None
+    for _ in range(args.warmup + args.steps):
+        r = cpu_reference_sample(args.rtol)
+        times.append(r["s_per_iteration"] * iters + r["eval_s"])
+    v = float(np.mean(times[args.warmup:]))
+    sample = r["sample"] + f"; x {iters} iterations (reference cg at {n_cal}^3 took {it_cal}, scaled linearly in n)"
+    return {
+        "metric": METRIC, "impl": "reference", "value": round(v, 3), "unit": "s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v * 1e3, 1), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "FD 200^3 nodes, 20000 value + 5000 normal pts, reg 0.1; reference default path "
+                               "(column-scaled scipy CG) to rtol %g; eval on 256^3" % args.rtol},
+        "cpu_baseline": {"value": round(v, 3), "unit": "s", "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": round(v, 3), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--rtol", type=float, default=1e-12)
+    ap.add_argument("--maxiter", type=int, default=400_000)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        out = reference_arm(args, rank, world)
+    else:
+        if world > 1:
+            import torch
+
+            torch.distributed.init_process_group("nccl")
+        out = gpu_arm(args, rank, world)
+    if rank == 0 and out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,222 @@
+/*
+ * ls_gb300.h -- C ABI of the GB300 (sm_103a) discrete implicit interpolation
+ * hot path: structured-grid finite-difference (FD) and structured-tetra P1
+ * constraint assembly, matrix-free normal-equations CG solve and field /
+ * gradient evaluation.
+ *
+ * Conventions
+ *   - Every pointer argument named d_* is a DEVICE pointer; h_* is a host
+ *     pointer; structs passed by pointer live in host memory.
+ *   - Node vectors use the reference's F-order numbering
+ *     gi = i + nx*j + nx*ny*k (x fastest), so a solution array is directly the
+ *     reference interpolator's `c`.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default).
+ *   - Every function returns an int status (ls_status); on a negative status
+ *     ls_last_error() returns a message for the calling thread.
+ *   - No function allocates on the caller's behalf except ls_*_create, which
+ *     owns its device workspace until ls_*_destroy.
+ *
+ * Reference files are cited relative to the LoopStructural 1.8.0 source tree:
+ *   S  packages/loop_common/src/loop_common/supports/_3d_base_structured.py
+ *   G  packages/loop_common/src/loop_common/supports/_3d_structured_grid.py
+ *   T  packages/loop_common/src/loop_common/supports/_3d_structured_tetra.py
+ *   FD packages/loop_interpolation/src/loop_interpolation/_finite_difference_interpolator.py
+ *   P1 packages/loop_interpolation/src/loop_interpolation/_p1interpolator.py
+ *   DI packages/loop_interpolation/src/loop_interpolation/_discrete_interpolator.py
+ *   SP packages/loop_interpolation/src/loop_interpolation/_solver_pipeline.py
+ *   SS packages/loop_interpolation/src/loop_interpolation/_solver_strategy.py
+ */
+#ifndef LS_GB300_H
+#define LS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LS_ABI_VERSION 1
+
+typedef enum ls_status {
+  LS_OK = 0,
+  LS_NOT_CONVERGED = 1, /* maxiter reached: the last iterate is returned (SS:66-71 warns, still True) */
+  LS_NAN = 2,           /* a NaN / Inf appeared in the CG recurrence */
+  LS_BREAKDOWN = 3,     /* p·Ap <= 0 */
+  LS_ERR_ARG = -1,
+  LS_ERR_CUDA = -2,
+  LS_ERR_ALLOC = -3,
+  LS_ERR_STATE = -4
+} ls_status;
+
+/* Structured support geometry: node counts per axis (cells + 1),
+ * origin and cell size.  The same struct describes a TetMesh. */
+typedef struct ls_grid3 {
+  int64_t nsteps[3];
+  double origin[3];
+  double step[3];
+} ls_grid3;
+
+/* Message describing the last negative status returned on this thread. */
+const char *ls_last_error(void);
+int ls_abi_version(void);
+
+/* ------------------------------------------------------------------ */
+/* FD constraint assembly (K1/K2)                                      */
+/* ------------------------------------------------------------------ */
+
+/* Row kinds of ls_fd_point_rows and the reference method each replaces. */
+typedef enum ls_row_kind {
+  LS_ROWS_VALUE = 0,    /* FD:236-269 add_value_constraints: 1 row/point, w = weight*point_w */
+  LS_ROWS_NORM = 1,     /* FD:403-476 add_norm_constraints: 3 rows/point (norm_0..2), w = weight/3*point_w */
+  LS_ROWS_GRADIENT = 2, /* FD:342-401 add_gradient_constraints: 2 rows/point (strike, dip), w = weight */
+  LS_ROWS_TANGENT = 3   /* FD:478-539 add_gradient_orthogonal_constraints: 1 row/point, w = weight */
+} ls_row_kind;
+
+/* Point-constraint rows on a StructuredGrid.  Replaces the per-family
+ * position_to_cell_corners + trilinear / element-gradient shape
+ * functions (G:90-162, G:393-454) + row normalisation
+ * (DI:361-366 add_constraints_to_least_squares).
+ *   d_pts     : npts x ld row-major FP64 (x, y, z, ...columns of the kind...)
+ *   outputs   : rows_per_point families, family f occupying rows
+ *               [f*npts, f*npts + *h_count): d_idc (int64 x 8) bit-identical to
+ *               the reference COO columns, d_a (x 8) normalised coefficients,
+ *               d_b, d_w.  Points outside the support are dropped in order.
+ *   h_count   : number of inside points (host int64, written after a sync).
+ *   h_nan     : set to 1 when a computed row holds a NaN (the reference then
+ *               skips the whole family, DI:355-359). */
+int ls_fd_point_rows(const ls_grid3 *grid, int kind, const double *d_pts, int64_t npts, int64_t ld,
+                     double weight, int64_t *d_idc, double *d_a, double *d_b, double *d_w,
+                     int64_t *h_count, int32_t *h_nan, void *stream);
+
+/* Interface pair rows (FD:297-340 add_interface_constraints): row p is
+ * [trilinear(i), -trilinear(j)] over 16 columns for d_pairs[p] = (i, j), both
+ * indices into d_pts (all points must be inside), b = 0, w = weight. */
+int ls_fd_pair_rows(const ls_grid3 *grid, const double *d_pts, int64_t ld, const int64_t *d_pairs,
+                    int64_t npairs, double weight, int64_t *d_idc, double *d_a, double *d_b, double *d_w,
+                    void *stream);
+
+/* Regularisation families, in the reference order: the six interior families
+ * of G:489-510 and the six border families of FD:1052-1144. */
+typedef enum ls_reg_family {
+  LS_REG_DXY = 0, LS_REG_DYZ = 1, LS_REG_DXZ = 2, LS_REG_DXX = 3, LS_REG_DYY = 4, LS_REG_DZZ = 5,
+  LS_REG_DX_LOWER = 6, LS_REG_DX_UPPER = 7, LS_REG_DY_LOWER = 8, LS_REG_DY_UPPER = 9,
+  LS_REG_DZ_LOWER = 10, LS_REG_DZ_UPPER = 11
+} ls_reg_family;
+
+/* Number of rows and taps of a regularisation family (FD:636-692). */
+int ls_fd_reg_shape(const ls_grid3 *grid, int family, int64_t *h_rows, int32_t *h_taps);
+
+/* Explicit column indices of a regularisation family (parity mode of the
+ * matrix-free operator): FD:643-692 _assemble_operator +
+ * G:164-293 neighbour_global_indexes, row-major rows x taps int64. */
+int ls_fd_reg_rows(const ls_grid3 *grid, int family, int64_t *d_idc, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* FD normal-equations system and CG solve (K4/K5/K6)                  */
+/* ------------------------------------------------------------------ */
+
+/* Weighted least-squares system
+ *    minimise  sum_rows w^2 (a.x - b)^2 + ridge^2 |x|^2
+ * whose normal equations (A^T W A + ridge^2 I) x = A^T W b are what
+ * DI:1221-1319 solve_system('cg') solves (SP:86-124, SS:48-72).  The
+ * regularisation rows are implicit (matrix-free stencils); data rows are
+ * given explicitly. */
+typedef struct ls_fd_system {
+  ls_grid3 grid;
+  /* row weights of the interior families as used by the reference, i.e. the
+   * cross-derivative weights already divided by 4 (G:502-509) */
+  double w_dxx, w_dyy, w_dzz, w_dxy, w_dyz, w_dxz;
+  /* border family weights (FD:1102-1139); 0 disables the pair of families */
+  double w_dx, w_dy, w_dz;
+  double ridge; /* ridge row weight (DI:78, 1e-8); 0 disables */
+  /* data rows (device, row-major nrows x width; a negative column is padding) */
+  int64_t nrows;
+  int32_t width;
+  const int64_t *d_idc;
+  const double *d_a; /* normalised coefficients */
+  const double *d_b; /* normalised right-hand side */
+  const double *d_w; /* row weights (W = w^2) */
+} ls_fd_system;
+
+typedef struct ls_fd_handle ls_fd_handle;
+
+int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *stream);
+int ls_fd_destroy(ls_fd_handle *h);
+/* number of degrees of freedom */
+int64_t ls_fd_dof(const ls_fd_handle *h);
+
+/* y = (A^T W A + ridge^2 I) x in FP64 (matrix-free). */
+int ls_fd_apply(ls_fd_handle *h, const double *d_x, double *d_y, void *stream);
+/* the same operator in FP32 (the inner-iteration kernel of the mixed solve) */
+int ls_fd_apply_f32(ls_fd_handle *h, const float *d_x, float *d_y, void *stream);
+/* A^T W b (FP64) */
+int ls_fd_rhs(ls_fd_handle *h, double *d_rhs, void *stream);
+/* diag(A^T W A + ridge^2 I): the squared column norms of the reference's
+ * column scaling (DI:815-833) */
+int ls_fd_diagonal(ls_fd_handle *h, double *d_diag, void *stream);
+
+typedef enum ls_precision { LS_FP64 = 0, LS_MIXED = 1 } ls_precision;
+
+typedef struct ls_solve_opts {
+  int32_t precision;      /* ls_precision */
+  int32_t use_x0;         /* d_x holds the initial guess (else zeros) */
+  double atol;            /* absolute tolerance on ||S r|| (scipy cg atol) */
+  double rtol;            /* relative tolerance (scipy cg rtol, default 1e-5) */
+  int64_t maxiter;        /* <= 0: 10 * dof (scipy default) */
+  double reliable_delta;  /* mixed: refresh the FP64 residual once ||S r|| fell by this factor (<=0: 0.1) */
+  int32_t check_every;    /* iterations per device batch between host checks (<=0: 64) */
+  int32_t reserved;
+} ls_solve_opts;
+
+typedef struct ls_solve_stats {
+  int64_t iterations;       /* CG iterations (scipy counting) */
+  int64_t reliable_updates; /* FP64 residual refreshes (mixed) */
+  double residual;          /* final ||S (rhs - N x)|| in FP64, S = diag^(-1/2) */
+  double rhs_norm;          /* ||S rhs|| */
+  double threshold;         /* max(atol, rtol * ||S rhs||) */
+  double device_ms;         /* device time of the solve (CUDA events) */
+  int32_t status;
+  int32_t reserved;
+} ls_solve_stats;
+
+/* Jacobi-preconditioned CG on the normal equations -- the iteration of the
+ * reference's column-scaled scipy cg (SS:48-72 with DI:815-833 scaling),
+ * stopping at the same criterion ||S r|| < max(atol, rtol ||S rhs||).
+ * d_x (device, dof FP64) receives the solution. */
+int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d_x, ls_solve_stats *stats, void *stream);
+
+/* Per-kernel device times of one CG iteration, measured with CUDA events on
+ * the handle's stream over `reps` back-to-back launches of each kernel class
+ * (no counterpart in the reference, which has no device code). */
+typedef struct ls_fd_profile {
+  double stencil_ms;    /* matrix-free stencil part of N p (+ p.Np) */
+  double data_ms;       /* data-row part of N p */
+  double update_ms;     /* x, r, z updates and r.z + the p update */
+  double iteration_ms;  /* one whole iteration */
+  double stencil_bytes; /* algorithmic bytes of one stencil launch: read p, write q */
+  double iteration_bytes; /* algorithmic bytes of one iteration (9 N s + 16 nnz_data) */
+} ls_fd_profile;
+
+int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps, ls_fd_profile *out, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* FD evaluation (K7)                                                   */
+/* ------------------------------------------------------------------ */
+
+/* Value / gradient of the trilinear field c at points (npts x ld, x y z
+ * first): G:295-391 with DI:1342-1379 semantics -- value NaN outside the
+ * support, 0 for a NaN input row; gradient 0 outside.  Either output may be
+ * NULL. */
+int ls_fd_eval_points(const ls_grid3 *grid, const double *d_c, const double *d_pts, int64_t npts, int64_t ld,
+                      double *d_value, double *d_grad, void *stream);
+
+/* The same on a regular lattice of points origin + step * (i, j, k),
+ * i < n[0] fastest; output index i + n0*j + n0*n1*k. */
+int ls_fd_eval_lattice(const ls_grid3 *grid, const double *d_c, const double lat_origin[3],
+                       const double lat_step[3], const int64_t lat_n[3], double *d_value, double *d_grad,
+                       void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LS_GB300_H */

@@ -1,0 +1,166 @@
+"""ctypes binding of ``libls_gb300.so`` (C ABI in ``include/ls_gb300.h``).
+
+The library is the only compute path: when it is missing or no CUDA device
+is visible, every compute entry point raises ``ExtensionUnavailable`` -- there
+is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import _build
+
+LS_OK = 0
+LS_NOT_CONVERGED = 1
+LS_NAN = 2
+LS_BREAKDOWN = 3
+LS_FP64 = 0
+LS_MIXED = 1
+
+ROWS_VALUE, ROWS_NORM, ROWS_GRADIENT, ROWS_TANGENT = 0, 1, 2, 3
+REG_FAMILIES = (
+    "dxy", "dyz", "dxz", "dxx", "dyy", "dzz",
+    "dx_lower", "dx_upper", "dy_lower", "dy_upper", "dz_lower", "dz_upper",
+)
+
+# every symbol include/ls_gb300.h declares
+EXPORTS = (
+    "ls_last_error", "ls_abi_version",
+    "ls_fd_point_rows", "ls_fd_pair_rows", "ls_fd_reg_shape", "ls_fd_reg_rows",
+    "ls_fd_create", "ls_fd_destroy", "ls_fd_dof", "ls_fd_apply", "ls_fd_apply_f32", "ls_fd_rhs",
+    "ls_fd_diagonal", "ls_fd_solve", "ls_fd_profile_iteration", "ls_fd_eval_points", "ls_fd_eval_lattice",
+)
+
+
+class ExtensionUnavailable(RuntimeError):
+    """The sm_103a library is not built or cannot run here."""
+
+
+class LsError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"libls_gb300 status {status}: {msg}")
+        self.status = status
+
+
+class Grid3(C.Structure):
+    _fields_ = [("nsteps", C.c_int64 * 3), ("origin", C.c_double * 3), ("step", C.c_double * 3)]
+
+    @classmethod
+    def make(cls, nsteps_nodes, origin, step):
+        g = cls()
+        for d in range(3):
+            g.nsteps[d] = int(nsteps_nodes[d])
+            g.origin[d] = float(origin[d])
+            g.step[d] = float(step[d])
+        return g
+
+
+class FdSystem(C.Structure):
+    _fields_ = [
+        ("grid", Grid3),
+        ("w_dxx", C.c_double), ("w_dyy", C.c_double), ("w_dzz", C.c_double),
+        ("w_dxy", C.c_double), ("w_dyz", C.c_double), ("w_dxz", C.c_double),
+        ("w_dx", C.c_double), ("w_dy", C.c_double), ("w_dz", C.c_double),
+        ("ridge", C.c_double),
+        ("nrows", C.c_int64), ("width", C.c_int32),
+        ("d_idc", C.c_void_p), ("d_a", C.c_void_p), ("d_b", C.c_void_p), ("d_w", C.c_void_p),
+    ]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int32), ("use_x0", C.c_int32), ("atol", C.c_double), ("rtol", C.c_double),
+        ("maxiter", C.c_int64), ("reliable_delta", C.c_double), ("check_every", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int64), ("reliable_updates", C.c_int64), ("residual", C.c_double),
+        ("rhs_norm", C.c_double), ("threshold", C.c_double), ("device_ms", C.c_double),
+        ("status", C.c_int32), ("reserved", C.c_int32),
+    ]
+
+
+class FdProfile(C.Structure):
+    _fields_ = [("stencil_ms", C.c_double), ("data_ms", C.c_double), ("update_ms", C.c_double),
+                ("iteration_ms", C.c_double), ("stencil_bytes", C.c_double), ("iteration_bytes", C.c_double)]
+
+
+_lock = threading.Lock()
+_lib = None
+
+_P = C.c_void_p
+_SIGS = {
+    "ls_last_error": (C.c_char_p, []),
+    "ls_abi_version": (C.c_int, []),
+    "ls_fd_point_rows": (C.c_int, [C.POINTER(Grid3), C.c_int, _P, C.c_int64, C.c_int64, C.c_double, _P, _P, _P, _P,
+                                   C.POINTER(C.c_int64), C.POINTER(C.c_int32), _P]),
+    "ls_fd_pair_rows": (C.c_int, [C.POINTER(Grid3), _P, C.c_int64, _P, C.c_int64, C.c_double, _P, _P, _P, _P, _P]),
+    "ls_fd_reg_shape": (C.c_int, [C.POINTER(Grid3), C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
+    "ls_fd_reg_rows": (C.c_int, [C.POINTER(Grid3), C.c_int, _P, _P]),
+    "ls_fd_create": (C.c_int, [C.POINTER(FdSystem), C.POINTER(_P), _P]),
+    "ls_fd_destroy": (C.c_int, [_P]),
+    "ls_fd_dof": (C.c_int64, [_P]),
+    "ls_fd_apply": (C.c_int, [_P, _P, _P, _P]),
+    "ls_fd_apply_f32": (C.c_int, [_P, _P, _P, _P]),
+    "ls_fd_rhs": (C.c_int, [_P, _P, _P]),
+    "ls_fd_diagonal": (C.c_int, [_P, _P, _P]),
+    "ls_fd_solve": (C.c_int, [_P, C.POINTER(SolveOpts), _P, C.POINTER(SolveStats), _P]),
+    "ls_fd_profile_iteration": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(FdProfile), _P]),
+    "ls_fd_eval_points": (C.c_int, [C.POINTER(Grid3), _P, _P, C.c_int64, C.c_int64, _P, _P, _P]),
+    "ls_fd_eval_lattice": (C.c_int, [C.POINTER(Grid3), _P, C.POINTER(C.c_double * 3), C.POINTER(C.c_double * 3),
+                                     C.POINTER(C.c_int64 * 3), _P, _P, _P]),
+}
+
+
+def load(build_if_missing: bool = False):
+    """Load the shared library (building it first when asked)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.lib_path()
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise ExtensionUnavailable(
+                    f"{path} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
+                    "(needs nvcc from CUDA 13)")
+            _build.build()
+        lib = C.CDLL(path)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def check(status: int, allow_positive: bool = False) -> int:
+    if status < 0 or (status > 0 and not allow_positive):
+        msg = _lib.ls_last_error().decode() if _lib is not None else "?"
+        raise LsError(status, msg)
+    return status
+
+
+def device():
+    """The CUDA device the kernels run on; raises when none is visible."""
+    import torch
+
+    if not torch.cuda.is_available():
+        raise ExtensionUnavailable("no CUDA device is visible: the GB300 kernels cannot run (no CPU fallback)")
+    load(build_if_missing=True)
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream_ptr():
+    import torch
+
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None

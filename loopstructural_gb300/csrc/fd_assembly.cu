@@ -1,0 +1,504 @@
+// FD constraint assembly on the GPU (K1 point rows, interface pair rows and
+// K2 explicit regularisation indices).
+//
+// Parity: column indices are bit-identical to the reference COO; values
+// follow the reference's floating-point evaluation order (no FMA contraction:
+// this file is compiled with -fmad=false) so they agree to ~1 ulp.
+#include <math.h>
+
+#include "ls_common.cuh"
+
+namespace ls {
+namespace {
+
+struct GridArgs {
+  double origin[3], step[3], lo[3], hi[3];
+  int64_t n[3], cells[3];
+};
+
+GridArgs make_grid_args(const ls_grid3 &g) {
+  GridArgs a;
+  for (int d = 0; d < 3; ++d) {
+    a.origin[d] = g.origin[d];
+    a.step[d] = g.step[d];
+    a.n[d] = g.nsteps[d];
+    a.cells[d] = g.nsteps[d] - 1;
+    // S:287-293 inside(): tolerance eps * 32 * max(|max - origin|, 1)
+    double mx = g.origin[d] + (double)a.cells[d] * g.step[d];
+    double ext = fabs(mx - g.origin[d]);
+    if (ext < 1.0) ext = 1.0;
+    double tol = 2.220446049250313e-16 * 32.0 * ext;
+    a.lo[d] = g.origin[d] - tol;
+    a.hi[d] = mx + tol;
+  }
+  return a;
+}
+
+__device__ __forceinline__ bool point_inside(const GridArgs &g, double x, double y, double z) {
+  return (x >= g.lo[0]) & (x <= g.hi[0]) & (y >= g.lo[1]) & (y <= g.hi[1]) & (z >= g.lo[2]) & (z <= g.hi[2]);
+}
+
+// S:251-282 cell index, S:386-412 corners, G:126-146 clipped local coords.
+__device__ __forceinline__ void locate(const GridArgs &g, const double p[3], int64_t idc[8], double l[3]) {
+  int64_t c[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double x = p[d] - g.origin[d];
+    int64_t ci = (int64_t)floor(x / g.step[d]);
+    if (ci < 0) ci = 0;
+    if (ci > g.cells[d] - 1) ci = g.cells[d] - 1;
+    c[d] = ci;
+    double co = g.origin[d] + g.step[d] * (double)ci;
+    double lc = (p[d] - co) / g.step[d];
+    l[d] = fmin(fmax(lc, 0.0), 1.0);
+  }
+  const int64_t nx = g.n[0], nxy = g.n[0] * g.n[1];
+  const int64_t g0 = c[0] + nx * c[1] + nxy * c[2];
+  idc[0] = g0;
+  idc[1] = g0 + 1;
+  idc[2] = g0 + nx;
+  idc[3] = g0 + nx + 1;
+  idc[4] = g0 + nxy;
+  idc[5] = g0 + nxy + 1;
+  idc[6] = g0 + nxy + nx;
+  idc[7] = g0 + nxy + nx + 1;
+}
+
+// G:90-124 (same operation order)
+__device__ __forceinline__ void trilinear(const double l[3], double a[8]) {
+  const double x = l[0], y = l[1], z = l[2];
+  a[0] = (1 - x) * (1 - y) * (1 - z);
+  a[1] = x * (1 - y) * (1 - z);
+  a[2] = (1 - x) * y * (1 - z);
+  a[4] = (1 - x) * (1 - y) * z;
+  a[5] = x * (1 - y) * z;
+  a[6] = (1 - x) * y * z;
+  a[3] = x * y * (1 - z);
+  a[7] = x * y * z;
+}
+
+// G:393-454 element gradient T (3 x 8) divided by the step
+__device__ __forceinline__ void element_gradient(const double l[3], const double step[3], double T[3][8]) {
+  const double x = l[0], y = l[1], z = l[2];
+  T[0][0] = (1 - z) * (y - 1);
+  T[0][1] = (1 - y) * (1 - z);
+  T[0][2] = -y * (1 - z);
+  T[0][4] = -(1 - y) * z;
+  T[0][5] = (1 - y) * z;
+  T[0][6] = -y * z;
+  T[0][3] = y * (1 - z);
+  T[0][7] = y * z;
+  T[1][0] = (x - 1) * (1 - z);
+  T[1][1] = -x * (1 - z);
+  T[1][2] = (1 - x) * (1 - z);
+  T[1][4] = -(1 - x) * z;
+  T[1][5] = -x * z;
+  T[1][6] = (1 - x) * z;
+  T[1][3] = x * (1 - z);
+  T[1][7] = x * z;
+  T[2][0] = -(1 - x) * (1 - y);
+  T[2][1] = -x * (1 - y);
+  T[2][2] = -(1 - x) * y;
+  T[2][4] = (1 - x) * (1 - y);
+  T[2][5] = x * (1 - y);
+  T[2][6] = (1 - x) * y;
+  T[2][3] = -x * y;
+  T[2][7] = x * y;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) T[d][k] = T[d][k] / step[d];
+}
+
+// numpy's add.reduce of 8 contiguous values (pairwise block of 8)
+__device__ __forceinline__ double sumsq8(const double a[8]) {
+  double r = ((a[0] * a[0] + a[1] * a[1]) + (a[2] * a[2] + a[3] * a[3])) +
+             ((a[4] * a[4] + a[5] * a[5]) + (a[6] * a[6] + a[7] * a[7]));
+  return 0.0 + r;
+}
+
+// DI:361-366 row normalisation
+__device__ __forceinline__ void normalise8(double a[8], double &b) {
+  double len = sqrt(sumsq8(a));
+  if (len > 0) {
+    b = b / len;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = a[k] / len;
+  }
+}
+
+__device__ __forceinline__ double norm3_seq(double a, double b, double c) {
+  return sqrt(((0.0 + a * a) + b * b) + c * c);
+}
+
+__device__ __forceinline__ void store_row(int64_t row, const int64_t idc[8], const double a[8], double b, double w,
+                                          int64_t *d_idc, double *d_a, double *d_b, double *d_w, int32_t *nan_flag) {
+  bool bad = isnan(b);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    d_idc[row * 8 + k] = idc[k];
+    d_a[row * 8 + k] = a[k];
+    bad |= isnan(a[k]);
+  }
+  d_b[row] = b;
+  d_w[row] = w;
+  if (bad) *nan_flag = 1;
+}
+
+__global__ void inside_flags_kernel(GridArgs g, const double *__restrict__ pts, int64_t n, int64_t ld,
+                                    int32_t *__restrict__ flag) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double *p = pts + i * ld;
+    flag[i] = point_inside(g, p[0], p[1], p[2]) ? 1 : 0;
+  }
+}
+
+// Single-block exclusive scan of int32 flags into int64 slots; writes the
+// total to *count.  Setup-time helper (n up to a few million points).
+__global__ void __launch_bounds__(1024) scan_flags_kernel(const int32_t *__restrict__ flag, int64_t n,
+                                                          int64_t *__restrict__ slot, int64_t *__restrict__ count) {
+  __shared__ int64_t warp_tot[32];
+  __shared__ int64_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t base = 0; base < n; base += 1024) {
+    int64_t i = base + threadIdx.x;
+    int64_t v = (i < n) ? flag[i] : 0;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int64_t t = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int64_t y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      warp_tot[lane] = t;  // inclusive over warps
+    }
+    __syncthreads();
+    int64_t excl = x - v + (warp > 0 ? warp_tot[warp - 1] : 0) + carry;
+    if (i < n) slot[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *count = carry;
+}
+
+template <int KIND>
+__global__ void point_rows_kernel(GridArgs g, const double *__restrict__ pts, int64_t n, int64_t ld, double weight,
+                                  const int32_t *__restrict__ flag, const int64_t *__restrict__ slot,
+                                  int64_t *__restrict__ d_idc, double *__restrict__ d_a, double *__restrict__ d_b,
+                                  double *__restrict__ d_w, int32_t *__restrict__ nan_flag) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (!flag[i]) continue;
+    const double *p = pts + i * ld;
+    const int64_t s = slot[i];
+    double pos[3] = {p[0], p[1], p[2]};
+    int64_t idc[8];
+    double l[3];
+    locate(g, pos, idc, l);
+    if (KIND == LS_ROWS_VALUE) {  // FD:236-269
+      double a[8];
+      trilinear(l, a);
+      double b = p[3];
+      normalise8(a, b);
+      store_row(s, idc, a, b, weight * p[4], d_idc, d_a, d_b, d_w, nan_flag);
+    } else if (KIND == LS_ROWS_NORM) {  // FD:403-476
+      double T[3][8];
+      element_gradient(l, g.step, T);
+      const double pw = (ld > 6) ? p[6] : 1.0;
+      const double w = (weight / 3.0) * pw;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        double b = p[3 + d];
+        normalise8(T[d], b);
+        store_row((int64_t)d * n + s, idc, T[d], b, w, d_idc, d_a, d_b, d_w, nan_flag);
+      }
+    } else if (KIND == LS_ROWS_GRADIENT) {  // FD:342-401 + get_vectors (M:276-298)
+      double T[3][8];
+      element_gradient(l, g.step, T);
+      double gv[3] = {p[3], p[4], p[5]};
+      double gn = norm3_seq(gv[0], gv[1], gv[2]);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) gv[d] = gv[d] / gn;
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int k = 0; k < 8; ++k) T[d][k] = T[d][k] / gn;
+      double len = norm3_seq(gv[0], gv[1], gv[2]);
+      double nv[3] = {gv[0] / len, gv[1] / len, gv[2] / len};
+      double len2 = norm3_seq(nv[0], nv[1], nv[2]);
+      double nn[3] = {nv[0] / len2, nv[1] / len2, nv[2] / len2};
+      double strike_deg = (-atan2(nn[1], nn[0])) * (180.0 / 3.141592653589793);
+      double srad = strike_deg * (3.141592653589793 / 180.0);
+      double sv[3] = {sin(-srad), -cos(-srad), 0.0};
+      double sl = norm3_seq(sv[0], sv[1], sv[2]);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) sv[d] = sv[d] / sl;
+      double dv[3] = {sv[1] * nv[2] - sv[2] * nv[1], sv[2] * nv[0] - sv[0] * nv[2], sv[0] * nv[1] - sv[1] * nv[0]};
+      double dl = norm3_seq(dv[0], dv[1], dv[2]);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        dv[d] = dv[d] / dl * len;
+        sv[d] = sv[d] * len;
+      }
+      double as[8], ad[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        as[k] = (sv[0] * T[0][k] + sv[1] * T[1][k]) + sv[2] * T[2][k];
+        ad[k] = (dv[0] * T[0][k] + dv[1] * T[1][k]) + dv[2] * T[2][k];
+      }
+      double b0 = 0.0, b1 = 0.0;
+      normalise8(as, b0);
+      normalise8(ad, b1);
+      store_row(s, idc, as, b0, weight, d_idc, d_a, d_b, d_w, nan_flag);
+      store_row(n + s, idc, ad, b1, weight, d_idc, d_a, d_b, d_w, nan_flag);
+    } else {  // LS_ROWS_TANGENT, FD:478-539
+      double T[3][8];
+      element_gradient(l, g.step, T);
+      double v[3] = {p[3], p[4], p[5]};
+      double vn = norm3_seq(v[0], v[1], v[2]);
+      if (vn > 0) {
+#pragma unroll
+        for (int d = 0; d < 3; ++d) v[d] = v[d] / vn;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+#pragma unroll
+          for (int k = 0; k < 8; ++k) T[d][k] = T[d][k] / vn;
+      }
+      double a[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) a[k] = (v[0] * T[0][k] + v[1] * T[1][k]) + v[2] * T[2][k];
+      double b = 0.0;
+      normalise8(a, b);
+      store_row(s, idc, a, b, weight, d_idc, d_a, d_b, d_w, nan_flag);
+    }
+  }
+}
+
+__global__ void pair_rows_kernel(GridArgs g, const double *__restrict__ pts, int64_t ld,
+                                 const int64_t *__restrict__ pairs, int64_t npairs, double weight,
+                                 int64_t *__restrict__ d_idc, double *__restrict__ d_a, double *__restrict__ d_b,
+                                 double *__restrict__ d_w) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < npairs;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    double a[16];
+    int64_t idc[16];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const double *p = pts + pairs[2 * r + h] * ld;
+      double pos[3] = {p[0], p[1], p[2]};
+      double l[3];
+      locate(g, pos, idc + 8 * h, l);
+      trilinear(l, a + 8 * h);
+    }
+#pragma unroll
+    for (int k = 8; k < 16; ++k) a[k] = -a[k];
+    // numpy pairwise sum of 16 squares: r[j] = a[j]^2 + a[8+j]^2, then the 8-tree
+    double q[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) q[k] = a[k] * a[k] + a[8 + k] * a[8 + k];
+    double len = sqrt(0.0 + (((q[0] + q[1]) + (q[2] + q[3])) + ((q[4] + q[5]) + (q[6] + q[7]))));
+    double b = 0.0;
+    if (len > 0) {
+      b = b / len;
+#pragma unroll
+      for (int k = 0; k < 16; ++k) a[k] = a[k] / len;
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      d_idc[r * 16 + k] = idc[k];
+      d_a[r * 16 + k] = a[k];
+    }
+    d_b[r] = b;
+    d_w[r] = weight;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// K2: explicit regularisation indices
+// ---------------------------------------------------------------------------
+struct RegShape {
+  int64_t rows;
+  int taps;
+  bool valid;
+};
+
+RegShape reg_shape(const ls_grid3 &g, int fam) {
+  const int64_t nx = g.nsteps[0], ny = g.nsteps[1], nz = g.nsteps[2];
+  RegShape s{0, 0, true};
+  if (fam >= LS_REG_DXY && fam <= LS_REG_DZZ) {
+    s.taps = (fam <= LS_REG_DXZ) ? 4 : 3;
+    if (nx >= 3 && ny >= 3 && nz >= 3) s.rows = (nx - 2) * (ny - 2) * (nz - 2);
+  } else if (fam >= LS_REG_DX_LOWER && fam <= LS_REG_DZ_UPPER) {
+    s.taps = 3;
+    const int axis = (fam - LS_REG_DX_LOWER) / 2;
+    const int64_t n[3] = {nx, ny, nz};
+    if (n[axis] >= 3) s.rows = n[(axis + 1) % 3] * n[(axis + 2) % 3];
+  } else {
+    s.valid = false;
+  }
+  return s;
+}
+
+__global__ void reg_rows_kernel(int64_t nx, int64_t ny, int64_t nz, int fam, int64_t rows, int64_t *__restrict__ idc) {
+  const int64_t nxy = nx * ny;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < rows; r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i, j, k;
+    if (fam <= LS_REG_DZZ) {  // interior nodes in ascending gi (G:176-190)
+      const int64_t mx = nx - 2, my = ny - 2;
+      i = 1 + r % mx;
+      j = 1 + (r / mx) % my;
+      k = 1 + r / (mx * my);
+    } else {  // FD:636-641 boundary layer nodes in ascending gi
+      const int axis = (fam - LS_REG_DX_LOWER) / 2;
+      const bool upper = ((fam - LS_REG_DX_LOWER) & 1) != 0;
+      if (axis == 0) {
+        i = upper ? nx - 2 : 1;
+        j = r % ny;
+        k = r / ny;
+      } else if (axis == 1) {
+        j = upper ? ny - 2 : 1;
+        i = r % nx;
+        k = r / nx;
+      } else {
+        k = upper ? nz - 2 : 1;
+        i = r % nx;
+        j = r / nx;
+      }
+    }
+    const int64_t gi = i + nx * j + nxy * k;
+    int64_t *o = idc + r * ((fam <= LS_REG_DXZ) ? 4 : 3);
+    switch (fam) {
+      case LS_REG_DXY:  // taps (dx,dy): (-1,-1) (+1,-1) (-1,+1) (+1,+1)
+        o[0] = gi - 1 - nx; o[1] = gi + 1 - nx; o[2] = gi - 1 + nx; o[3] = gi + 1 + nx;
+        break;
+      case LS_REG_DYZ:  // (dz,dy): (-1,-1) (-1,+1) (+1,-1) (+1,+1)
+        o[0] = gi - nxy - nx; o[1] = gi - nxy + nx; o[2] = gi + nxy - nx; o[3] = gi + nxy + nx;
+        break;
+      case LS_REG_DXZ:  // (dz,dx): (-1,-1) (-1,+1) (+1,-1) (+1,+1)
+        o[0] = gi - nxy - 1; o[1] = gi - nxy + 1; o[2] = gi + nxy - 1; o[3] = gi + nxy + 1;
+        break;
+      case LS_REG_DXX: case LS_REG_DX_LOWER: case LS_REG_DX_UPPER:
+        o[0] = gi - 1; o[1] = gi; o[2] = gi + 1;
+        break;
+      case LS_REG_DYY: case LS_REG_DY_LOWER: case LS_REG_DY_UPPER:
+        o[0] = gi - nx; o[1] = gi; o[2] = gi + nx;
+        break;
+      default:
+        o[0] = gi - nxy; o[1] = gi; o[2] = gi + nxy;
+        break;
+    }
+  }
+}
+
+int check_grid(const ls_grid3 *g) {
+  LS_ARG_CHECK(g != nullptr, "grid is NULL");
+  for (int d = 0; d < 3; ++d) {
+    LS_ARG_CHECK(g->nsteps[d] >= 2, "every axis needs at least 2 nodes");
+    LS_ARG_CHECK(g->step[d] > 0.0, "step must be positive");
+  }
+  return LS_OK;
+}
+
+}  // namespace
+}  // namespace ls
+
+using namespace ls;
+
+extern "C" int ls_fd_point_rows(const ls_grid3 *grid, int kind, const double *d_pts, int64_t npts, int64_t ld,
+                                double weight, int64_t *d_idc, double *d_a, double *d_b, double *d_w,
+                                int64_t *h_count, int32_t *h_nan, void *stream) {
+  LS_TRY(check_grid(grid));
+  LS_ARG_CHECK(kind >= LS_ROWS_VALUE && kind <= LS_ROWS_TANGENT, "unknown row kind");
+  LS_ARG_CHECK(npts >= 0, "npts < 0");
+  const int64_t min_ld = (kind == LS_ROWS_VALUE) ? 5 : 6;
+  LS_ARG_CHECK(ld >= min_ld, "ld too small for the row kind");
+  LS_ARG_CHECK(h_count != nullptr && h_nan != nullptr, "h_count / h_nan NULL");
+  *h_count = 0;
+  *h_nan = 0;
+  if (npts == 0) return LS_OK;
+  LS_ARG_CHECK(d_pts && d_idc && d_a && d_b && d_w, "NULL device buffer");
+  cudaStream_t s = as_stream(stream);
+  GridArgs g = make_grid_args(*grid);
+  int32_t *flag = nullptr;
+  int64_t *slot = nullptr;
+  int64_t *cnt = nullptr;
+  int32_t *nanf = nullptr;
+  LS_CUDA_TRY(cudaMallocAsync((void **)&flag, npts * sizeof(int32_t), s));
+  LS_CUDA_TRY(cudaMallocAsync((void **)&slot, npts * sizeof(int64_t), s));
+  LS_CUDA_TRY(cudaMallocAsync((void **)&cnt, 2 * sizeof(int64_t), s));
+  nanf = (int32_t *)(cnt + 1);
+  LS_CUDA_TRY(cudaMemsetAsync(cnt, 0, 2 * sizeof(int64_t), s));
+  const int blk = 256, grd = stream_grid(npts, blk);
+  inside_flags_kernel<<<grd, blk, 0, s>>>(g, d_pts, npts, ld, flag);
+  scan_flags_kernel<<<1, 1024, 0, s>>>(flag, npts, slot, cnt);
+  switch (kind) {
+    case LS_ROWS_VALUE:
+      point_rows_kernel<LS_ROWS_VALUE><<<grd, blk, 0, s>>>(g, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w, nanf);
+      break;
+    case LS_ROWS_NORM:
+      point_rows_kernel<LS_ROWS_NORM><<<grd, blk, 0, s>>>(g, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w, nanf);
+      break;
+    case LS_ROWS_GRADIENT:
+      point_rows_kernel<LS_ROWS_GRADIENT><<<grd, blk, 0, s>>>(g, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w, nanf);
+      break;
+    default:
+      point_rows_kernel<LS_ROWS_TANGENT><<<grd, blk, 0, s>>>(g, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w, nanf);
+      break;
+  }
+  LS_CUDA_TRY(cudaGetLastError());
+  int64_t host[2] = {0, 0};
+  LS_CUDA_TRY(cudaMemcpyAsync(host, cnt, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  LS_CUDA_TRY(cudaFreeAsync(flag, s));
+  LS_CUDA_TRY(cudaFreeAsync(slot, s));
+  LS_CUDA_TRY(cudaFreeAsync(cnt, s));
+  LS_CUDA_TRY(cudaStreamSynchronize(s));
+  *h_count = host[0];
+  *h_nan = ((int32_t *)&host[1])[0] != 0 ? 1 : 0;
+  return LS_OK;
+}
+
+extern "C" int ls_fd_pair_rows(const ls_grid3 *grid, const double *d_pts, int64_t ld, const int64_t *d_pairs,
+                               int64_t npairs, double weight, int64_t *d_idc, double *d_a, double *d_b, double *d_w,
+                               void *stream) {
+  LS_TRY(check_grid(grid));
+  LS_ARG_CHECK(ld >= 3 && npairs >= 0, "bad ld / npairs");
+  if (npairs == 0) return LS_OK;
+  LS_ARG_CHECK(d_pts && d_pairs && d_idc && d_a && d_b && d_w, "NULL device buffer");
+  GridArgs g = make_grid_args(*grid);
+  cudaStream_t s = as_stream(stream);
+  pair_rows_kernel<<<stream_grid(npairs, 128), 128, 0, s>>>(g, d_pts, ld, d_pairs, npairs, weight, d_idc, d_a, d_b, d_w);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
+
+extern "C" int ls_fd_reg_shape(const ls_grid3 *grid, int family, int64_t *h_rows, int32_t *h_taps) {
+  LS_TRY(check_grid(grid));
+  RegShape sh = reg_shape(*grid, family);
+  LS_ARG_CHECK(sh.valid, "unknown regularisation family");
+  if (h_rows) *h_rows = sh.rows;
+  if (h_taps) *h_taps = sh.taps;
+  return LS_OK;
+}
+
+extern "C" int ls_fd_reg_rows(const ls_grid3 *grid, int family, int64_t *d_idc, void *stream) {
+  LS_TRY(check_grid(grid));
+  RegShape sh = reg_shape(*grid, family);
+  LS_ARG_CHECK(sh.valid, "unknown regularisation family");
+  if (sh.rows == 0) return LS_OK;
+  LS_ARG_CHECK(d_idc != nullptr, "NULL device buffer");
+  cudaStream_t s = as_stream(stream);
+  reg_rows_kernel<<<stream_grid(sh.rows, 256), 256, 0, s>>>(grid->nsteps[0], grid->nsteps[1], grid->nsteps[2], family,
+                                                          sh.rows, d_idc);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}

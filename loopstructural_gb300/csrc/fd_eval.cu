@@ -1,0 +1,192 @@
+// K7: value / gradient of the trilinear FD field at points or on a lattice.
+// G:295-391 (StructuredGrid.evaluate_value / evaluate_gradient) with the
+// interpolator-level conventions of DI:1342-1379.  Sums follow numpy's
+// pairwise order for 8 terms, so results agree with the reference to ~1 ulp.
+// Compiled with -fmad=false (value parity, not speed, decides here: the
+// kernel is bound by the 8 coefficient gathers per point).
+#include <math.h>
+
+#include "ls_common.cuh"
+
+namespace ls {
+namespace {
+
+struct EvalGrid {
+  double origin[3], step[3], lo[3], hi[3];
+  int64_t n[3], cells[3];
+};
+
+EvalGrid make_eval_grid(const ls_grid3 &g) {
+  EvalGrid a;
+  for (int d = 0; d < 3; ++d) {
+    a.origin[d] = g.origin[d];
+    a.step[d] = g.step[d];
+    a.n[d] = g.nsteps[d];
+    a.cells[d] = g.nsteps[d] - 1;
+    double mx = g.origin[d] + (double)a.cells[d] * g.step[d];
+    double ext = fabs(mx - g.origin[d]);
+    if (ext < 1.0) ext = 1.0;
+    double tol = 2.220446049250313e-16 * 32.0 * ext;
+    a.lo[d] = g.origin[d] - tol;
+    a.hi[d] = mx + tol;
+  }
+  return a;
+}
+
+__device__ __forceinline__ double sum8(const double v[8]) {
+  return 0.0 + (((v[0] + v[1]) + (v[2] + v[3])) + ((v[4] + v[5]) + (v[6] + v[7])));
+}
+
+__device__ __forceinline__ void eval_one(const EvalGrid &g, const double *__restrict__ c, double px, double py,
+                                         double pz, double *value, double *grad) {
+  const bool nanrow = isnan(px) | isnan(py) | isnan(pz);
+  const bool inside = (px >= g.lo[0]) & (px <= g.hi[0]) & (py >= g.lo[1]) & (py <= g.hi[1]) & (pz >= g.lo[2]) &
+                      (pz <= g.hi[2]);
+  if (!inside) {
+    if (value) *value = nanrow ? 0.0 : __longlong_as_double(0x7ff8000000000000LL);
+    if (grad) grad[0] = grad[1] = grad[2] = 0.0;
+    return;
+  }
+  const double p[3] = {px, py, pz};
+  int64_t ci[3];
+  double l[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    double x = p[d] - g.origin[d];
+    int64_t k = (int64_t)floor(x / g.step[d]);
+    if (k < 0) k = 0;
+    if (k > g.cells[d] - 1) k = g.cells[d] - 1;
+    ci[d] = k;
+    double co = g.origin[d] + g.step[d] * (double)k;
+    l[d] = fmin(fmax((p[d] - co) / g.step[d], 0.0), 1.0);
+  }
+  const int64_t nx = g.n[0], nxy = g.n[0] * g.n[1];
+  const int64_t g0 = ci[0] + nx * ci[1] + nxy * ci[2];
+  double cv[8];
+  cv[0] = c[g0];
+  cv[1] = c[g0 + 1];
+  cv[2] = c[g0 + nx];
+  cv[3] = c[g0 + nx + 1];
+  cv[4] = c[g0 + nxy];
+  cv[5] = c[g0 + nxy + 1];
+  cv[6] = c[g0 + nxy + nx];
+  cv[7] = c[g0 + nxy + nx + 1];
+  const double x = l[0], y = l[1], z = l[2];
+  if (value) {
+    double a[8];
+    a[0] = (1 - x) * (1 - y) * (1 - z);
+    a[1] = x * (1 - y) * (1 - z);
+    a[2] = (1 - x) * y * (1 - z);
+    a[4] = (1 - x) * (1 - y) * z;
+    a[5] = x * (1 - y) * z;
+    a[6] = (1 - x) * y * z;
+    a[3] = x * y * (1 - z);
+    a[7] = x * y * z;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = a[k] * cv[k];
+    *value = sum8(a);
+  }
+  if (grad) {
+    double T[8];
+    T[0] = (1 - z) * (y - 1);
+    T[1] = (1 - y) * (1 - z);
+    T[2] = -y * (1 - z);
+    T[4] = -(1 - y) * z;
+    T[5] = (1 - y) * z;
+    T[6] = -y * z;
+    T[3] = y * (1 - z);
+    T[7] = y * z;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) T[k] = (T[k] / g.step[0]) * cv[k];
+    grad[0] = sum8(T);
+    T[0] = (x - 1) * (1 - z);
+    T[1] = -x * (1 - z);
+    T[2] = (1 - x) * (1 - z);
+    T[4] = -(1 - x) * z;
+    T[5] = -x * z;
+    T[6] = (1 - x) * z;
+    T[3] = x * (1 - z);
+    T[7] = x * z;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) T[k] = (T[k] / g.step[1]) * cv[k];
+    grad[1] = sum8(T);
+    T[0] = -(1 - x) * (1 - y);
+    T[1] = -x * (1 - y);
+    T[2] = -(1 - x) * y;
+    T[4] = (1 - x) * (1 - y);
+    T[5] = x * (1 - y);
+    T[6] = (1 - x) * y;
+    T[3] = -x * y;
+    T[7] = x * y;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) T[k] = (T[k] / g.step[2]) * cv[k];
+    grad[2] = sum8(T);
+  }
+}
+
+__global__ void eval_points_kernel(EvalGrid g, const double *__restrict__ c, const double *__restrict__ pts,
+                                   int64_t n, int64_t ld, double *__restrict__ value, double *__restrict__ grad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double *p = pts + i * ld;
+    double v, gr[3];
+    eval_one(g, c, p[0], p[1], p[2], value ? &v : nullptr, grad ? gr : nullptr);
+    if (value) value[i] = v;
+    if (grad) {
+      grad[3 * i] = gr[0];
+      grad[3 * i + 1] = gr[1];
+      grad[3 * i + 2] = gr[2];
+    }
+  }
+}
+
+__global__ void eval_lattice_kernel(EvalGrid g, const double *__restrict__ c, double ox, double oy, double oz,
+                                    double hx, double hy, double hz, int64_t n0, int64_t n1, int64_t n2,
+                                    double *__restrict__ value, double *__restrict__ grad) {
+  const int64_t total = n0 * n1 * n2;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = i % n0, b = (i / n0) % n1, k = i / (n0 * n1);
+    const double px = ox + hx * (double)a, py = oy + hy * (double)b, pz = oz + hz * (double)k;
+    double v, gr[3];
+    eval_one(g, c, px, py, pz, value ? &v : nullptr, grad ? gr : nullptr);
+    if (value) value[i] = v;
+    if (grad) {
+      grad[3 * i] = gr[0];
+      grad[3 * i + 1] = gr[1];
+      grad[3 * i + 2] = gr[2];
+    }
+  }
+}
+
+}  // namespace
+}  // namespace ls
+
+using namespace ls;
+
+extern "C" int ls_fd_eval_points(const ls_grid3 *grid, const double *d_c, const double *d_pts, int64_t npts, int64_t ld,
+                                 double *d_value, double *d_grad, void *stream) {
+  LS_ARG_CHECK(grid && d_c, "NULL argument");
+  LS_ARG_CHECK(npts >= 0 && ld >= 3, "bad npts / ld");
+  if (npts == 0 || (!d_value && !d_grad)) return LS_OK;
+  LS_ARG_CHECK(d_pts != nullptr, "NULL points");
+  EvalGrid g = make_eval_grid(*grid);
+  cudaStream_t s = as_stream(stream);
+  eval_points_kernel<<<stream_grid(npts, 256), 256, 0, s>>>(g, d_c, d_pts, npts, ld, d_value, d_grad);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
+
+extern "C" int ls_fd_eval_lattice(const ls_grid3 *grid, const double *d_c, const double lat_origin[3],
+                                  const double lat_step[3], const int64_t lat_n[3], double *d_value, double *d_grad,
+                                  void *stream) {
+  LS_ARG_CHECK(grid && d_c && lat_origin && lat_step && lat_n, "NULL argument");
+  LS_ARG_CHECK(lat_n[0] >= 0 && lat_n[1] >= 0 && lat_n[2] >= 0, "negative lattice size");
+  const int64_t total = lat_n[0] * lat_n[1] * lat_n[2];
+  if (total == 0 || (!d_value && !d_grad)) return LS_OK;
+  EvalGrid g = make_eval_grid(*grid);
+  cudaStream_t s = as_stream(stream);
+  eval_lattice_kernel<<<stream_grid(total, 256), 256, 0, s>>>(g, d_c, lat_origin[0], lat_origin[1], lat_origin[2],
+                                                              lat_step[0], lat_step[1], lat_step[2], lat_n[0],
+                                                              lat_n[1], lat_n[2], d_value, d_grad);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}

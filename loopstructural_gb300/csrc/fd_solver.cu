@@ -1,0 +1,791 @@
+// Matrix-free normal-equations operator and CG solvers for the FD
+// (StructuredGrid) interpolator.
+//
+// The least-squares system of the reference (DI:684-755 build_matrix,
+// SP:86-124 ridge + column scaling) is
+//     N = sum_f w_f^2 R_f^T R_f  +  A_d^T W A_d  +  ridge^2 I
+// where R_f are the twelve second-derivative stencil families (six interior,
+// six border, FD:643-692 / FD:1052-1144) and A_d the explicit data rows.
+// N is never assembled: the stencil part is applied from node coordinates,
+// the data part from a row list and a node->row incidence list.
+//
+// The solver is Jacobi-preconditioned CG, which is the reference's
+// column-scaled CG (SS:48-72 on A S, S = diag(N)^-1/2) written without the
+// explicit scaling: identical iterates x_k = S y_k and identical stopping test
+// ||S r|| < max(atol, rtol ||S rhs||).
+#include <math.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "fd_stencil.cuh"
+#include "ls_common.cuh"
+
+namespace ls {
+namespace {
+
+constexpr int kBlock = 256;
+
+// Device-resident CG scalars.  All reductions land here so that a whole batch
+// of iterations runs without host round trips.
+struct CgScalars {
+  double rz;       // r . z of the current residual
+  double pq_s;     // p . (stencil part of N p)
+  double pq_d;     // p . (data part of N p)
+  double beta;
+  double thresh2;  // stopping threshold squared (on r . z)
+  double rz64;     // FP64 refresh: r64 . D^-1 r64
+  double rz32;     // FP64 refresh: r32 . D^-1 r32 (after rounding)
+  double scratch;
+  long long iters;
+  long long maxiter;
+  int done;        // 0 running, 1 converged, LS_NOT_CONVERGED, LS_NAN, LS_BREAKDOWN
+  int pad;
+};
+
+struct DataTerm {
+  int64_t nrows = 0;
+  int32_t width = 0;
+  int64_t ntouched = 0;
+  int32_t *cols = nullptr;     // nrows * width (padding = -1)
+  double *a64 = nullptr;       // nrows * width
+  float *a32 = nullptr;
+  double *w2_64 = nullptr;     // nrows
+  float *w2_32 = nullptr;
+  double *b = nullptr;         // nrows
+  int64_t *touched = nullptr;  // ntouched node ids, ascending
+  int64_t *inc_ptr = nullptr;  // ntouched + 1
+  int32_t *inc_row = nullptr;  // incidences (row of each)
+  double *inc_a64 = nullptr;   // coefficient of each incidence
+  float *inc_a32 = nullptr;
+};
+
+}  // namespace
+}  // namespace ls
+
+struct ls_fd_handle {
+  ls_grid3 grid;
+  ls::StencilCoef coef;
+  int64_t n = 0;
+  ls::DataTerm data;
+  cudaStream_t stream = nullptr;
+  // persistent vectors
+  double *rhs = nullptr, *diag = nullptr, *dinv64 = nullptr;
+  float *dinv32 = nullptr;
+  double *x64 = nullptr, *r64 = nullptr, *p64 = nullptr, *q64 = nullptr, *s64 = nullptr;
+  float *x32 = nullptr, *r32 = nullptr, *p32 = nullptr, *q32 = nullptr, *s32 = nullptr;
+  double rhs_norm2 = 0.0;  // rhs . D^-1 rhs
+  // reductions
+  ls::CgScalars *sc = nullptr;     // iteration scalars (device)
+  ls::CgScalars *sc_h = nullptr;   // pinned host mirror
+  double *partials = nullptr;      // 2 * max_blocks
+  unsigned int *tickets = nullptr; // one per reduction site
+  int red_blocks = 0;
+  // graphs of one batch of iterations
+  cudaGraphExec_t g64 = nullptr, g32 = nullptr;
+  int g64_batch = 0, g32_batch = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace ls {
+namespace {
+
+enum Ticket { T_STENCIL = 0, T_DATA = 1, T_UPDATE = 2, T_REFRESH = 3, T_MISC = 4, T_COUNT = 5 };
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// q = (stencil part of N) p  and  p . q  (grid-reduced into sc->pq_s)
+template <typename T>
+__global__ void __launch_bounds__(kBlock) stencil_kernel(StencilCoef c, const T *__restrict__ p, T *__restrict__ q,
+                                                         CgScalars *sc, double *partials, unsigned int *ticket,
+                                                         bool check_done) {
+  if (check_done && sc->done) return;
+  double local = 0.0;
+  const int64_t n = c.nx * c.ny * c.nz;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = g % c.nx, j = (g / c.nx) % c.ny, k = g / (c.nx * c.ny);
+    T v = stencil_apply_node<T>(c, p, g, i, j, k);
+    q[g] = v;
+    local += (double)p[g] * (double)v;
+  }
+  double tot;
+  if (grid_sum<kBlock>(local, partials, ticket, &tot)) sc->pq_s = tot;
+}
+
+// s_r = w_r^2 (a_r . p) ; p . N_d p = sum_r w_r^2 (a_r . p)^2 into sc->pq_d
+template <typename T>
+__global__ void __launch_bounds__(kBlock) data_rows_kernel(int64_t nrows, int width, const int32_t *__restrict__ cols,
+                                                           const T *__restrict__ a, const T *__restrict__ w2,
+                                                           const T *__restrict__ p, T *__restrict__ s, CgScalars *sc,
+                                                           double *partials, unsigned int *ticket, bool check_done) {
+  if (check_done && sc->done) return;
+  double local = 0.0;
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
+    T acc = 0;
+    for (int k = 0; k < width; ++k) {
+      const int32_t col = cols[r * width + k];
+      if (col >= 0) acc += a[r * width + k] * p[col];
+    }
+    const T sr = w2[r] * acc;
+    s[r] = sr;
+    local += (double)sr * (double)acc;
+  }
+  double tot;
+  if (grid_sum<kBlock>(local, partials, ticket, &tot)) sc->pq_d = tot;
+}
+
+// q[n] += sum over the rows touching node n of a_rk s_r
+template <typename T>
+__global__ void __launch_bounds__(kBlock) data_nodes_kernel(int64_t ntouched, const int64_t *__restrict__ touched,
+                                                            const int64_t *__restrict__ ptr,
+                                                            const int32_t *__restrict__ row, const T *__restrict__ ia,
+                                                            const T *__restrict__ s, T *__restrict__ q,
+                                                            const CgScalars *sc, bool check_done) {
+  if (check_done && sc->done) return;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntouched;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    T acc = 0;
+    for (int64_t e = ptr[t]; e < ptr[t + 1]; ++e) acc += ia[e] * s[row[e]];
+    q[touched[t]] += acc;
+  }
+}
+
+// alpha = rz / pq ; x += alpha p ; r -= alpha q ; rz' = r . D^-1 r ;
+// the last block publishes beta = rz'/rz and tests convergence.
+template <typename T>
+__global__ void __launch_bounds__(kBlock) update_xr_kernel(int64_t n, T *__restrict__ x, T *__restrict__ r,
+                                                           const T *__restrict__ p, const T *__restrict__ q,
+                                                           const T *__restrict__ dinv, CgScalars *sc,
+                                                           double *partials, unsigned int *ticket) {
+  if (sc->done) return;
+  const double pq = sc->pq_s + sc->pq_d;
+  const double rz = sc->rz;
+  const double alpha_d = rz / pq;
+  if (!(pq > 0.0) || !isfinite(alpha_d)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = isfinite(pq) ? LS_BREAKDOWN : LS_NAN;
+    return;
+  }
+  const T alpha = (T)alpha_d;
+  double local = 0.0;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    x[g] += alpha * p[g];
+    const T rn = r[g] - alpha * q[g];
+    r[g] = rn;
+    local += (double)rn * (double)(dinv[g] * rn);
+  }
+  double rz_new;
+  if (grid_sum<kBlock>(local, partials, ticket, &rz_new)) {
+    sc->iters += 1;
+    sc->beta = rz_new / rz;
+    sc->rz = rz_new;
+    if (!isfinite(rz_new)) sc->done = LS_NAN;
+    else if (rz_new < sc->thresh2) sc->done = 1;
+    else if (sc->iters >= sc->maxiter) sc->done = LS_NOT_CONVERGED;
+  }
+}
+
+// p = D^-1 r + beta p
+template <typename T>
+__global__ void __launch_bounds__(kBlock) update_p_kernel(int64_t n, const T *__restrict__ r, const T *__restrict__ dinv,
+                                                          T *__restrict__ p, const CgScalars *sc) {
+  if (sc->done) return;
+  const T beta = (T)sc->beta;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+    p[g] = dinv[g] * r[g] + beta * p[g];
+}
+
+// FP64 residual refresh: r64 = rhs - q64 ; rz64 = r64 . D^-1 r64.
+// With r32 given: r32 = (float) r64, rz32 = r32 . D^-1 r32 (FP64 sum),
+// x32 = 0, and p32 = D^-1 r32 when init_p.  With p64 given (FP64 solver
+// start): p64 = D^-1 r64.
+__global__ void __launch_bounds__(kBlock) refresh_kernel(int64_t n, const double *__restrict__ rhs,
+                                                         const double *__restrict__ q64, const double *__restrict__ dinv64,
+                                                         double *__restrict__ r64, double *__restrict__ p64,
+                                                         const float *__restrict__ dinv32, float *__restrict__ r32,
+                                                         float *__restrict__ p32, float *__restrict__ x32,
+                                                         CgScalars *sc, double *partials, unsigned int *ticket) {
+  double l64 = 0.0, l32 = 0.0;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const double rv = rhs[g] - (q64 ? q64[g] : 0.0);
+    r64[g] = rv;
+    const double zv = dinv64[g] * rv;
+    l64 += rv * zv;
+    if (p64) p64[g] = zv;
+    if (r32) {
+      const float rf = (float)rv;
+      r32[g] = rf;
+      const float zf = dinv32[g] * rf;
+      l32 += (double)rf * (double)zf;
+      if (p32) p32[g] = zf;
+      x32[g] = 0.0f;
+    }
+  }
+  double t0, t1;
+  if (grid_sum2<kBlock>(l64, l32, partials, ticket, &t0, &t1)) {
+    sc->rz64 = t0;
+    sc->rz32 = t1;
+  }
+}
+
+template <typename T>
+__global__ void fill_kernel(int64_t n, T *__restrict__ v, T value) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+    v[g] = value;
+}
+
+// x64 += x32
+__global__ void fold_kernel(int64_t n, double *__restrict__ x64, const float *__restrict__ x32) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+    x64[g] += (double)x32[g];
+}
+
+template <typename T>
+__global__ void convert_kernel(int64_t n, const double *__restrict__ src, T *__restrict__ dst) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+    dst[g] = (T)src[g];
+}
+
+// diag = ridge^2 + stencil diagonal (+ data diagonal added by diag_data_kernel)
+__global__ void diag_stencil_kernel(StencilCoef c, double *__restrict__ d) {
+  const int64_t n = c.nx * c.ny * c.nz;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = g % c.nx, j = (g / c.nx) % c.ny, k = g / (c.nx * c.ny);
+    d[g] = stencil_diag_node(c, i, j, k);
+  }
+}
+
+// touched nodes: diag += sum w2 a^2 ; rhs = sum a w2 b
+__global__ void data_node_setup_kernel(int64_t ntouched, const int64_t *__restrict__ touched,
+                                       const int64_t *__restrict__ ptr, const int32_t *__restrict__ row,
+                                       const double *__restrict__ ia, const double *__restrict__ w2,
+                                       const double *__restrict__ b, double *__restrict__ diag,
+                                       double *__restrict__ rhs) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntouched;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    double dd = 0.0, rr = 0.0;
+    for (int64_t e = ptr[t]; e < ptr[t + 1]; ++e) {
+      const double a = ia[e];
+      const int32_t r = row[e];
+      dd += w2[r] * a * a;
+      rr += a * w2[r] * b[r];
+    }
+    const int64_t g = touched[t];
+    diag[g] += dd;
+    rhs[g] = rr;
+  }
+}
+
+__global__ void dinv_kernel(int64_t n, const double *__restrict__ d, double *__restrict__ i64, float *__restrict__ i32) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const double v = d[g] > 0.0 ? 1.0 / d[g] : 1.0;
+    i64[g] = v;
+    i32[g] = (float)v;
+  }
+}
+
+__global__ void norm2_kernel(int64_t n, const double *__restrict__ v, const double *__restrict__ w, CgScalars *sc,
+                             double *partials, unsigned int *ticket) {
+  double l = 0.0;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+    l += v[g] * (w[g] * v[g]);
+  double tot;
+  if (grid_sum<kBlock>(l, partials, ticket, &tot)) sc->scratch = tot;
+}
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+template <typename P>
+int dev_alloc(P **ptr, size_t count) {
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void **)ptr, count * sizeof(P));
+  if (e != cudaSuccess) {
+    set_error("cudaMalloc(%zu bytes): %s", count * sizeof(P), cudaGetErrorString(e));
+    return LS_ERR_ALLOC;
+  }
+  return LS_OK;
+}
+
+int grid_for(const ls_fd_handle *h, int64_t n) {
+  int g = stream_grid(n, kBlock, 8);
+  return std::min(g, h->red_blocks);
+}
+
+// N p for the precision T, leaving q; p.q in sc->pq_s + sc->pq_d
+template <typename T>
+void launch_apply(ls_fd_handle *h, const T *p, T *q, T *s, const T *a, const T *w2, const T *ia, bool check_done,
+                  cudaStream_t st) {
+  const DataTerm &d = h->data;
+  stencil_kernel<T><<<grid_for(h, h->n), kBlock, 0, st>>>(h->coef, p, q, h->sc, h->partials, h->tickets + T_STENCIL,
+                                                        check_done);
+  if (d.nrows > 0) {
+    data_rows_kernel<T><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, a, w2, p, s, h->sc,
+                                                               h->partials + 2 * h->red_blocks,
+                                                               h->tickets + T_DATA, check_done);
+    data_nodes_kernel<T><<<grid_for(h, d.ntouched), kBlock, 0, st>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row, ia, s,
+                                                                   q, h->sc, check_done);
+  }
+}
+
+void launch_apply64(ls_fd_handle *h, const double *p, double *q, bool check_done, cudaStream_t st) {
+  launch_apply<double>(h, p, q, h->s64, h->data.a64, h->data.w2_64, h->data.inc_a64, check_done, st);
+}
+void launch_apply32(ls_fd_handle *h, const float *p, float *q, bool check_done, cudaStream_t st) {
+  launch_apply<float>(h, p, q, h->s32, h->data.a32, h->data.w2_32, h->data.inc_a32, check_done, st);
+}
+
+template <typename T>
+void launch_iteration(ls_fd_handle *h, T *x, T *r, T *p, T *q, const T *dinv, cudaStream_t st) {
+  if (sizeof(T) == 8)
+    launch_apply64(h, (const double *)p, (double *)q, true, st);
+  else
+    launch_apply32(h, (const float *)p, (float *)q, true, st);
+  const int g = grid_for(h, h->n);
+  update_xr_kernel<T><<<g, kBlock, 0, st>>>(h->n, x, r, p, q, dinv, h->sc, h->partials, h->tickets + T_UPDATE);
+  update_p_kernel<T><<<g, kBlock, 0, st>>>(h->n, r, dinv, p, h->sc);
+}
+
+template <typename T>
+int build_graph(ls_fd_handle *h, int batch, cudaGraphExec_t *out, T *x, T *r, T *p, T *q, const T *dinv) {
+  cudaStream_t st = h->stream;
+  LS_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  for (int it = 0; it < batch; ++it) launch_iteration<T>(h, x, r, p, q, dinv, st);
+  cudaGraph_t graph;
+  LS_CUDA_TRY(cudaStreamEndCapture(st, &graph));
+  cudaError_t e = cudaGraphInstantiate(out, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
+    return LS_ERR_CUDA;
+  }
+  return LS_OK;
+}
+
+int read_scalars(ls_fd_handle *h) {
+  LS_CUDA_TRY(cudaMemcpyAsync(h->sc_h, h->sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
+  LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return LS_OK;
+}
+
+int write_scalars(ls_fd_handle *h) {
+  LS_CUDA_TRY(cudaMemcpyAsync(h->sc, h->sc_h, sizeof(CgScalars), cudaMemcpyHostToDevice, h->stream));
+  return LS_OK;
+}
+
+// true FP64 residual of x64: r64 = rhs - N x64 (and r32 / p32 / x32 when given)
+int refresh(ls_fd_handle *h, bool have_x, float *r32, float *p32) {
+  cudaStream_t st = h->stream;
+  if (have_x) launch_apply64(h, h->x64, h->q64, false, st);
+  refresh_kernel<<<grid_for(h, h->n), kBlock, 0, st>>>(h->n, h->rhs, have_x ? h->q64 : nullptr, h->dinv64, h->r64,
+                                                       r32 ? nullptr : h->p64, h->dinv32, r32, p32, h->x32, h->sc,
+                                                       h->partials, h->tickets + T_REFRESH);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
+
+}  // namespace
+}  // namespace ls
+
+using namespace ls;
+
+extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *stream) {
+  LS_ARG_CHECK(sys != nullptr && out != nullptr, "NULL argument");
+  *out = nullptr;
+  const ls_grid3 &g = sys->grid;
+  for (int d = 0; d < 3; ++d) {
+    LS_ARG_CHECK(g.nsteps[d] >= 2, "every axis needs at least 2 nodes");
+    LS_ARG_CHECK(g.step[d] > 0.0, "step must be positive");
+  }
+  const int64_t n = g.nsteps[0] * g.nsteps[1] * g.nsteps[2];
+  LS_ARG_CHECK(n < (int64_t)2000000000, "grid too large for 32-bit data-row columns");
+  LS_ARG_CHECK(sys->nrows >= 0, "nrows < 0");
+  LS_ARG_CHECK(sys->nrows == 0 || (sys->width >= 1 && sys->width <= 64), "width must be in [1, 64]");
+  LS_ARG_CHECK(sys->nrows == 0 || (sys->d_idc && sys->d_a && sys->d_b && sys->d_w), "NULL data-row buffer");
+  cudaStream_t cs = as_stream(stream);
+  LS_CUDA_TRY(cudaStreamSynchronize(cs));
+
+  ls_fd_handle *h = new ls_fd_handle();
+  h->grid = g;
+  h->n = n;
+  h->coef = make_stencil_coef(g, sys->w_dxx, sys->w_dyy, sys->w_dzz, sys->w_dxy, sys->w_dyz, sys->w_dxz, sys->w_dx,
+                              sys->w_dy, sys->w_dz, sys->ridge);
+  int st = LS_OK;
+  auto fail = [&](int s) {
+    ls_fd_destroy(h);
+    return s;
+  };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    set_error("cudaStreamCreate failed");
+    return fail(LS_ERR_CUDA);
+  }
+  h->red_blocks = sm_count() * 8;
+  if ((st = dev_alloc(&h->partials, 4 * (size_t)h->red_blocks)) < 0) return fail(st);
+  if ((st = dev_alloc(&h->tickets, T_COUNT)) < 0) return fail(st);
+  if ((st = dev_alloc(&h->sc, 1)) < 0) return fail(st);
+  if (cudaMallocHost((void **)&h->sc_h, sizeof(CgScalars)) != cudaSuccess) {
+    set_error("cudaMallocHost failed");
+    return fail(LS_ERR_ALLOC);
+  }
+  cudaMemsetAsync(h->tickets, 0, T_COUNT * sizeof(unsigned int), h->stream);
+  cudaMemsetAsync(h->sc, 0, sizeof(CgScalars), h->stream);
+  // vectors
+  double **v64[] = {&h->rhs, &h->diag, &h->dinv64, &h->x64, &h->r64, &h->p64, &h->q64};
+  for (auto pp : v64)
+    if ((st = dev_alloc(pp, n)) < 0) return fail(st);
+  float **v32[] = {&h->dinv32, &h->x32, &h->r32, &h->p32, &h->q32};
+  for (auto pp : v32)
+    if ((st = dev_alloc(pp, n)) < 0) return fail(st);
+
+  // ---- data rows: device copies and the node -> row incidence list ----
+  DataTerm &d = h->data;
+  d.nrows = sys->nrows;
+  d.width = sys->nrows > 0 ? sys->width : 0;
+  const int64_t ne = d.nrows * d.width;
+  std::vector<int64_t> idc(ne);
+  std::vector<double> av(ne), wv(d.nrows), bv(d.nrows);
+  if (ne > 0) {
+    if (cudaMemcpy(idc.data(), sys->d_idc, ne * sizeof(int64_t), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(av.data(), sys->d_a, ne * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(wv.data(), sys->d_w, d.nrows * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(bv.data(), sys->d_b, d.nrows * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+      set_error("copying data rows failed");
+      return fail(LS_ERR_CUDA);
+    }
+  }
+  std::vector<int32_t> cols(ne);
+  std::vector<std::pair<int64_t, int64_t>> inc;  // (node, entry)
+  inc.reserve(ne);
+  for (int64_t e = 0; e < ne; ++e) {
+    const int64_t c = idc[e];
+    if (c >= n) {
+      set_error("data-row column %lld out of range (dof %lld)", (long long)c, (long long)n);
+      return fail(LS_ERR_ARG);
+    }
+    cols[e] = c < 0 ? -1 : (int32_t)c;
+    if (c >= 0) inc.emplace_back(c, e);
+  }
+  std::stable_sort(inc.begin(), inc.end(),
+                   [](const std::pair<int64_t, int64_t> &x, const std::pair<int64_t, int64_t> &y) { return x.first < y.first; });
+  std::vector<int64_t> touched, ptr;
+  std::vector<int32_t> irow;
+  std::vector<double> ia64;
+  std::vector<float> ia32, a32(ne), w2_32(d.nrows);
+  std::vector<double> w2_64(d.nrows);
+  for (size_t t = 0; t < inc.size(); ++t) {
+    if (t == 0 || inc[t].first != inc[t - 1].first) {
+      touched.push_back(inc[t].first);
+      ptr.push_back((int64_t)t);
+    }
+    irow.push_back((int32_t)(inc[t].second / d.width));
+    ia64.push_back(av[inc[t].second]);
+    ia32.push_back((float)av[inc[t].second]);
+  }
+  ptr.push_back((int64_t)inc.size());
+  for (int64_t e = 0; e < ne; ++e) a32[e] = (float)av[e];
+  for (int64_t r = 0; r < d.nrows; ++r) {
+    w2_64[r] = wv[r] * wv[r];
+    w2_32[r] = (float)w2_64[r];
+  }
+  d.ntouched = (int64_t)touched.size();
+  const int64_t ni = (int64_t)inc.size();
+  if ((st = dev_alloc(&d.cols, ne)) < 0 || (st = dev_alloc(&d.a64, ne)) < 0 || (st = dev_alloc(&d.a32, ne)) < 0 ||
+      (st = dev_alloc(&d.w2_64, d.nrows)) < 0 || (st = dev_alloc(&d.w2_32, d.nrows)) < 0 ||
+      (st = dev_alloc(&d.b, d.nrows)) < 0 || (st = dev_alloc(&d.touched, d.ntouched)) < 0 ||
+      (st = dev_alloc(&d.inc_ptr, d.ntouched + 1)) < 0 || (st = dev_alloc(&d.inc_row, ni)) < 0 ||
+      (st = dev_alloc(&d.inc_a64, ni)) < 0 || (st = dev_alloc(&d.inc_a32, ni)) < 0 ||
+      (st = dev_alloc(&h->s64, d.nrows)) < 0 || (st = dev_alloc(&h->s32, d.nrows)) < 0)
+    return fail(st);
+  cudaStream_t hs = h->stream;
+#define UP(dst, src, cnt)                                                                                        \
+  if ((cnt) > 0 && cudaMemcpyAsync(dst, (src).data(), (cnt) * sizeof((src)[0]), cudaMemcpyHostToDevice, hs) != \
+                       cudaSuccess) {                                                                            \
+    set_error("upload failed");                                                                                  \
+    return fail(LS_ERR_CUDA);                                                                                    \
+  }
+  UP(d.cols, cols, ne);
+  UP(d.a64, av, ne);
+  UP(d.a32, a32, ne);
+  UP(d.w2_64, w2_64, d.nrows);
+  UP(d.w2_32, w2_32, d.nrows);
+  UP(d.b, bv, d.nrows);
+  UP(d.touched, touched, d.ntouched);
+  UP(d.inc_ptr, ptr, d.ntouched + 1);
+  UP(d.inc_row, irow, ni);
+  UP(d.inc_a64, ia64, ni);
+  UP(d.inc_a32, ia32, ni);
+#undef UP
+  // ---- rhs, diagonal, inverse diagonal ----
+  const int gn = grid_for(h, n);
+  cudaMemsetAsync(h->rhs, 0, n * sizeof(double), hs);
+  diag_stencil_kernel<<<gn, kBlock, 0, hs>>>(h->coef, h->diag);
+  if (d.ntouched > 0)
+    data_node_setup_kernel<<<grid_for(h, d.ntouched), kBlock, 0, hs>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row,
+                                                                       d.inc_a64, d.w2_64, d.b, h->diag, h->rhs);
+  dinv_kernel<<<gn, kBlock, 0, hs>>>(n, h->diag, h->dinv64, h->dinv32);
+  norm2_kernel<<<gn, kBlock, 0, hs>>>(n, h->rhs, h->dinv64, h->sc, h->partials, h->tickets + T_MISC);
+  if (cudaGetLastError() != cudaSuccess || read_scalars(h) < 0) {
+    set_error("setup kernels failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return fail(LS_ERR_CUDA);
+  }
+  h->rhs_norm2 = h->sc_h->scratch;
+  cudaEventCreate(&h->ev0);
+  cudaEventCreate(&h->ev1);
+  *out = h;
+  return LS_OK;
+}
+
+extern "C" int ls_fd_destroy(ls_fd_handle *h) {
+  if (!h) return LS_OK;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->g64) cudaGraphExecDestroy(h->g64);
+  if (h->g32) cudaGraphExecDestroy(h->g32);
+  void *ptrs[] = {h->rhs, h->diag, h->dinv64, h->dinv32, h->x64, h->r64, h->p64, h->q64, h->s64, h->x32, h->r32,
+                  h->p32, h->q32, h->s32, h->sc, h->partials, h->tickets, h->data.cols, h->data.a64, h->data.a32,
+                  h->data.w2_64, h->data.w2_32, h->data.b, h->data.touched, h->data.inc_ptr, h->data.inc_row,
+                  h->data.inc_a64, h->data.inc_a32};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (h->sc_h) cudaFreeHost(h->sc_h);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return LS_OK;
+}
+
+extern "C" int64_t ls_fd_dof(const ls_fd_handle *h) { return h ? h->n : -1; }
+
+extern "C" int ls_fd_rhs(ls_fd_handle *h, double *d_rhs, void *stream) {
+  LS_ARG_CHECK(h && d_rhs, "NULL argument");
+  LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  LS_CUDA_TRY(cudaMemcpyAsync(d_rhs, h->rhs, h->n * sizeof(double), cudaMemcpyDeviceToDevice, as_stream(stream)));
+  return LS_OK;
+}
+
+extern "C" int ls_fd_diagonal(ls_fd_handle *h, double *d_diag, void *stream) {
+  LS_ARG_CHECK(h && d_diag, "NULL argument");
+  LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  LS_CUDA_TRY(cudaMemcpyAsync(d_diag, h->diag, h->n * sizeof(double), cudaMemcpyDeviceToDevice, as_stream(stream)));
+  return LS_OK;
+}
+
+extern "C" int ls_fd_apply(ls_fd_handle *h, const double *d_x, double *d_y, void *stream) {
+  LS_ARG_CHECK(h && d_x && d_y, "NULL argument");
+  cudaStream_t cs = as_stream(stream);
+  LS_CUDA_TRY(cudaStreamSynchronize(cs));
+  launch_apply64(h, d_x, d_y, false, h->stream);
+  LS_CUDA_TRY(cudaGetLastError());
+  LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return LS_OK;
+}
+
+extern "C" int ls_fd_apply_f32(ls_fd_handle *h, const float *d_x, float *d_y, void *stream) {
+  LS_ARG_CHECK(h && d_x && d_y, "NULL argument");
+  cudaStream_t cs = as_stream(stream);
+  LS_CUDA_TRY(cudaStreamSynchronize(cs));
+  launch_apply32(h, d_x, d_y, false, h->stream);
+  LS_CUDA_TRY(cudaGetLastError());
+  LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return LS_OK;
+}
+
+extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d_x, ls_solve_stats *stats,
+                           void *stream) {
+  LS_ARG_CHECK(h && opts && d_x && stats, "NULL argument");
+  LS_ARG_CHECK(opts->precision == LS_FP64 || opts->precision == LS_MIXED, "unknown precision");
+  LS_ARG_CHECK(opts->atol >= 0.0 && opts->rtol >= 0.0, "tolerances must be >= 0");
+  cudaStream_t cs = as_stream(stream);
+  cudaStream_t st = h->stream;
+  LS_CUDA_TRY(cudaStreamSynchronize(cs));
+  const int64_t n = h->n;
+  const int batch = opts->check_every > 0 ? opts->check_every : 64;
+  const int64_t maxiter = opts->maxiter > 0 ? opts->maxiter : 10 * n;
+  const double delta = opts->reliable_delta > 0.0 ? opts->reliable_delta : 0.1;
+  *stats = ls_solve_stats{};
+  const double bnorm = sqrt(h->rhs_norm2);
+  const double thresh = std::max(opts->atol, opts->rtol * bnorm);
+  stats->rhs_norm = bnorm;
+  stats->threshold = thresh;
+
+  LS_CUDA_TRY(cudaEventRecord(h->ev0, st));
+  if (opts->use_x0)
+    LS_CUDA_TRY(cudaMemcpyAsync(h->x64, d_x, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  else
+    LS_CUDA_TRY(cudaMemsetAsync(h->x64, 0, n * sizeof(double), st));
+  CgScalars &s = *h->sc_h;
+  int status = LS_OK;
+  long long iters = 0, updates = 0;
+
+  if (bnorm == 0.0) {  // scipy returns b (= 0) immediately
+    LS_CUDA_TRY(cudaMemsetAsync(h->x64, 0, n * sizeof(double), st));
+  } else if (opts->precision == LS_FP64) {
+    LS_TRY(refresh(h, opts->use_x0 != 0, nullptr, nullptr));  // r64, p64 = D^-1 r64, rz64
+    LS_TRY(read_scalars(h));
+    s.rz = s.rz64;
+    s.pq_s = s.pq_d = 0.0;
+    s.thresh2 = thresh * thresh;
+    s.iters = 0;
+    s.maxiter = maxiter;
+    s.done = (s.rz < s.thresh2) ? 1 : 0;
+    LS_TRY(write_scalars(h));
+    if (!h->g64 || h->g64_batch != batch) {
+      if (h->g64) cudaGraphExecDestroy(h->g64);
+      h->g64 = nullptr;
+      LS_TRY(build_graph<double>(h, batch, &h->g64, h->x64, h->r64, h->p64, h->q64, h->dinv64));
+      h->g64_batch = batch;
+    }
+    while (!s.done) {
+      LS_CUDA_TRY(cudaGraphLaunch(h->g64, st));
+      LS_TRY(read_scalars(h));
+    }
+    iters = s.iters;
+    status = s.done == 1 ? LS_OK : s.done;
+  } else {
+    // FP32 CG on the correction, FP64 residual refreshed whenever the
+    // recurrence residual fell by `delta` (reliable updates).
+    LS_TRY(refresh(h, opts->use_x0 != 0, h->r32, h->p32));  // r64, r32, p32, x32 = 0
+    LS_TRY(read_scalars(h));
+    double true_r = sqrt(std::max(s.rz64, 0.0));
+    if (!(true_r < thresh)) {
+      s.rz = s.rz32;
+      s.pq_s = s.pq_d = 0.0;
+      s.thresh2 = thresh * thresh;
+      s.iters = 0;
+      s.maxiter = maxiter;
+      s.done = 0;
+      LS_TRY(write_scalars(h));
+      if (!h->g32 || h->g32_batch != batch) {
+        if (h->g32) cudaGraphExecDestroy(h->g32);
+        h->g32 = nullptr;
+        LS_TRY(build_graph<float>(h, batch, &h->g32, h->x32, h->r32, h->p32, h->q32, h->dinv32));
+        h->g32_batch = batch;
+      }
+      double rz_ref = s.rz32;
+      for (;;) {
+        LS_CUDA_TRY(cudaGraphLaunch(h->g32, st));
+        LS_TRY(read_scalars(h));
+        const bool trigger = s.done != 0 || s.rz < delta * delta * rz_ref;
+        if (!trigger) continue;
+        if (s.done == LS_NAN || s.done == LS_BREAKDOWN) {
+          status = s.done;
+          break;
+        }
+        // reliable update
+        fold_kernel<<<grid_for(h, n), kBlock, 0, st>>>(n, h->x64, h->x32);
+        LS_TRY(refresh(h, true, h->r32, nullptr));
+        const long long it_now = s.iters;
+        LS_TRY(read_scalars(h));
+        ++updates;
+        true_r = sqrt(std::max(s.rz64, 0.0));
+        if (true_r < thresh) {
+          status = LS_OK;
+          break;
+        }
+        if (it_now >= maxiter) {
+          status = LS_NOT_CONVERGED;
+          break;
+        }
+        if (!isfinite(true_r)) {
+          status = LS_NAN;
+          break;
+        }
+        s.rz = s.rz32;
+        s.done = 0;
+        rz_ref = s.rz32;
+        LS_TRY(write_scalars(h));
+      }
+      iters = s.iters;
+    }
+  }
+  // final FP64 residual of the returned iterate
+  LS_TRY(refresh(h, true, nullptr, nullptr));
+  LS_CUDA_TRY(cudaMemcpyAsync(d_x, h->x64, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  LS_CUDA_TRY(cudaEventRecord(h->ev1, st));
+  LS_TRY(read_scalars(h));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  stats->iterations = iters;
+  stats->reliable_updates = updates;
+  stats->residual = sqrt(std::max(s.rz64, 0.0));
+  stats->device_ms = ms;
+  stats->status = status;
+  LS_CUDA_TRY(cudaGetLastError());
+  return status;
+}
+
+extern "C" int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps, ls_fd_profile *out, void *stream) {
+  LS_ARG_CHECK(h && out && reps > 0, "bad argument");
+  LS_ARG_CHECK(precision == LS_FP64 || precision == LS_MIXED, "unknown precision");
+  LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+  cudaStream_t st = h->stream;
+  const bool f32 = precision == LS_MIXED;
+  const size_t s = f32 ? 4 : 8;
+  const int64_t n = h->n;
+  // keep every kernel running: done = 0, far-away threshold and iteration cap
+  CgScalars &sc = *h->sc_h;
+  sc = CgScalars{};
+  sc.rz = 1.0;
+  sc.pq_s = 1.0;
+  sc.thresh2 = -1.0;
+  sc.maxiter = (long long)1 << 60;
+  LS_TRY(write_scalars(h));
+  // p = r = 1: p.Np > 0, so every launch does its full work
+  const int gf = grid_for(h, n);
+  if (f32) {
+    fill_kernel<float><<<gf, kBlock, 0, st>>>(n, h->p32, 1.0f);
+    fill_kernel<float><<<gf, kBlock, 0, st>>>(n, h->r32, 1.0f);
+    fill_kernel<float><<<gf, kBlock, 0, st>>>(n, h->x32, 0.0f);
+  } else {
+    fill_kernel<double><<<gf, kBlock, 0, st>>>(n, h->p64, 1.0);
+    fill_kernel<double><<<gf, kBlock, 0, st>>>(n, h->r64, 1.0);
+    fill_kernel<double><<<gf, kBlock, 0, st>>>(n, h->x64, 0.0);
+  }
+  auto timed = [&](auto &&fn, double *ms_out) -> int {
+    fn();  // warm-up
+    LS_CUDA_TRY(cudaEventRecord(h->ev0, st));
+    for (int i = 0; i < reps; ++i) fn();
+    LS_CUDA_TRY(cudaEventRecord(h->ev1, st));
+    LS_CUDA_TRY(cudaEventSynchronize(h->ev1));
+    float ms = 0.0f;
+    LS_CUDA_TRY(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    *ms_out = ms / reps;
+    return LS_OK;
+  };
+  const int g = grid_for(h, n);
+  const DataTerm &d = h->data;
+  LS_TRY(timed([&] {
+    if (f32) stencil_kernel<float><<<g, kBlock, 0, st>>>(h->coef, h->p32, h->q32, h->sc, h->partials, h->tickets + T_STENCIL, false);
+    else stencil_kernel<double><<<g, kBlock, 0, st>>>(h->coef, h->p64, h->q64, h->sc, h->partials, h->tickets + T_STENCIL, false);
+  }, &out->stencil_ms));
+  out->data_ms = 0.0;
+  if (d.nrows > 0) {
+    LS_TRY(timed([&] {
+      if (f32) {
+        data_rows_kernel<float><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, d.a32, d.w2_32, h->p32, h->s32, h->sc, h->partials + 2 * h->red_blocks, h->tickets + T_DATA, false);
+        data_nodes_kernel<float><<<grid_for(h, d.ntouched), kBlock, 0, st>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row, d.inc_a32, h->s32, h->q32, h->sc, false);
+      } else {
+        data_rows_kernel<double><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, d.a64, d.w2_64, h->p64, h->s64, h->sc, h->partials + 2 * h->red_blocks, h->tickets + T_DATA, false);
+        data_nodes_kernel<double><<<grid_for(h, d.ntouched), kBlock, 0, st>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row, d.inc_a64, h->s64, h->q64, h->sc, false);
+      }
+    }, &out->data_ms));
+  }
+  LS_TRY(timed([&] {
+    if (f32) {
+      update_xr_kernel<float><<<g, kBlock, 0, st>>>(n, h->x32, h->r32, h->p32, h->q32, h->dinv32, h->sc, h->partials, h->tickets + T_UPDATE);
+      update_p_kernel<float><<<g, kBlock, 0, st>>>(n, h->r32, h->dinv32, h->p32, h->sc);
+    } else {
+      update_xr_kernel<double><<<g, kBlock, 0, st>>>(n, h->x64, h->r64, h->p64, h->q64, h->dinv64, h->sc, h->partials, h->tickets + T_UPDATE);
+      update_p_kernel<double><<<g, kBlock, 0, st>>>(n, h->r64, h->dinv64, h->p64, h->sc);
+    }
+  }, &out->update_ms));
+  LS_TRY(timed([&] {
+    if (f32) launch_iteration<float>(h, h->x32, h->r32, h->p32, h->q32, h->dinv32, st);
+    else launch_iteration<double>(h, h->x64, h->r64, h->p64, h->q64, h->dinv64, st);
+  }, &out->iteration_ms));
+  out->stencil_bytes = 2.0 * (double)n * (double)s;
+  out->iteration_bytes = 9.0 * (double)n * (double)s + 16.0 * (double)(d.nrows * d.width);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}

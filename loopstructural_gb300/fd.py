@@ -1,0 +1,243 @@
+"""Device-side FD engine: thin Python wrappers over the C ABI that own the
+device buffers (torch tensors) handed to the kernels."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+
+REG_TAP_VALUES = {
+    # normalised stencil values in the reference column order (OP:10-43 masks
+    # divided by their L2 norm, DI:361-366)
+    "dxx": np.array([1.0, -2.0, 1.0]) / np.sqrt(6.0),
+    "dxy": np.array([-0.5, 0.5, 0.5, -0.5]),
+}
+for _n in ("dyy", "dzz", "dx_lower", "dx_upper", "dy_lower", "dy_upper", "dz_lower", "dz_upper"):
+    REG_TAP_VALUES[_n] = REG_TAP_VALUES["dxx"]
+for _n in ("dyz", "dxz"):
+    REG_TAP_VALUES[_n] = REG_TAP_VALUES["dxy"]
+
+
+def _torch():
+    import torch
+
+    return torch
+
+
+def point_rows(support, kind: int, pts: np.ndarray, weight: float):
+    """Constraint rows of ``kind`` for the point array (GPU, K1).
+
+    Returns (count, [(idc, a, b, w) per family], nan_flag) with device
+    tensors restricted to the inside points."""
+    torch = _torch()
+    dev = _lib.device()
+    lib = _lib.load()
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    npts, ld = pts.shape
+    fam = {_lib.ROWS_VALUE: 1, _lib.ROWS_NORM: 3, _lib.ROWS_GRADIENT: 2, _lib.ROWS_TANGENT: 1}[kind]
+    d_pts = torch.from_numpy(pts).to(dev)
+    idc = torch.empty((fam * npts, 8), dtype=torch.int64, device=dev)
+    a = torch.empty((fam * npts, 8), dtype=torch.float64, device=dev)
+    b = torch.empty(fam * npts, dtype=torch.float64, device=dev)
+    w = torch.empty(fam * npts, dtype=torch.float64, device=dev)
+    count = C.c_int64(0)
+    nan = C.c_int32(0)
+    g = support.grid3()
+    _lib.check(lib.ls_fd_point_rows(C.byref(g), kind, _lib.ptr(d_pts), npts, ld, float(weight), _lib.ptr(idc),
+                                    _lib.ptr(a), _lib.ptr(b), _lib.ptr(w), C.byref(count), C.byref(nan),
+                                    _lib.stream_ptr()))
+    n = count.value
+    out = [(idc[f * npts:f * npts + n], a[f * npts:f * npts + n], b[f * npts:f * npts + n], w[f * npts:f * npts + n])
+           for f in range(fam)]
+    return n, out, bool(nan.value)
+
+
+def pair_rows(support, pts: np.ndarray, pairs: np.ndarray, weight: float):
+    """Interface pair rows (GPU): 16 columns per row."""
+    torch = _torch()
+    dev = _lib.device()
+    lib = _lib.load()
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    pairs = np.ascontiguousarray(pairs, dtype=np.int64)
+    n = pairs.shape[0]
+    d_pts = torch.from_numpy(pts).to(dev)
+    d_pairs = torch.from_numpy(pairs).to(dev)
+    idc = torch.empty((n, 16), dtype=torch.int64, device=dev)
+    a = torch.empty((n, 16), dtype=torch.float64, device=dev)
+    b = torch.empty(n, dtype=torch.float64, device=dev)
+    w = torch.empty(n, dtype=torch.float64, device=dev)
+    g = support.grid3()
+    _lib.check(lib.ls_fd_pair_rows(C.byref(g), _lib.ptr(d_pts), pts.shape[1], _lib.ptr(d_pairs), n, float(weight),
+                                   _lib.ptr(idc), _lib.ptr(a), _lib.ptr(b), _lib.ptr(w), _lib.stream_ptr()))
+    return idc, a, b, w
+
+
+def reg_shape(support, family: str):
+    lib = _lib.load()
+    rows = C.c_int64(0)
+    taps = C.c_int32(0)
+    g = support.grid3()
+    _lib.check(lib.ls_fd_reg_shape(C.byref(g), _lib.REG_FAMILIES.index(family), C.byref(rows), C.byref(taps)))
+    return rows.value, taps.value
+
+
+def reg_rows(support, family: str):
+    """Explicit column indices of a regularisation family (GPU, K2)."""
+    torch = _torch()
+    dev = _lib.device()
+    lib = _lib.load()
+    rows, taps = reg_shape(support, family)
+    idc = torch.empty((rows, taps), dtype=torch.int64, device=dev)
+    g = support.grid3()
+    _lib.check(lib.ls_fd_reg_rows(C.byref(g), _lib.REG_FAMILIES.index(family), _lib.ptr(idc), _lib.stream_ptr()))
+    return idc
+
+
+class FdSystem:
+    """Owns an ``ls_fd_handle``: the matrix-free normal equations of one
+    interpolator setup."""
+
+    def __init__(self, support, reg_weights: dict, rows, ridge: float):
+        torch = _torch()
+        self.dev = _lib.device()
+        self.lib = _lib.load()
+        self.support = support
+        if rows:
+            width = max(r[0].shape[1] for r in rows)
+            idc, a, b, w = [], [], [], []
+            for ri, ra, rb, rw in rows:
+                k = ri.shape[1]
+                if k < width:
+                    pad_i = torch.full((ri.shape[0], width - k), -1, dtype=torch.int64, device=self.dev)
+                    pad_a = torch.zeros((ri.shape[0], width - k), dtype=torch.float64, device=self.dev)
+                    ri = torch.cat([ri, pad_i], 1)
+                    ra = torch.cat([ra, pad_a], 1)
+                idc.append(ri)
+                a.append(ra)
+                b.append(rb)
+                w.append(rw)
+            self._idc = torch.cat(idc).contiguous()
+            self._a = torch.cat(a).contiguous()
+            self._b = torch.cat(b).contiguous()
+            self._w = torch.cat(w).contiguous()
+            nrows = self._idc.shape[0]
+        else:
+            width, nrows = 8, 0
+            self._idc = self._a = self._b = self._w = None
+        s = _lib.FdSystem()
+        s.grid = support.grid3()
+        for k in ("dxx", "dyy", "dzz", "dxy", "dyz", "dxz", "dx", "dy", "dz"):
+            setattr(s, "w_" + k, float(reg_weights.get(k, 0.0)))
+        s.ridge = float(ridge)
+        s.nrows = nrows
+        s.width = width
+        s.d_idc = _lib.ptr(self._idc)
+        s.d_a = _lib.ptr(self._a)
+        s.d_b = _lib.ptr(self._b)
+        s.d_w = _lib.ptr(self._w)
+        self.nrows = nrows
+        self.handle = C.c_void_p()
+        _lib.check(self.lib.ls_fd_create(C.byref(s), C.byref(self.handle), _lib.stream_ptr()))
+        self.n = int(self.lib.ls_fd_dof(self.handle))
+
+    def close(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            self.lib.ls_fd_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def apply(self, x):
+        torch = _torch()
+        x = x.to(self.dev).contiguous()
+        y = torch.empty_like(x)
+        fn = self.lib.ls_fd_apply if x.dtype == torch.float64 else self.lib.ls_fd_apply_f32
+        _lib.check(fn(self.handle, _lib.ptr(x), _lib.ptr(y), _lib.stream_ptr()))
+        return y
+
+    def rhs(self):
+        torch = _torch()
+        y = torch.empty(self.n, dtype=torch.float64, device=self.dev)
+        _lib.check(self.lib.ls_fd_rhs(self.handle, _lib.ptr(y), _lib.stream_ptr()))
+        return y
+
+    def diagonal(self):
+        torch = _torch()
+        y = torch.empty(self.n, dtype=torch.float64, device=self.dev)
+        _lib.check(self.lib.ls_fd_diagonal(self.handle, _lib.ptr(y), _lib.stream_ptr()))
+        return y
+
+    def solve(self, x=None, atol=0.0, rtol=1e-5, maxiter=None, precision="mixed", reliable_delta=0.1,
+              check_every=64):
+        """Returns (x device tensor, stats dict)."""
+        torch = _torch()
+        o = _lib.SolveOpts()
+        o.precision = _lib.LS_MIXED if precision == "mixed" else _lib.LS_FP64
+        if x is None:
+            x = torch.zeros(self.n, dtype=torch.float64, device=self.dev)
+            o.use_x0 = 0
+        else:
+            x = x.to(device=self.dev, dtype=torch.float64).contiguous().clone()
+            o.use_x0 = 1
+        o.atol = float(atol)
+        o.rtol = float(rtol)
+        o.maxiter = int(maxiter) if maxiter is not None else 0
+        o.reliable_delta = float(reliable_delta)
+        o.check_every = int(check_every)
+        st = _lib.SolveStats()
+        status = self.lib.ls_fd_solve(self.handle, C.byref(o), _lib.ptr(x), C.byref(st), _lib.stream_ptr())
+        _lib.check(status, allow_positive=True)
+        stats = {k: getattr(st, k) for k, _ in _lib.SolveStats._fields_ if k != "reserved"}
+        return x, stats
+
+
+def profile_iteration(system: "FdSystem", precision="mixed", reps=20):
+    """Device time per launch of each kernel class of one CG iteration."""
+    prof = _lib.FdProfile()
+    prec = _lib.LS_MIXED if precision == "mixed" else _lib.LS_FP64
+    _lib.check(system.lib.ls_fd_profile_iteration(system.handle, prec, int(reps), C.byref(prof), _lib.stream_ptr()))
+    return {k: getattr(prof, k) for k, _ in _lib.FdProfile._fields_}
+
+
+def eval_points(support, c, pts: np.ndarray, value=True, gradient=True):
+    torch = _torch()
+    dev = _lib.device()
+    lib = _lib.load()
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    if pts.ndim == 1:
+        pts = pts[None, :]
+    n = pts.shape[0]
+    c_t = c if isinstance(c, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(c, dtype=np.float64))
+    c_t = c_t.to(device=dev, dtype=torch.float64).contiguous()
+    if c_t.shape[0] != support.n_nodes:
+        raise ValueError(f"cannot assign {c_t.shape[0]} vlaues to array of shape {support.n_nodes}")
+    d_pts = torch.from_numpy(pts).to(dev)
+    v = torch.empty(n, dtype=torch.float64, device=dev) if value else None
+    gr = torch.empty((n, 3), dtype=torch.float64, device=dev) if gradient else None
+    g = support.grid3()
+    _lib.check(lib.ls_fd_eval_points(C.byref(g), _lib.ptr(c_t), _lib.ptr(d_pts), n, pts.shape[1], _lib.ptr(v),
+                                     _lib.ptr(gr), _lib.stream_ptr()))
+    return (v.cpu().numpy() if value else None, gr.cpu().numpy() if gradient else None)
+
+
+def eval_lattice(support, c_dev, origin, step, counts, value=True, gradient=True):
+    """Device tensors of value (Q,) and gradient (Q, 3) on a regular lattice."""
+    torch = _torch()
+    dev = _lib.device()
+    lib = _lib.load()
+    q = int(np.prod(counts))
+    v = torch.empty(q, dtype=torch.float64, device=dev) if value else None
+    gr = torch.empty((q, 3), dtype=torch.float64, device=dev) if gradient else None
+    g = support.grid3()
+    o3 = (C.c_double * 3)(*[float(x) for x in origin])
+    s3 = (C.c_double * 3)(*[float(x) for x in step])
+    n3 = (C.c_int64 * 3)(*[int(x) for x in counts])
+    _lib.check(lib.ls_fd_eval_lattice(C.byref(g), _lib.ptr(c_dev), C.byref(o3), C.byref(s3), C.byref(n3), _lib.ptr(v),
+                                      _lib.ptr(gr), _lib.stream_ptr()))
+    return v, gr

@@ -1,0 +1,462 @@
+"""Drop-in interpolators: the reference's discrete-interpolator API
+(setters, setup_interpolator, solve_system, evaluate_value/gradient,
+get_last_solve_timing) backed by the sm_103a kernels.
+
+Reference: packages/loop_interpolation/src/loop_interpolation/
+  _geological_interpolator.py (GI)  setters :303-460, evaluate :723-742, clean :864-885
+  _discrete_interpolator.py   (DI)  add_constraints_to_least_squares :316-389,
+                                    solve_system :1221-1319, evaluate :1342-1379
+  _finite_difference_interpolator.py (FD) setup_interpolator :132-224
+  _solver_strategy.py (SS) solve_with_cg :48-72
+"""
+from __future__ import annotations
+
+import logging
+from time import perf_counter
+
+import numpy as np
+
+from . import _lib, constraints, fd
+
+logger = logging.getLogger(__name__)
+
+RIDGE_FACTOR = 1e-8
+
+
+class ConstraintFamily:
+    """One constraint family as the reference stores it after
+    add_constraints_to_least_squares: normalised rows on the device."""
+
+    def __init__(self, name, idc, a, b, w):
+        self.name, self.idc, self.a, self.b, self.w = name, idc, a, b, w
+
+    @property
+    def n_rows(self):
+        return int(self.idc.shape[0])
+
+    def numpy(self):
+        return {"idc": self.idc.cpu().numpy(), "A": self.a.cpu().numpy(), "B": self.b.cpu().numpy(),
+                "w": self.w.cpu().numpy()}
+
+
+class SetupReport(dict):
+    """Row counts per constraint family (the reference returns a
+    ConstraintDiagnosticsReport with the same information)."""
+
+
+class _DiscreteInterpolatorBase:
+    def __init__(self, support, data=None):
+        self.support = support
+        self.dimensions = 3
+        self.bounding_box = None
+        self.solver = "cg"
+        self.apply_scaling_matrix = True
+        self.add_ridge_regulatisation = True
+        self.ridge_factor = RIDGE_FACTOR
+        self.interpolation_weights = {}
+        self.latest_solve_timing = {}
+        self.constraints: dict[str, ConstraintFamily] = {}
+        self.up_to_date = False
+        self._c = np.zeros(self.support.n_nodes)
+        self._c_dev = None
+        self._system = None
+        self.clean()
+        if data:
+            for k, v in data.items():
+                self.data[k] = np.array(v)
+
+    # -- data (GI:303-460, GI:864-885) -------------------------------------
+    def clean(self):
+        self.data = {
+            "gradient": np.zeros((0, 7)), "value": np.zeros((0, 5)), "normal": np.zeros((0, 7)),
+            "tangent": np.zeros((0, 7)), "interface": np.zeros((0, 5)), "inequality": np.zeros((0, 6)),
+            "inequality_pairs": np.zeros((0, 4)),
+        }
+        self.up_to_date = False
+
+    def _project(self, points, has_vector=False):
+        if self.bounding_box is None or points.shape[0] == 0:
+            return points
+        points = points.copy()
+        points[:, :3] = self.bounding_box.project(points[:, :3])
+        if has_vector:
+            points[:, 3:6] = self.bounding_box.project_vectors(points[:, 3:6])
+        return points
+
+    def set_value_constraints(self, points):
+        try:
+            self.data["value"] = self._project(constraints.value_array(points)).copy()
+        except constraints.ValidationError as e:
+            raise constraints.ValidationError(f"Failed to set value constraints: {e}") from e
+        self.up_to_date = False
+
+    def set_gradient_constraints(self, points):
+        try:
+            self.data["gradient"] = self._project(constraints.gradient_array(points), True).copy()
+        except constraints.ValidationError as e:
+            raise constraints.ValidationError(f"Failed to set gradient constraints: {e}") from e
+        self.up_to_date = False
+
+    def set_normal_constraints(self, points):
+        try:
+            self.data["normal"] = self._project(constraints.gradient_array(points, is_normal=True), True).copy()
+        except constraints.ValidationError as e:
+            raise constraints.ValidationError(f"Failed to set normal constraints: {e}") from e
+        self.up_to_date = False
+
+    def set_tangent_constraints(self, points):
+        try:
+            self.data["tangent"] = self._project(constraints.gradient_array(points, name="Tangent"), True).copy()
+        except constraints.ValidationError as e:
+            raise constraints.ValidationError(f"Failed to set tangent constraints: {e}") from e
+        self.up_to_date = False
+
+    def set_interface_constraints(self, points):
+        try:
+            self.data["interface"] = self._project(constraints.value_array(points, name="Interface constraint")).copy()
+        except constraints.ValidationError as e:
+            raise constraints.ValidationError(f"Failed to set interface constraints: {e}") from e
+        self.up_to_date = False
+
+    def get_value_constraints(self):
+        return self.data["value"]
+
+    def get_gradient_constraints(self):
+        return self.data["gradient"]
+
+    def get_norm_constraints(self):
+        return self.data["normal"]
+
+    def get_tangent_constraints(self):
+        return self.data["tangent"]
+
+    def get_interface_constraints(self):
+        return self.data["interface"]
+
+    def set_interpolation_weights(self, weights):
+        for k, v in weights.items():
+            self.up_to_date = False
+            self.interpolation_weights[k] = v
+
+    @property
+    def dof(self):
+        return int(self.support.n_nodes)
+
+    @property
+    def n_elements(self):
+        return self.support.n_elements
+
+    # -- solution vector ------------------------------------------------------
+    @property
+    def c(self):
+        return self._c
+
+    @c.setter
+    def c(self, value):
+        self._c = np.asarray(value, dtype=float)
+        self._c_dev = None
+
+    def _c_device(self):
+        import torch
+
+        if self._c_dev is None:
+            self._c_dev = torch.from_numpy(np.ascontiguousarray(self._c)).to(_lib.device())
+        return self._c_dev
+
+    def get_last_solve_timing(self) -> dict:
+        return dict(self.latest_solve_timing)
+
+    # -- least squares container (DI:316-389 semantics on device rows) ------
+    def _add_family(self, name, idc, a, b, w):
+        import torch
+
+        if idc.shape[0] == 0:
+            return
+        if bool(torch.isnan(a).any()) or bool(torch.isnan(b).any()):
+            logger.warning("Constraints contain nan not adding constraints: %s", name)
+            return
+        base = name
+        while name in self.constraints:
+            count = 0
+            if "_" in name:
+                count = int(name.split("_")[1]) + 1
+            name = base + f"_{count}"
+        self.constraints[name] = ConstraintFamily(name, idc, a, b, w)
+
+    def reset(self):
+        self.constraints = {}
+        self._release_system()
+
+    def _release_system(self):
+        if self._system is not None:
+            self._system.close()
+            self._system = None
+
+    def update(self) -> bool:
+        if not self.up_to_date:
+            self.setup_interpolator()
+            self.up_to_date = self.solve_system(self.solver)
+        return bool(self.up_to_date)
+
+    # -- solve (DI:1221-1319, SS:48-72) ---------------------------------------
+    def _solver_options(self, solver, tol, solver_kwargs):
+        if callable(solver):
+            raise NotImplementedError("custom solver callables need an explicit matrix; use solver='cg'")
+        if solver not in ("cg", "lsmr", "admm", None):
+            logger.warning("Unknown solver %s using cg. Available solvers are cg, lsmr, admm", solver)
+            solver = "cg"
+        solver = "cg" if solver is None else solver
+        if solver == "admm":
+            raise NotImplementedError("the ADMM inequality solver is not part of the GPU path")
+        kw = dict(solver_kwargs or {})
+        kw.pop("backend", None)
+        if solver == "lsmr":  # same least-squares solution; lsmr's btol maps to the relative tolerance
+            if "btol" in kw:
+                kw["rtol"] = kw.pop("btol")
+            elif tol is not None:
+                kw["rtol"] = tol
+            kw.pop("atol", None)
+            kw.setdefault("atol", 0.0)
+            tol = None
+        elif ("atol" not in kw or "rtol" not in kw) and tol is not None:
+            kw["atol"] = tol
+        opts = {
+            "atol": float(kw.pop("atol", 0.0)),
+            "rtol": float(kw.pop("rtol", 1e-5)),
+            "maxiter": kw.pop("maxiter", None),
+            "precision": kw.pop("precision", "mixed"),
+            "reliable_delta": float(kw.pop("reliable_delta", 0.1)),
+            "check_every": int(kw.pop("check_every", 64)),
+        }
+        x0 = kw.pop("x0", None)
+        if callable(x0):
+            x0 = x0(self.support)
+        opts["x0"] = x0
+        for k in list(kw):
+            logger.info("solver kwarg %s ignored by the GPU CG", k)
+        return solver, opts
+
+    def _build_system(self):
+        raise NotImplementedError
+
+    def solve_system(self, solver=None, tol=None, solver_kwargs=None) -> bool:
+        import torch
+
+        solve_started = perf_counter()
+        self._c = np.full(self.support.n_nodes, np.nan)
+        self._c_dev = None
+        solver, opts = self._solver_options(solver, tol, solver_kwargs)
+        timing = {"solver": solver, "backend": "gb300"}
+        t0 = perf_counter()
+        self._release_system()
+        self._system = self._build_system()
+        torch.cuda.synchronize()
+        timing["assembly_seconds"] = perf_counter() - t0
+        timing["matrix_rows"] = int(self._matrix_rows())
+        timing["matrix_cols"] = int(self.dof)
+        timing["matrix_nnz"] = int(self._matrix_nnz())
+        timing["preprocess_seconds"] = 0.0
+        x0 = opts.pop("x0")
+        if x0 is not None:
+            x0 = torch.as_tensor(np.asarray(x0, dtype=float))
+        t1 = perf_counter()
+        x, stats = self._system.solve(x=x0, **opts)
+        timing["solve_seconds"] = perf_counter() - t1
+        status = stats["status"]
+        if status == _lib.LS_NOT_CONVERGED:
+            logger.warning("CG reached iteration limit (%s) and did not converge; using last iteration",
+                           stats["iterations"])
+        elif status in (_lib.LS_NAN, _lib.LS_BREAKDOWN):
+            logger.warning("CG stopped early (status %d: %s)", status, "nan" if status == _lib.LS_NAN else "breakdown")
+        self._c_dev = x
+        self._c = x.cpu().numpy()
+        timing.update({"iterations": int(stats["iterations"]), "reliable_updates": int(stats["reliable_updates"]),
+                       "residual": stats["residual"], "threshold": stats["threshold"],
+                       "device_ms": stats["device_ms"], "precision": opts["precision"], "status": int(status)})
+        self.up_to_date = True
+        timing["total_seconds"] = perf_counter() - solve_started
+        timing["up_to_date"] = True
+        self.latest_solve_timing = timing
+        return True
+
+    # -- evaluation (GI:723-742, DI:1342-1379) ---------------------------------
+    def evaluate_value(self, locations):
+        loc = np.asarray(locations, dtype=float)
+        if self.bounding_box is not None:
+            loc = self.bounding_box.project(loc)
+        return self._evaluate_value_local(loc)
+
+    def evaluate_gradient(self, locations):
+        loc = np.asarray(locations, dtype=float)
+        if self.bounding_box is not None:
+            loc = self.bounding_box.project(loc)
+        g = self._evaluate_gradient_local(loc)
+        if self.bounding_box is not None:
+            g = self.bounding_box.reproject_vectors(g)
+        return g
+
+
+class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
+    """FD interpolator on a StructuredGrid (FD:91-224)."""
+
+    REG_WEIGHT_KEYS = ("dxy", "dyz", "dxz", "dxx", "dyy", "dzz")
+
+    def __init__(self, grid, data=None):
+        super().__init__(grid, data)
+        self.set_interpolation_weights({  # FD:102-119
+            "dxy": 1.0, "dyz": 1.0, "dxz": 1.0, "dxx": 1.0, "dyy": 1.0, "dzz": 1.0,
+            "dx": 1.0, "dy": 1.0, "dz": 1.0,
+            "cpw": 1.0, "gpw": 1.0, "npw": 10.0, "tpw": 1.0, "ipw": 1.0,
+        })
+        self.interface_pair_mode = "auto"
+        self.interface_pair_threshold = 200
+        self.interface_pair_fallback = "star"
+        self.regularisation_families = {}
+
+    def setup_interpolator(self, **kwargs) -> SetupReport:
+        self.reset()
+        reg = kwargs.get("regularisation", None)
+        if reg is not None:
+            if isinstance(reg, dict):
+                reg = reg.get("isotropic", reg.get("weight", None))
+            if reg is not None:
+                for k in self.REG_WEIGHT_KEYS:
+                    self.interpolation_weights[k] = float(reg)
+        if kwargs.get("directional_regularisation") is not None:
+            raise NotImplementedError("directional regularisation is not part of the GPU path")
+        for k, v in kwargs.items():
+            self.up_to_date = False
+            if k in ("regularisation", "directional_regularisation"):
+                continue
+            self.interpolation_weights[k] = v
+        if kwargs.get("use_regularisation_weight_scale", False):
+            raise NotImplementedError("use_regularisation_weight_scale is not part of the GPU path")
+        self.interface_pair_mode = kwargs.get("interface_pair_mode", self.interface_pair_mode)
+        self.interface_pair_threshold = int(kwargs.get("interface_pair_threshold", self.interface_pair_threshold))
+        self.interface_pair_fallback = kwargs.get("interface_pair_fallback", self.interface_pair_fallback)
+        w = self.interpolation_weights
+        t0 = perf_counter()
+        self._add_point_rows(_lib.ROWS_NORM, self.get_norm_constraints(), w["npw"], ["norm_0", "norm_1", "norm_2"])
+        self._add_point_rows(_lib.ROWS_GRADIENT, self.get_gradient_constraints(), w["gpw"], ["gradient", "gradient"])
+        self._add_point_rows(_lib.ROWS_VALUE, self.get_value_constraints(), w["cpw"], ["value"])
+        self._add_point_rows(_lib.ROWS_TANGENT, self.get_tangent_constraints(), w["tpw"], ["gradient orthogonal"])
+        self._add_interface_rows(w["ipw"])
+        self._add_regularisation_families()
+        self.setup_seconds = perf_counter() - t0
+        self.up_to_date = False
+        report = SetupReport({name: f.n_rows for name, f in self.constraints.items()})
+        for name, (rows, _w) in self.regularisation_families.items():
+            report[name] = rows
+        return report
+
+    def _add_point_rows(self, kind, points, weight, names):
+        if points.shape[0] == 0:
+            return
+        n, fams, _nan = fd.point_rows(self.support, kind, points, weight)
+        if n <= 0:
+            logger.warning("%d constraints not added: outside of model bounding box", points.shape[0])
+            return
+        for name, (idc, a, b, w) in zip(names, fams):
+            self._add_family(name, idc, a, b, w)
+
+    def _interface_pairs(self, n):
+        if n < 2:
+            return np.zeros((0, 2), dtype=int)
+        mode = str(self.interface_pair_mode).lower()
+        threshold = max(2, int(self.interface_pair_threshold))
+        fallback = str(self.interface_pair_fallback).lower()
+        if fallback not in ("star", "chain"):
+            fallback = "star"
+        if mode == "auto":
+            mode = fallback if n > threshold else "all"
+        if mode == "all":
+            ii, jj = np.triu_indices(n, k=1)
+            return np.column_stack([ii, jj]).astype(int)
+        if mode == "star":
+            return np.column_stack([np.zeros(n - 1, dtype=int), np.arange(1, n, dtype=int)])
+        if mode == "chain":
+            return np.column_stack([np.arange(0, n - 1, dtype=int), np.arange(1, n, dtype=int)])
+        raise ValueError(f"Unknown interface_pair_mode '{self.interface_pair_mode}'. Use one of: auto, all, star, chain")
+
+    def _add_interface_rows(self, weight):  # FD:297-340
+        points = self.get_interface_constraints()
+        if points.shape[0] <= 1:
+            return
+        inside = self.support.inside(points[:, :3])
+        pin = points[inside]
+        ids = points[np.logical_and(~np.isnan(points[:, 3]), inside), 3]
+        for uid in np.unique(ids):
+            sel = np.nonzero(pin[:, 3] == uid)[0]
+            pairs = self._interface_pairs(sel.shape[0])
+            if pairs.shape[0] == 0:
+                continue
+            idc, a, b, w = fd.pair_rows(self.support, pin, sel[pairs], weight)
+            self._add_family(f"interface_{uid}", idc, a, b, w)
+
+    def _add_regularisation_families(self):
+        """Matrix-free: record (rows, weight) per family in the reference order
+        (G:489-510 then FD:1052-1144)."""
+        w = self.interpolation_weights
+        self.regularisation_families = {}
+        rw = {"dxy": w["dxy"] / 4, "dyz": w["dyz"] / 4, "dxz": w["dxz"] / 4, "dxx": w["dxx"], "dyy": w["dyy"],
+              "dzz": w["dzz"]}
+        for name, weight in rw.items():
+            rows, _ = fd.reg_shape(self.support, name)
+            if rows > 0:
+                self.regularisation_families[name] = (rows, float(weight))
+        for name, key in (("dx_lower", "dx"), ("dx_upper", "dx"), ("dy_lower", "dy"), ("dy_upper", "dy"),
+                          ("dz_lower", "dz"), ("dz_upper", "dz")):
+            rows, _ = fd.reg_shape(self.support, name)
+            if w[key] != 0 and rows > 0:
+                self.regularisation_families[name] = (rows, float(w[key]))
+
+    def regularisation_rows(self, name):
+        """Explicit (idc, A, B, w) of a matrix-free family, as the reference's
+        explicit path would store it (parity inspection)."""
+        rows, weight = self.regularisation_families[name]
+        idc = fd.reg_rows(self.support, name).cpu().numpy()
+        vals = fd.REG_TAP_VALUES[name]
+        return {"idc": idc, "A": np.tile(vals, (rows, 1)), "B": np.zeros(rows), "w": np.full(rows, weight)}
+
+    def _reg_weights(self):
+        fam = self.regularisation_families
+        out = {}
+        for k in ("dxx", "dyy", "dzz", "dxy", "dyz", "dxz"):
+            out[k] = fam[k][1] if k in fam else 0.0
+        for k in ("dx", "dy", "dz"):
+            out[k] = fam[k + "_lower"][1] if (k + "_lower") in fam else 0.0
+        return out
+
+    def _build_system(self):
+        rows = [(f.idc, f.a, f.b, f.w) for f in self.constraints.values()]
+        ridge = self.ridge_factor if self.add_ridge_regulatisation else 0.0
+        return fd.FdSystem(self.support, self._reg_weights(), rows, ridge)
+
+    def _matrix_rows(self):
+        return sum(f.n_rows for f in self.constraints.values()) + sum(r for r, _ in self.regularisation_families.values())
+
+    def _matrix_nnz(self):
+        nnz = sum(f.n_rows * f.idc.shape[1] for f in self.constraints.values())
+        for name, (r, _) in self.regularisation_families.items():
+            nnz += r * (4 if name in ("dxy", "dyz", "dxz") else 3)
+        return nnz
+
+    def _evaluate_value_local(self, locations):
+        self.update()
+        loc = np.asarray(locations, dtype=float)
+        if loc.shape[0] == 0:
+            return np.zeros(0)
+        return fd.eval_points(self.support, self._c_device(), loc, value=True, gradient=False)[0]
+
+    def _evaluate_gradient_local(self, locations):
+        self.update()
+        loc = np.asarray(locations, dtype=float)
+        if loc.shape[0] == 0:
+            return np.zeros((0, 3))
+        return fd.eval_points(self.support, self._c_device(), loc, value=False, gradient=True)[1]
+
+    def evaluate_lattice(self, origin, step, counts, value=True, gradient=True):
+        """Dense-lattice evaluation on the device (K7 lattice kernel); returns
+        device tensors (value (Q,), gradient (Q, 3)), i fastest."""
+        self.update()
+        return fd.eval_lattice(self.support, self._c_device(), origin, step, counts, value, gradient)
