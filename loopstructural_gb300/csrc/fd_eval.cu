@@ -97,8 +97,8 @@ __device__ __forceinline__ void eval_one(const EvalGrid &g, const double *__rest
     T[3] = y * (1 - z);
     T[7] = y * z;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) T[k] = (T[k] / g.step[0]) * cv[k];
-    grad[0] = sum8(T);
+    for (int k = 0; k < 8; ++k) T[k] = T[k] * cv[k];
+    grad[0] = sum8(T) / g.step[0];
     T[0] = (x - 1) * (1 - z);
     T[1] = -x * (1 - z);
     T[2] = (1 - x) * (1 - z);
@@ -108,8 +108,8 @@ __device__ __forceinline__ void eval_one(const EvalGrid &g, const double *__rest
     T[3] = x * (1 - z);
     T[7] = x * z;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) T[k] = (T[k] / g.step[1]) * cv[k];
-    grad[1] = sum8(T);
+    for (int k = 0; k < 8; ++k) T[k] = T[k] * cv[k];
+    grad[1] = sum8(T) / g.step[1];
     T[0] = -(1 - x) * (1 - y);
     T[1] = -x * (1 - y);
     T[2] = -(1 - x) * y;
@@ -119,8 +119,8 @@ __device__ __forceinline__ void eval_one(const EvalGrid &g, const double *__rest
     T[3] = -x * y;
     T[7] = x * y;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) T[k] = (T[k] / g.step[2]) * cv[k];
-    grad[2] = sum8(T);
+    for (int k = 0; k < 8; ++k) T[k] = T[k] * cv[k];
+    grad[2] = sum8(T) / g.step[2];
   }
 }
 
@@ -139,21 +139,102 @@ __global__ void eval_points_kernel(EvalGrid g, const double *__restrict__ c, con
   }
 }
 
-__global__ void eval_lattice_kernel(EvalGrid g, const double *__restrict__ c, double ox, double oy, double oz,
-                                    double hx, double hy, double hz, int64_t n0, int64_t n1, int64_t n2,
-                                    double *__restrict__ value, double *__restrict__ grad) {
-  const int64_t total = n0 * n1 * n2;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t a = i % n0, b = (i / n0) % n1, k = i / (n0 * n1);
-    const double px = ox + hx * (double)a, py = oy + hy * (double)b, pz = oz + hz * (double)k;
-    double v, gr[3];
-    eval_one(g, c, px, py, pz, value ? &v : nullptr, grad ? gr : nullptr);
-    if (value) value[i] = v;
-    if (grad) {
-      grad[3 * i] = gr[0];
-      grad[3 * i + 1] = gr[1];
-      grad[3 * i + 2] = gr[2];
-    }
+// per-axis part of the point location: inside flag, cell index, local coordinate
+struct AxisLoc {
+  double l;
+  int64_t cell;
+  bool inside;
+};
+
+__device__ __forceinline__ AxisLoc locate_axis(const EvalGrid &g, int d, double p) {
+  AxisLoc a;
+  a.inside = (p >= g.lo[d]) & (p <= g.hi[d]);
+  int64_t k = (int64_t)floor((p - g.origin[d]) / g.step[d]);
+  if (k < 0) k = 0;
+  if (k > g.cells[d] - 1) k = g.cells[d] - 1;
+  a.cell = k;
+  const double co = g.origin[d] + g.step[d] * (double)k;
+  a.l = fmin(fmax((p - co) / g.step[d], 0.0), 1.0);
+  return a;
+}
+
+// Lattice evaluation: block (256) covers a run of lattice x-indices of one
+// (j, k) lattice row, so the y / z location is computed once per block.
+__global__ void __launch_bounds__(256) eval_lattice_kernel(EvalGrid g, const double *__restrict__ c, double ox,
+                                                           double oy, double oz, double hx, double hy, double hz,
+                                                           int64_t n0, int64_t n1, int64_t n2,
+                                                           double *__restrict__ value, double *__restrict__ grad) {
+  __shared__ AxisLoc ly, lz;
+  const int64_t b = blockIdx.y, kk = blockIdx.z;
+  if (threadIdx.x == 0) {
+    ly = locate_axis(g, 1, oy + hy * (double)b);
+    lz = locate_axis(g, 2, oz + hz * (double)kk);
+  }
+  __syncthreads();
+  const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (a >= n0) return;
+  const AxisLoc lx = locate_axis(g, 0, ox + hx * (double)a);
+  const int64_t i = a + n0 * (b + n1 * kk);
+  if (!(lx.inside & ly.inside & lz.inside)) {
+    if (value) value[i] = __longlong_as_double(0x7ff8000000000000LL);
+    if (grad) grad[3 * i] = grad[3 * i + 1] = grad[3 * i + 2] = 0.0;
+    return;
+  }
+  const int64_t nx = g.n[0], nxy = g.n[0] * g.n[1];
+  const int64_t g0 = lx.cell + nx * ly.cell + nxy * lz.cell;
+  double cv[8];
+  cv[0] = __ldg(c + g0);
+  cv[1] = __ldg(c + g0 + 1);
+  cv[2] = __ldg(c + g0 + nx);
+  cv[3] = __ldg(c + g0 + nx + 1);
+  cv[4] = __ldg(c + g0 + nxy);
+  cv[5] = __ldg(c + g0 + nxy + 1);
+  cv[6] = __ldg(c + g0 + nxy + nx);
+  cv[7] = __ldg(c + g0 + nxy + nx + 1);
+  const double x = lx.l, y = ly.l, z = lz.l;
+  if (value) {
+    double w[8];
+    w[0] = (1 - x) * (1 - y) * (1 - z);
+    w[1] = x * (1 - y) * (1 - z);
+    w[2] = (1 - x) * y * (1 - z);
+    w[4] = (1 - x) * (1 - y) * z;
+    w[5] = x * (1 - y) * z;
+    w[6] = (1 - x) * y * z;
+    w[3] = x * y * (1 - z);
+    w[7] = x * y * z;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) w[k] = w[k] * cv[k];
+    value[i] = sum8(w);
+  }
+  if (grad) {
+    double T[8];
+    T[0] = (1 - z) * (y - 1) * cv[0];
+    T[1] = (1 - y) * (1 - z) * cv[1];
+    T[2] = -y * (1 - z) * cv[2];
+    T[4] = -(1 - y) * z * cv[4];
+    T[5] = (1 - y) * z * cv[5];
+    T[6] = -y * z * cv[6];
+    T[3] = y * (1 - z) * cv[3];
+    T[7] = y * z * cv[7];
+    grad[3 * i] = sum8(T) / g.step[0];
+    T[0] = (x - 1) * (1 - z) * cv[0];
+    T[1] = -x * (1 - z) * cv[1];
+    T[2] = (1 - x) * (1 - z) * cv[2];
+    T[4] = -(1 - x) * z * cv[4];
+    T[5] = -x * z * cv[5];
+    T[6] = (1 - x) * z * cv[6];
+    T[3] = x * (1 - z) * cv[3];
+    T[7] = x * z * cv[7];
+    grad[3 * i + 1] = sum8(T) / g.step[1];
+    T[0] = -(1 - x) * (1 - y) * cv[0];
+    T[1] = -x * (1 - y) * cv[1];
+    T[2] = -(1 - x) * y * cv[2];
+    T[4] = (1 - x) * (1 - y) * cv[4];
+    T[5] = x * (1 - y) * cv[5];
+    T[6] = (1 - x) * y * cv[6];
+    T[3] = -x * y * cv[3];
+    T[7] = x * y * cv[7];
+    grad[3 * i + 2] = sum8(T) / g.step[2];
   }
 }
 
@@ -184,7 +265,9 @@ extern "C" int ls_fd_eval_lattice(const ls_grid3 *grid, const double *d_c, const
   if (total == 0 || (!d_value && !d_grad)) return LS_OK;
   EvalGrid g = make_eval_grid(*grid);
   cudaStream_t s = as_stream(stream);
-  eval_lattice_kernel<<<stream_grid(total, 256), 256, 0, s>>>(g, d_c, lat_origin[0], lat_origin[1], lat_origin[2],
+  LS_ARG_CHECK(lat_n[1] <= 65535 && lat_n[2] <= 65535, "lattice y / z extent above 65535");
+  const dim3 lgrid((unsigned)((lat_n[0] + 255) / 256), (unsigned)lat_n[1], (unsigned)lat_n[2]);
+  eval_lattice_kernel<<<lgrid, 256, 0, s>>>(g, d_c, lat_origin[0], lat_origin[1], lat_origin[2],
                                                               lat_step[0], lat_step[1], lat_step[2], lat_n[0],
                                                               lat_n[1], lat_n[2], d_value, d_grad);
   LS_CUDA_TRY(cudaGetLastError());

@@ -39,8 +39,8 @@ struct CgScalars {
   double scratch;
   long long iters;
   long long maxiter;
-  int done;        // 0 running, 1 converged, LS_NOT_CONVERGED, LS_NAN, LS_BREAKDOWN
-  int pad;
+  int done;        // DONE_* stop code
+  int profile;     // timing mode: never stop, never flag a breakdown
 };
 
 struct DataTerm {
@@ -90,28 +90,49 @@ struct ls_fd_handle {
 namespace ls {
 namespace {
 
+// device-side stop codes (CgScalars::done); mapped to ls_status on the host
+enum : int { DONE_RUNNING = 0, DONE_CONVERGED = 1, DONE_MAXITER = 2, DONE_NAN = 3, DONE_BREAKDOWN = 4 };
+
+int done_to_status(int d) {
+  switch (d) {
+    case DONE_CONVERGED: return LS_OK;
+    case DONE_MAXITER: return LS_NOT_CONVERGED;
+    case DONE_NAN: return LS_NAN;
+    case DONE_BREAKDOWN: return LS_BREAKDOWN;
+    default: return LS_OK;
+  }
+}
+
 enum Ticket { T_STENCIL = 0, T_DATA = 1, T_UPDATE = 2, T_REFRESH = 3, T_MISC = 4, T_COUNT = 5 };
 
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
 
-// q = (stencil part of N) p  and  p . q  (grid-reduced into sc->pq_s)
+// q = (stencil part of N) p  and  p . q  (grid-reduced into sc->pq_s).
+// 3-D launch: block (32, 8) covers an x-y tile, blockIdx.z strides over z.
+constexpr int kTX = 32, kTY = 8;
 template <typename T>
-__global__ void __launch_bounds__(kBlock) stencil_kernel(StencilCoef c, const T *__restrict__ p, T *__restrict__ q,
-                                                         CgScalars *sc, double *partials, unsigned int *ticket,
-                                                         bool check_done) {
+__global__ void __launch_bounds__(kTX * kTY) stencil_kernel(CoefT<T> c, const T *__restrict__ p, T *__restrict__ q,
+                                                             CgScalars *sc, double *partials, unsigned int *ticket,
+                                                             bool check_done) {
   if (check_done && sc->done) return;
-  double local = 0.0;
-  const int64_t n = c.nx * c.ny * c.nz;
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = g % c.nx, j = (g / c.nx) % c.ny, k = g / (c.nx * c.ny);
-    T v = stencil_apply_node<T>(c, p, g, i, j, k);
-    q[g] = v;
-    local += (double)p[g] * (double)v;
+  const int nx = c.nx, ny = c.ny, nz = c.nz;
+  const int i = blockIdx.x * kTX + threadIdx.x, j = blockIdx.y * kTY + threadIdx.y;
+  T local = 0;  // per-thread partial in the kernel's precision; FP64 from the block sum on
+  if (i < nx && j < ny) {
+    for (int k = blockIdx.z; k < nz; k += gridDim.z) {
+      const int g = i + nx * (j + ny * k);
+      const T v = stencil_node32<T>(c, p, g, i, j, k);
+      q[g] = v;
+      local += __ldg(p + g) * v;
+    }
   }
   double tot;
-  if (grid_sum<kBlock>(local, partials, ticket, &tot)) sc->pq_s = tot;
+  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+  if (grid_sum_ex<kTX * kTY>((double)local, partials, ticket, &tot, threadIdx.x + kTX * threadIdx.y, bid,
+                             gridDim.x * gridDim.y * gridDim.z))
+    sc->pq_s = tot;
 }
 
 // s_r = w_r^2 (a_r . p) ; p . N_d p = sum_r w_r^2 (a_r . p)^2 into sc->pq_d
@@ -121,7 +142,7 @@ __global__ void __launch_bounds__(kBlock) data_rows_kernel(int64_t nrows, int wi
                                                            const T *__restrict__ p, T *__restrict__ s, CgScalars *sc,
                                                            double *partials, unsigned int *ticket, bool check_done) {
   if (check_done && sc->done) return;
-  double local = 0.0;
+  T local = 0;
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
     T acc = 0;
     for (int k = 0; k < width; ++k) {
@@ -130,10 +151,10 @@ __global__ void __launch_bounds__(kBlock) data_rows_kernel(int64_t nrows, int wi
     }
     const T sr = w2[r] * acc;
     s[r] = sr;
-    local += (double)sr * (double)acc;
+    local += sr * acc;
   }
   double tot;
-  if (grid_sum<kBlock>(local, partials, ticket, &tot)) sc->pq_d = tot;
+  if (grid_sum<kBlock>((double)local, partials, ticket, &tot)) sc->pq_d = tot;
 }
 
 // q[n] += sum over the rows touching node n of a_rk s_r
@@ -163,26 +184,29 @@ __global__ void __launch_bounds__(kBlock) update_xr_kernel(int64_t n, T *__restr
   const double pq = sc->pq_s + sc->pq_d;
   const double rz = sc->rz;
   const double alpha_d = rz / pq;
-  if (!(pq > 0.0) || !isfinite(alpha_d)) {
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = isfinite(pq) ? LS_BREAKDOWN : LS_NAN;
+  if (!sc->profile && (!(pq > 0.0) || !isfinite(alpha_d))) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = isfinite(pq) ? DONE_BREAKDOWN : DONE_NAN;
     return;
   }
   const T alpha = (T)alpha_d;
-  double local = 0.0;
+  T local = 0;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
     x[g] += alpha * p[g];
     const T rn = r[g] - alpha * q[g];
     r[g] = rn;
-    local += (double)rn * (double)(dinv[g] * rn);
+    local += rn * (dinv[g] * rn);
   }
   double rz_new;
-  if (grid_sum<kBlock>(local, partials, ticket, &rz_new)) {
+  if (grid_sum<kBlock>((double)local, partials, ticket, &rz_new)) {
     sc->iters += 1;
     sc->beta = rz_new / rz;
     sc->rz = rz_new;
-    if (!isfinite(rz_new)) sc->done = LS_NAN;
-    else if (rz_new < sc->thresh2) sc->done = 1;
-    else if (sc->iters >= sc->maxiter) sc->done = LS_NOT_CONVERGED;
+    if (sc->profile) {
+      sc->rz = 1.0;  // keep alpha and beta finite while timing
+      sc->beta = 0.5;
+    } else if (!isfinite(rz_new)) sc->done = DONE_NAN;
+    else if (rz_new < sc->thresh2) sc->done = DONE_CONVERGED;
+    else if (sc->iters >= sc->maxiter) sc->done = DONE_MAXITER;
   }
 }
 
@@ -313,13 +337,20 @@ int grid_for(const ls_fd_handle *h, int64_t n) {
   return std::min(g, h->red_blocks);
 }
 
+dim3 stencil_grid(const ls_fd_handle *h) {
+  const int gx = (int)((h->coef.nx + kTX - 1) / kTX), gy = (int)((h->coef.ny + kTY - 1) / kTY);
+  int gz = std::max(1, h->red_blocks / std::max(1, gx * gy));
+  gz = std::min<int>(gz, (int)h->coef.nz);
+  return dim3(gx, gy, gz);
+}
+
 // N p for the precision T, leaving q; p.q in sc->pq_s + sc->pq_d
 template <typename T>
 void launch_apply(ls_fd_handle *h, const T *p, T *q, T *s, const T *a, const T *w2, const T *ia, bool check_done,
                   cudaStream_t st) {
   const DataTerm &d = h->data;
-  stencil_kernel<T><<<grid_for(h, h->n), kBlock, 0, st>>>(h->coef, p, q, h->sc, h->partials, h->tickets + T_STENCIL,
-                                                        check_done);
+  stencil_kernel<T><<<stencil_grid(h), dim3(kTX, kTY), 0, st>>>(coef_as<T>(h->coef), p, q, h->sc, h->partials,
+                                                                 h->tickets + T_STENCIL, check_done);
   if (d.nrows > 0) {
     data_rows_kernel<T><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, a, w2, p, s, h->sc,
                                                                h->partials + 2 * h->red_blocks,
@@ -421,7 +452,11 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
     return fail(LS_ERR_CUDA);
   }
   h->red_blocks = sm_count() * 8;
-  if ((st = dev_alloc(&h->partials, 4 * (size_t)h->red_blocks)) < 0) return fail(st);
+  {
+    const size_t gxy = (size_t)((g.nsteps[0] + 31) / 32) * (size_t)((g.nsteps[1] + 7) / 8);
+    const size_t nb = std::max<size_t>((size_t)h->red_blocks, gxy);
+    if ((st = dev_alloc(&h->partials, 4 * nb)) < 0) return fail(st);
+  }
   if ((st = dev_alloc(&h->tickets, T_COUNT)) < 0) return fail(st);
   if ((st = dev_alloc(&h->sc, 1)) < 0) return fail(st);
   if (cudaMallocHost((void **)&h->sc_h, sizeof(CgScalars)) != cudaSuccess) {
@@ -628,7 +663,7 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
     s.thresh2 = thresh * thresh;
     s.iters = 0;
     s.maxiter = maxiter;
-    s.done = (s.rz < s.thresh2) ? 1 : 0;
+    s.done = (s.rz < s.thresh2) ? DONE_CONVERGED : DONE_RUNNING;
     LS_TRY(write_scalars(h));
     if (!h->g64 || h->g64_batch != batch) {
       if (h->g64) cudaGraphExecDestroy(h->g64);
@@ -641,7 +676,7 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
       LS_TRY(read_scalars(h));
     }
     iters = s.iters;
-    status = s.done == 1 ? LS_OK : s.done;
+    status = done_to_status(s.done);
   } else {
     // FP32 CG on the correction, FP64 residual refreshed whenever the
     // recurrence residual fell by `delta` (reliable updates).
@@ -668,8 +703,8 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
         LS_TRY(read_scalars(h));
         const bool trigger = s.done != 0 || s.rz < delta * delta * rz_ref;
         if (!trigger) continue;
-        if (s.done == LS_NAN || s.done == LS_BREAKDOWN) {
-          status = s.done;
+        if (s.done == DONE_NAN || s.done == DONE_BREAKDOWN) {
+          status = done_to_status(s.done);
           break;
         }
         // reliable update
@@ -730,6 +765,7 @@ extern "C" int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps,
   sc.pq_s = 1.0;
   sc.thresh2 = -1.0;
   sc.maxiter = (long long)1 << 60;
+  sc.profile = 1;
   LS_TRY(write_scalars(h));
   // p = r = 1: p.Np > 0, so every launch does its full work
   const int gf = grid_for(h, n);
@@ -756,8 +792,8 @@ extern "C" int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps,
   const int g = grid_for(h, n);
   const DataTerm &d = h->data;
   LS_TRY(timed([&] {
-    if (f32) stencil_kernel<float><<<g, kBlock, 0, st>>>(h->coef, h->p32, h->q32, h->sc, h->partials, h->tickets + T_STENCIL, false);
-    else stencil_kernel<double><<<g, kBlock, 0, st>>>(h->coef, h->p64, h->q64, h->sc, h->partials, h->tickets + T_STENCIL, false);
+    if (f32) stencil_kernel<float><<<stencil_grid(h), dim3(kTX, kTY), 0, st>>>(coef_as<float>(h->coef), h->p32, h->q32, h->sc, h->partials, h->tickets + T_STENCIL, false);
+    else stencil_kernel<double><<<stencil_grid(h), dim3(kTX, kTY), 0, st>>>(coef_as<double>(h->coef), h->p64, h->q64, h->sc, h->partials, h->tickets + T_STENCIL, false);
   }, &out->stencil_ms));
   out->data_ms = 0.0;
   if (d.nrows > 0) {
@@ -784,6 +820,8 @@ extern "C" int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps,
     if (f32) launch_iteration<float>(h, h->x32, h->r32, h->p32, h->q32, h->dinv32, st);
     else launch_iteration<double>(h, h->x64, h->r64, h->p64, h->q64, h->dinv64, st);
   }, &out->iteration_ms));
+  sc = CgScalars{};
+  LS_TRY(write_scalars(h));
   out->stencil_bytes = 2.0 * (double)n * (double)s;
   out->iteration_bytes = 9.0 * (double)n * (double)s + 16.0 * (double)(d.nrows * d.width);
   LS_CUDA_TRY(cudaGetLastError());

@@ -126,6 +126,124 @@ __device__ __forceinline__ T stencil_apply_node(const StencilCoef &c, const T *_
   return acc;
 }
 
+// Coefficients in the arithmetic type of the kernel (FP32 kernels must not
+// touch the FP64 pipe: GB300's FP64 rate is a small fraction of FP32).
+template <typename T>
+struct CoefT {
+  int nx, ny, nz;
+  T xx_int, yy_int, zz_int, xx_bdr, yy_bdr, zz_bdr, xy, xz, yz, ridge2;
+};
+
+template <typename T>
+inline CoefT<T> coef_as(const StencilCoef &c) {
+  CoefT<T> o;
+  o.nx = (int)c.nx;
+  o.ny = (int)c.ny;
+  o.nz = (int)c.nz;
+  o.xx_int = (T)c.xx_int;
+  o.yy_int = (T)c.yy_int;
+  o.zz_int = (T)c.zz_int;
+  o.xx_bdr = (T)c.xx_bdr;
+  o.yy_bdr = (T)c.yy_bdr;
+  o.zz_bdr = (T)c.zz_bdr;
+  o.xy = (T)c.xy;
+  o.xz = (T)c.xz;
+  o.yz = (T)c.yz;
+  o.ridge2 = (T)c.ridge2;
+  return o;
+}
+
+template <typename T>
+__device__ __forceinline__ T alpha_axis32(const CoefT<T> &c, int axis, int i, int j, int k) {
+  if (i < 0 || i >= c.nx || j < 0 || j >= c.ny || k < 0 || k >= c.nz) return (T)0;
+  const bool inter = (i >= 1) & (i <= c.nx - 2) & (j >= 1) & (j <= c.ny - 2) & (k >= 1) & (k <= c.nz - 2);
+  if (axis == 0) return (inter ? c.xx_int : (T)0) + c.xx_bdr * (T)((i == 1) + (i == c.nx - 2));
+  if (axis == 1) return (inter ? c.yy_int : (T)0) + c.yy_bdr * (T)((j == 1) + (j == c.ny - 2));
+  return (inter ? c.zz_int : (T)0) + c.zz_bdr * (T)((k == 1) + (k == c.nz - 2));
+}
+
+// Exact two-pass evaluation at any node (boundary shell).
+template <typename T>
+__device__ __forceinline__ T stencil_node_general(const CoefT<T> &c, const T *__restrict__ p, int g, int i, int j,
+                                                  int k) {
+  const int sy = c.nx, sz = c.nx * c.ny;
+  T acc = c.ridge2 * __ldg(p + g);
+  const int strides[3] = {1, sy, sz};
+#pragma unroll
+  for (int axis = 0; axis < 3; ++axis) {
+    const int st = strides[axis];
+#pragma unroll
+    for (int o = -1; o <= 1; ++o) {
+      const int ci = i - (axis == 0 ? o : 0), cj = j - (axis == 1 ? o : 0), ck = k - (axis == 2 ? o : 0);
+      const T al = alpha_axis32<T>(c, axis, ci, cj, ck);
+      if (al != (T)0) {
+        const int gc = g - o * st;
+        const T s = __ldg(p + gc - st) - (T)2 * __ldg(p + gc) + __ldg(p + gc + st);
+        acc += ((o == 0) ? (T)-2 : (T)1) * al * s;
+      }
+    }
+  }
+#pragma unroll
+  for (int plane = 0; plane < 3; ++plane) {
+    const T w = plane == 0 ? c.xy : (plane == 1 ? c.xz : c.yz);
+    if (w == (T)0) continue;
+    const int s1 = plane == 2 ? sy : 1;
+    const int s2 = plane == 0 ? sy : sz;
+#pragma unroll
+    for (int a = -1; a <= 1; a += 2) {
+#pragma unroll
+      for (int b = -1; b <= 1; b += 2) {
+        int ci = i, cj = j, ck = k;
+        if (plane == 0) { ci -= a; cj -= b; }
+        else if (plane == 1) { ci -= a; ck -= b; }
+        else { cj -= a; ck -= b; }
+        if (!((ci >= 1) & (ci <= c.nx - 2) & (cj >= 1) & (cj <= c.ny - 2) & (ck >= 1) & (ck <= c.nz - 2))) continue;
+        const int gc = g - a * s1 - b * s2;
+        const T e = -__ldg(p + gc - s1 - s2) + __ldg(p + gc + s1 - s2) + __ldg(p + gc - s1 + s2) - __ldg(p + gc + s1 + s2);
+        acc += ((a == b) ? (T)-1 : (T)1) * w * e;
+      }
+    }
+  }
+  return acc;
+}
+
+// Deep interior (every index in [3, n-4]): all contributing rows carry the
+// interior weights, and the two-pass sum collapses to the composite stencil
+//   ridge^2 p + sum_a (w_a^2/6) d4_a p + sum_{a<b} (w_ab^2/4) C_a C_b p,
+// d4 = (1,-4,6,-4,1) and C = (1,0,-2,0,1) (stride-2 second difference).
+template <typename T>
+__device__ __forceinline__ T stencil_node_deep(const CoefT<T> &c, const T *__restrict__ p, int g) {
+  const int sy = c.nx, sz = c.nx * c.ny;
+  const T p0 = __ldg(p + g);
+  auto d4 = [&](int s) {
+    return (__ldg(p + g - 2 * s) + __ldg(p + g + 2 * s)) - (T)4 * (__ldg(p + g - s) + __ldg(p + g + s)) + (T)6 * p0;
+  };
+  auto cc = [&](int s1, int s2) {
+    const T corners = (__ldg(p + g - 2 * s1 - 2 * s2) + __ldg(p + g + 2 * s1 - 2 * s2)) +
+                      (__ldg(p + g - 2 * s1 + 2 * s2) + __ldg(p + g + 2 * s1 + 2 * s2));
+    const T edges = (__ldg(p + g - 2 * s1) + __ldg(p + g + 2 * s1)) + (__ldg(p + g - 2 * s2) + __ldg(p + g + 2 * s2));
+    return corners - (T)2 * edges + (T)4 * p0;
+  };
+  T acc = c.ridge2 * p0;
+  acc += c.xx_int * d4(1);
+  acc += c.yy_int * d4(sy);
+  acc += c.zz_int * d4(sz);
+  acc += c.xy * cc(1, sy);
+  acc += c.xz * cc(1, sz);
+  acc += c.yz * cc(sy, sz);
+  return acc;
+}
+
+template <typename T>
+__device__ __forceinline__ bool is_deep(const CoefT<T> &c, int i, int j, int k) {
+  return (i >= 3) & (i <= c.nx - 4) & (j >= 3) & (j <= c.ny - 4) & (k >= 3) & (k <= c.nz - 4);
+}
+
+template <typename T>
+__device__ __forceinline__ T stencil_node32(const CoefT<T> &c, const T *__restrict__ p, int g, int i, int j, int k) {
+  return is_deep(c, i, j, k) ? stencil_node_deep<T>(c, p, g) : stencil_node_general<T>(c, p, g, i, j, k);
+}
+
 // diagonal of the stencil part + ridge^2
 __host__ __device__ __forceinline__ double stencil_diag_node(const StencilCoef &c, int64_t i, int64_t j, int64_t k) {
   double d = c.ridge2;

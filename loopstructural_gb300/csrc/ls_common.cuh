@@ -56,11 +56,16 @@ inline int stream_grid(int64_t n, int block, int per_sm = 8) {
 // index order and hands the total to `finish` -- no float atomics, so the
 // result is bit-reproducible run to run.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ int linear_tid() {
+  return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+}
+
 template <int BLOCK>
 __device__ __forceinline__ double block_sum(double v, double *smem) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int t = linear_tid();
+  const int lane = t & 31, warp = t >> 5;
   if (lane == 0) smem[warp] = v;
   __syncthreads();
   v = 0.0;
@@ -74,29 +79,37 @@ __device__ __forceinline__ double block_sum(double v, double *smem) {
 }
 
 // Returns true in thread 0 of the last block; *total then holds the sum.
+// `tid` is the thread's linear index in its block, `bid` / `nblocks` the
+// block's linear index and the grid size (3-D grids pass their own).
 template <int BLOCK>
-__device__ __forceinline__ bool grid_sum(double v, double *partials, unsigned int *ticket, double *total) {
+__device__ __forceinline__ bool grid_sum_ex(double v, double *partials, unsigned int *ticket, double *total,
+                                            int tid, unsigned int bid, unsigned int nblocks) {
   __shared__ double red[BLOCK / 32];
   __shared__ bool last;
   double b = block_sum<BLOCK>(v, red);
-  if (threadIdx.x == 0) {
-    partials[blockIdx.x] = b;
+  if (tid == 0) {
+    partials[bid] = b;
     __threadfence();
     unsigned int t = atomicAdd(ticket, 1u);
-    last = (t == gridDim.x - 1);
+    last = (t == nblocks - 1);
   }
   __syncthreads();
   if (!last) return false;
   __threadfence();
   // last block: fixed-order sum of the partials
   double s = 0.0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += BLOCK) s += ((volatile double *)partials)[i];
+  for (int i = tid; i < (int)nblocks; i += BLOCK) s += ((volatile double *)partials)[i];
   s = block_sum<BLOCK>(s, red);
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     *total = s;
     *ticket = 0u;  // re-arm for the next launch
   }
-  return threadIdx.x == 0;
+  return tid == 0;
+}
+
+template <int BLOCK>
+__device__ __forceinline__ bool grid_sum(double v, double *partials, unsigned int *ticket, double *total) {
+  return grid_sum_ex<BLOCK>(v, partials, ticket, total, threadIdx.x, blockIdx.x, gridDim.x);
 }
 
 // Two sums in one pass.

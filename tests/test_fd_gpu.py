@@ -216,9 +216,10 @@ def test_edge_cases():
     assert "value" not in rep
     # maxiter=1: the last iterate is returned (reference warns, still True)
     interp = L.FiniteDifferenceInterpolator(grid)
-    interp.set_value_constraints(np.array([[0.5, 0.5, 0.5, 1.0], [0.1, 0.2, 0.9, 0.0]]))
+    pts = np.random.default_rng(5).uniform(0, 1, size=(20, 3))
+    interp.set_value_constraints(np.column_stack([pts, pts[:, 2]]))
     interp.setup_interpolator(regularisation=0.1)
-    assert interp.solve_system("cg", solver_kwargs={"maxiter": 1, "precision": "fp64"})
+    assert interp.solve_system("cg", solver_kwargs={"maxiter": 1, "rtol": 1e-14, "precision": "fp64"})
     t = interp.get_last_solve_timing()
     assert t["iterations"] == 1 and t["status"] == _lib.LS_NOT_CONVERGED
     # a single-cell-thick grid has no interior rows
