@@ -18,6 +18,7 @@ LS_NAN = 2
 LS_BREAKDOWN = 3
 LS_FP64 = 0
 LS_MIXED = 1
+NOALLOC_MAX_ROWS = 1048576
 
 ROWS_VALUE, ROWS_NORM, ROWS_GRADIENT, ROWS_TANGENT = 0, 1, 2, 3
 REG_FAMILIES = (
@@ -29,7 +30,7 @@ REG_FAMILIES = (
 EXPORTS = (
     "ls_last_error", "ls_abi_version",
     "ls_fd_point_rows", "ls_fd_pair_rows", "ls_fd_reg_shape", "ls_fd_reg_rows",
-    "ls_fd_create", "ls_fd_destroy", "ls_fd_dof", "ls_fd_apply", "ls_fd_apply_f32", "ls_fd_rhs",
+    "ls_fd_create", "ls_fd_destroy", "ls_fd_dof", "ls_fd_apply", "ls_fd_apply_f32", "ls_fd_apply_noalloc", "ls_fd_rhs",
     "ls_fd_diagonal", "ls_fd_solve", "ls_fd_profile_iteration", "ls_fd_eval_points", "ls_fd_eval_lattice",
 )
 
@@ -107,6 +108,7 @@ _SIGS = {
     "ls_fd_dof": (C.c_int64, [_P]),
     "ls_fd_apply": (C.c_int, [_P, _P, _P, _P]),
     "ls_fd_apply_f32": (C.c_int, [_P, _P, _P, _P]),
+    "ls_fd_apply_noalloc": (C.c_int, [C.POINTER(FdSystem), _P, _P, C.POINTER(C.c_double), _P]),
     "ls_fd_rhs": (C.c_int, [_P, _P, _P]),
     "ls_fd_diagonal": (C.c_int, [_P, _P, _P]),
     "ls_fd_solve": (C.c_int, [_P, C.POINTER(SolveOpts), _P, C.POINTER(SolveStats), _P]),
