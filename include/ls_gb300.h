@@ -175,6 +175,14 @@ int ls_fd_diagonal(ls_fd_handle *h, double *d_diag, void *stream);
 
 typedef enum ls_precision { LS_FP64 = 0, LS_MIXED = 1 } ls_precision;
 
+/* CG preconditioner.  JACOBI reproduces the reference's column-scaled CG
+ * iteration; MG (mixed precision only) is a geometric-multigrid V-cycle that
+ * changes only the iteration path -- the stopping test stays the reference's
+ * ||S r|| < max(atol, rtol ||S rhs||).  MG falls back to JACOBI for grids it
+ * cannot coarsen (an axis below 5 nodes while the coarsest level is still
+ * above 1000 nodes); ls_solve_stats.preconditioner reports the one used. */
+typedef enum ls_preconditioner { LS_PRECOND_JACOBI = 0, LS_PRECOND_MG = 1 } ls_preconditioner;
+
 typedef struct ls_solve_opts {
   int32_t precision;      /* ls_precision */
   int32_t use_x0;         /* d_x holds the initial guess (else zeros) */
@@ -183,7 +191,7 @@ typedef struct ls_solve_opts {
   int64_t maxiter;        /* <= 0: 10 * dof (scipy default) */
   double reliable_delta;  /* mixed: refresh the FP64 residual once ||S r|| fell by this factor (<=0: 0.1) */
   int32_t check_every;    /* iterations per device batch between host checks (<=0: 64) */
-  int32_t reserved;
+  int32_t preconditioner; /* ls_preconditioner */
 } ls_solve_opts;
 
 typedef struct ls_solve_stats {
@@ -194,7 +202,7 @@ typedef struct ls_solve_stats {
   double threshold;         /* max(atol, rtol * ||S rhs||) */
   double device_ms;         /* device time of the solve (CUDA events) */
   int32_t status;
-  int32_t reserved;
+  int32_t preconditioner;   /* ls_preconditioner actually used */
 } ls_solve_stats;
 
 /* Jacobi-preconditioned CG on the normal equations -- the iteration of the

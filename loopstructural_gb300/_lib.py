@@ -18,6 +18,8 @@ LS_NAN = 2
 LS_BREAKDOWN = 3
 LS_FP64 = 0
 LS_MIXED = 1
+LS_PRECOND_JACOBI = 0
+LS_PRECOND_MG = 1
 NOALLOC_MAX_ROWS = 1048576
 
 ROWS_VALUE, ROWS_NORM, ROWS_GRADIENT, ROWS_TANGENT = 0, 1, 2, 3
@@ -74,7 +76,7 @@ class SolveOpts(C.Structure):
     _fields_ = [
         ("precision", C.c_int32), ("use_x0", C.c_int32), ("atol", C.c_double), ("rtol", C.c_double),
         ("maxiter", C.c_int64), ("reliable_delta", C.c_double), ("check_every", C.c_int32),
-        ("reserved", C.c_int32),
+        ("preconditioner", C.c_int32),
     ]
 
 
@@ -82,7 +84,7 @@ class SolveStats(C.Structure):
     _fields_ = [
         ("iterations", C.c_int64), ("reliable_updates", C.c_int64), ("residual", C.c_double),
         ("rhs_norm", C.c_double), ("threshold", C.c_double), ("device_ms", C.c_double),
-        ("status", C.c_int32), ("reserved", C.c_int32),
+        ("status", C.c_int32), ("preconditioner", C.c_int32),
     ]
 
 

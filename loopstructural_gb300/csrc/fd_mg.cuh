@@ -1,0 +1,152 @@
+// Geometric multigrid V-cycle (FP32) used as the CG preconditioner of the
+// mixed-precision FD solve.  Not a reference algorithm: it changes only the
+// iteration path; the solution is still the one of the reference's normal
+// equations (the outer CG stops on the reference's scaled-residual test).
+//
+// Hierarchy: level l+1 has n_{l+1} = n_l / 2 + 1 nodes per axis, coarse node J
+// sitting on fine node 2J (the coarse grid may reach one fine cell past an
+// even-sized fine grid).  Prolongation P is trilinear (weights 1 and 1/2 per
+// axis), restriction is P^T.
+//   * regularisation: re-discretised on the coarse grid -- the same stencil
+//     families with volume weights w^2 scaled by 1/2 and border-layer weights
+//     by 1/4 per level (the energy of P u_c matches in the continuum limit);
+//   * data rows: Galerkin, row_{l+1} = row_l P (at most 27 coarse columns);
+//   * ridge^2 scaled by 8 per level;
+//   * smoother: Chebyshev polynomial of D^-1 A on [lmax/20, 1.05 lmax]
+//     (lmax by power iteration), `deg` steps pre and post -- symmetric, so the
+//     V-cycle is an SPD preconditioner;
+//   * coarsest level (<= 512 nodes): dense inverse.
+#pragma once
+
+#include <vector>
+
+#include "fd_apply.cuh"
+#include "ls_common.cuh"
+
+namespace ls {
+
+struct MgLevel {
+  int nx = 0, ny = 0, nz = 0;
+  int64_t n = 0;
+  StencilCoef coef64{};
+  CoefT<float> coef{};
+  // data rows (FP32)
+  int64_t nrows = 0;
+  int width = 0;
+  int32_t *cols = nullptr;
+  float *a = nullptr, *w2 = nullptr, *s = nullptr;
+  int64_t ntouched = 0;
+  uint32_t *mask = nullptr;
+  int32_t *word_rank = nullptr;
+  int64_t *inc_ptr = nullptr;
+  int32_t *inc_row = nullptr;
+  float *inc_a = nullptr;
+  float *dinv = nullptr;
+  // vectors: b (rhs), x (solution), r (residual), d[2] (Chebyshev directions)
+  float *b = nullptr, *x = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;
+  bool owns_bx = true;
+  // Chebyshev
+  float lmax = 0.f;
+  std::vector<float> c1, c2;  // per step
+  float inv_theta = 0.f;
+};
+
+struct MgHierarchy {
+  std::vector<MgLevel> levels;
+  double *coarse_inv64 = nullptr;  // dense inverse of the coarsest operator (FP64), row-major
+  int deg = 3;
+  bool built = false;
+  std::vector<void *> allocations;
+};
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+__global__ void mg_cheb_init_kernel(int64_t n, const float *__restrict__ b, const float *__restrict__ dinv,
+                                    float inv_theta, float *__restrict__ r, float *__restrict__ d,
+                                    float *__restrict__ x, const int *done) {
+  if (done && *done) return;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const float bv = b[g];
+    r[g] = bv;
+    d[g] = inv_theta * dinv[g] * bv;
+    x[g] = 0.f;
+  }
+}
+
+// b_c = P^T r_f (3-D launch: block 32 x 8 over coarse x-y, blockIdx.z = coarse z)
+__global__ void mg_restrict_kernel(int nfx, int nfy, int nfz, int ncx, int ncy, int ncz, const float *__restrict__ rf,
+                                   float *__restrict__ bc, const int *done) {
+  if (done && *done) return;
+  const int I = blockIdx.x * blockDim.x + threadIdx.x, J = blockIdx.y * blockDim.y + threadIdx.y, K = blockIdx.z;
+  if (I >= ncx || J >= ncy || K >= ncz) return;
+  float acc = 0.f;
+#pragma unroll
+  for (int dz = -1; dz <= 1; ++dz) {
+    const int k = 2 * K + dz;
+    if (k < 0 || k >= nfz) continue;
+    const float wz = dz == 0 ? 1.f : 0.5f;
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int j = 2 * J + dy;
+      if (j < 0 || j >= nfy) continue;
+      const float wyz = wz * (dy == 0 ? 1.f : 0.5f);
+      const float *row = rf + ((size_t)k * nfy + j) * nfx;
+#pragma unroll
+      for (int dx = -1; dx <= 1; ++dx) {
+        const int i = 2 * I + dx;
+        if (i < 0 || i >= nfx) continue;
+        acc += wyz * (dx == 0 ? 1.f : 0.5f) * __ldg(row + i);
+      }
+    }
+  }
+  bc[((size_t)K * ncy + J) * ncx + I] = acc;
+}
+
+// x_f += P x_c (3-D launch over fine x-y, blockIdx.z = fine z)
+__global__ void mg_prolong_kernel(int nfx, int nfy, int nfz, int ncx, int ncy, const float *__restrict__ xc,
+                                  float *__restrict__ xf, const int *done) {
+  if (done && *done) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+  if (i >= nfx || j >= nfy || k >= nfz) return;
+  const int i0 = i >> 1, j0 = j >> 1, k0 = k >> 1;
+  const int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
+  const float w = ((i & 1) ? 0.5f : 1.f) * ((j & 1) ? 0.5f : 1.f) * ((k & 1) ? 0.5f : 1.f);
+  float acc = 0.f;
+  for (int c = 0; c < nk; ++c)
+    for (int b = 0; b < nj; ++b)
+      for (int a = 0; a < ni; ++a) acc += __ldg(xc + ((size_t)(k0 + c) * ncy + (j0 + b)) * ncx + (i0 + a));
+  xf[((size_t)k * nfy + j) * nfx + i] += w * acc;
+}
+
+// x = Minv b in FP64 (the coarsest operator can be ill-conditioned), one warp per row
+__global__ void mg_dense_kernel(int nc, const double *__restrict__ minv, const float *__restrict__ b,
+                                float *__restrict__ x, const int *done) {
+  if (done && *done) return;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= nc) return;
+  double acc = 0.0;
+  for (int j = lane; j < nc; j += 32) acc += minv[(int64_t)warp * nc + j] * (double)__ldg(b + j);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) x[warp] = (float)acc;
+}
+
+// sum of a.(w b) with an optional weight vector (FP32 in, FP64 out)
+__global__ void __launch_bounds__(256) mg_dot_kernel(int64_t n, const float *__restrict__ a, const float *__restrict__ b,
+                                                     const float *__restrict__ w, double *partials,
+                                                     unsigned int *ticket, double *out) {
+  float l = 0.f;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+    l += a[g] * (w ? w[g] * b[g] : b[g]);
+  double tot;
+  if (grid_sum<256>((double)l, partials, ticket, &tot)) *out = tot;
+}
+
+__global__ void mg_scale_kernel(int64_t n, const float *__restrict__ src, const float *__restrict__ w, float scale,
+                                float *__restrict__ dst) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+    dst[g] = scale * (w ? w[g] : 1.f) * src[g];
+}
+
+}  // namespace ls

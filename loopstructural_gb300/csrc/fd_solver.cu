@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <vector>
 
+#include "fd_apply.cuh"
+#include "fd_mg.cuh"
 #include "fd_stencil.cuh"
 #include "ls_common.cuh"
 
@@ -34,6 +36,7 @@ struct CgScalars {
   double pq_d;     // p . (data part of N p)
   double beta;
   double thresh2;  // stopping threshold squared (on r . z)
+  double rrj;      // r . D^-1 r of the current FP32 residual (MG stopping test)
   double rz64;     // FP64 refresh: r64 . D^-1 r64
   double rz32;     // FP64 refresh: r32 . D^-1 r32 (after rounding)
   double scratch;
@@ -58,6 +61,8 @@ struct DataTerm {
   int32_t *inc_row = nullptr;  // incidences (row of each)
   double *inc_a64 = nullptr;   // coefficient of each incidence
   float *inc_a32 = nullptr;
+  uint32_t *mask = nullptr;    // touched-node bit mask, ceil(n/32) words
+  int32_t *word_rank = nullptr;
 };
 
 }  // namespace
@@ -82,9 +87,15 @@ struct ls_fd_handle {
   unsigned int *tickets = nullptr; // one per reduction site
   int red_blocks = 0;
   // graphs of one batch of iterations
-  cudaGraphExec_t g64 = nullptr, g32 = nullptr;
-  int g64_batch = 0, g32_batch = 0;
+  cudaGraphExec_t g64 = nullptr, g32 = nullptr, gmg = nullptr;
+  int g64_batch = 0, g32_batch = 0, gmg_batch = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // multigrid preconditioner (built on first use)
+  ls::MgHierarchy mg;
+  float *z32 = nullptr;                 // preconditioned residual
+  std::vector<int64_t> h_idc;           // host copy of the data rows (Galerkin coarsening)
+  std::vector<double> h_a, h_w2;
+  int h_width = 0;
 };
 
 namespace ls {
@@ -108,70 +119,6 @@ enum Ticket { T_STENCIL = 0, T_DATA = 1, T_UPDATE = 2, T_REFRESH = 3, T_MISC = 4
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
-
-// q = (stencil part of N) p  and  p . q  (grid-reduced into sc->pq_s).
-// 3-D launch: block (32, 8) covers an x-y tile, blockIdx.z strides over z.
-constexpr int kTX = 32, kTY = 8;
-template <typename T>
-__global__ void __launch_bounds__(kTX * kTY) stencil_kernel(CoefT<T> c, const T *__restrict__ p, T *__restrict__ q,
-                                                             CgScalars *sc, double *partials, unsigned int *ticket,
-                                                             bool check_done) {
-  if (check_done && sc->done) return;
-  const int nx = c.nx, ny = c.ny, nz = c.nz;
-  const int i = blockIdx.x * kTX + threadIdx.x, j = blockIdx.y * kTY + threadIdx.y;
-  T local = 0;  // per-thread partial in the kernel's precision; FP64 from the block sum on
-  if (i < nx && j < ny) {
-    for (int k = blockIdx.z; k < nz; k += gridDim.z) {
-      const int g = i + nx * (j + ny * k);
-      const T v = stencil_node32<T>(c, p, g, i, j, k);
-      q[g] = v;
-      local += __ldg(p + g) * v;
-    }
-  }
-  double tot;
-  const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-  if (grid_sum_ex<kTX * kTY>((double)local, partials, ticket, &tot, threadIdx.x + kTX * threadIdx.y, bid,
-                             gridDim.x * gridDim.y * gridDim.z))
-    sc->pq_s = tot;
-}
-
-// s_r = w_r^2 (a_r . p) ; p . N_d p = sum_r w_r^2 (a_r . p)^2 into sc->pq_d
-template <typename T>
-__global__ void __launch_bounds__(kBlock) data_rows_kernel(int64_t nrows, int width, const int32_t *__restrict__ cols,
-                                                           const T *__restrict__ a, const T *__restrict__ w2,
-                                                           const T *__restrict__ p, T *__restrict__ s, CgScalars *sc,
-                                                           double *partials, unsigned int *ticket, bool check_done) {
-  if (check_done && sc->done) return;
-  T local = 0;
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
-    T acc = 0;
-    for (int k = 0; k < width; ++k) {
-      const int32_t col = cols[r * width + k];
-      if (col >= 0) acc += a[r * width + k] * p[col];
-    }
-    const T sr = w2[r] * acc;
-    s[r] = sr;
-    local += sr * acc;
-  }
-  double tot;
-  if (grid_sum<kBlock>((double)local, partials, ticket, &tot)) sc->pq_d = tot;
-}
-
-// q[n] += sum over the rows touching node n of a_rk s_r
-template <typename T>
-__global__ void __launch_bounds__(kBlock) data_nodes_kernel(int64_t ntouched, const int64_t *__restrict__ touched,
-                                                            const int64_t *__restrict__ ptr,
-                                                            const int32_t *__restrict__ row, const T *__restrict__ ia,
-                                                            const T *__restrict__ s, T *__restrict__ q,
-                                                            const CgScalars *sc, bool check_done) {
-  if (check_done && sc->done) return;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntouched;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    T acc = 0;
-    for (int64_t e = ptr[t]; e < ptr[t + 1]; ++e) acc += ia[e] * s[row[e]];
-    q[touched[t]] += acc;
-  }
-}
 
 // alpha = rz / pq ; x += alpha p ; r -= alpha q ; rz' = r . D^-1 r ;
 // the last block publishes beta = rz'/rz and tests convergence.
@@ -337,27 +284,33 @@ int grid_for(const ls_fd_handle *h, int64_t n) {
   return std::min(g, h->red_blocks);
 }
 
-dim3 stencil_grid(const ls_fd_handle *h) {
-  const int gx = (int)((h->coef.nx + kTX - 1) / kTX), gy = (int)((h->coef.ny + kTY - 1) / kTY);
-  int gz = std::max(1, h->red_blocks / std::max(1, gx * gy));
-  gz = std::min<int>(gz, (int)h->coef.nz);
-  return dim3(gx, gy, gz);
+template <typename T>
+DataView<T> data_view(const ls_fd_handle *h, const T *s_rows, const T *inc_a) {
+  DataView<T> dv;
+  dv.mask = h->data.mask;
+  dv.word_rank = h->data.word_rank;
+  dv.inc_ptr = h->data.inc_ptr;
+  dv.inc_row = h->data.inc_row;
+  dv.inc_a = inc_a;
+  dv.s_rows = s_rows;
+  dv.enabled = h->data.ntouched > 0;
+  return dv;
 }
 
-// N p for the precision T, leaving q; p.q in sc->pq_s + sc->pq_d
+// q = N p (rows kernel + fused apply); p.q lands in sc->pq_s (sc->pq_d = 0)
 template <typename T>
 void launch_apply(ls_fd_handle *h, const T *p, T *q, T *s, const T *a, const T *w2, const T *ia, bool check_done,
                   cudaStream_t st) {
   const DataTerm &d = h->data;
-  stencil_kernel<T><<<stencil_grid(h), dim3(kTX, kTY), 0, st>>>(coef_as<T>(h->coef), p, q, h->sc, h->partials,
-                                                                 h->tickets + T_STENCIL, check_done);
-  if (d.nrows > 0) {
-    data_rows_kernel<T><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, a, w2, p, s, h->sc,
-                                                               h->partials + 2 * h->red_blocks,
-                                                               h->tickets + T_DATA, check_done);
-    data_nodes_kernel<T><<<grid_for(h, d.ntouched), kBlock, 0, st>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row, ia, s,
-                                                                   q, h->sc, check_done);
-  }
+  const int *done = check_done ? &h->sc->done : nullptr;
+  if (d.nrows > 0)
+    rows_kernel<T><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, a, w2, p, s, done);
+  EpiArgs<T> e{};
+  e.q = q;
+  const int nx = (int)h->coef.nx, ny = (int)h->coef.ny, nz = (int)h->coef.nz;
+  const int zc = apply_zchunk(nx, ny, nz, sm_count());
+  fd_apply_kernel<T, EPI_STORE><<<apply_grid(nx, ny, nz, zc), dim3(kAX, kAY), 0, st>>>(
+      coef_as<T>(h->coef), p, data_view<T>(h, s, ia), e, zc, done, h->partials, h->tickets + T_STENCIL, &h->sc->pq_s);
 }
 
 void launch_apply64(ls_fd_handle *h, const double *p, double *q, bool check_done, cudaStream_t st) {
@@ -416,6 +369,545 @@ int refresh(ls_fd_handle *h, bool have_x, float *r32, float *p32) {
   return LS_OK;
 }
 
+
+// ---------------------------------------------------------------------------
+// multigrid: hierarchy construction and the V-cycle launch sequence
+// ---------------------------------------------------------------------------
+struct HostRows {
+  int64_t nrows = 0;
+  int width = 0;
+  std::vector<int64_t> cols;  // nrows * width, -1 = padding
+  std::vector<double> a;
+  std::vector<double> w2;
+};
+
+template <typename P>
+int mg_alloc(MgHierarchy &mg, P **ptr, size_t count) {
+  LS_TRY(dev_alloc(ptr, count));
+  mg.allocations.push_back((void *)*ptr);
+  return LS_OK;
+}
+
+// Galerkin coarsening of data rows: row_c = row_f P (trilinear P, weights 1 / 1/2 per axis)
+HostRows galerkin_rows(const HostRows &f, int nfx, int nfy, int ncx, int ncy) {
+  HostRows c;
+  c.nrows = f.nrows;
+  c.width = 27;
+  c.cols.assign((size_t)c.nrows * 27, -1);
+  c.a.assign((size_t)c.nrows * 27, 0.0);
+  c.w2 = f.w2;
+  std::vector<std::pair<int64_t, double>> acc;
+  for (int64_t r = 0; r < f.nrows; ++r) {
+    acc.clear();
+    for (int k = 0; k < f.width; ++k) {
+      const int64_t col = f.cols[r * f.width + k];
+      if (col < 0) continue;
+      const double v = f.a[r * f.width + k];
+      const int i = (int)(col % nfx), j = (int)((col / nfx) % nfy), kk = (int)(col / ((int64_t)nfx * nfy));
+      int ci[2], cj[2], ck[2];
+      double wi[2], wj[2], wk[2];
+      const int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (kk & 1) ? 2 : 1;
+      ci[0] = i >> 1; ci[1] = (i >> 1) + 1; wi[0] = wi[1] = (i & 1) ? 0.5 : 1.0;
+      cj[0] = j >> 1; cj[1] = (j >> 1) + 1; wj[0] = wj[1] = (j & 1) ? 0.5 : 1.0;
+      ck[0] = kk >> 1; ck[1] = (kk >> 1) + 1; wk[0] = wk[1] = (kk & 1) ? 0.5 : 1.0;
+      for (int c3 = 0; c3 < nk; ++c3)
+        for (int b = 0; b < nj; ++b)
+          for (int a = 0; a < ni; ++a) {
+            const int64_t cc = ci[a] + (int64_t)ncx * (cj[b] + (int64_t)ncy * ck[c3]);
+            const double w = v * wi[a] * wj[b] * wk[c3];
+            bool found = false;
+            for (auto &e : acc)
+              if (e.first == cc) {
+                e.second += w;
+                found = true;
+                break;
+              }
+            if (!found) acc.emplace_back(cc, w);
+          }
+    }
+    std::sort(acc.begin(), acc.end());
+    for (size_t e = 0; e < acc.size() && e < 27; ++e) {
+      c.cols[r * 27 + e] = acc[e].first;
+      c.a[r * 27 + e] = acc[e].second;
+    }
+  }
+  return c;
+}
+
+__global__ void mg_diag_finish_kernel(int64_t n, double *__restrict__ diag, int64_t ntouched,
+                                      const int64_t *__restrict__ touched, const double *__restrict__ ddata) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntouched; t += (int64_t)gridDim.x * blockDim.x)
+    diag[touched[t]] += ddata[t];
+}
+
+__global__ void mg_invert_kernel(int64_t n, const double *__restrict__ diag, float *__restrict__ dinv) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+    dinv[g] = diag[g] > 0.0 ? (float)(1.0 / diag[g]) : 1.0f;
+}
+
+__global__ void mg_fill_hash_kernel(int64_t n, float *__restrict__ v) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t h = (uint32_t)g * 2654435761u + 12345u;
+    h ^= h >> 13;
+    h *= 0x5bd1e995u;
+    h ^= h >> 15;
+    v[g] = 0.5f + (float)(h & 0xffffu) / 65536.0f;
+  }
+}
+
+// device data of one level from host rows (incidence list, bit mask, FP32 copies)
+int mg_upload_level(ls_fd_handle *h, MgLevel &lv, const HostRows &rows, std::vector<int64_t> &touched,
+                    std::vector<double> &data_diag) {
+  MgHierarchy &mg = h->mg;
+  const int64_t ne = rows.nrows * rows.width;
+  std::vector<int32_t> cols(ne);
+  std::vector<float> a32(ne), w2(rows.nrows);
+  std::vector<std::pair<int64_t, int64_t>> inc;
+  inc.reserve(ne);
+  for (int64_t e = 0; e < ne; ++e) {
+    cols[e] = rows.cols[e] < 0 ? -1 : (int32_t)rows.cols[e];
+    a32[e] = (float)rows.a[e];
+    if (rows.cols[e] >= 0) inc.emplace_back(rows.cols[e], e);
+  }
+  for (int64_t r = 0; r < rows.nrows; ++r) w2[r] = (float)rows.w2[r];
+  std::stable_sort(inc.begin(), inc.end(), [](const std::pair<int64_t, int64_t> &x, const std::pair<int64_t, int64_t> &y) {
+    return x.first < y.first;
+  });
+  std::vector<int64_t> ptr;
+  std::vector<int32_t> irow;
+  std::vector<float> ia;
+  touched.clear();
+  data_diag.clear();
+  for (size_t t = 0; t < inc.size(); ++t) {
+    if (t == 0 || inc[t].first != inc[t - 1].first) {
+      touched.push_back(inc[t].first);
+      ptr.push_back((int64_t)t);
+      data_diag.push_back(0.0);
+    }
+    const int64_t e = inc[t].second, r = e / rows.width;
+    irow.push_back((int32_t)r);
+    ia.push_back((float)rows.a[e]);
+    data_diag.back() += rows.w2[r] * rows.a[e] * rows.a[e];
+  }
+  ptr.push_back((int64_t)inc.size());
+  const int64_t nwords = (lv.n + 31) / 32;
+  std::vector<uint32_t> mask(nwords, 0u);
+  std::vector<int32_t> wr(nwords, 0);
+  for (int64_t t : touched) mask[t >> 5] |= 1u << (t & 31);
+  int32_t run = 0;
+  for (int64_t w = 0; w < nwords; ++w) {
+    wr[w] = run;
+    run += __builtin_popcount(mask[w]);
+  }
+  lv.nrows = rows.nrows;
+  lv.width = rows.width;
+  lv.ntouched = (int64_t)touched.size();
+  const int64_t ni = (int64_t)inc.size();
+  LS_TRY(mg_alloc(mg, &lv.cols, ne));
+  LS_TRY(mg_alloc(mg, &lv.a, ne));
+  LS_TRY(mg_alloc(mg, &lv.w2, rows.nrows));
+  LS_TRY(mg_alloc(mg, &lv.s, rows.nrows));
+  LS_TRY(mg_alloc(mg, &lv.mask, nwords));
+  LS_TRY(mg_alloc(mg, &lv.word_rank, nwords));
+  LS_TRY(mg_alloc(mg, &lv.inc_ptr, lv.ntouched + 1));
+  LS_TRY(mg_alloc(mg, &lv.inc_row, ni));
+  LS_TRY(mg_alloc(mg, &lv.inc_a, ni));
+  cudaStream_t st = h->stream;
+#define UPL(dst, src, cnt) \
+  if ((cnt) > 0) LS_CUDA_TRY(cudaMemcpyAsync(dst, (src).data(), (cnt) * sizeof((src)[0]), cudaMemcpyHostToDevice, st));
+  UPL(lv.cols, cols, ne);
+  UPL(lv.a, a32, ne);
+  UPL(lv.w2, w2, rows.nrows);
+  UPL(lv.mask, mask, nwords);
+  UPL(lv.word_rank, wr, nwords);
+  UPL(lv.inc_ptr, ptr, lv.ntouched + 1);
+  UPL(lv.inc_row, irow, ni);
+  UPL(lv.inc_a, ia, ni);
+#undef UPL
+  LS_CUDA_TRY(cudaStreamSynchronize(st));
+  return LS_OK;
+}
+
+DataView<float> mg_view(const MgLevel &lv) {
+  DataView<float> dv;
+  dv.mask = lv.mask;
+  dv.word_rank = lv.word_rank;
+  dv.inc_ptr = lv.inc_ptr;
+  dv.inc_row = lv.inc_row;
+  dv.inc_a = lv.inc_a;
+  dv.s_rows = lv.s;
+  dv.enabled = lv.ntouched > 0;
+  return dv;
+}
+
+// q = A_l p on level l (rows + fused apply with an epilogue)
+template <int EPI>
+void mg_apply(ls_fd_handle *h, const MgLevel &lv, const float *p, const EpiArgs<float> &e, const int *done,
+              cudaStream_t st) {
+  if (lv.nrows > 0)
+    rows_kernel<float><<<grid_for(h, lv.nrows), kBlock, 0, st>>>(lv.nrows, lv.width, lv.cols, lv.a, lv.w2, p, lv.s, done);
+  const int zc = apply_zchunk(lv.nx, lv.ny, lv.nz, sm_count());
+  fd_apply_kernel<float, EPI><<<apply_grid(lv.nx, lv.ny, lv.nz, zc), dim3(kAX, kAY), 0, st>>>(
+      lv.coef, p, mg_view(lv), e, zc, done, nullptr, nullptr, nullptr);
+}
+
+int mg_read_scalar(ls_fd_handle *h, double *dev, double *out) {
+  LS_CUDA_TRY(cudaMemcpyAsync(out, dev, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return LS_OK;
+}
+
+int mg_lambda_max(ls_fd_handle *h, MgLevel &lv, float *lmax_out) {
+  cudaStream_t st = h->stream;
+  const int g = grid_for(h, lv.n);
+  float *v = lv.d0, *q = lv.d1;
+  mg_fill_hash_kernel<<<g, kBlock, 0, st>>>(lv.n, v);
+  double nv = 0.0, nq = 0.0;
+  double *slot = &h->sc->scratch;
+  mg_dot_kernel<<<g, 256, 0, st>>>(lv.n, v, v, nullptr, h->partials, h->tickets + T_MISC, slot);
+  LS_TRY(mg_read_scalar(h, slot, &nv));
+  double lam = 0.0;
+  for (int it = 0; it < 20; ++it) {
+    mg_scale_kernel<<<g, kBlock, 0, st>>>(lv.n, v, nullptr, (float)(1.0 / sqrt(nv)), v);
+    EpiArgs<float> e{};
+    e.q = q;
+    mg_apply<EPI_STORE>(h, lv, v, e, nullptr, st);
+    mg_scale_kernel<<<g, kBlock, 0, st>>>(lv.n, q, lv.dinv, 1.0f, v);
+    mg_dot_kernel<<<g, 256, 0, st>>>(lv.n, v, v, nullptr, h->partials, h->tickets + T_MISC, slot);
+    LS_TRY(mg_read_scalar(h, slot, &nq));
+    lam = sqrt(nq);  // |D^-1 A v| with |v| = 1
+    nv = nq;
+    if (!(nv > 0.0) || !isfinite(nv)) break;
+  }
+  LS_CUDA_TRY(cudaGetLastError());
+  *lmax_out = (float)(lam > 0.0 && isfinite(lam) ? lam : 1.0);
+  return LS_OK;
+}
+
+// dense inverse of the coarsest operator (Gauss-Jordan with partial pivoting, FP64)
+int mg_coarse_inverse(ls_fd_handle *h, MgLevel &lv) {
+  MgHierarchy &mg = h->mg;
+  cudaStream_t st = h->stream;
+  const int nc = (int)lv.n;
+  std::vector<double> A((size_t)nc * nc);
+  std::vector<float> col(nc);
+  const float one = 1.0f;
+  for (int j = 0; j < nc; ++j) {
+    LS_CUDA_TRY(cudaMemsetAsync(lv.d0, 0, nc * sizeof(float), st));
+    LS_CUDA_TRY(cudaMemcpyAsync(lv.d0 + j, &one, sizeof(float), cudaMemcpyHostToDevice, st));
+    EpiArgs<float> e{};
+    e.q = lv.d1;
+    mg_apply<EPI_STORE>(h, lv, lv.d0, e, nullptr, st);
+    LS_CUDA_TRY(cudaMemcpyAsync(col.data(), lv.d1, nc * sizeof(float), cudaMemcpyDeviceToHost, st));
+    LS_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int i = 0; i < nc; ++i) A[(size_t)i * nc + j] = col[i];
+  }
+  // symmetrise (the FP32 apply is symmetric up to rounding)
+  for (int i = 0; i < nc; ++i)
+    for (int j = i + 1; j < nc; ++j) {
+      const double m = 0.5 * (A[(size_t)i * nc + j] + A[(size_t)j * nc + i]);
+      A[(size_t)i * nc + j] = A[(size_t)j * nc + i] = m;
+    }
+  std::vector<double> inv((size_t)nc * nc, 0.0);
+  for (int i = 0; i < nc; ++i) inv[(size_t)i * nc + i] = 1.0;
+  double maxdiag = 0.0;
+  for (int i = 0; i < nc; ++i) maxdiag = std::max(maxdiag, fabs(A[(size_t)i * nc + i]));
+  for (int c = 0; c < nc; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < nc; ++r)
+      if (fabs(A[(size_t)r * nc + c]) > fabs(A[(size_t)piv * nc + c])) piv = r;
+    if (piv != c)
+      for (int k = 0; k < nc; ++k) {
+        std::swap(A[(size_t)c * nc + k], A[(size_t)piv * nc + k]);
+        std::swap(inv[(size_t)c * nc + k], inv[(size_t)piv * nc + k]);
+      }
+    double d = A[(size_t)c * nc + c];
+    if (fabs(d) < 1e-14 * maxdiag) d = (d < 0 ? -1.0 : 1.0) * 1e-14 * maxdiag;  // guard a singular pivot
+    const double id = 1.0 / d;
+    for (int k = 0; k < nc; ++k) {
+      A[(size_t)c * nc + k] *= id;
+      inv[(size_t)c * nc + k] *= id;
+    }
+    for (int r = 0; r < nc; ++r) {
+      if (r == c) continue;
+      const double f = A[(size_t)r * nc + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < nc; ++k) {
+        A[(size_t)r * nc + k] -= f * A[(size_t)c * nc + k];
+        inv[(size_t)r * nc + k] -= f * inv[(size_t)c * nc + k];
+      }
+    }
+  }
+  LS_TRY(mg_alloc(mg, &mg.coarse_inv64, (size_t)nc * nc));
+  LS_CUDA_TRY(cudaMemcpyAsync(mg.coarse_inv64, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaStreamSynchronize(st));
+  return LS_OK;
+}
+
+int mg_level_dinv(ls_fd_handle *h, MgLevel &lv, const std::vector<int64_t> &touched,
+                  const std::vector<double> &data_diag) {
+  cudaStream_t st = h->stream;
+  double *diag = nullptr;
+  int64_t *dt = nullptr;
+  double *dd = nullptr;
+  LS_TRY(dev_alloc(&diag, lv.n));
+  LS_TRY(dev_alloc(&dt, touched.size()));
+  LS_TRY(dev_alloc(&dd, data_diag.size()));
+  if (!touched.empty()) {
+    LS_CUDA_TRY(cudaMemcpyAsync(dt, touched.data(), touched.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    LS_CUDA_TRY(cudaMemcpyAsync(dd, data_diag.data(), data_diag.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  const int g = grid_for(h, lv.n);
+  diag_stencil_kernel<<<g, kBlock, 0, st>>>(lv.coef64, diag);
+  if (!touched.empty())
+    mg_diag_finish_kernel<<<grid_for(h, (int64_t)touched.size()), kBlock, 0, st>>>(lv.n, diag, (int64_t)touched.size(), dt, dd);
+  mg_invert_kernel<<<g, kBlock, 0, st>>>(lv.n, diag, lv.dinv);
+  LS_CUDA_TRY(cudaStreamSynchronize(st));
+  cudaFree(diag);
+  cudaFree(dt);
+  cudaFree(dd);
+  return LS_OK;
+}
+
+StencilCoef coarsen_coef(const StencilCoef &f, int nx, int ny, int nz) {
+  StencilCoef c = f;
+  c.nx = nx;
+  c.ny = ny;
+  c.nz = nz;
+  c.xx_int *= 0.5;
+  c.yy_int *= 0.5;
+  c.zz_int *= 0.5;
+  c.xy *= 0.5;
+  c.xz *= 0.5;
+  c.yz *= 0.5;
+  c.xx_bdr = nx >= 3 ? f.xx_bdr * 0.25 : 0.0;
+  c.yy_bdr = ny >= 3 ? f.yy_bdr * 0.25 : 0.0;
+  c.zz_bdr = nz >= 3 ? f.zz_bdr * 0.25 : 0.0;
+  c.ridge2 *= 8.0;
+  return c;
+}
+
+constexpr int64_t kMgMaxCoarse = 1000;  // largest dense coarsest level
+
+// Builds the hierarchy; returns LS_OK with mg.built == false when the grid
+// cannot be coarsened to a dense-solvable size (the solve then uses Jacobi).
+int mg_build(ls_fd_handle *h, int deg) {
+  MgHierarchy &mg = h->mg;
+  if (mg.built || !mg.levels.empty()) return LS_OK;  // built, or tried and not applicable
+  mg.deg = deg;
+  MgLevel L0;
+  L0.nx = (int)h->grid.nsteps[0];
+  L0.ny = (int)h->grid.nsteps[1];
+  L0.nz = (int)h->grid.nsteps[2];
+  L0.n = h->n;
+  L0.coef64 = h->coef;
+  L0.coef = coef_as<float>(h->coef);
+  L0.nrows = h->data.nrows;
+  L0.width = h->data.width;
+  L0.cols = h->data.cols;
+  L0.a = h->data.a32;
+  L0.w2 = h->data.w2_32;
+  L0.s = h->s32;
+  L0.ntouched = h->data.ntouched;
+  L0.mask = h->data.mask;
+  L0.word_rank = h->data.word_rank;
+  L0.inc_ptr = h->data.inc_ptr;
+  L0.inc_row = h->data.inc_row;
+  L0.inc_a = h->data.inc_a32;
+  L0.dinv = h->dinv32;
+  L0.owns_bx = false;
+  L0.b = h->r32;
+  if (!h->z32) LS_TRY(dev_alloc(&h->z32, h->n));
+  L0.x = h->z32;
+  LS_TRY(mg_alloc(mg, &L0.r, L0.n));
+  LS_TRY(mg_alloc(mg, &L0.d0, L0.n));
+  LS_TRY(mg_alloc(mg, &L0.d1, L0.n));
+  mg.levels.push_back(L0);
+  HostRows rows;
+  rows.nrows = h->data.nrows;
+  rows.width = h->h_width;
+  rows.cols = h->h_idc;
+  rows.a = h->h_a;
+  rows.w2 = h->h_w2;
+  for (;;) {
+    const MgLevel &f = mg.levels.back();
+    if (f.n <= kMgMaxCoarse) break;
+    if (f.nx < 5 || f.ny < 5 || f.nz < 5) break;
+    MgLevel c;
+    c.nx = f.nx / 2 + 1;
+    c.ny = f.ny / 2 + 1;
+    c.nz = f.nz / 2 + 1;
+    c.n = (int64_t)c.nx * c.ny * c.nz;
+    c.coef64 = coarsen_coef(f.coef64, c.nx, c.ny, c.nz);
+    c.coef = coef_as<float>(c.coef64);
+    if (rows.nrows > 0) rows = galerkin_rows(rows, f.nx, f.ny, c.nx, c.ny);
+    std::vector<int64_t> touched;
+    std::vector<double> ddiag;
+    LS_TRY(mg_alloc(mg, &c.b, c.n));
+    LS_TRY(mg_alloc(mg, &c.x, c.n));
+    LS_TRY(mg_alloc(mg, &c.r, c.n));
+    LS_TRY(mg_alloc(mg, &c.d0, c.n));
+    LS_TRY(mg_alloc(mg, &c.d1, c.n));
+    LS_TRY(mg_alloc(mg, &c.dinv, c.n));
+    LS_TRY(mg_upload_level(h, c, rows, touched, ddiag));
+    LS_TRY(mg_level_dinv(h, c, touched, ddiag));
+    mg.levels.push_back(c);
+  }
+  if (mg.levels.back().n > kMgMaxCoarse) return LS_OK;  // not built: Jacobi fallback
+  for (size_t l = 0; l + 1 < mg.levels.size(); ++l) {
+    MgLevel &lv = mg.levels[l];
+    float est = 1.0f;
+    LS_TRY(mg_lambda_max(h, lv, &est));
+    const double lmax = 1.05 * est, lmin = est / 20.0;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    lv.lmax = est;
+    lv.inv_theta = (float)(1.0 / theta);
+    lv.c1.resize(deg);
+    lv.c2.resize(deg);
+    for (int k = 0; k < deg; ++k) {
+      const double rn = 1.0 / (2.0 * sigma - rho);
+      lv.c1[k] = (float)(rn * rho);
+      lv.c2[k] = (float)(2.0 * rn / delta);
+      rho = rn;
+    }
+  }
+  LS_TRY(mg_coarse_inverse(h, mg.levels.back()));
+  mg.built = true;
+  return LS_OK;
+}
+
+// z = V(r): levels[0].b must alias the residual, levels[0].x the output
+void mg_vcycle(ls_fd_handle *h, const int *done, cudaStream_t st) {
+  MgHierarchy &mg = h->mg;
+  const int L = (int)mg.levels.size();
+  for (int l = 0; l + 1 < L; ++l) {
+    MgLevel &lv = mg.levels[l];
+    mg_cheb_init_kernel<<<grid_for(h, lv.n), kBlock, 0, st>>>(lv.n, lv.b, lv.dinv, lv.inv_theta, lv.r, lv.d0, lv.x, done);
+    float *dc = lv.d0, *dn = lv.d1;
+    for (int k = 0; k < mg.deg; ++k) {
+      EpiArgs<float> e{};
+      e.x = lv.x;
+      e.r = lv.r;
+      e.dinv = lv.dinv;
+      e.d_out = dn;
+      e.c1 = lv.c1[k];
+      e.c2 = lv.c2[k];
+      mg_apply<EPI_CHEB>(h, lv, dc, e, done, st);
+      std::swap(dc, dn);
+    }
+    const MgLevel &cl = mg.levels[l + 1];
+    mg_restrict_kernel<<<dim3((cl.nx + 31) / 32, (cl.ny + 7) / 8, cl.nz), dim3(32, 8), 0, st>>>(
+        lv.nx, lv.ny, lv.nz, cl.nx, cl.ny, cl.nz, lv.r, cl.b, done);
+  }
+  {
+    MgLevel &cl = mg.levels[L - 1];
+    mg_dense_kernel<<<(int)((cl.n * 32 + 255) / 256), 256, 0, st>>>((int)cl.n, mg.coarse_inv64, cl.b, cl.x, done);
+  }
+  for (int l = L - 2; l >= 0; --l) {
+    MgLevel &lv = mg.levels[l];
+    const MgLevel &cl = mg.levels[l + 1];
+    mg_prolong_kernel<<<dim3((lv.nx + 31) / 32, (lv.ny + 7) / 8, lv.nz), dim3(32, 8), 0, st>>>(
+        lv.nx, lv.ny, lv.nz, cl.nx, cl.ny, cl.x, lv.x, done);
+    EpiArgs<float> e{};
+    e.r = lv.r;
+    e.b = lv.b;
+    e.dinv = lv.dinv;
+    e.d_out = lv.d0;
+    e.c2 = lv.inv_theta;
+    mg_apply<EPI_RESID>(h, lv, lv.x, e, done, st);
+    float *dc = lv.d0, *dn = lv.d1;
+    for (int k = 0; k < mg.deg; ++k) {
+      EpiArgs<float> e2{};
+      e2.x = lv.x;
+      e2.r = lv.r;
+      e2.dinv = lv.dinv;
+      e2.d_out = dn;
+      e2.c1 = lv.c1[k];
+      e2.c2 = lv.c2[k];
+      mg_apply<EPI_CHEB>(h, lv, dc, e2, done, st);
+      std::swap(dc, dn);
+    }
+  }
+}
+
+// MG-CG kernels -------------------------------------------------------------
+// x += alpha p, r -= alpha q, rrj = r . D^-1 r (stopping test only)
+__global__ void __launch_bounds__(kBlock) mg_update_xr_kernel(int64_t n, float *__restrict__ x, float *__restrict__ r,
+                                                              const float *__restrict__ p, const float *__restrict__ q,
+                                                              const float *__restrict__ dinv, CgScalars *sc,
+                                                              double *partials, unsigned int *ticket) {
+  if (sc->done) return;
+  const double pq = sc->pq_s;
+  const double alpha_d = sc->rz / pq;
+  if (!(pq > 0.0) || !isfinite(alpha_d)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = isfinite(pq) ? DONE_BREAKDOWN : DONE_NAN;
+    return;
+  }
+  const float alpha = (float)alpha_d;
+  float local = 0.f;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    x[g] += alpha * p[g];
+    const float rn = r[g] - alpha * q[g];
+    r[g] = rn;
+    local += rn * (dinv[g] * rn);
+  }
+  double rrj;
+  if (grid_sum<kBlock>((double)local, partials, ticket, &rrj)) {
+    sc->iters += 1;
+    sc->rrj = rrj;
+    if (!isfinite(rrj)) sc->done = DONE_NAN;
+    else if (rrj < sc->thresh2) sc->done = DONE_CONVERGED;
+    else if (sc->iters >= sc->maxiter) sc->done = DONE_MAXITER;
+  }
+}
+
+// rz' = r . z ; beta = rz'/rz (set_only: just rz = rz')
+__global__ void __launch_bounds__(kBlock) mg_rz_kernel(int64_t n, const float *__restrict__ r,
+                                                       const float *__restrict__ z, CgScalars *sc, double *partials,
+                                                       unsigned int *ticket, int set_only) {
+  if (!set_only && sc->done) return;
+  float local = 0.f;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+    local += r[g] * z[g];
+  double rz;
+  if (grid_sum<kBlock>((double)local, partials, ticket, &rz)) {
+    if (!set_only) sc->beta = rz / sc->rz;
+    sc->rz = rz;
+    if (!isfinite(rz)) sc->done = DONE_NAN;
+  }
+}
+
+// p = z + beta p  (or p = z)
+__global__ void mg_update_p_kernel(int64_t n, const float *__restrict__ z, float *__restrict__ p, const CgScalars *sc,
+                                   int reset) {
+  if (!reset && sc->done) return;
+  const float beta = reset ? 0.f : (float)sc->beta;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
+    p[g] = z[g] + beta * (reset ? 0.f : p[g]);
+}
+
+void mg_iteration(ls_fd_handle *h, cudaStream_t st) {
+  launch_apply32(h, h->p32, h->q32, true, st);
+  const int g = grid_for(h, h->n);
+  mg_update_xr_kernel<<<g, kBlock, 0, st>>>(h->n, h->x32, h->r32, h->p32, h->q32, h->dinv32, h->sc, h->partials,
+                                            h->tickets + T_UPDATE);
+  mg_vcycle(h, &h->sc->done, st);
+  mg_rz_kernel<<<g, kBlock, 0, st>>>(h->n, h->r32, h->z32, h->sc, h->partials, h->tickets + T_UPDATE, 0);
+  mg_update_p_kernel<<<g, kBlock, 0, st>>>(h->n, h->z32, h->p32, h->sc, 0);
+}
+
+// after a residual refresh: z = V(r), rz = r.z, optionally p = z
+int mg_restart(ls_fd_handle *h, bool reset_p) {
+  cudaStream_t st = h->stream;
+  const int g = grid_for(h, h->n);
+  mg_vcycle(h, nullptr, st);
+  mg_rz_kernel<<<g, kBlock, 0, st>>>(h->n, h->r32, h->z32, h->sc, h->partials, h->tickets + T_UPDATE, 1);
+  if (reset_p) mg_update_p_kernel<<<g, kBlock, 0, st>>>(h->n, h->z32, h->p32, h->sc, 1);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
+
 }  // namespace
 }  // namespace ls
 
@@ -453,8 +945,9 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
   }
   h->red_blocks = sm_count() * 8;
   {
-    const size_t gxy = (size_t)((g.nsteps[0] + 31) / 32) * (size_t)((g.nsteps[1] + 7) / 8);
-    const size_t nb = std::max<size_t>((size_t)h->red_blocks, gxy);
+    const int zc = apply_zchunk((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], sm_count());
+    const dim3 ag = apply_grid((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], zc);
+    const size_t nb = std::max<size_t>((size_t)h->red_blocks, (size_t)ag.x * ag.y * ag.z);
     if ((st = dev_alloc(&h->partials, 4 * nb)) < 0) return fail(st);
   }
   if ((st = dev_alloc(&h->tickets, T_COUNT)) < 0) return fail(st);
@@ -523,14 +1016,30 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
     w2_64[r] = wv[r] * wv[r];
     w2_32[r] = (float)w2_64[r];
   }
+  h->h_idc = idc;
+  h->h_a = av;
+  h->h_w2 = w2_64;
+  h->h_width = d.width;
   d.ntouched = (int64_t)touched.size();
   const int64_t ni = (int64_t)inc.size();
+  const int64_t nwords = (n + 31) / 32;
+  std::vector<uint32_t> mask(nwords, 0u);
+  std::vector<int32_t> word_rank(nwords, 0);
+  for (int64_t t : touched) mask[t >> 5] |= 1u << (t & 31);
+  {
+    int32_t run = 0;
+    for (int64_t w = 0; w < nwords; ++w) {
+      word_rank[w] = run;
+      run += __builtin_popcount(mask[w]);
+    }
+  }
   if ((st = dev_alloc(&d.cols, ne)) < 0 || (st = dev_alloc(&d.a64, ne)) < 0 || (st = dev_alloc(&d.a32, ne)) < 0 ||
       (st = dev_alloc(&d.w2_64, d.nrows)) < 0 || (st = dev_alloc(&d.w2_32, d.nrows)) < 0 ||
       (st = dev_alloc(&d.b, d.nrows)) < 0 || (st = dev_alloc(&d.touched, d.ntouched)) < 0 ||
       (st = dev_alloc(&d.inc_ptr, d.ntouched + 1)) < 0 || (st = dev_alloc(&d.inc_row, ni)) < 0 ||
       (st = dev_alloc(&d.inc_a64, ni)) < 0 || (st = dev_alloc(&d.inc_a32, ni)) < 0 ||
-      (st = dev_alloc(&h->s64, d.nrows)) < 0 || (st = dev_alloc(&h->s32, d.nrows)) < 0)
+      (st = dev_alloc(&h->s64, d.nrows)) < 0 || (st = dev_alloc(&h->s32, d.nrows)) < 0 ||
+      (st = dev_alloc(&d.mask, nwords)) < 0 || (st = dev_alloc(&d.word_rank, nwords)) < 0)
     return fail(st);
   cudaStream_t hs = h->stream;
 #define UP(dst, src, cnt)                                                                                        \
@@ -550,6 +1059,8 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
   UP(d.inc_row, irow, ni);
   UP(d.inc_a64, ia64, ni);
   UP(d.inc_a32, ia32, ni);
+  UP(d.mask, mask, nwords);
+  UP(d.word_rank, word_rank, nwords);
 #undef UP
   // ---- rhs, diagonal, inverse diagonal ----
   const int gn = grid_for(h, n);
@@ -576,10 +1087,13 @@ extern "C" int ls_fd_destroy(ls_fd_handle *h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->g64) cudaGraphExecDestroy(h->g64);
   if (h->g32) cudaGraphExecDestroy(h->g32);
+  if (h->gmg) cudaGraphExecDestroy(h->gmg);
+  for (void *p : h->mg.allocations) cudaFree(p);
+  if (h->z32) cudaFree(h->z32);
   void *ptrs[] = {h->rhs, h->diag, h->dinv64, h->dinv32, h->x64, h->r64, h->p64, h->q64, h->s64, h->x32, h->r32,
                   h->p32, h->q32, h->s32, h->sc, h->partials, h->tickets, h->data.cols, h->data.a64, h->data.a32,
                   h->data.w2_64, h->data.w2_32, h->data.b, h->data.touched, h->data.inc_ptr, h->data.inc_row,
-                  h->data.inc_a64, h->data.inc_a32};
+                  h->data.inc_a64, h->data.inc_a32, h->data.mask, h->data.word_rank};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->sc_h) cudaFreeHost(h->sc_h);
@@ -644,6 +1158,11 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
   stats->rhs_norm = bnorm;
   stats->threshold = thresh;
 
+  bool use_mg = false;
+  if (opts->precision == LS_MIXED && opts->preconditioner == LS_PRECOND_MG && bnorm > 0.0) {
+    LS_TRY(mg_build(h, 3));
+    use_mg = h->mg.built;
+  }
   LS_CUDA_TRY(cudaEventRecord(h->ev0, st));
   if (opts->use_x0)
     LS_CUDA_TRY(cudaMemcpyAsync(h->x64, d_x, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
@@ -652,6 +1171,69 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
   CgScalars &s = *h->sc_h;
   int status = LS_OK;
   long long iters = 0, updates = 0;
+
+  // FP32 Jacobi-CG on the correction, FP64 residual refreshed whenever the
+  // recurrence residual fell by `delta` (reliable updates).  Also the
+  // fallback after a multigrid breakdown (then started from x64).
+  auto run_mixed_jacobi = [&](bool have_x) -> int {
+    LS_TRY(refresh(h, have_x, h->r32, h->p32));  // r64, r32, p32, x32 = 0
+    LS_TRY(read_scalars(h));
+    double true_r = sqrt(std::max(s.rz64, 0.0));
+    if (true_r < thresh) {
+      status = LS_OK;
+      return LS_OK;
+    }
+    const long long iters0 = iters;
+    s.rz = s.rz32;
+    s.pq_s = s.pq_d = 0.0;
+    s.thresh2 = thresh * thresh;
+    s.iters = iters0;
+    s.maxiter = maxiter;
+    s.done = 0;
+    LS_TRY(write_scalars(h));
+    if (!h->g32 || h->g32_batch != batch) {
+      if (h->g32) cudaGraphExecDestroy(h->g32);
+      h->g32 = nullptr;
+      LS_TRY(build_graph<float>(h, batch, &h->g32, h->x32, h->r32, h->p32, h->q32, h->dinv32));
+      h->g32_batch = batch;
+    }
+    double rz_ref = s.rz32;
+    for (;;) {
+      LS_CUDA_TRY(cudaGraphLaunch(h->g32, st));
+      LS_TRY(read_scalars(h));
+      const bool trigger = s.done != 0 || s.rz < delta * delta * rz_ref;
+      if (!trigger) continue;
+      if (s.done == DONE_NAN || s.done == DONE_BREAKDOWN) {
+        status = done_to_status(s.done);
+        break;
+      }
+      // reliable update
+      fold_kernel<<<grid_for(h, n), kBlock, 0, st>>>(n, h->x64, h->x32);
+      LS_TRY(refresh(h, true, h->r32, nullptr));
+      const long long it_now = s.iters;
+      LS_TRY(read_scalars(h));
+      ++updates;
+      true_r = sqrt(std::max(s.rz64, 0.0));
+      if (true_r < thresh) {
+        status = LS_OK;
+        break;
+      }
+      if (it_now >= maxiter) {
+        status = LS_NOT_CONVERGED;
+        break;
+      }
+      if (!isfinite(true_r)) {
+        status = LS_NAN;
+        break;
+      }
+      s.rz = s.rz32;
+      s.done = 0;
+      rz_ref = s.rz32;
+      LS_TRY(write_scalars(h));
+    }
+    iters = s.iters;
+    return LS_OK;
+  };
 
   if (bnorm == 0.0) {  // scipy returns b (= 0) immediately
     LS_CUDA_TRY(cudaMemsetAsync(h->x64, 0, n * sizeof(double), st));
@@ -677,37 +1259,51 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
     }
     iters = s.iters;
     status = done_to_status(s.done);
-  } else {
-    // FP32 CG on the correction, FP64 residual refreshed whenever the
-    // recurrence residual fell by `delta` (reliable updates).
-    LS_TRY(refresh(h, opts->use_x0 != 0, h->r32, h->p32));  // r64, r32, p32, x32 = 0
+  } else if (use_mg) {
+    // FP32 CG with the multigrid V-cycle as preconditioner; FP64 reliable
+    // updates as below.  Stopping test on the Jacobi-scaled residual.
+    LS_TRY(refresh(h, opts->use_x0 != 0, h->r32, nullptr));  // r64, r32, x32 = 0
     LS_TRY(read_scalars(h));
     double true_r = sqrt(std::max(s.rz64, 0.0));
     if (!(true_r < thresh)) {
-      s.rz = s.rz32;
+      s.done = 0;
+      s.iters = 0;
+      LS_TRY(write_scalars(h));
+      LS_TRY(mg_restart(h, true));
+      LS_TRY(read_scalars(h));
       s.pq_s = s.pq_d = 0.0;
       s.thresh2 = thresh * thresh;
       s.iters = 0;
       s.maxiter = maxiter;
       s.done = 0;
+      s.rrj = s.rz32;
       LS_TRY(write_scalars(h));
-      if (!h->g32 || h->g32_batch != batch) {
-        if (h->g32) cudaGraphExecDestroy(h->g32);
-        h->g32 = nullptr;
-        LS_TRY(build_graph<float>(h, batch, &h->g32, h->x32, h->r32, h->p32, h->q32, h->dinv32));
-        h->g32_batch = batch;
+      const int mbatch = std::max(1, std::min(batch, 8));
+      if (!h->gmg || h->gmg_batch != mbatch) {
+        if (h->gmg) cudaGraphExecDestroy(h->gmg);
+        h->gmg = nullptr;
+        LS_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int it = 0; it < mbatch; ++it) mg_iteration(h, st);
+        cudaGraph_t graph;
+        LS_CUDA_TRY(cudaStreamEndCapture(st, &graph));
+        cudaError_t e = cudaGraphInstantiate(&h->gmg, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+          set_error("cudaGraphInstantiate: %s", cudaGetErrorString(e));
+          return LS_ERR_CUDA;
+        }
+        h->gmg_batch = mbatch;
       }
-      double rz_ref = s.rz32;
+      double rrj_ref = s.rz32;
       for (;;) {
-        LS_CUDA_TRY(cudaGraphLaunch(h->g32, st));
+        LS_CUDA_TRY(cudaGraphLaunch(h->gmg, st));
         LS_TRY(read_scalars(h));
-        const bool trigger = s.done != 0 || s.rz < delta * delta * rz_ref;
+        const bool trigger = s.done != 0 || s.rrj < delta * delta * rrj_ref;
         if (!trigger) continue;
         if (s.done == DONE_NAN || s.done == DONE_BREAKDOWN) {
           status = done_to_status(s.done);
           break;
         }
-        // reliable update
         fold_kernel<<<grid_for(h, n), kBlock, 0, st>>>(n, h->x64, h->x32);
         LS_TRY(refresh(h, true, h->r32, nullptr));
         const long long it_now = s.iters;
@@ -726,13 +1322,25 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
           status = LS_NAN;
           break;
         }
-        s.rz = s.rz32;
         s.done = 0;
-        rz_ref = s.rz32;
+        LS_TRY(write_scalars(h));
+        LS_TRY(mg_restart(h, false));
+        LS_TRY(read_scalars(h));
+        s.done = 0;
+        s.rrj = s.rz32;
+        rrj_ref = s.rz32;
         LS_TRY(write_scalars(h));
       }
       iters = s.iters;
     }
+    if (status == LS_NAN || status == LS_BREAKDOWN) {
+      // the V-cycle lost definiteness in FP32: finish with Jacobi from x64
+      use_mg = false;
+      status = LS_OK;
+      LS_TRY(run_mixed_jacobi(true));
+    }
+  } else {
+    LS_TRY(run_mixed_jacobi(opts->use_x0 != 0));
   }
   // final FP64 residual of the returned iterate
   LS_TRY(refresh(h, true, nullptr, nullptr));
@@ -746,6 +1354,7 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
   stats->residual = sqrt(std::max(s.rz64, 0.0));
   stats->device_ms = ms;
   stats->status = status;
+  stats->preconditioner = use_mg ? LS_PRECOND_MG : LS_PRECOND_JACOBI;
   LS_CUDA_TRY(cudaGetLastError());
   return status;
 }
@@ -792,19 +1401,25 @@ extern "C" int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps,
   const int g = grid_for(h, n);
   const DataTerm &d = h->data;
   LS_TRY(timed([&] {
-    if (f32) stencil_kernel<float><<<stencil_grid(h), dim3(kTX, kTY), 0, st>>>(coef_as<float>(h->coef), h->p32, h->q32, h->sc, h->partials, h->tickets + T_STENCIL, false);
-    else stencil_kernel<double><<<stencil_grid(h), dim3(kTX, kTY), 0, st>>>(coef_as<double>(h->coef), h->p64, h->q64, h->sc, h->partials, h->tickets + T_STENCIL, false);
+    if (f32) {
+      EpiArgs<float> e{};
+      e.q = h->q32;
+      const int zc = apply_zchunk((int)h->coef.nx, (int)h->coef.ny, (int)h->coef.nz, sm_count());
+      fd_apply_kernel<float, EPI_STORE><<<apply_grid((int)h->coef.nx, (int)h->coef.ny, (int)h->coef.nz, zc), dim3(kAX, kAY), 0, st>>>(
+          coef_as<float>(h->coef), h->p32, data_view<float>(h, h->s32, d.inc_a32), e, zc, nullptr, h->partials, h->tickets + T_STENCIL, &h->sc->pq_s);
+    } else {
+      EpiArgs<double> e{};
+      e.q = h->q64;
+      const int zc = apply_zchunk((int)h->coef.nx, (int)h->coef.ny, (int)h->coef.nz, sm_count());
+      fd_apply_kernel<double, EPI_STORE><<<apply_grid((int)h->coef.nx, (int)h->coef.ny, (int)h->coef.nz, zc), dim3(kAX, kAY), 0, st>>>(
+          coef_as<double>(h->coef), h->p64, data_view<double>(h, h->s64, d.inc_a64), e, zc, nullptr, h->partials, h->tickets + T_STENCIL, &h->sc->pq_s);
+    }
   }, &out->stencil_ms));
   out->data_ms = 0.0;
   if (d.nrows > 0) {
     LS_TRY(timed([&] {
-      if (f32) {
-        data_rows_kernel<float><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, d.a32, d.w2_32, h->p32, h->s32, h->sc, h->partials + 2 * h->red_blocks, h->tickets + T_DATA, false);
-        data_nodes_kernel<float><<<grid_for(h, d.ntouched), kBlock, 0, st>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row, d.inc_a32, h->s32, h->q32, h->sc, false);
-      } else {
-        data_rows_kernel<double><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, d.a64, d.w2_64, h->p64, h->s64, h->sc, h->partials + 2 * h->red_blocks, h->tickets + T_DATA, false);
-        data_nodes_kernel<double><<<grid_for(h, d.ntouched), kBlock, 0, st>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row, d.inc_a64, h->s64, h->q64, h->sc, false);
-      }
+      if (f32) rows_kernel<float><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, d.a32, d.w2_32, h->p32, h->s32, nullptr);
+      else rows_kernel<double><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, d.a64, d.w2_64, h->p64, h->s64, nullptr);
     }, &out->data_ms));
   }
   LS_TRY(timed([&] {

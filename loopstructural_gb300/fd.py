@@ -174,7 +174,7 @@ class FdSystem:
         return y
 
     def solve(self, x=None, atol=0.0, rtol=1e-5, maxiter=None, precision="mixed", reliable_delta=0.1,
-              check_every=64):
+              check_every=64, preconditioner="mg"):
         """Returns (x device tensor, stats dict)."""
         torch = _torch()
         o = _lib.SolveOpts()
@@ -190,10 +190,14 @@ class FdSystem:
         o.maxiter = int(maxiter) if maxiter is not None else 0
         o.reliable_delta = float(reliable_delta)
         o.check_every = int(check_every)
+        if preconditioner not in ("mg", "jacobi"):
+            raise ValueError(f"preconditioner must be 'mg' or 'jacobi', not {preconditioner!r}")
+        o.preconditioner = _lib.LS_PRECOND_MG if preconditioner == "mg" else _lib.LS_PRECOND_JACOBI
         st = _lib.SolveStats()
         status = self.lib.ls_fd_solve(self.handle, C.byref(o), _lib.ptr(x), C.byref(st), _lib.stream_ptr())
         _lib.check(status, allow_positive=True)
-        stats = {k: getattr(st, k) for k, _ in _lib.SolveStats._fields_ if k != "reserved"}
+        stats = {k: getattr(st, k) for k, _ in _lib.SolveStats._fields_}
+        stats["preconditioner"] = "mg" if st.preconditioner == _lib.LS_PRECOND_MG else "jacobi"
         return x, stats
 
 

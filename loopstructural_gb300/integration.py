@@ -1,0 +1,104 @@
+"""Drop-in registration into the reference's loop_interpolation package.
+
+    import loop_interpolation as li
+    from loopstructural_gb300.integration import gpu_interpolator_classes, register
+    register(li)   # FINITE_DIFFERENCE now builds GPU interpolators
+
+``gpu_interpolator_classes(li)`` returns a subclass of the reference's own
+``FiniteDifferenceInterpolator`` that keeps every setter, getter, weight
+dictionary, bounding-box projection and serialisation method of the reference
+and overrides only the hot path, delegating to the GB300 engine:
+
+  setup_interpolator     (_finite_difference_interpolator.py:132-224)
+  solve_system           (_discrete_interpolator.py:1221-1319)
+  _evaluate_value_local / _evaluate_gradient_local (_discrete_interpolator.py:1342-1379)
+
+The reference setters have already projected the data into the local frame,
+so the engine receives ``self.data`` as is.
+"""
+from __future__ import annotations
+
+from types import SimpleNamespace
+
+import numpy as np
+
+from . import interpolators, supports
+
+
+def _grid_of(support):
+    return supports.StructuredGrid(origin=np.asarray(support.origin, dtype=float),
+                                   nsteps_cells=np.asarray(support.nsteps_cells, dtype=int),
+                                   step_vector=np.asarray(support.step_vector, dtype=float))
+
+
+def gpu_interpolator_classes(li):
+    """Subclasses of the reference interpolators with the GPU hot path."""
+    base = li.FiniteDifferenceInterpolator
+
+    class GpuFiniteDifferenceInterpolator(base):
+        """Reference FiniteDifferenceInterpolator with GB300 assembly, solve and evaluation."""
+
+        def _engine(self):
+            eng = getattr(self, "_gb300_engine", None)
+            grid = _grid_of(self.support)
+            if eng is None or eng.support.n_nodes != grid.n_nodes or not np.array_equal(
+                    eng.support.origin, grid.origin) or not np.array_equal(eng.support.step_vector, grid.step_vector):
+                eng = interpolators.FiniteDifferenceInterpolator(grid)
+                self._gb300_engine = eng
+            return eng
+
+        def setup_interpolator(self, **kwargs):
+            eng = self._engine()
+            eng.data = {k: np.array(v, dtype=float) for k, v in self.data.items()}
+            eng.interpolation_weights = dict(self.interpolation_weights)
+            for attr in ("interface_pair_mode", "interface_pair_threshold", "interface_pair_fallback"):
+                if hasattr(self, attr):
+                    setattr(eng, attr, getattr(self, attr))
+            eng.ridge_factor = self.ridge_factor
+            eng.add_ridge_regulatisation = self.add_ridge_regulatisation
+            eng.setup_interpolator(**kwargs)
+            self.interpolation_weights = dict(eng.interpolation_weights)
+            # row counts for the reference's diagnostics report (matrix shape only)
+            self.constraints = {}
+            for name, fam in eng.constraints.items():
+                self.constraints[name] = {"matrix": SimpleNamespace(shape=(fam.n_rows, self.dof)), "b": None,
+                                          "w": fam.w.cpu().numpy()}
+            for name, (rows, w) in eng.regularisation_families.items():
+                self.constraints[name] = {"matrix": SimpleNamespace(shape=(rows, self.dof)), "b": None,
+                                          "w": np.full(rows, w)}
+            self.up_to_date = False
+            return self.finalize_setup_diagnostics_report()
+
+        def solve_system(self, solver=None, tol=None, solver_kwargs=None):
+            eng = self._engine()
+            ok = eng.solve_system(solver, tol, solver_kwargs)
+            self.c = np.array(eng.c)
+            self.latest_solve_timing = eng.get_last_solve_timing()
+            self.up_to_date = bool(ok)
+            return self.up_to_date
+
+        def _sync_engine_c(self, eng):
+            if eng._c is not self.c and (eng._c.shape != np.shape(self.c) or not np.array_equal(eng._c, self.c)):
+                eng.c = np.array(self.c, dtype=float)
+            eng.up_to_date = True
+
+        def _evaluate_value_local(self, locations):
+            self.update()
+            eng = self._engine()
+            self._sync_engine_c(eng)
+            return eng._evaluate_value_local(np.asarray(locations, dtype=float))
+
+        def _evaluate_gradient_local(self, locations):
+            self.update()
+            eng = self._engine()
+            self._sync_engine_c(eng)
+            return eng._evaluate_gradient_local(np.asarray(locations, dtype=float))
+
+    return (GpuFiniteDifferenceInterpolator,)
+
+
+def register(li):
+    """Point the reference factory's FINITE_DIFFERENCE entry at the GPU class."""
+    (gpu_fd,) = gpu_interpolator_classes(li)
+    li.interpolator_map[li.InterpolatorType.FINITE_DIFFERENCE] = gpu_fd
+    return gpu_fd

@@ -227,6 +227,7 @@ class _DiscreteInterpolatorBase:
             "precision": kw.pop("precision", "mixed"),
             "reliable_delta": float(kw.pop("reliable_delta", 0.1)),
             "check_every": int(kw.pop("check_every", 64)),
+            "preconditioner": kw.pop("preconditioner", "mg"),
         }
         x0 = kw.pop("x0", None)
         if callable(x0):
@@ -272,7 +273,8 @@ class _DiscreteInterpolatorBase:
         self._c = x.cpu().numpy()
         timing.update({"iterations": int(stats["iterations"]), "reliable_updates": int(stats["reliable_updates"]),
                        "residual": stats["residual"], "threshold": stats["threshold"],
-                       "device_ms": stats["device_ms"], "precision": opts["precision"], "status": int(status)})
+                       "device_ms": stats["device_ms"], "precision": opts["precision"], "status": int(status),
+                       "preconditioner": stats["preconditioner"]})
         self.up_to_date = True
         timing["total_seconds"] = perf_counter() - solve_started
         timing["up_to_date"] = True

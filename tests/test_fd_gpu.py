@@ -231,3 +231,49 @@ def test_edge_cases():
     # empty evaluation
     assert interp.evaluate_value(np.zeros((0, 3))).shape == (0,)
     assert interp.evaluate_gradient(np.zeros((0, 3))).shape == (0, 3)
+
+
+def _synthetic(n_nodes, n_val, n_nrm, seed=0):
+    rng = np.random.default_rng(seed)
+    cells = np.array([n_nodes - 1] * 3)
+    vp = rng.uniform(0, 1, size=(n_val, 3))
+    val = np.column_stack([vp, vp[:, 2] + 0.1 * np.sin(2 * np.pi * vp[:, 0]) + 0.2 * (vp[:, 0] > 0.5), np.ones(n_val)])
+    npnt = rng.uniform(0, 1, size=(n_nrm, 3))
+    g = np.column_stack([0.2 * np.pi * np.cos(2 * np.pi * npnt[:, 0]), np.zeros(n_nrm), np.ones(n_nrm)])
+    nrm = np.column_stack([npnt, g + rng.normal(0, 0.02, g.shape), np.ones(n_nrm)])
+    return cells, val, nrm
+
+
+@pytest.mark.parametrize("n_nodes", [21, 34])
+def test_multigrid_matches_jacobi_solution_with_fewer_iterations(n_nodes):
+    """The MG preconditioner changes only the iteration path: the FP32+FP64
+    MG solve lands on the FP64 Jacobi solve (1e-8) in far fewer iterations."""
+    cells, val, nrm = _synthetic(n_nodes, 400, 100)
+    out = {}
+    for prec, pc in (("fp64", "jacobi"), ("mixed", "mg"), ("mixed", "jacobi")):
+        interp = L.FiniteDifferenceInterpolator(_grid(cells))
+        interp.set_value_constraints(val)
+        interp.set_normal_constraints(nrm)
+        interp.setup_interpolator(regularisation=0.1, cpw=1.0, npw=1.0)
+        interp.solve_system("cg", solver_kwargs={"rtol": 1e-13, "atol": 0.0, "precision": prec,
+                                                 "preconditioner": pc, "maxiter": 500000})
+        t = interp.get_last_solve_timing()
+        assert t["status"] == 0 and t["preconditioner"] == (pc if prec == "mixed" else "jacobi")
+        out[(prec, pc)] = (interp.c.copy(), t["iterations"])
+    ref = out[("fp64", "jacobi")][0]
+    for key in (("mixed", "mg"), ("mixed", "jacobi")):
+        err = np.linalg.norm(out[key][0] - ref) / np.linalg.norm(ref)
+        assert err <= 1e-8, (key, err)
+    assert out[("mixed", "mg")][1] * 5 < out[("fp64", "jacobi")][1], {k: v[1] for k, v in out.items()}
+
+
+def test_multigrid_falls_back_to_jacobi_on_thin_grids():
+    cells = np.array([30, 30, 2])
+    interp = L.FiniteDifferenceInterpolator(_grid(cells))
+    rng = np.random.default_rng(1)
+    vp = rng.uniform(0, 1, size=(100, 3))
+    interp.set_value_constraints(np.column_stack([vp, vp[:, 0]]))
+    interp.setup_interpolator(regularisation=0.1)
+    assert interp.solve_system("cg", solver_kwargs={"rtol": 1e-10, "preconditioner": "mg"})
+    t = interp.get_last_solve_timing()
+    assert t["preconditioner"] == "jacobi" and t["status"] == 0

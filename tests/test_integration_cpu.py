@@ -1,0 +1,68 @@
+"""Registration of the GPU interpolator into the reference's own factory.
+
+Needs the reference's loop_interpolation package importable (only where the
+reference source is available); the compute path itself needs a GPU and is
+covered by the -m gpu tests, so here it must fail loudly."""
+import os
+import sys
+import types
+
+import numpy as np
+import pytest
+
+REF = os.environ.get("LOOPSTRUCTURAL_REFERENCE", "/root/reference")
+
+
+@pytest.fixture(scope="module")
+def li():
+    if not os.path.isdir(os.path.join(REF, "packages", "loop_interpolation")):
+        pytest.skip("reference source not available")
+    for name in ("pyvista", "yaml"):
+        if name not in sys.modules:
+            try:
+                __import__(name)
+            except Exception:
+                sys.modules[name] = types.ModuleType(name)
+    for sub in ("loop_common", "loop_interpolation"):
+        p = os.path.join(REF, "packages", sub, "src")
+        if p not in sys.path:
+            sys.path.append(p)
+    import loop_interpolation
+
+    return loop_interpolation
+
+
+def test_factory_builds_gpu_subclass(li):
+    from loop_common.geometry import BoundingBox
+
+    from loopstructural_gb300 import integration
+
+    saved = li.interpolator_map[li.InterpolatorType.FINITE_DIFFERENCE]
+    try:
+        gpu_cls = integration.register(li)
+        assert issubclass(gpu_cls, li.FiniteDifferenceInterpolator)
+        bb = BoundingBox(origin=np.zeros(3), maximum=np.ones(3))
+        interp = li.InterpolatorFactory.create_interpolator("FDI", boundingbox=bb, nelements=1000)
+        assert isinstance(interp, gpu_cls)
+        # the reference setters, projection and weights are inherited unchanged
+        interp.set_value_constraints(np.array([[0.5, 0.5, 0.5, 1.0], [0.2, 0.3, 0.4, 0.0]]))
+        assert interp.get_value_constraints().shape == (2, 5)
+        assert interp.interpolation_weights["npw"] == 10.0
+    finally:
+        li.interpolator_map[li.InterpolatorType.FINITE_DIFFERENCE] = saved
+
+
+def test_gpu_subclass_fails_loudly_without_gpu(li):
+    import torch
+
+    import loopstructural_gb300 as L
+    from loopstructural_gb300 import integration
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    (gpu_cls,) = integration.gpu_interpolator_classes(li)
+    grid = li.StructuredGrid(origin=np.zeros(3), nsteps=np.array([5, 5, 5]), step_vector=np.ones(3) * 0.2)
+    interp = gpu_cls(grid)
+    interp.set_value_constraints(np.array([[0.5, 0.5, 0.5, 1.0]]))
+    with pytest.raises(L.ExtensionUnavailable):
+        interp.setup_interpolator(regularisation=0.1)
