@@ -1,11 +1,18 @@
 #!/usr/bin/env python
 """Benchmark: FD solve + evaluate at 200^3 nodes on one GB300.
 
-Workload (one "step"): the mixed-precision (FP32 CG + FP64 reliable updates)
-Jacobi-CG solve of the FD normal equations of a 200x200x200-node
-StructuredGrid (8,000,000 DOF) constrained by 20,000 value points and 5,000
-noisy normals of a faulted layered field, followed by value + gradient
-evaluation on a 256^3 lattice.  Synthetic, seeded inputs (no dataset).
+Workload (one "step"): the mixed-precision solve (FP32 CG preconditioned by a
+geometric-multigrid V-cycle, FP64 reliable updates) of the FD normal
+equations of a 200x200x200-node StructuredGrid (8,000,000 DOF) constrained by
+20,000 value points and 5,000 noisy normals of a faulted layered field,
+followed by value + gradient evaluation on a 256^3 lattice.  Synthetic,
+seeded inputs (no dataset).
+
+After the timed steps the same system is solved once by plain FP64
+Jacobi-CG on the GPU (the straightforward GPU port of the reference's
+iteration) to rtol 1e-12; the line reports its time, the speed-up of the
+mixed step, and the relative field error of the mixed solution against it on
+the 64^3 subsample (every 4th point) of the 256^3 lattice.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -158,10 +165,13 @@ def gpu_arm(args, rank, world):
     system = interp._build_system()
     lo, hs, ln = lattice_points()
     solve_kw = dict(atol=0.0, rtol=args.rtol, precision="mixed", maxiter=args.maxiter)
+    last = {}
 
     def step():
         x, st = system.solve(**solve_kw)
         v, g = fd.eval_lattice(grid, x, lo, hs, ln)
+        st["kernel_launches"] += 1  # the lattice evaluation kernel
+        last["x"] = x
         return st
 
     def barrier():
@@ -188,6 +198,27 @@ def gpu_arm(args, rank, world):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     iters = int(np.mean([s["iterations"] for s in stats]))
+    launches = int(sum(s["kernel_launches"] for s in stats))
+    out_solve_ms = float(np.mean([s["device_ms"] for s in stats]))
+    x_mixed = last["x"]
+
+    # FP64 GPU leg: plain FP64 Jacobi-CG (the iteration of the reference's
+    # column-scaled CG) to the same rtol, timed; then continued to rtol 1e-12
+    # (untimed) as the tight reference for the field error of the mixed
+    # solution on the 64^3 subsample of the 256^3 lattice
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    x64, st64 = system.solve(atol=0.0, rtol=args.rtol, precision="fp64", maxiter=args.maxiter)
+    f1.record()
+    torch.cuda.synchronize()
+    fp64_s = f0.elapsed_time(f1) / 1e3
+    x64, st64t = system.solve(x=x64, atol=0.0, rtol=1e-12, precision="fp64", maxiter=args.maxiter)
+    sub_step = tuple(4 * h for h in hs)
+    v_mix, _ = fd.eval_lattice(grid, x_mixed, lo, sub_step, (64, 64, 64), gradient=False)
+    v_ref, _ = fd.eval_lattice(grid, x64, lo, sub_step, (64, 64, 64), gradient=False)
+    field_err = float(torch.linalg.norm(v_mix - v_ref) / torch.linalg.norm(v_ref))
+    coef_err = float(torch.linalg.norm(x_mixed - x64) / torch.linalg.norm(x64))
 
     # dominant-kernel roofline from CUDA-event timings of each kernel class
     prof = fd.profile_iteration(system, "mixed", reps=50)
@@ -248,9 +279,15 @@ def gpu_arm(args, rank, world):
             "parallelism": "replicas" if world > 1 else "single GPU",
         },
         "solve": {"iterations": iters, "reliable_updates": int(np.mean([s["reliable_updates"] for s in stats])),
+                  "preconditioner": stats[-1]["preconditioner"], "solve_ms": float(np.mean([s["device_ms"] for s in stats])),
                   "residual": stats[-1]["residual"], "threshold": stats[-1]["threshold"],
-                  "iteration_ms": prof["iteration_ms"], "iteration_GBps": round(it_gbs, 1),
-                  "dof_iterations_per_s": system.n * iters / (ms / 1e3)},
+                  "ms_per_iteration": float(np.mean([s["device_ms"] for s in stats])) / max(iters, 1)},
+        "fp64_gpu": {"solve_s": round(fp64_s, 3), "iterations": int(st64["iterations"]), "status": int(st64["status"]),
+                     "rtol": args.rtol, "preconditioner": "jacobi",
+                     "speedup_of_mixed_solve": round(fp64_s / (out_solve_ms / 1e3), 2),
+                     "tight_reference": {"rtol": 1e-12, "extra_iterations": int(st64t["iterations"])},
+                     "field_rel_error_64cubed": field_err, "coef_rel_error": coef_err},
+        "jacobi_cg_iteration": {"iteration_ms": prof["iteration_ms"], "iteration_GBps": round(it_gbs, 1)},
         "kernels_ms": {k: prof[k] for k in ("stencil_ms", "data_ms", "update_ms", "iteration_ms")},
         "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
@@ -259,12 +296,13 @@ def gpu_arm(args, rank, world):
         "gpu_launches": None,
         "clocks": clk.summary(),
     }
-    # kernel launches per step: setup-free solve = per iteration 5 (stencil, data rows, data nodes,
-    # update x/r, update p) + per reliable update 5; eval 1
-    upd = out["solve"]["reliable_updates"]
-    out["gpu_launches"] = int(args.steps * (5 * iters + 6 * upd + 8 + 1))
+    # counted by the solver: direct launches plus the kernel nodes of every
+    # CUDA-graph launch (iterations past convergence inside the last graph
+    # launch return at once but are counted), plus the evaluation kernel
+    out["gpu_launches"] = launches
     if args.cpu_baseline and rank == 0:
-        out["cpu_baseline"] = cpu_baseline(iters, args.rtol)
+        # the reference's CG is the Jacobi iteration: its count is the FP64 leg's
+        out["cpu_baseline"] = cpu_baseline(int(st64["iterations"]), args.rtol)
     system.close()
     return out
 
@@ -306,7 +344,8 @@ def cpu_baseline(gpu_iters, rtol):
     r = cpu_reference_sample(rtol)
     total = r["s_per_iteration"] * gpu_iters + r["eval_s"]
     return {"value": round(total, 3), "unit": "s", "cores": 1, "kind": "port",
-            "sample": r["sample"] + f"; x {gpu_iters} iterations (the GPU solve's count at rtol {rtol:g})"}
+            "sample": r["sample"] + f"; x {gpu_iters} iterations (extrapolated: the FP64 Jacobi-CG count on the GPU "
+                                    f"at rtol {rtol:g}, the reference's iteration)"}
 
 
 def reference_arm(args, rank, world):
@@ -349,7 +388,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--rtol", type=float, default=1e-12)
+    ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--maxiter", type=int, default=400_000)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()

@@ -203,6 +203,7 @@ typedef struct ls_solve_stats {
   double device_ms;         /* device time of the solve (CUDA events) */
   int32_t status;
   int32_t preconditioner;   /* ls_preconditioner actually used */
+  int64_t kernel_launches;  /* kernels launched by this call (graph launches count their kernel nodes) */
 } ls_solve_stats;
 
 /* Jacobi-preconditioned CG on the normal equations -- the iteration of the
@@ -241,6 +242,39 @@ int ls_fd_eval_points(const ls_grid3 *grid, const double *d_c, const double *d_p
 int ls_fd_eval_lattice(const ls_grid3 *grid, const double *d_c, const double lat_origin[3],
                        const double lat_step[3], const int64_t lat_n[3], double *d_value, double *d_grad,
                        void *stream);
+
+/* ------------------------------------------------------------------ */
+/* P1 on a structured TetMesh (5 tetrahedra per cell) (K3)              */
+/* ------------------------------------------------------------------ */
+
+/* Number of face-sharing tetrahedron pairs of the mesh (T:120-184). */
+int ls_p1_face_count(const ls_grid3 *mesh, int64_t *h_faces);
+
+/* Constant-gradient face rows of P1:115-166 minimise_edge_jumps, in the
+ * reference's face order (pairs (i, j), i > j, sorted by i then j; T:120-184):
+ * row f = [n.grad(phi_i), -n.grad(phi_j)] over the 8 nodes of the two tets,
+ * normalised, b = 0, w = weight.  d_pairs (F x 2) and d_shared (F x 3, the
+ * shared face nodes ascending) may be NULL.  The row sign follows the order of
+ * the shared nodes (the normal's orientation); it does not change A^T W A. */
+int ls_p1_face_rows(const ls_grid3 *mesh, double weight, int64_t *d_pairs, int64_t *d_shared, int64_t *d_idc,
+                    double *d_a, double *d_b, double *d_w, void *stream);
+
+/* Containing tetrahedron (-1 outside) and barycentric coordinates of points
+ * (T:274-365: last containing tet of the 5 candidates wins; strict inside). */
+int ls_p1_locate(const ls_grid3 *mesh, const double *d_pts, int64_t npts, int64_t ld, int64_t *d_tet, double *d_bc,
+                 void *stream);
+
+/* Value rows (kind LS_ROWS_VALUE, P1:98-113: barycentric, per-point weight
+ * column ignored, w = weight) or normal rows (LS_ROWS_NORM, P1:73-96: 3
+ * gradient rows per point, point-major, w = weight) of the inside points,
+ * compacted in input order; 4 columns per row. */
+int ls_p1_point_rows(const ls_grid3 *mesh, int kind, const double *d_pts, int64_t npts, int64_t ld, double weight,
+                     int64_t *d_idc, double *d_a, double *d_b, double *d_w, int64_t *h_count, void *stream);
+
+/* Value / gradient of the P1 field (T:208-262): NaN outside; a NaN input row
+ * gives value 0 (DI:1342-1362). */
+int ls_p1_eval_points(const ls_grid3 *mesh, const double *d_c, const double *d_pts, int64_t npts, int64_t ld,
+                      double *d_value, double *d_grad, void *stream);
 
 #ifdef __cplusplus
 }

@@ -9,10 +9,13 @@ from . import constraints
 from ._lib import ExtensionUnavailable, LsError
 from .constraints import ValidationError
 from .interpolators import FiniteDifferenceInterpolator
+from .p1 import P1Interpolator, PiecewiseLinearInterpolator
 from .supports import StructuredGrid, TetMesh
 
 __all__ = [
     "FiniteDifferenceInterpolator",
+    "P1Interpolator",
+    "PiecewiseLinearInterpolator",
     "StructuredGrid",
     "TetMesh",
     "ValidationError",

@@ -34,6 +34,7 @@ EXPORTS = (
     "ls_fd_point_rows", "ls_fd_pair_rows", "ls_fd_reg_shape", "ls_fd_reg_rows",
     "ls_fd_create", "ls_fd_destroy", "ls_fd_dof", "ls_fd_apply", "ls_fd_apply_f32", "ls_fd_apply_noalloc", "ls_fd_rhs",
     "ls_fd_diagonal", "ls_fd_solve", "ls_fd_profile_iteration", "ls_fd_eval_points", "ls_fd_eval_lattice",
+    "ls_p1_face_count", "ls_p1_face_rows", "ls_p1_locate", "ls_p1_point_rows", "ls_p1_eval_points",
 )
 
 
@@ -84,7 +85,7 @@ class SolveStats(C.Structure):
     _fields_ = [
         ("iterations", C.c_int64), ("reliable_updates", C.c_int64), ("residual", C.c_double),
         ("rhs_norm", C.c_double), ("threshold", C.c_double), ("device_ms", C.c_double),
-        ("status", C.c_int32), ("preconditioner", C.c_int32),
+        ("status", C.c_int32), ("preconditioner", C.c_int32), ("kernel_launches", C.c_int64),
     ]
 
 
@@ -118,6 +119,12 @@ _SIGS = {
     "ls_fd_eval_points": (C.c_int, [C.POINTER(Grid3), _P, _P, C.c_int64, C.c_int64, _P, _P, _P]),
     "ls_fd_eval_lattice": (C.c_int, [C.POINTER(Grid3), _P, C.POINTER(C.c_double * 3), C.POINTER(C.c_double * 3),
                                      C.POINTER(C.c_int64 * 3), _P, _P, _P]),
+    "ls_p1_face_count": (C.c_int, [C.POINTER(Grid3), C.POINTER(C.c_int64)]),
+    "ls_p1_face_rows": (C.c_int, [C.POINTER(Grid3), C.c_double, _P, _P, _P, _P, _P, _P, _P]),
+    "ls_p1_locate": (C.c_int, [C.POINTER(Grid3), _P, C.c_int64, C.c_int64, _P, _P, _P]),
+    "ls_p1_point_rows": (C.c_int, [C.POINTER(Grid3), C.c_int, _P, C.c_int64, C.c_int64, C.c_double, _P, _P, _P, _P,
+                                   C.POINTER(C.c_int64), _P]),
+    "ls_p1_eval_points": (C.c_int, [C.POINTER(Grid3), _P, _P, C.c_int64, C.c_int64, _P, _P, _P]),
 }
 
 

@@ -2,23 +2,24 @@
 //     q = (sum_f w_f^2 R_f^T R_f + A_d^T W A_d + ridge^2 I) p
 // with a per-use epilogue, as one z-marching kernel.
 //
-// Tiling: a block of 32 x 8 threads owns a 32 x 8 column tile of (x, y) and
-// marches over a chunk of z planes.  Plane s is staged in shared memory with a
-// 2-node halo in x and y (double-buffered: one __syncthreads per plane).  From
-// it every thread forms, for its own column, the in-plane quantities of the
-// composite deep-interior stencil
+// Tiling: a block of 32 x 8 threads owns a 32 x 8 x 8 node tile; the tile and
+// a 2-node halo are staged in shared memory in one cp.async burst.  Every
+// thread forms, for its own (x, y) column and each staged plane, the in-plane
+// quantities of the composite deep-interior stencil
 //     S(s)  = a_x d4_x p + a_y d4_y p + b_xy C_x C_y p      (12 shared reads)
 //     Cx(s) = C_x p,  Cy(s) = C_y p,  P(s) = p
-// and keeps them in register windows over z, so that at plane z = s - 2
+// in register windows over z, so that at plane z
 //     q = ridge^2 P + S(z) + a_z d4_z P + b_xz C_z Cx + b_yz C_z Cy
 // needs no further memory traffic (d4 = (1,-4,6,-4,1), C = (1,0,-2,0,1) at
-// stride 2; a = w^2/6, b = w^2/4).  Nodes within 3 of a face take the exact
-// two-pass path (fd_stencil.cuh stencil_node_general) straight from L1/L2.
+// stride 2; a = w^2/6, b = w^2/4).  Nodes within 3 of a face evaluate the exact
+// two-pass sum branch-free from the staged neighbourhood (shell_node).
 //
 // Data rows: the touched nodes are marked in a bit mask (x-fastest words); a
 // touched node adds sum_e a_e s_row(e) over its incidence list, where
 // s_row = w^2 (a_row . p) was produced by the rows kernel launched just before.
 #pragma once
+
+#include <algorithm>
 
 #include "fd_stencil.cuh"
 #include "ls_common.cuh"
@@ -36,6 +37,7 @@ struct DataView {
   const int32_t *inc_row;
   const T *inc_a;
   const T *s_rows;           // w^2 (a_row . p) of the current p
+  const T *qd;               // optional: per-touched-node totals from data_nodes_warp_kernel
   int enabled;
 };
 
@@ -78,6 +80,7 @@ __device__ __forceinline__ T data_term(const DataView<T> &dv, int g) {
   const uint32_t bit = 1u << (g & 31);
   if (!(word & bit)) return (T)0;
   const int rank = __ldg(dv.word_rank + (g >> 5)) + __popc(word & (bit - 1u));
+  if (dv.qd) return dv.qd[rank];
   T acc = 0;
   const int64_t e1 = __ldg(dv.inc_ptr + rank + 1);
   for (int64_t e = __ldg(dv.inc_ptr + rank); e < e1; ++e) acc += __ldg(dv.inc_a + e) * __ldg(dv.s_rows + __ldg(dv.inc_row + e));
@@ -141,16 +144,27 @@ __device__ __forceinline__ T shell_node(const CoefT<T> &c, const PR &pr, int i, 
   return q;
 }
 
-constexpr int kRing = 8;  // staged planes: window s-4 .. s plus two in flight
-constexpr int kPrefetch = 2;
-
+// Output planes per block: 16 in FP32 (20 staged planes, 34.6 KB of shared
+// memory), 8 in FP64 (12 staged planes, 41.5 KB) -- both under the 48 KB static limit.
 template <typename T>
-struct ApplySmem {
-  T ring[kRing][kHY][kHX];
+struct Tile {
+  static constexpr int TZ = sizeof(T) == 4 ? 16 : 8;
+  static constexpr int SZ = TZ + 4;
+  static constexpr int PLANE = kHY * kHX;  // 432 staged nodes per plane
 };
 
-// Asynchronous global -> shared copy of one element (cp.async, Ampere+); a
-// zero src size fills zeros (outside the grid).
+// Operator modes: FULL evaluates every node of the grid (the boundary shell
+// through the exact branch-free sum); DEEP covers only the deep box
+// [3, n-4]^3 with the composite stencil and no branch, the shell being left to
+// fd_shell_kernel.
+enum ApplyMode { MODE_FULL = 0, MODE_DEEP = 1 };
+
+// The deep box is split off when every axis has at least this many nodes.
+constexpr int kSplitMin = 24;
+inline bool apply_split(int nx, int ny, int nz) { return nx >= kSplitMin && ny >= kSplitMin && nz >= kSplitMin; }
+
+// Asynchronous global -> shared copy of one element (cp.async); a zero source
+// size fills zeros (outside the grid).
 template <typename T>
 __device__ __forceinline__ void cp_async_elem(T *dst, const T *src, bool valid) {
   const unsigned saddr = (unsigned)__cvta_generic_to_shared(dst);
@@ -161,119 +175,96 @@ __device__ __forceinline__ void cp_async_elem(T *dst, const T *src, bool valid) 
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(saddr), "l"(src), "r"(n));
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
 
-// issue the copy of plane s (2-node halo) into ring slot `slot`; planes outside
-// the grid are zero-filled synchronously
-template <typename T>
-__device__ __forceinline__ void stage_plane(const CoefT<T> &c, const T *__restrict__ p, T (&dst)[kHY][kHX], int s,
-                                            int x0, int y0, int tid) {
-  const int nx = c.nx, ny = c.ny;
-  if (s >= 0 && s < c.nz) {
-    const T *ps = p + (size_t)s * nx * ny;
-    for (int e2 = tid; e2 < kHX * kHY; e2 += kAX * kAY) {
+// Block = 32 x 8 threads owning a 32 x 8 x TZ output tile.  The tile and a
+// 2-node halo ((32+4) x (8+4) x (TZ+4)) are staged in one cp.async burst (each
+// thread copies the same one or two in-plane positions of every plane), then
+// one barrier.  Each thread walks its own column through the staged planes in
+// a fully unrolled loop: the in-plane quantities P, Cx, Cy of plane s are
+// formed when s is reached and the output of plane s-2 is emitted as soon as
+// they are, so only a 5-plane window stays live in registers.
+// Returns the block's sum of the epilogue contributions (p.q for EPI_STORE)
+// through the deterministic grid reduction when `dot_out` is set.
+template <typename T, int EPI, int MODE>
+__global__ void __launch_bounds__(kAX * kAY) fd_apply_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv,
+                                                             EpiArgs<T> e, const int *done, double *partials,
+                                                             unsigned int *ticket, double *dot_out) {
+  if (done && *done) return;
+  constexpr int TZ = Tile<T>::TZ, SZ = Tile<T>::SZ, PLANE = Tile<T>::PLANE;
+  __shared__ T sm[SZ][kHY][kHX];
+  const int nx = c.nx, ny = c.ny, nz = c.nz;
+  const int org = MODE == MODE_DEEP ? 3 : 0;  // first node of the covered box
+  const int xe = MODE == MODE_DEEP ? nx - 3 : nx, ye = MODE == MODE_DEEP ? ny - 3 : ny,
+            ze = MODE == MODE_DEEP ? nz - 3 : nz;  // one past the last covered node
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + kAX * ty;
+  const int x0 = org + blockIdx.x * kAX, y0 = org + blockIdx.y * kAY, z0 = org + blockIdx.z * TZ;
+  const size_t sxy = (size_t)nx * ny;
+  // ---- stage the tile ----
+  {
+    int off[2];
+    bool vxy[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int e2 = tid + u * kAX * kAY;
       const int hy = e2 / kHX, hx = e2 - hy * kHX;
       const int gx = x0 - 2 + hx, gy = y0 - 2 + hy;
-      const bool ok = (gx >= 0) & (gx < nx) & (gy >= 0) & (gy < ny);
-      cp_async_elem<T>(&dst[hy][hx], ok ? ps + gx + nx * gy : p, ok);
+      vxy[u] = (e2 < PLANE) & (gx >= 0) & (gx < nx) & (gy >= 0) & (gy < ny);
+      off[u] = vxy[u] ? gy * nx + gx : 0;
     }
-  } else {
-    for (int e2 = tid; e2 < kHX * kHY; e2 += kAX * kAY) (&dst[0][0])[e2] = (T)0;
+    T *base = &sm[0][0][0];
+#pragma unroll
+    for (int hz = 0; hz < SZ; ++hz) {
+      const int gz = z0 - 2 + hz;
+      const bool vz = (gz >= 0) & (gz < nz);
+      const T *src = p + (vz ? (size_t)gz * sxy : 0);
+      cp_async_elem<T>(base + hz * PLANE + tid, src + off[0], vz & vxy[0]);
+      if (tid + kAX * kAY < PLANE) cp_async_elem<T>(base + hz * PLANE + tid + kAX * kAY, src + off[1], vz & vxy[1]);
+    }
   }
   cp_async_commit();
-}
-
-// One plane step of the z-march, unrolled by the ring size so that every
-// ring / window index is a compile-time constant.  On entry planes s and s+1
-// are in flight; the step issues plane s + 2, waits for plane s, and outputs
-// plane z = s - 2.
-template <typename T, int EPI, int M>
-__device__ __forceinline__ void apply_step(const CoefT<T> &c, const T *__restrict__ p, const DataView<T> &dv,
-                                           const EpiArgs<T> &e, ApplySmem<T> &sm, int s, int x0, int y0, int z0,
-                                           int z1, int tx, int ty, int tid, bool own, bool col_deep, int i, int j,
-                                           T (&P)[kRing], T (&Cx)[kRing], T (&Cy)[kRing], T (&S)[kRing], T &local) {
-  const int nx = c.nx, ny = c.ny, nz = c.nz;
-  const int sxy = nx * ny;
-  constexpr int MP = (M + kPrefetch) % kRing;
-  if (s + kPrefetch <= z1 + 1)
-    stage_plane<T>(c, p, sm.ring[MP], s + kPrefetch, x0, y0, tid);
-  else
-    cp_async_commit();  // keep one group per step
-  cp_async_wait<kPrefetch>();
+  cp_async_wait_all();
   __syncthreads();
-  {
-    const int hx = tx + 2, hy = ty + 2;
-    const T(&pl)[kHY][kHX] = sm.ring[M];
-    const T p0 = pl[hy][hx];
-    const T ex = pl[hy][hx - 2] + pl[hy][hx + 2], ey = pl[hy - 2][hx] + pl[hy + 2][hx];
-    const T d4x = ex - (T)4 * (pl[hy][hx - 1] + pl[hy][hx + 1]) + (T)6 * p0;
-    const T d4y = ey - (T)4 * (pl[hy - 1][hx] + pl[hy + 1][hx]) + (T)6 * p0;
-    const T corners = (pl[hy - 2][hx - 2] + pl[hy - 2][hx + 2]) + (pl[hy + 2][hx - 2] + pl[hy + 2][hx + 2]);
-    const T cxy = corners - (T)2 * (ex + ey) + (T)4 * p0;
-    P[M] = p0;
-    Cx[M] = ex - (T)2 * p0;
-    Cy[M] = ey - (T)2 * p0;
-    S[M] = c.xx_int * d4x + c.yy_int * d4y + c.xy * cxy;
-  }
-  const int z = s - 2;
-  if (z >= z0 && z < nz && own) {
-    constexpr int m0 = (M + kRing - 4) % kRing, m1 = (M + kRing - 3) % kRing, m2 = (M + kRing - 2) % kRing,
-                  m3 = (M + kRing - 1) % kRing;
-    // window: plane z-2 -> m0, z-1 -> m1, z -> m2, z+1 -> m3, z+2 -> M
-    const int g = i + nx * j + sxy * z;
-    T q;
-    if (col_deep && z >= 3 && z <= nz - 4) {
-      const T d4z = (P[m0] + P[M]) - (T)4 * (P[m1] + P[m3]) + (T)6 * P[m2];
-      q = c.ridge2 * P[m2] + S[m2] + c.zz_int * d4z + c.xz * ((Cx[m0] + Cx[M]) - (T)2 * Cx[m2]) +
-          c.yz * ((Cy[m0] + Cy[M]) - (T)2 * Cy[m2]);
-    } else {
-      const int hx = tx + 2, hy = ty + 2;
-      auto pr = [&](int dz, int dy, int dx) -> T {
-        const int slot = dz == -2 ? m0 : dz == -1 ? m1 : dz == 0 ? m2 : dz == 1 ? m3 : M;
-        return sm.ring[slot][hy + dy][hx + dx];
-      };
-      q = shell_node<T>(c, pr, i, j, z);
-    }
-    if (dv.enabled) q += data_term<T>(dv, g);
-    local += epilogue<T, EPI>(e, g, P[m2], q);
-  }
-}
-
-// Returns the block's sum of the epilogue's per-node contributions (p.q for
-// EPI_STORE) through the deterministic grid reduction when `dot_out` is set.
-// `zc` is the z chunk of one block (gridDim.z = ceil(nz / zc)).
-template <typename T, int EPI>
-__global__ void __launch_bounds__(kAX * kAY) fd_apply_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv,
-                                                             EpiArgs<T> e, int zc, const int *done,
-                                                             double *partials, unsigned int *ticket,
-                                                             double *dot_out) {
-  if (done && *done) return;
-  __shared__ ApplySmem<T> sm;
-  const int nx = c.nx, ny = c.ny, nz = c.nz;
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + kAX * ty;
-  const int x0 = blockIdx.x * kAX, y0 = blockIdx.y * kAY, z0 = blockIdx.z * zc;
-  const int z1 = min(z0 + zc, nz);
   const int i = x0 + tx, j = y0 + ty;
-  const bool own = (i < nx) & (j < ny);
-  const bool col_deep = (i >= 3) & (i <= nx - 4) & (j >= 3) & (j <= ny - 4);
-  T P[kRing], Cx[kRing], Cy[kRing], S[kRing];
-#pragma unroll
-  for (int w = 0; w < kRing; ++w) P[w] = Cx[w] = Cy[w] = S[w] = (T)0;
   T local = 0;
-  const int s0 = z0 - 2;
-  // prologue: planes s0 and s0 + 1 in flight
-  stage_plane<T>(c, p, sm.ring[0], s0, x0, y0, tid);
-  stage_plane<T>(c, p, sm.ring[1], s0 + 1, x0, y0, tid);
-  for (int s = s0; s <= z1 + 1; s += kRing) {
-#define LS_STEP(MM)                                                                                                  \
-  if (s + MM > z1 + 1) break;                                                                                        \
-  apply_step<T, EPI, MM>(c, p, dv, e, sm, s + MM, x0, y0, z0, z1, tx, ty, tid, own, col_deep, i, j, P, Cx, Cy, S, \
-                         local);
-    LS_STEP(0) LS_STEP(1) LS_STEP(2) LS_STEP(3) LS_STEP(4) LS_STEP(5) LS_STEP(6) LS_STEP(7)
-#undef LS_STEP
+  if ((i < xe) & (j < ye)) {
+    const bool col_deep = MODE == MODE_DEEP || ((i >= 3) & (i <= nx - 4) & (j >= 3) & (j <= ny - 4));
+    const int hx = tx + 2, hy = ty + 2;
+    T P[SZ], Cx[SZ], Cy[SZ];
+#pragma unroll
+    for (int hz = 0; hz < SZ; ++hz) {
+      const T(&pl)[kHY][kHX] = sm[hz];
+      const T p0 = pl[hy][hx];
+      P[hz] = p0;
+      Cx[hz] = (pl[hy][hx - 2] + pl[hy][hx + 2]) - (T)2 * p0;
+      Cy[hz] = (pl[hy - 2][hx] + pl[hy + 2][hx]) - (T)2 * p0;
+      if (hz >= 4) {
+        const int ho = hz - 2;  // staged plane of the output
+        const int z = z0 + ho - 2;
+        if (z < ze) {
+          const size_t g = (size_t)z * sxy + (size_t)j * nx + i;
+          T q;
+          if (col_deep & (MODE == MODE_DEEP || ((z >= 3) & (z <= nz - 4)))) {
+            const T(&po)[kHY][kHX] = sm[ho];
+            const T q0 = P[ho];
+            const T ex = po[hy][hx - 2] + po[hy][hx + 2], ey = po[hy - 2][hx] + po[hy + 2][hx];
+            const T d4x = ex - (T)4 * (po[hy][hx - 1] + po[hy][hx + 1]) + (T)6 * q0;
+            const T d4y = ey - (T)4 * (po[hy - 1][hx] + po[hy + 1][hx]) + (T)6 * q0;
+            const T corners = (po[hy - 2][hx - 2] + po[hy - 2][hx + 2]) + (po[hy + 2][hx - 2] + po[hy + 2][hx + 2]);
+            const T d4z = (P[ho - 2] + P[ho + 2]) - (T)4 * (P[ho - 1] + P[ho + 1]) + (T)6 * q0;
+            q = c.ridge2 * q0 + c.xx_int * d4x + c.yy_int * d4y + c.zz_int * d4z +
+                c.xy * (corners - (T)2 * (ex + ey) + (T)4 * q0) +
+                c.xz * ((Cx[ho - 2] + Cx[ho + 2]) - (T)2 * Cx[ho]) + c.yz * ((Cy[ho - 2] + Cy[ho + 2]) - (T)2 * Cy[ho]);
+          } else {
+            auto pr = [&](int dz, int dy, int dx) -> T { return sm[ho + dz][hy + dy][hx + dx]; };
+            q = shell_node<T>(c, pr, i, j, z);
+          }
+          if (dv.enabled) q += data_term<T>(dv, (int)g);
+          local += epilogue<T, EPI>(e, (int)g, P[ho], q);
+        }
+      }
+    }
   }
-  cp_async_wait<0>();
   if (dot_out) {
     double tot;
     const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
@@ -282,19 +273,118 @@ __global__ void __launch_bounds__(kAX * kAY) fd_apply_kernel(CoefT<T> c, const T
   }
 }
 
-// z chunk giving at least ~2 waves of blocks (short chunks cost halo re-reads,
-// long ones serialise the march)
-inline int apply_zchunk(int nx, int ny, int nz, int sms) {
-  const int gxy = ((nx + kAX - 1) / kAX) * ((ny + kAY - 1) / kAY);
-  const int want_blocks = 6 * sms;
-  int zc = (int)(((int64_t)nz * gxy + want_blocks - 1) / want_blocks);
-  if (zc < 4) zc = 4;
-  if (zc > 32) zc = 32;
-  return zc;
+template <typename T>
+inline dim3 apply_grid(int nx, int ny, int nz, int mode) {
+  constexpr int TZ = Tile<T>::TZ;
+  if (mode == MODE_DEEP) {
+    nx -= 6;
+    ny -= 6;
+    nz -= 6;
+  }
+  return dim3((nx + kAX - 1) / kAX, (ny + kAY - 1) / kAY, (nz + TZ - 1) / TZ);
 }
 
-inline dim3 apply_grid(int nx, int ny, int nz, int zc) {
-  return dim3((nx + kAX - 1) / kAX, (ny + kAY - 1) / kAY, (nz + zc - 1) / zc);
+// Boundary shell of a split grid: nodes with some coordinate in {0,1,2,n-3,n-2,n-1}
+// (all axes >= 7), enumerated in three slabs: the 6 z-planes; then, for
+// 3 <= k <= nz-4, the 6 y-rows; then, for 3 <= j <= ny-4, the 6 x-columns.
+__host__ __device__ inline int64_t shell_count(int nx, int ny, int nz) {
+  return (int64_t)nx * ny * nz - (int64_t)(nx - 6) * (ny - 6) * (nz - 6);
+}
+__device__ __forceinline__ void shell_node_index(int64_t s, int nx, int ny, int nz, int &i, int &j, int &k) {
+  const int64_t zs = 6 * (int64_t)nx * ny, ys = 6 * (int64_t)nx * (nz - 6);
+  if (s < zs) {
+    const int t = (int)(s / ((int64_t)nx * ny));
+    const int rem = (int)(s - (int64_t)t * nx * ny);
+    k = t < 3 ? t : nz - 6 + t;
+    j = rem / nx;
+    i = rem - j * nx;
+  } else if (s < zs + ys) {
+    const int64_t u = s - zs;
+    const int kk = (int)(u / (6 * nx));
+    const int rem = (int)(u - (int64_t)kk * 6 * nx);
+    const int t = rem / nx;
+    k = 3 + kk;
+    j = t < 3 ? t : ny - 6 + t;
+    i = rem - t * nx;
+  } else {
+    const int64_t u = s - zs - ys;
+    const int kk = (int)(u / (6 * (ny - 6)));
+    const int rem = (int)(u - (int64_t)kk * 6 * (ny - 6));
+    const int jj = rem / 6, t = rem - jj * 6;
+    k = 3 + kk;
+    j = 3 + jj;
+    i = t < 3 ? t : nx - 6 + t;
+  }
+}
+
+// The exact operator at the shell nodes of a split grid (one thread per node,
+// neighbours straight from L1/L2), with the data term and the epilogue.
+template <typename T, int EPI>
+__global__ void __launch_bounds__(256) fd_shell_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv,
+                                                       EpiArgs<T> e, const int *done, double *partials,
+                                                       unsigned int *ticket, double *dot_out) {
+  if (done && *done) return;
+  const int nx = c.nx, ny = c.ny, nz = c.nz;
+  const int64_t ns = shell_count(nx, ny, nz);
+  T local = 0;
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns; s += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    shell_node_index(s, nx, ny, nz, i, j, k);
+    auto pr = [&](int dz, int dy, int dx) -> T {
+      const int a = i + dx, b = j + dy, cz = k + dz;
+      return ((a >= 0) & (a < nx) & (b >= 0) & (b < ny) & (cz >= 0) & (cz < nz))
+                 ? __ldg(p + ((size_t)cz * ny + b) * nx + a)
+                 : (T)0;
+    };
+    T q = shell_node<T>(c, pr, i, j, k);
+    const int g = (int)(((size_t)k * ny + j) * nx + i);
+    if (dv.enabled) q += data_term<T>(dv, g);
+    local += epilogue<T, EPI>(e, g, __ldg(p + g), q);
+  }
+  if (dot_out) {
+    double tot;
+    if (grid_sum<256>((double)local, partials, ticket, &tot)) *dot_out = tot;
+  }
+}
+
+// q = N_reg p (+ data term) with an epilogue: the deep-box kernel plus the
+// shell kernel on split grids, else one full-grid kernel.  The epilogue sums
+// land in dot_main (full grid / deep box) and dot_shell (shell; untouched on
+// unsplit grids).  Returns the number of kernels launched.
+template <typename T, int EPI>
+inline int launch_operator(const CoefT<T> &c, const T *p, const DataView<T> &dv, const EpiArgs<T> &e, const int *done,
+                           double *partials, unsigned int *ticket_main, double *dot_main, unsigned int *ticket_shell,
+                           double *dot_shell, int max_blocks, cudaStream_t st) {
+  const dim3 blk(kAX, kAY);
+  if (apply_split(c.nx, c.ny, c.nz)) {
+    fd_apply_kernel<T, EPI, MODE_DEEP><<<apply_grid<T>(c.nx, c.ny, c.nz, MODE_DEEP), blk, 0, st>>>(
+        c, p, dv, e, done, partials, ticket_main, dot_main);
+    const int64_t ns = shell_count(c.nx, c.ny, c.nz);
+    const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((ns + 255) / 256, max_blocks));
+    fd_shell_kernel<T, EPI><<<gs, 256, 0, st>>>(c, p, dv, e, done, partials, ticket_shell, dot_shell);
+    return 2;
+  }
+  fd_apply_kernel<T, EPI, MODE_FULL><<<apply_grid<T>(c.nx, c.ny, c.nz, MODE_FULL), blk, 0, st>>>(
+      c, p, dv, e, done, partials, ticket_main, dot_main);
+  return 1;
+}
+
+// Data term of the touched nodes with one warp per node (coarse multigrid
+// levels, where many Galerkin rows pile up on each node): qd[rank] = sum_e a_e s_row(e)
+template <typename T>
+__global__ void data_nodes_warp_kernel(int64_t ntouched, const int64_t *__restrict__ inc_ptr,
+                                       const int32_t *__restrict__ inc_row, const T *__restrict__ inc_a,
+                                       const T *__restrict__ s_rows, T *__restrict__ qd, const int *done) {
+  if (done && *done) return;
+  const int lane = threadIdx.x & 31;
+  for (int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; t < ntouched;
+       t += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    T acc = 0;
+    for (int64_t e = inc_ptr[t] + lane; e < inc_ptr[t + 1]; e += 32) acc += inc_a[e] * s_rows[inc_row[e]];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) qd[t] = acc;
+  }
 }
 
 // s_r = w_r^2 (a_r . p)  (no reduction)

@@ -41,6 +41,7 @@ struct MgLevel {
   int64_t *inc_ptr = nullptr;
   int32_t *inc_row = nullptr;
   float *inc_a = nullptr;
+  float *qd = nullptr;  // per-touched-node data totals (levels with long incidence lists)
   float *dinv = nullptr;
   // vectors: b (rhs), x (solution), r (residual), d[2] (Chebyshev directions)
   float *b = nullptr, *x = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;

@@ -40,9 +40,11 @@ struct CgScalars {
   double rz64;     // FP64 refresh: r64 . D^-1 r64
   double rz32;     // FP64 refresh: r32 . D^-1 r32 (after rounding)
   double scratch;
+  double trig2;    // mixed precision: stop the FP32 batch for a reliable update below this (0 = never)
   long long iters;
   long long maxiter;
   int done;        // DONE_* stop code
+  int pending;     // stop code raised mid-iteration; becomes `done` once p is updated
   int profile;     // timing mode: never stop, never flag a breakdown
 };
 
@@ -89,6 +91,10 @@ struct ls_fd_handle {
   // graphs of one batch of iterations
   cudaGraphExec_t g64 = nullptr, g32 = nullptr, gmg = nullptr;
   int g64_batch = 0, g32_batch = 0, gmg_batch = 0;
+  // kernel launches issued on the handle's stream (a graph launch counts its
+  // kernel nodes); g*_kernels = kernel nodes of each cached graph
+  int64_t launches = 0;
+  int64_t g64_kernels = 0, g32_kernels = 0, gmg_kernels = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // multigrid preconditioner (built on first use)
   ls::MgHierarchy mg;
@@ -102,7 +108,14 @@ namespace ls {
 namespace {
 
 // device-side stop codes (CgScalars::done); mapped to ls_status on the host
-enum : int { DONE_RUNNING = 0, DONE_CONVERGED = 1, DONE_MAXITER = 2, DONE_NAN = 3, DONE_BREAKDOWN = 4 };
+enum : int {
+  DONE_RUNNING = 0,
+  DONE_CONVERGED = 1,
+  DONE_MAXITER = 2,
+  DONE_NAN = 3,
+  DONE_BREAKDOWN = 4,
+  DONE_REFRESH = 5  // FP32 residual fell below trig2: reliable update due
+};
 
 int done_to_status(int d) {
   switch (d) {
@@ -114,14 +127,17 @@ int done_to_status(int d) {
   }
 }
 
-enum Ticket { T_STENCIL = 0, T_DATA = 1, T_UPDATE = 2, T_REFRESH = 3, T_MISC = 4, T_COUNT = 5 };
+enum Ticket { T_STENCIL = 0, T_DATA = 1, T_UPDATE = 2, T_REFRESH = 3, T_MISC = 4, T_PUPD = 5, T_SHELL = 6, T_COUNT = 7 };
 
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
 
 // alpha = rz / pq ; x += alpha p ; r -= alpha q ; rz' = r . D^-1 r ;
-// the last block publishes beta = rz'/rz and tests convergence.
+// the last block publishes beta = rz'/rz and tests convergence.  Converged,
+// maximum-iteration and refresh stops are raised as `pending` so that the
+// iteration completes (p updated) before the batch stops; NaN and breakdown
+// stop at once (x and r untouched).
 template <typename T>
 __global__ void __launch_bounds__(kBlock) update_xr_kernel(int64_t n, T *__restrict__ x, T *__restrict__ r,
                                                            const T *__restrict__ p, const T *__restrict__ q,
@@ -152,19 +168,24 @@ __global__ void __launch_bounds__(kBlock) update_xr_kernel(int64_t n, T *__restr
       sc->rz = 1.0;  // keep alpha and beta finite while timing
       sc->beta = 0.5;
     } else if (!isfinite(rz_new)) sc->done = DONE_NAN;
-    else if (rz_new < sc->thresh2) sc->done = DONE_CONVERGED;
-    else if (sc->iters >= sc->maxiter) sc->done = DONE_MAXITER;
+    else if (rz_new < sc->thresh2) sc->pending = DONE_CONVERGED;
+    else if (sc->iters >= sc->maxiter) sc->pending = DONE_MAXITER;
+    else if (rz_new < sc->trig2) sc->pending = DONE_REFRESH;
   }
 }
 
-// p = D^-1 r + beta p
+// p = D^-1 r + beta p ; the last block turns a pending stop into `done`
 template <typename T>
 __global__ void __launch_bounds__(kBlock) update_p_kernel(int64_t n, const T *__restrict__ r, const T *__restrict__ dinv,
-                                                          T *__restrict__ p, const CgScalars *sc) {
+                                                          T *__restrict__ p, CgScalars *sc, unsigned int *ticket) {
   if (sc->done) return;
   const T beta = (T)sc->beta;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
     p[g] = dinv[g] * r[g] + beta * p[g];
+  if (sc->pending && grid_last_block(ticket)) {
+    sc->done = sc->pending;
+    sc->pending = 0;
+  }
 }
 
 // FP64 residual refresh: r64 = rhs - q64 ; rz64 = r64 . D^-1 r64.
@@ -293,24 +314,27 @@ DataView<T> data_view(const ls_fd_handle *h, const T *s_rows, const T *inc_a) {
   dv.inc_row = h->data.inc_row;
   dv.inc_a = inc_a;
   dv.s_rows = s_rows;
+  dv.qd = nullptr;
   dv.enabled = h->data.ntouched > 0;
   return dv;
 }
 
-// q = N p (rows kernel + fused apply); p.q lands in sc->pq_s (sc->pq_d = 0)
+// q = N p (rows kernel + fused apply); p.q lands in sc->pq_s (deep box or full
+// grid) and sc->pq_d (boundary shell of a split grid; stays 0 otherwise)
 template <typename T>
 void launch_apply(ls_fd_handle *h, const T *p, T *q, T *s, const T *a, const T *w2, const T *ia, bool check_done,
                   cudaStream_t st) {
   const DataTerm &d = h->data;
   const int *done = check_done ? &h->sc->done : nullptr;
-  if (d.nrows > 0)
+  if (d.nrows > 0) {
     rows_kernel<T><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, a, w2, p, s, done);
+    ++h->launches;
+  }
   EpiArgs<T> e{};
   e.q = q;
-  const int nx = (int)h->coef.nx, ny = (int)h->coef.ny, nz = (int)h->coef.nz;
-  const int zc = apply_zchunk(nx, ny, nz, sm_count());
-  fd_apply_kernel<T, EPI_STORE><<<apply_grid(nx, ny, nz, zc), dim3(kAX, kAY), 0, st>>>(
-      coef_as<T>(h->coef), p, data_view<T>(h, s, ia), e, zc, done, h->partials, h->tickets + T_STENCIL, &h->sc->pq_s);
+  h->launches += launch_operator<T, EPI_STORE>(coef_as<T>(h->coef), p, data_view<T>(h, s, ia), e, done, h->partials,
+                                               h->tickets + T_STENCIL, &h->sc->pq_s, h->tickets + T_SHELL,
+                                               &h->sc->pq_d, h->red_blocks, st);
 }
 
 void launch_apply64(ls_fd_handle *h, const double *p, double *q, bool check_done, cudaStream_t st) {
@@ -328,14 +352,20 @@ void launch_iteration(ls_fd_handle *h, T *x, T *r, T *p, T *q, const T *dinv, cu
     launch_apply32(h, (const float *)p, (float *)q, true, st);
   const int g = grid_for(h, h->n);
   update_xr_kernel<T><<<g, kBlock, 0, st>>>(h->n, x, r, p, q, dinv, h->sc, h->partials, h->tickets + T_UPDATE);
-  update_p_kernel<T><<<g, kBlock, 0, st>>>(h->n, r, dinv, p, h->sc);
+  ++h->launches;
+  update_p_kernel<T><<<g, kBlock, 0, st>>>(h->n, r, dinv, p, h->sc, h->tickets + T_PUPD);
+  ++h->launches;
 }
 
 template <typename T>
-int build_graph(ls_fd_handle *h, int batch, cudaGraphExec_t *out, T *x, T *r, T *p, T *q, const T *dinv) {
+int build_graph(ls_fd_handle *h, int batch, cudaGraphExec_t *out, int64_t *kernels, T *x, T *r, T *p, T *q,
+                const T *dinv) {
   cudaStream_t st = h->stream;
+  const int64_t before = h->launches;
   LS_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
   for (int it = 0; it < batch; ++it) launch_iteration<T>(h, x, r, p, q, dinv, st);
+  *kernels = h->launches - before;
+  h->launches = before;
   cudaGraph_t graph;
   LS_CUDA_TRY(cudaStreamEndCapture(st, &graph));
   cudaError_t e = cudaGraphInstantiate(out, graph, 0);
@@ -354,6 +384,7 @@ int read_scalars(ls_fd_handle *h) {
 }
 
 int write_scalars(ls_fd_handle *h) {
+  h->sc_h->pending = 0;
   LS_CUDA_TRY(cudaMemcpyAsync(h->sc, h->sc_h, sizeof(CgScalars), cudaMemcpyHostToDevice, h->stream));
   return LS_OK;
 }
@@ -365,6 +396,7 @@ int refresh(ls_fd_handle *h, bool have_x, float *r32, float *p32) {
   refresh_kernel<<<grid_for(h, h->n), kBlock, 0, st>>>(h->n, h->rhs, have_x ? h->q64 : nullptr, h->dinv64, h->r64,
                                                        r32 ? nullptr : h->p64, h->dinv32, r32, p32, h->x32, h->sc,
                                                        h->partials, h->tickets + T_REFRESH);
+  ++h->launches;
   LS_CUDA_TRY(cudaGetLastError());
   return LS_OK;
 }
@@ -512,6 +544,7 @@ int mg_upload_level(ls_fd_handle *h, MgLevel &lv, const HostRows &rows, std::vec
   LS_TRY(mg_alloc(mg, &lv.inc_ptr, lv.ntouched + 1));
   LS_TRY(mg_alloc(mg, &lv.inc_row, ni));
   LS_TRY(mg_alloc(mg, &lv.inc_a, ni));
+  if (lv.ntouched > 0 && ni > 16 * lv.ntouched) LS_TRY(mg_alloc(mg, &lv.qd, lv.ntouched));
   cudaStream_t st = h->stream;
 #define UPL(dst, src, cnt) \
   if ((cnt) > 0) LS_CUDA_TRY(cudaMemcpyAsync(dst, (src).data(), (cnt) * sizeof((src)[0]), cudaMemcpyHostToDevice, st));
@@ -536,6 +569,7 @@ DataView<float> mg_view(const MgLevel &lv) {
   dv.inc_row = lv.inc_row;
   dv.inc_a = lv.inc_a;
   dv.s_rows = lv.s;
+  dv.qd = lv.qd;
   dv.enabled = lv.ntouched > 0;
   return dv;
 }
@@ -544,11 +578,17 @@ DataView<float> mg_view(const MgLevel &lv) {
 template <int EPI>
 void mg_apply(ls_fd_handle *h, const MgLevel &lv, const float *p, const EpiArgs<float> &e, const int *done,
               cudaStream_t st) {
-  if (lv.nrows > 0)
+  if (lv.nrows > 0) {
     rows_kernel<float><<<grid_for(h, lv.nrows), kBlock, 0, st>>>(lv.nrows, lv.width, lv.cols, lv.a, lv.w2, p, lv.s, done);
-  const int zc = apply_zchunk(lv.nx, lv.ny, lv.nz, sm_count());
-  fd_apply_kernel<float, EPI><<<apply_grid(lv.nx, lv.ny, lv.nz, zc), dim3(kAX, kAY), 0, st>>>(
-      lv.coef, p, mg_view(lv), e, zc, done, nullptr, nullptr, nullptr);
+    ++h->launches;
+  }
+  if (lv.qd) {
+    data_nodes_warp_kernel<float><<<std::max<int64_t>(1, std::min<int64_t>((lv.ntouched * 32 + 255) / 256, 8 * sm_count())), 256, 0, st>>>(
+        lv.ntouched, lv.inc_ptr, lv.inc_row, lv.inc_a, lv.s, lv.qd, done);
+    ++h->launches;
+  }
+  h->launches += launch_operator<float, EPI>(lv.coef, p, mg_view(lv), e, done, nullptr, nullptr, nullptr, nullptr,
+                                             nullptr, h->red_blocks, st);
 }
 
 int mg_read_scalar(ls_fd_handle *h, double *dev, double *out) {
@@ -562,18 +602,23 @@ int mg_lambda_max(ls_fd_handle *h, MgLevel &lv, float *lmax_out) {
   const int g = grid_for(h, lv.n);
   float *v = lv.d0, *q = lv.d1;
   mg_fill_hash_kernel<<<g, kBlock, 0, st>>>(lv.n, v);
+  ++h->launches;
   double nv = 0.0, nq = 0.0;
   double *slot = &h->sc->scratch;
   mg_dot_kernel<<<g, 256, 0, st>>>(lv.n, v, v, nullptr, h->partials, h->tickets + T_MISC, slot);
+  ++h->launches;
   LS_TRY(mg_read_scalar(h, slot, &nv));
   double lam = 0.0;
   for (int it = 0; it < 20; ++it) {
     mg_scale_kernel<<<g, kBlock, 0, st>>>(lv.n, v, nullptr, (float)(1.0 / sqrt(nv)), v);
+    ++h->launches;
     EpiArgs<float> e{};
     e.q = q;
     mg_apply<EPI_STORE>(h, lv, v, e, nullptr, st);
     mg_scale_kernel<<<g, kBlock, 0, st>>>(lv.n, q, lv.dinv, 1.0f, v);
+    ++h->launches;
     mg_dot_kernel<<<g, 256, 0, st>>>(lv.n, v, v, nullptr, h->partials, h->tickets + T_MISC, slot);
+    ++h->launches;
     LS_TRY(mg_read_scalar(h, slot, &nq));
     lam = sqrt(nq);  // |D^-1 A v| with |v| = 1
     nv = nq;
@@ -659,9 +704,13 @@ int mg_level_dinv(ls_fd_handle *h, MgLevel &lv, const std::vector<int64_t> &touc
   }
   const int g = grid_for(h, lv.n);
   diag_stencil_kernel<<<g, kBlock, 0, st>>>(lv.coef64, diag);
-  if (!touched.empty())
+  ++h->launches;
+  if (!touched.empty()) {
     mg_diag_finish_kernel<<<grid_for(h, (int64_t)touched.size()), kBlock, 0, st>>>(lv.n, diag, (int64_t)touched.size(), dt, dd);
+    ++h->launches;
+  }
   mg_invert_kernel<<<g, kBlock, 0, st>>>(lv.n, diag, lv.dinv);
+  ++h->launches;
   LS_CUDA_TRY(cudaStreamSynchronize(st));
   cudaFree(diag);
   cudaFree(dt);
@@ -784,6 +833,7 @@ void mg_vcycle(ls_fd_handle *h, const int *done, cudaStream_t st) {
   for (int l = 0; l + 1 < L; ++l) {
     MgLevel &lv = mg.levels[l];
     mg_cheb_init_kernel<<<grid_for(h, lv.n), kBlock, 0, st>>>(lv.n, lv.b, lv.dinv, lv.inv_theta, lv.r, lv.d0, lv.x, done);
+    ++h->launches;
     float *dc = lv.d0, *dn = lv.d1;
     for (int k = 0; k < mg.deg; ++k) {
       EpiArgs<float> e{};
@@ -799,16 +849,19 @@ void mg_vcycle(ls_fd_handle *h, const int *done, cudaStream_t st) {
     const MgLevel &cl = mg.levels[l + 1];
     mg_restrict_kernel<<<dim3((cl.nx + 31) / 32, (cl.ny + 7) / 8, cl.nz), dim3(32, 8), 0, st>>>(
         lv.nx, lv.ny, lv.nz, cl.nx, cl.ny, cl.nz, lv.r, cl.b, done);
+    ++h->launches;
   }
   {
     MgLevel &cl = mg.levels[L - 1];
     mg_dense_kernel<<<(int)((cl.n * 32 + 255) / 256), 256, 0, st>>>((int)cl.n, mg.coarse_inv64, cl.b, cl.x, done);
+    ++h->launches;
   }
   for (int l = L - 2; l >= 0; --l) {
     MgLevel &lv = mg.levels[l];
     const MgLevel &cl = mg.levels[l + 1];
     mg_prolong_kernel<<<dim3((lv.nx + 31) / 32, (lv.ny + 7) / 8, lv.nz), dim3(32, 8), 0, st>>>(
         lv.nx, lv.ny, lv.nz, cl.nx, cl.ny, cl.x, lv.x, done);
+    ++h->launches;
     EpiArgs<float> e{};
     e.r = lv.r;
     e.b = lv.b;
@@ -838,7 +891,7 @@ __global__ void __launch_bounds__(kBlock) mg_update_xr_kernel(int64_t n, float *
                                                               const float *__restrict__ dinv, CgScalars *sc,
                                                               double *partials, unsigned int *ticket) {
   if (sc->done) return;
-  const double pq = sc->pq_s;
+  const double pq = sc->pq_s + sc->pq_d;
   const double alpha_d = sc->rz / pq;
   if (!(pq > 0.0) || !isfinite(alpha_d)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = isfinite(pq) ? DONE_BREAKDOWN : DONE_NAN;
@@ -857,8 +910,9 @@ __global__ void __launch_bounds__(kBlock) mg_update_xr_kernel(int64_t n, float *
     sc->iters += 1;
     sc->rrj = rrj;
     if (!isfinite(rrj)) sc->done = DONE_NAN;
-    else if (rrj < sc->thresh2) sc->done = DONE_CONVERGED;
-    else if (sc->iters >= sc->maxiter) sc->done = DONE_MAXITER;
+    else if (rrj < sc->thresh2) sc->pending = DONE_CONVERGED;
+    else if (sc->iters >= sc->maxiter) sc->pending = DONE_MAXITER;
+    else if (rrj < sc->trig2) sc->pending = DONE_REFRESH;
   }
 }
 
@@ -878,13 +932,17 @@ __global__ void __launch_bounds__(kBlock) mg_rz_kernel(int64_t n, const float *_
   }
 }
 
-// p = z + beta p  (or p = z)
-__global__ void mg_update_p_kernel(int64_t n, const float *__restrict__ z, float *__restrict__ p, const CgScalars *sc,
-                                   int reset) {
+// p = z + beta p  (or p = z); the last block turns a pending stop into `done`
+__global__ void mg_update_p_kernel(int64_t n, const float *__restrict__ z, float *__restrict__ p, CgScalars *sc,
+                                   unsigned int *ticket, int reset) {
   if (!reset && sc->done) return;
   const float beta = reset ? 0.f : (float)sc->beta;
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
     p[g] = z[g] + beta * (reset ? 0.f : p[g]);
+  if (!reset && sc->pending && grid_last_block(ticket)) {
+    sc->done = sc->pending;
+    sc->pending = 0;
+  }
 }
 
 void mg_iteration(ls_fd_handle *h, cudaStream_t st) {
@@ -892,9 +950,12 @@ void mg_iteration(ls_fd_handle *h, cudaStream_t st) {
   const int g = grid_for(h, h->n);
   mg_update_xr_kernel<<<g, kBlock, 0, st>>>(h->n, h->x32, h->r32, h->p32, h->q32, h->dinv32, h->sc, h->partials,
                                             h->tickets + T_UPDATE);
+  ++h->launches;
   mg_vcycle(h, &h->sc->done, st);
   mg_rz_kernel<<<g, kBlock, 0, st>>>(h->n, h->r32, h->z32, h->sc, h->partials, h->tickets + T_UPDATE, 0);
-  mg_update_p_kernel<<<g, kBlock, 0, st>>>(h->n, h->z32, h->p32, h->sc, 0);
+  ++h->launches;
+  mg_update_p_kernel<<<g, kBlock, 0, st>>>(h->n, h->z32, h->p32, h->sc, h->tickets + T_PUPD, 0);
+  ++h->launches;
 }
 
 // after a residual refresh: z = V(r), rz = r.z, optionally p = z
@@ -903,7 +964,11 @@ int mg_restart(ls_fd_handle *h, bool reset_p) {
   const int g = grid_for(h, h->n);
   mg_vcycle(h, nullptr, st);
   mg_rz_kernel<<<g, kBlock, 0, st>>>(h->n, h->r32, h->z32, h->sc, h->partials, h->tickets + T_UPDATE, 1);
-  if (reset_p) mg_update_p_kernel<<<g, kBlock, 0, st>>>(h->n, h->z32, h->p32, h->sc, 1);
+  ++h->launches;
+  if (reset_p) {
+    mg_update_p_kernel<<<g, kBlock, 0, st>>>(h->n, h->z32, h->p32, h->sc, h->tickets + T_PUPD, 1);
+    ++h->launches;
+  }
   LS_CUDA_TRY(cudaGetLastError());
   return LS_OK;
 }
@@ -945,9 +1010,9 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
   }
   h->red_blocks = sm_count() * 8;
   {
-    const int zc = apply_zchunk((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], sm_count());
-    const dim3 ag = apply_grid((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], zc);
-    const size_t nb = std::max<size_t>((size_t)h->red_blocks, (size_t)ag.x * ag.y * ag.z);
+    const dim3 a4 = apply_grid<float>((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], MODE_FULL);
+    const dim3 a8 = apply_grid<double>((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], MODE_FULL);
+    const size_t nb = std::max<size_t>({(size_t)h->red_blocks, (size_t)a4.x * a4.y * a4.z, (size_t)a8.x * a8.y * a8.z});
     if ((st = dev_alloc(&h->partials, 4 * nb)) < 0) return fail(st);
   }
   if ((st = dev_alloc(&h->tickets, T_COUNT)) < 0) return fail(st);
@@ -1066,11 +1131,16 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
   const int gn = grid_for(h, n);
   cudaMemsetAsync(h->rhs, 0, n * sizeof(double), hs);
   diag_stencil_kernel<<<gn, kBlock, 0, hs>>>(h->coef, h->diag);
-  if (d.ntouched > 0)
+  ++h->launches;
+  if (d.ntouched > 0) {
     data_node_setup_kernel<<<grid_for(h, d.ntouched), kBlock, 0, hs>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row,
                                                                        d.inc_a64, d.w2_64, d.b, h->diag, h->rhs);
+    ++h->launches;
+  }
   dinv_kernel<<<gn, kBlock, 0, hs>>>(n, h->diag, h->dinv64, h->dinv32);
+  ++h->launches;
   norm2_kernel<<<gn, kBlock, 0, hs>>>(n, h->rhs, h->dinv64, h->sc, h->partials, h->tickets + T_MISC);
+  ++h->launches;
   if (cudaGetLastError() != cudaSuccess || read_scalars(h) < 0) {
     set_error("setup kernels failed: %s", cudaGetErrorString(cudaGetLastError()));
     return fail(LS_ERR_CUDA);
@@ -1153,6 +1223,7 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
   const int64_t maxiter = opts->maxiter > 0 ? opts->maxiter : 10 * n;
   const double delta = opts->reliable_delta > 0.0 ? opts->reliable_delta : 0.1;
   *stats = ls_solve_stats{};
+  const int64_t launches0 = h->launches;
   const double bnorm = sqrt(h->rhs_norm2);
   const double thresh = std::max(opts->atol, opts->rtol * bnorm);
   stats->rhs_norm = bnorm;
@@ -1190,26 +1261,31 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
     s.iters = iters0;
     s.maxiter = maxiter;
     s.done = 0;
+    s.trig2 = delta * delta * s.rz32;
     LS_TRY(write_scalars(h));
     if (!h->g32 || h->g32_batch != batch) {
       if (h->g32) cudaGraphExecDestroy(h->g32);
       h->g32 = nullptr;
-      LS_TRY(build_graph<float>(h, batch, &h->g32, h->x32, h->r32, h->p32, h->q32, h->dinv32));
+      LS_TRY(build_graph<float>(h, batch, &h->g32, &h->g32_kernels, h->x32, h->r32, h->p32, h->q32, h->dinv32));
       h->g32_batch = batch;
     }
-    double rz_ref = s.rz32;
+    double last_true_r = true_r;
     for (;;) {
       LS_CUDA_TRY(cudaGraphLaunch(h->g32, st));
+      h->launches += h->g32_kernels;
       LS_TRY(read_scalars(h));
-      const bool trigger = s.done != 0 || s.rz < delta * delta * rz_ref;
-      if (!trigger) continue;
-      if (s.done == DONE_NAN || s.done == DONE_BREAKDOWN) {
-        status = done_to_status(s.done);
+      if (s.done == DONE_RUNNING) continue;
+      if (s.done == DONE_NAN) {
+        status = LS_NAN;
         break;
       }
-      // reliable update
+      // reliable update.  An FP32 breakdown (the recurrence residual reached
+      // zero, or p.Np lost its sign in rounding) restarts the direction from
+      // the refreshed residual; x32 still holds the last finite iterate.
+      const bool broke = s.done == DONE_BREAKDOWN;
       fold_kernel<<<grid_for(h, n), kBlock, 0, st>>>(n, h->x64, h->x32);
-      LS_TRY(refresh(h, true, h->r32, nullptr));
+      ++h->launches;
+      LS_TRY(refresh(h, true, h->r32, broke ? h->p32 : nullptr));
       const long long it_now = s.iters;
       LS_TRY(read_scalars(h));
       ++updates;
@@ -1218,6 +1294,11 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
         status = LS_OK;
         break;
       }
+      if (broke && !(true_r < 0.5 * last_true_r)) {  // no progress since the last refresh
+        status = LS_BREAKDOWN;
+        break;
+      }
+      last_true_r = true_r;
       if (it_now >= maxiter) {
         status = LS_NOT_CONVERGED;
         break;
@@ -1228,7 +1309,7 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
       }
       s.rz = s.rz32;
       s.done = 0;
-      rz_ref = s.rz32;
+      s.trig2 = delta * delta * s.rz32;
       LS_TRY(write_scalars(h));
     }
     iters = s.iters;
@@ -1246,15 +1327,17 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
     s.iters = 0;
     s.maxiter = maxiter;
     s.done = (s.rz < s.thresh2) ? DONE_CONVERGED : DONE_RUNNING;
+    s.trig2 = 0.0;
     LS_TRY(write_scalars(h));
     if (!h->g64 || h->g64_batch != batch) {
       if (h->g64) cudaGraphExecDestroy(h->g64);
       h->g64 = nullptr;
-      LS_TRY(build_graph<double>(h, batch, &h->g64, h->x64, h->r64, h->p64, h->q64, h->dinv64));
+      LS_TRY(build_graph<double>(h, batch, &h->g64, &h->g64_kernels, h->x64, h->r64, h->p64, h->q64, h->dinv64));
       h->g64_batch = batch;
     }
     while (!s.done) {
       LS_CUDA_TRY(cudaGraphLaunch(h->g64, st));
+      h->launches += h->g64_kernels;
       LS_TRY(read_scalars(h));
     }
     iters = s.iters;
@@ -1277,13 +1360,17 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
       s.maxiter = maxiter;
       s.done = 0;
       s.rrj = s.rz32;
+      s.trig2 = delta * delta * s.rz32;
       LS_TRY(write_scalars(h));
       const int mbatch = std::max(1, std::min(batch, 8));
       if (!h->gmg || h->gmg_batch != mbatch) {
         if (h->gmg) cudaGraphExecDestroy(h->gmg);
         h->gmg = nullptr;
+        const int64_t before = h->launches;
         LS_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         for (int it = 0; it < mbatch; ++it) mg_iteration(h, st);
+        h->gmg_kernels = h->launches - before;
+        h->launches = before;
         cudaGraph_t graph;
         LS_CUDA_TRY(cudaStreamEndCapture(st, &graph));
         cudaError_t e = cudaGraphInstantiate(&h->gmg, graph, 0);
@@ -1294,17 +1381,17 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
         }
         h->gmg_batch = mbatch;
       }
-      double rrj_ref = s.rz32;
       for (;;) {
         LS_CUDA_TRY(cudaGraphLaunch(h->gmg, st));
+        h->launches += h->gmg_kernels;
         LS_TRY(read_scalars(h));
-        const bool trigger = s.done != 0 || s.rrj < delta * delta * rrj_ref;
-        if (!trigger) continue;
+        if (s.done == DONE_RUNNING) continue;
         if (s.done == DONE_NAN || s.done == DONE_BREAKDOWN) {
           status = done_to_status(s.done);
           break;
         }
         fold_kernel<<<grid_for(h, n), kBlock, 0, st>>>(n, h->x64, h->x32);
+        ++h->launches;
         LS_TRY(refresh(h, true, h->r32, nullptr));
         const long long it_now = s.iters;
         LS_TRY(read_scalars(h));
@@ -1328,7 +1415,7 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
         LS_TRY(read_scalars(h));
         s.done = 0;
         s.rrj = s.rz32;
-        rrj_ref = s.rz32;
+        s.trig2 = delta * delta * s.rz32;
         LS_TRY(write_scalars(h));
       }
       iters = s.iters;
@@ -1355,6 +1442,7 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
   stats->device_ms = ms;
   stats->status = status;
   stats->preconditioner = use_mg ? LS_PRECOND_MG : LS_PRECOND_JACOBI;
+  stats->kernel_launches = h->launches - launches0;
   LS_CUDA_TRY(cudaGetLastError());
   return status;
 }
@@ -1380,12 +1468,18 @@ extern "C" int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps,
   const int gf = grid_for(h, n);
   if (f32) {
     fill_kernel<float><<<gf, kBlock, 0, st>>>(n, h->p32, 1.0f);
+    ++h->launches;
     fill_kernel<float><<<gf, kBlock, 0, st>>>(n, h->r32, 1.0f);
+    ++h->launches;
     fill_kernel<float><<<gf, kBlock, 0, st>>>(n, h->x32, 0.0f);
+    ++h->launches;
   } else {
     fill_kernel<double><<<gf, kBlock, 0, st>>>(n, h->p64, 1.0);
+    ++h->launches;
     fill_kernel<double><<<gf, kBlock, 0, st>>>(n, h->r64, 1.0);
+    ++h->launches;
     fill_kernel<double><<<gf, kBlock, 0, st>>>(n, h->x64, 0.0);
+    ++h->launches;
   }
   auto timed = [&](auto &&fn, double *ms_out) -> int {
     fn();  // warm-up
@@ -1404,31 +1498,42 @@ extern "C" int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps,
     if (f32) {
       EpiArgs<float> e{};
       e.q = h->q32;
-      const int zc = apply_zchunk((int)h->coef.nx, (int)h->coef.ny, (int)h->coef.nz, sm_count());
-      fd_apply_kernel<float, EPI_STORE><<<apply_grid((int)h->coef.nx, (int)h->coef.ny, (int)h->coef.nz, zc), dim3(kAX, kAY), 0, st>>>(
-          coef_as<float>(h->coef), h->p32, data_view<float>(h, h->s32, d.inc_a32), e, zc, nullptr, h->partials, h->tickets + T_STENCIL, &h->sc->pq_s);
+      h->launches += launch_operator<float, EPI_STORE>(coef_as<float>(h->coef), h->p32,
+                                                       data_view<float>(h, h->s32, d.inc_a32), e, nullptr, h->partials,
+                                                       h->tickets + T_STENCIL, &h->sc->pq_s, h->tickets + T_SHELL,
+                                                       &h->sc->pq_d, h->red_blocks, st);
     } else {
       EpiArgs<double> e{};
       e.q = h->q64;
-      const int zc = apply_zchunk((int)h->coef.nx, (int)h->coef.ny, (int)h->coef.nz, sm_count());
-      fd_apply_kernel<double, EPI_STORE><<<apply_grid((int)h->coef.nx, (int)h->coef.ny, (int)h->coef.nz, zc), dim3(kAX, kAY), 0, st>>>(
-          coef_as<double>(h->coef), h->p64, data_view<double>(h, h->s64, d.inc_a64), e, zc, nullptr, h->partials, h->tickets + T_STENCIL, &h->sc->pq_s);
+      h->launches += launch_operator<double, EPI_STORE>(coef_as<double>(h->coef), h->p64,
+                                                        data_view<double>(h, h->s64, d.inc_a64), e, nullptr, h->partials,
+                                                        h->tickets + T_STENCIL, &h->sc->pq_s, h->tickets + T_SHELL,
+                                                        &h->sc->pq_d, h->red_blocks, st);
     }
   }, &out->stencil_ms));
   out->data_ms = 0.0;
   if (d.nrows > 0) {
     LS_TRY(timed([&] {
-      if (f32) rows_kernel<float><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, d.a32, d.w2_32, h->p32, h->s32, nullptr);
-      else rows_kernel<double><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, d.a64, d.w2_64, h->p64, h->s64, nullptr);
+      if (f32) {
+        rows_kernel<float><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, d.a32, d.w2_32, h->p32, h->s32, nullptr);
+        ++h->launches;
+      } else {
+        rows_kernel<double><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, d.a64, d.w2_64, h->p64, h->s64, nullptr);
+        ++h->launches;
+      }
     }, &out->data_ms));
   }
   LS_TRY(timed([&] {
     if (f32) {
       update_xr_kernel<float><<<g, kBlock, 0, st>>>(n, h->x32, h->r32, h->p32, h->q32, h->dinv32, h->sc, h->partials, h->tickets + T_UPDATE);
-      update_p_kernel<float><<<g, kBlock, 0, st>>>(n, h->r32, h->dinv32, h->p32, h->sc);
+      ++h->launches;
+      update_p_kernel<float><<<g, kBlock, 0, st>>>(n, h->r32, h->dinv32, h->p32, h->sc, h->tickets + T_PUPD);
+      ++h->launches;
     } else {
       update_xr_kernel<double><<<g, kBlock, 0, st>>>(n, h->x64, h->r64, h->p64, h->q64, h->dinv64, h->sc, h->partials, h->tickets + T_UPDATE);
-      update_p_kernel<double><<<g, kBlock, 0, st>>>(n, h->r64, h->dinv64, h->p64, h->sc);
+      ++h->launches;
+      update_p_kernel<double><<<g, kBlock, 0, st>>>(n, h->r64, h->dinv64, h->p64, h->sc, h->tickets + T_PUPD);
+      ++h->launches;
     }
   }, &out->update_ms));
   LS_TRY(timed([&] {

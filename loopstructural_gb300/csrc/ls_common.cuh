@@ -107,6 +107,21 @@ __device__ __forceinline__ bool grid_sum_ex(double v, double *partials, unsigned
   return tid == 0;
 }
 
+// True in thread 0 of the last block of a 1-D grid to arrive here (all other
+// blocks' writes fenced before); re-arms the ticket.  Every block must call it.
+__device__ __forceinline__ bool grid_last_block(unsigned int *ticket) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned int t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+    if (last) *ticket = 0u;
+  }
+  __syncthreads();
+  return last && threadIdx.x == 0;
+}
+
 template <int BLOCK>
 __device__ __forceinline__ bool grid_sum(double v, double *partials, unsigned int *ticket, double *total) {
   return grid_sum_ex<BLOCK>(v, partials, ticket, total, threadIdx.x, blockIdx.x, gridDim.x);

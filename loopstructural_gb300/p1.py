@@ -1,0 +1,171 @@
+"""P1 (structured TetMesh) interpolator on the GPU.
+
+Mirrors packages/loop_interpolation/src/loop_interpolation/_p1interpolator.py
+(P1): constant-gradient face regularisation (P1:115-166), normal rows
+(P1:73-96, w = npw, no /3), value rows (P1:98-113, per-point weight column
+ignored), gradient constraints a no-op (P1:70-71), setup order P1:180-246.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import logging
+
+import numpy as np
+
+from . import _lib, fd
+from .interpolators import SetupReport, _DiscreteInterpolatorBase
+
+logger = logging.getLogger(__name__)
+
+
+def face_rows(mesh, weight: float, with_topology: bool = False):
+    """All face rows of the mesh on the device (K3): (idc (F,8), a, b, w[, pairs, shared])."""
+    import torch
+
+    dev = _lib.device()
+    lib = _lib.load()
+    g = mesh.grid3()
+    nf = C.c_int64(0)
+    _lib.check(lib.ls_p1_face_count(C.byref(g), C.byref(nf)))
+    F = nf.value
+    idc = torch.empty((F, 8), dtype=torch.int64, device=dev)
+    a = torch.empty((F, 8), dtype=torch.float64, device=dev)
+    b = torch.empty(F, dtype=torch.float64, device=dev)
+    w = torch.empty(F, dtype=torch.float64, device=dev)
+    pairs = torch.empty((F, 2), dtype=torch.int64, device=dev) if with_topology else None
+    shared = torch.empty((F, 3), dtype=torch.int64, device=dev) if with_topology else None
+    _lib.check(lib.ls_p1_face_rows(C.byref(g), float(weight), _lib.ptr(pairs), _lib.ptr(shared), _lib.ptr(idc),
+                                   _lib.ptr(a), _lib.ptr(b), _lib.ptr(w), _lib.stream_ptr()))
+    if with_topology:
+        return idc, a, b, w, pairs, shared
+    return idc, a, b, w
+
+
+def locate(mesh, pts: np.ndarray):
+    import torch
+
+    dev = _lib.device()
+    lib = _lib.load()
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    n = pts.shape[0]
+    d_pts = torch.from_numpy(pts).to(dev)
+    tet = torch.empty(n, dtype=torch.int64, device=dev)
+    bc = torch.empty((n, 4), dtype=torch.float64, device=dev)
+    g = mesh.grid3()
+    _lib.check(lib.ls_p1_locate(C.byref(g), _lib.ptr(d_pts), n, pts.shape[1], _lib.ptr(tet), _lib.ptr(bc),
+                                _lib.stream_ptr()))
+    return tet.cpu().numpy(), bc.cpu().numpy()
+
+
+def point_rows(mesh, kind: int, pts: np.ndarray, weight: float):
+    import torch
+
+    dev = _lib.device()
+    lib = _lib.load()
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    n, ld = pts.shape
+    per = 3 if kind == _lib.ROWS_NORM else 1
+    d_pts = torch.from_numpy(pts).to(dev)
+    idc = torch.empty((per * n, 4), dtype=torch.int64, device=dev)
+    a = torch.empty((per * n, 4), dtype=torch.float64, device=dev)
+    b = torch.empty(per * n, dtype=torch.float64, device=dev)
+    w = torch.empty(per * n, dtype=torch.float64, device=dev)
+    cnt = C.c_int64(0)
+    g = mesh.grid3()
+    _lib.check(lib.ls_p1_point_rows(C.byref(g), kind, _lib.ptr(d_pts), n, ld, float(weight), _lib.ptr(idc),
+                                    _lib.ptr(a), _lib.ptr(b), _lib.ptr(w), C.byref(cnt), _lib.stream_ptr()))
+    r = per * cnt.value
+    return idc[:r], a[:r], b[:r], w[:r]
+
+
+def eval_points(mesh, c, pts: np.ndarray, value=True, gradient=True):
+    import torch
+
+    dev = _lib.device()
+    lib = _lib.load()
+    pts = np.ascontiguousarray(pts, dtype=np.float64)
+    n = pts.shape[0]
+    c_t = c if isinstance(c, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(c, dtype=np.float64))
+    c_t = c_t.to(device=dev, dtype=torch.float64).contiguous()
+    d_pts = torch.from_numpy(pts).to(dev)
+    v = torch.empty(n, dtype=torch.float64, device=dev) if value else None
+    gr = torch.empty((n, 3), dtype=torch.float64, device=dev) if gradient else None
+    g = mesh.grid3()
+    _lib.check(lib.ls_p1_eval_points(C.byref(g), _lib.ptr(c_t), _lib.ptr(d_pts), n, pts.shape[1], _lib.ptr(v),
+                                     _lib.ptr(gr), _lib.stream_ptr()))
+    return (v.cpu().numpy() if value else None, gr.cpu().numpy() if gradient else None)
+
+
+class P1Interpolator(_DiscreteInterpolatorBase):
+    """Piecewise-linear interpolator on a TetMesh (P1:23-299)."""
+
+    def __init__(self, mesh):
+        super().__init__(mesh)
+        self.interpolation_weights = {"cgw": 0.1, "cpw": 1.0, "npw": 1.0, "gpw": 1.0, "tpw": 1.0, "ipw": 1.0}
+        self.use_regularisation_weight_scale = False
+
+    def setup_interpolator(self, **kwargs) -> SetupReport:
+        self.reset()
+        reg = kwargs.get("regularisation", None)
+        if isinstance(reg, dict):
+            reg = reg.get("isotropic", reg.get("weight", None))
+        if reg is not None:
+            self.interpolation_weights["cgw"] = float(reg)
+        if kwargs.get("directional_regularisation") is not None:
+            raise NotImplementedError("directional regularisation is not part of the GPU path")
+        for k, v in kwargs.items():
+            self.up_to_date = False
+            if k in ("regularisation", "directional_regularisation"):
+                continue
+            self.interpolation_weights[k] = v
+        if kwargs.get("use_regularisation_weight_scale", False):
+            raise NotImplementedError("use_regularisation_weight_scale is not part of the GPU path")
+        w = self.interpolation_weights
+        if w["cgw"] > 0.0:
+            idc, a, b, ww = face_rows(self.support, w["cgw"])
+            self._add_family("edge jump", idc, a, b, ww)
+        # gradient constraints: no-op in the reference P1 (P1:70-71)
+        normals = self.get_norm_constraints()
+        if normals.shape[0] > 0:
+            self._add_family("norm", *point_rows(self.support, _lib.ROWS_NORM, normals, w["npw"]))
+        values = self.get_value_constraints()
+        if values.shape[0] > 0:
+            self._add_family("value", *point_rows(self.support, _lib.ROWS_VALUE, values, w["cpw"]))
+        if self.get_tangent_constraints().shape[0] > 0:
+            raise NotImplementedError("P1 tangent constraints are not part of the GPU path")
+        self.up_to_date = False
+        return SetupReport({name: f.n_rows for name, f in self.constraints.items()})
+
+    def _build_system(self):
+        rows = [(f.idc, f.a, f.b, f.w) for f in self.constraints.values()]
+        ridge = self.ridge_factor if self.add_ridge_regulatisation else 0.0
+        zero = {k: 0.0 for k in ("dxx", "dyy", "dzz", "dxy", "dyz", "dxz", "dx", "dy", "dz")}
+        return fd.FdSystem(self.support, zero, rows, ridge)
+
+    def _solver_options(self, solver, tol, solver_kwargs):
+        solver, opts = super()._solver_options(solver, tol, solver_kwargs)
+        opts["preconditioner"] = "jacobi"  # the multigrid hierarchy is the FD stencil's
+        return solver, opts
+
+    def _matrix_rows(self):
+        return sum(f.n_rows for f in self.constraints.values())
+
+    def _matrix_nnz(self):
+        return sum(f.n_rows * f.idc.shape[1] for f in self.constraints.values())
+
+    def _evaluate_value_local(self, locations):
+        self.update()
+        loc = np.asarray(locations, dtype=float)
+        if loc.shape[0] == 0:
+            return np.zeros(0)
+        return eval_points(self.support, self._c_device(), loc, value=True, gradient=False)[0]
+
+    def _evaluate_gradient_local(self, locations):
+        self.update()
+        loc = np.asarray(locations, dtype=float)
+        if loc.shape[0] == 0:
+            return np.zeros((0, 3))
+        return eval_points(self.support, self._c_device(), loc, value=False, gradient=True)[1]
+
+
+PiecewiseLinearInterpolator = P1Interpolator

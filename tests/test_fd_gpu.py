@@ -116,7 +116,8 @@ def test_normal_operator_rhs_diagonal_match_oracle(golden, name):
     system.close()
 
 
-@pytest.mark.parametrize("cells", [(5, 5, 5), (8, 6, 12), (14, 14, 14), (1, 4, 5), (2, 2, 9)])
+@pytest.mark.parametrize("cells", [(5, 5, 5), (8, 6, 12), (14, 14, 14), (1, 4, 5), (2, 2, 9), (23, 23, 23),
+                                   (26, 24, 33)])
 def test_regularisation_operator_matches_explicit_gram_everywhere(cells):
     """The reference's fused-operator test (every DOF, non-uniform family weights)."""
     kw = dict(dxx=1.0, dyy=0.8, dzz=1.3, dxy=0.5, dxz=0.4, dyz=0.6, dx=0.7, dy=0.9, dz=1.1,
@@ -129,6 +130,28 @@ def test_regularisation_operator_matches_explicit_gram_everywhere(cells):
     fdo.add_regularisation(grid, cs, fdo.resolve_weights(**kw))
     A, _ = cs.matrix()
     _check_operator(system, A, x_seed=11)
+    system.close()
+
+
+def test_normal_operator_with_data_on_split_grid():
+    """Grids of >= 24 nodes per axis run the deep-box kernel plus the boundary-shell
+    kernel; the data term must land on both."""
+    cells = np.array([25, 24, 27])
+    rng = np.random.default_rng(5)
+    vp = rng.uniform(0, 1, size=(400, 3))
+    val = np.column_stack([vp, vp[:, 2] + 0.1 * vp[:, 0], np.ones(400)])
+    npnt = rng.uniform(0, 1, size=(80, 3))
+    nrm = np.column_stack([npnt, rng.normal(size=(80, 3)), np.ones(80)])
+    setup = dict(regularisation=0.1, cpw=1.0, npw=1.0)
+    interp = L.FiniteDifferenceInterpolator(_grid(cells))
+    interp.set_value_constraints(val)
+    interp.set_normal_constraints(nrm)
+    interp.setup_interpolator(**setup)
+    system = interp._build_system()
+    grid = fdo.Grid(np.zeros(3), cells, 1.0 / cells.astype(float))
+    cs = fdo.assemble(grid, {"value": val, "normal": nrm}, fdo.resolve_weights(**setup))
+    A, _ = cs.matrix()
+    _check_operator(system, A, x_seed=3)
     system.close()
 
 
