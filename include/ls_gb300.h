@@ -226,6 +226,18 @@ typedef struct ls_fd_profile {
 
 int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps, ls_fd_profile *out, void *stream);
 
+/* Device time per launch (ms, CUDA events over `reps` back-to-back launches on
+ * the handle's stream) of the parts of the multigrid V-cycle on every level,
+ * building the hierarchy if needed.  out[l * LS_MG_PROFILE_FIELDS + f] for
+ * level l < *levels (at most max_levels): f = 0 nodes, 1 operator apply
+ * (plain), 2 apply with the Chebyshev epilogue, 3 apply with the residual
+ * epilogue, 4 restriction to level l+1, 5 prolongation from level l+1,
+ * 6 data rows (row form), 7 the coarsest dense solve (last level only).
+ * Returns 0 with *levels = 0 when the grid does not coarsen.  The solver
+ * vectors are overwritten.  No counterpart in the reference. */
+#define LS_MG_PROFILE_FIELDS 8
+int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_levels, int *levels, void *stream);
+
 /* ------------------------------------------------------------------ */
 /* FD evaluation (K7)                                                   */
 /* ------------------------------------------------------------------ */

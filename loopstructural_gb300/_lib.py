@@ -33,7 +33,7 @@ EXPORTS = (
     "ls_last_error", "ls_abi_version",
     "ls_fd_point_rows", "ls_fd_pair_rows", "ls_fd_reg_shape", "ls_fd_reg_rows",
     "ls_fd_create", "ls_fd_destroy", "ls_fd_dof", "ls_fd_apply", "ls_fd_apply_f32", "ls_fd_apply_noalloc", "ls_fd_rhs",
-    "ls_fd_diagonal", "ls_fd_solve", "ls_fd_profile_iteration", "ls_fd_eval_points", "ls_fd_eval_lattice",
+    "ls_fd_diagonal", "ls_fd_solve", "ls_fd_profile_iteration", "ls_fd_profile_mg", "ls_fd_eval_points", "ls_fd_eval_lattice",
     "ls_p1_face_count", "ls_p1_face_rows", "ls_p1_locate", "ls_p1_point_rows", "ls_p1_eval_points",
 )
 
@@ -116,6 +116,7 @@ _SIGS = {
     "ls_fd_diagonal": (C.c_int, [_P, _P, _P]),
     "ls_fd_solve": (C.c_int, [_P, C.POINTER(SolveOpts), _P, C.POINTER(SolveStats), _P]),
     "ls_fd_profile_iteration": (C.c_int, [_P, C.c_int, C.c_int, C.POINTER(FdProfile), _P]),
+    "ls_fd_profile_mg": (C.c_int, [_P, C.c_int, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int), _P]),
     "ls_fd_eval_points": (C.c_int, [C.POINTER(Grid3), _P, _P, C.c_int64, C.c_int64, _P, _P, _P]),
     "ls_fd_eval_lattice": (C.c_int, [C.POINTER(Grid3), _P, C.POINTER(C.c_double * 3), C.POINTER(C.c_double * 3),
                                      C.POINTER(C.c_int64 * 3), _P, _P, _P]),

@@ -39,6 +39,12 @@ struct DataView {
   const T *s_rows;           // w^2 (a_row . p) of the current p
   const T *qd;               // optional: per-touched-node totals from data_nodes_warp_kernel
   int enabled;
+  // optional 27-point form of data rows confined to one cell (coarse
+  // multigrid levels): q += sum_o k27[o][rank] p(node + o) at marked nodes
+  const uint32_t *kmask;
+  const int32_t *krank;
+  const T *k27;  // 27 x knt, offset o = 9 (dz+1) + 3 (dy+1) + (dx+1)
+  int64_t knt;
 };
 
 // Epilogues -----------------------------------------------------------------
@@ -55,23 +61,62 @@ struct EpiArgs {
   T c1, c2;
 };
 
+// Epilogue operands read at the output node, loaded ahead of the stencil
+// (software prefetch) so that their latency overlaps the arithmetic.
+template <typename T>
+struct EpiIn {
+  T x, r, dinv;
+};
+
 template <typename T, int EPI>
-__device__ __forceinline__ T epilogue(const EpiArgs<T> &e, int g, T p_own, T q) {
+__device__ __forceinline__ EpiIn<T> epi_load(const EpiArgs<T> &e, int g) {
+  EpiIn<T> v{};
+  if (EPI == EPI_CHEB) {
+    v.x = e.x[g];
+    v.r = e.r[g];
+    v.dinv = e.dinv[g];
+  } else if (EPI == EPI_RESID) {
+    v.r = e.b[g];
+    v.dinv = e.dinv[g];
+  }
+  return v;
+}
+
+template <typename T, int EPI>
+__device__ __forceinline__ T epi_store(const EpiArgs<T> &e, int g, T p_own, T q, const EpiIn<T> &v) {
   if (EPI == EPI_STORE) {
     e.q[g] = q;
     return p_own * q;
   } else if (EPI == EPI_CHEB) {
-    e.x[g] += p_own;
-    const T rn = e.r[g] - q;
+    e.x[g] = v.x + p_own;
+    const T rn = v.r - q;
     e.r[g] = rn;
-    e.d_out[g] = e.c1 * p_own + e.c2 * e.dinv[g] * rn;
+    e.d_out[g] = e.c1 * p_own + e.c2 * v.dinv * rn;
     return (T)0;
   } else {
-    const T rn = e.b[g] - q;
+    const T rn = v.r - q;  // v.r holds b
     e.r[g] = rn;
-    e.d_out[g] = e.c2 * e.dinv[g] * rn;
+    e.d_out[g] = e.c2 * v.dinv * rn;
     return (T)0;
   }
+}
+
+template <typename T, int EPI>
+__device__ __forceinline__ T epilogue(const EpiArgs<T> &e, int g, T p_own, T q) {
+  return epi_store<T, EPI>(e, g, p_own, q, epi_load<T, EPI>(e, g));
+}
+
+// Data term at node g whose mask word has been loaded already.
+template <typename T>
+__device__ __forceinline__ T data_term_w(const DataView<T> &dv, int g, uint32_t word) {
+  const uint32_t bit = 1u << (g & 31);
+  if (!(word & bit)) return (T)0;
+  const int rank = __ldg(dv.word_rank + (g >> 5)) + __popc(word & (bit - 1u));
+  if (dv.qd) return dv.qd[rank];
+  T acc = 0;
+  const int64_t e1 = __ldg(dv.inc_ptr + rank + 1);
+  for (int64_t e = __ldg(dv.inc_ptr + rank); e < e1; ++e) acc += __ldg(dv.inc_a + e) * __ldg(dv.s_rows + __ldg(dv.inc_row + e));
+  return acc;
 }
 
 template <typename T>
@@ -85,6 +130,22 @@ __device__ __forceinline__ T data_term(const DataView<T> &dv, int g) {
   const int64_t e1 = __ldg(dv.inc_ptr + rank + 1);
   for (int64_t e = __ldg(dv.inc_ptr + rank); e < e1; ++e) acc += __ldg(dv.inc_a + e) * __ldg(dv.s_rows + __ldg(dv.inc_row + e));
   return acc;
+}
+
+template <typename T, typename PR>
+__device__ __forceinline__ T k27_term_w(const DataView<T> &dv, int g, uint32_t word, const PR &pr) {
+  const uint32_t bit = 1u << (g & 31);
+  if (!(word & bit)) return (T)0;
+  const int rank = __ldg(dv.krank + (g >> 5)) + __popc(word & (bit - 1u));
+  T acc = 0;
+#pragma unroll
+  for (int o = 0; o < 27; ++o) acc += __ldg(dv.k27 + (int64_t)o * dv.knt + rank) * pr(o / 9 - 1, (o / 3) % 3 - 1, o % 3 - 1);
+  return acc;
+}
+
+template <typename T, typename PR>
+__device__ __forceinline__ T k27_term(const DataView<T> &dv, int g, const PR &pr) {
+  return k27_term_w<T>(dv, g, __ldg(dv.kmask + (g >> 5)), pr);
 }
 
 // Per-axis row-existence factors of a node coordinate a on an axis of n nodes:
@@ -186,8 +247,8 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // they are, so only a 5-plane window stays live in registers.
 // Returns the block's sum of the epilogue contributions (p.q for EPI_STORE)
 // through the deterministic grid reduction when `dot_out` is set.
-template <typename T, int EPI, int MODE>
-__global__ void __launch_bounds__(kAX * kAY) fd_apply_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv,
+template <typename T, int EPI, int MODE, bool K27>
+__global__ void __launch_bounds__(kAX * kAY, MODE == MODE_DEEP ? 4 : 1) fd_apply_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv,
                                                              EpiArgs<T> e, const int *done, double *partials,
                                                              unsigned int *ticket, double *dot_out) {
   if (done && *done) return;
@@ -199,7 +260,21 @@ __global__ void __launch_bounds__(kAX * kAY) fd_apply_kernel(CoefT<T> c, const T
             ze = MODE == MODE_DEEP ? nz - 3 : nz;  // one past the last covered node
   const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + kAX * ty;
   const int x0 = org + blockIdx.x * kAX, y0 = org + blockIdx.y * kAY, z0 = org + blockIdx.z * TZ;
-  const size_t sxy = (size_t)nx * ny;
+  const int sxy = nx * ny;  // node counts stay below 2^31
+  const int i = x0 + tx, j = y0 + ty;
+  const bool col_in = (i < xe) & (j < ye);
+  const int gcol = j * nx + i;
+  // mask words of the column's output nodes, loaded before the staging burst
+  // and reduced to one bit per output plane while it is in flight
+  uint32_t mw[TZ], kw[TZ];
+#pragma unroll
+  for (int oz = 0; oz < TZ; ++oz) {
+    const int g = (z0 + oz) * sxy + gcol;
+    const bool ok = col_in & (z0 + oz < ze);
+    mw[oz] = (dv.enabled && ok) ? __ldg(dv.mask + (g >> 5)) : 0u;
+    kw[oz] = (K27 && ok) ? __ldg(dv.kmask + (g >> 5)) : 0u;
+  }
+  uint32_t dbits = 0u, kbits = 0u;
   // ---- stage the tile ----
   {
     int off[2];
@@ -217,22 +292,30 @@ __global__ void __launch_bounds__(kAX * kAY) fd_apply_kernel(CoefT<T> c, const T
     for (int hz = 0; hz < SZ; ++hz) {
       const int gz = z0 - 2 + hz;
       const bool vz = (gz >= 0) & (gz < nz);
-      const T *src = p + (vz ? (size_t)gz * sxy : 0);
+      const T *src = p + (vz ? gz * sxy : 0);
       cp_async_elem<T>(base + hz * PLANE + tid, src + off[0], vz & vxy[0]);
       if (tid + kAX * kAY < PLANE) cp_async_elem<T>(base + hz * PLANE + tid + kAX * kAY, src + off[1], vz & vxy[1]);
     }
   }
   cp_async_commit();
+#pragma unroll
+  for (int oz = 0; oz < TZ; ++oz) {
+    const int g = (z0 + oz) * sxy + gcol;
+    dbits |= ((mw[oz] >> (g & 31)) & 1u) << oz;
+    if (K27) kbits |= ((kw[oz] >> (g & 31)) & 1u) << oz;
+  }
   cp_async_wait_all();
   __syncthreads();
-  const int i = x0 + tx, j = y0 + ty;
   T local = 0;
-  if ((i < xe) & (j < ye)) {
+  if (col_in) {
     const bool col_deep = MODE == MODE_DEEP || ((i >= 3) & (i <= nx - 4) & (j >= 3) & (j <= ny - 4));
     const int hx = tx + 2, hy = ty + 2;
     T P[SZ], Cx[SZ], Cy[SZ];
+    EpiIn<T> pre[TZ];
 #pragma unroll
     for (int hz = 0; hz < SZ; ++hz) {
+      // epilogue operands of output plane hz - 2, two planes ahead of their use
+      if (hz >= 2 && hz - 2 < TZ && z0 + hz - 2 < ze) pre[hz - 2] = epi_load<T, EPI>(e, (z0 + hz - 2) * sxy + gcol);
       const T(&pl)[kHY][kHX] = sm[hz];
       const T p0 = pl[hy][hx];
       P[hz] = p0;
@@ -240,9 +323,10 @@ __global__ void __launch_bounds__(kAX * kAY) fd_apply_kernel(CoefT<T> c, const T
       Cy[hz] = (pl[hy - 2][hx] + pl[hy + 2][hx]) - (T)2 * p0;
       if (hz >= 4) {
         const int ho = hz - 2;  // staged plane of the output
-        const int z = z0 + ho - 2;
+        const int oz = ho - 2;
+        const int z = z0 + oz;
         if (z < ze) {
-          const size_t g = (size_t)z * sxy + (size_t)j * nx + i;
+          const int g = z * sxy + gcol;
           T q;
           if (col_deep & (MODE == MODE_DEEP || ((z >= 3) & (z <= nz - 4)))) {
             const T(&po)[kHY][kHX] = sm[ho];
@@ -259,8 +343,12 @@ __global__ void __launch_bounds__(kAX * kAY) fd_apply_kernel(CoefT<T> c, const T
             auto pr = [&](int dz, int dy, int dx) -> T { return sm[ho + dz][hy + dy][hx + dx]; };
             q = shell_node<T>(c, pr, i, j, z);
           }
-          if (dv.enabled) q += data_term<T>(dv, (int)g);
-          local += epilogue<T, EPI>(e, (int)g, P[ho], q);
+          if ((dbits >> oz) & 1u) q += data_term<T>(dv, g);
+          if (K27 && ((kbits >> oz) & 1u)) {
+            auto pk = [&](int dz, int dy, int dx) -> T { return sm[ho + dz][hy + dy][hx + dx]; };
+            q += k27_term<T>(dv, g, pk);
+          }
+          local += epi_store<T, EPI>(e, g, P[ho], q, pre[oz]);
         }
       }
     }
@@ -268,7 +356,7 @@ __global__ void __launch_bounds__(kAX * kAY) fd_apply_kernel(CoefT<T> c, const T
   if (dot_out) {
     double tot;
     const unsigned int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    if (grid_sum_ex<kAX * kAY>((double)local, partials, ticket, &tot, tid, bid, gridDim.x * gridDim.y * gridDim.z))
+    if (grid_sum_ex<kAX * kAY, T>(local, partials, ticket, &tot, tid, bid, gridDim.x * gridDim.y * gridDim.z))
       *dot_out = tot;
   }
 }
@@ -317,56 +405,94 @@ __device__ __forceinline__ void shell_node_index(int64_t s, int nx, int ny, int 
   }
 }
 
-// The exact operator at the shell nodes of a split grid (one thread per node,
-// neighbours straight from L1/L2), with the data term and the epilogue.
-template <typename T, int EPI>
-__global__ void __launch_bounds__(256) fd_shell_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv,
+// The exact operator node by node (one thread per node, neighbours straight
+// from L1/L2), with the data term and the epilogue: the boundary shell of a
+// split grid (ALL = false), or every node of a small grid (ALL = true), where
+// a thread per node exposes more parallelism than the staged tiles.
+template <typename T, int EPI, bool ALL, bool K27>
+__global__ void __launch_bounds__(256) fd_point_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv,
                                                        EpiArgs<T> e, const int *done, double *partials,
                                                        unsigned int *ticket, double *dot_out) {
   if (done && *done) return;
   const int nx = c.nx, ny = c.ny, nz = c.nz;
-  const int64_t ns = shell_count(nx, ny, nz);
+  const int64_t ns = ALL ? (int64_t)nx * ny * nz : shell_count(nx, ny, nz);
   T local = 0;
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns; s += (int64_t)gridDim.x * blockDim.x) {
     int i, j, k;
-    shell_node_index(s, nx, ny, nz, i, j, k);
+    if (ALL) {
+      k = (int)(s / ((int64_t)nx * ny));
+      const int rem = (int)(s - (int64_t)k * nx * ny);
+      j = rem / nx;
+      i = rem - j * nx;
+    } else {
+      shell_node_index(s, nx, ny, nz, i, j, k);
+    }
+    // neighbours at offsets -2..2: per-axis validity bits, one predicated load each
+    unsigned vx = 0u, vy = 0u, vz = 0u;
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) {
+      vx |= (unsigned)((i + d >= 0) & (i + d < nx)) << (d + 2);
+      vy |= (unsigned)((j + d >= 0) & (j + d < ny)) << (d + 2);
+      vz |= (unsigned)((k + d >= 0) & (k + d < nz)) << (d + 2);
+    }
+    const int g = (k * ny + j) * nx + i;
+    const int sxy = nx * ny;
     auto pr = [&](int dz, int dy, int dx) -> T {
-      const int a = i + dx, b = j + dy, cz = k + dz;
-      return ((a >= 0) & (a < nx) & (b >= 0) & (b < ny) & (cz >= 0) & (cz < nz))
-                 ? __ldg(p + ((size_t)cz * ny + b) * nx + a)
-                 : (T)0;
+      const bool ok = (vz >> (dz + 2)) & (vy >> (dy + 2)) & (vx >> (dx + 2)) & 1u;
+      return ok ? __ldg(p + (g + dz * sxy + dy * nx + dx)) : (T)0;
     };
     T q = shell_node<T>(c, pr, i, j, k);
-    const int g = (int)(((size_t)k * ny + j) * nx + i);
     if (dv.enabled) q += data_term<T>(dv, g);
+    if (K27) q += k27_term<T>(dv, g, pr);
     local += epilogue<T, EPI>(e, g, __ldg(p + g), q);
   }
   if (dot_out) {
     double tot;
-    if (grid_sum<256>((double)local, partials, ticket, &tot)) *dot_out = tot;
+    if (grid_sum<256, T>(local, partials, ticket, &tot)) *dot_out = tot;
   }
 }
 
-// q = N_reg p (+ data term) with an epilogue: the deep-box kernel plus the
-// shell kernel on split grids, else one full-grid kernel.  The epilogue sums
-// land in dot_main (full grid / deep box) and dot_shell (shell; untouched on
-// unsplit grids).  Returns the number of kernels launched.
+// Grids with fewer nodes than this run the node-per-thread kernel alone.
+constexpr int64_t kPointMaxNodes = 300000;
+
+template <typename T, int EPI, bool K27>
+inline int launch_operator_k(const CoefT<T> &c, const T *p, const DataView<T> &dv, const EpiArgs<T> &e,
+                             const int *done, double *partials, unsigned int *ticket_main, double *dot_main,
+                             unsigned int *ticket_shell, double *dot_shell, int max_blocks, cudaStream_t st) {
+  const dim3 blk(kAX, kAY);
+  const int64_t n = (int64_t)c.nx * c.ny * c.nz;
+  if (n <= kPointMaxNodes) {
+    const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, max_blocks));
+    fd_point_kernel<T, EPI, true, K27><<<gs, 256, 0, st>>>(c, p, dv, e, done, partials, ticket_main, dot_main);
+    return 1;
+  }
+  if (apply_split(c.nx, c.ny, c.nz)) {
+    fd_apply_kernel<T, EPI, MODE_DEEP, K27><<<apply_grid<T>(c.nx, c.ny, c.nz, MODE_DEEP), blk, 0, st>>>(
+        c, p, dv, e, done, partials, ticket_main, dot_main);
+    const int64_t ns = shell_count(c.nx, c.ny, c.nz);
+    const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((ns + 255) / 256, max_blocks));
+    fd_point_kernel<T, EPI, false, K27><<<gs, 256, 0, st>>>(c, p, dv, e, done, partials, ticket_shell, dot_shell);
+    return 2;
+  }
+  fd_apply_kernel<T, EPI, MODE_FULL, K27><<<apply_grid<T>(c.nx, c.ny, c.nz, MODE_FULL), blk, 0, st>>>(
+      c, p, dv, e, done, partials, ticket_main, dot_main);
+  return 1;
+}
+
+// q = N_reg p (+ data term) with an epilogue: one node-per-thread kernel on
+// small grids; the deep-box kernel plus the shell kernel on split grids; else
+// one staged full-grid kernel.  The epilogue sums land in dot_main (full grid
+// / deep box) and dot_shell (shell; untouched otherwise).  Returns the number
+// of kernels launched.
 template <typename T, int EPI>
 inline int launch_operator(const CoefT<T> &c, const T *p, const DataView<T> &dv, const EpiArgs<T> &e, const int *done,
                            double *partials, unsigned int *ticket_main, double *dot_main, unsigned int *ticket_shell,
                            double *dot_shell, int max_blocks, cudaStream_t st) {
-  const dim3 blk(kAX, kAY);
-  if (apply_split(c.nx, c.ny, c.nz)) {
-    fd_apply_kernel<T, EPI, MODE_DEEP><<<apply_grid<T>(c.nx, c.ny, c.nz, MODE_DEEP), blk, 0, st>>>(
-        c, p, dv, e, done, partials, ticket_main, dot_main);
-    const int64_t ns = shell_count(c.nx, c.ny, c.nz);
-    const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((ns + 255) / 256, max_blocks));
-    fd_shell_kernel<T, EPI><<<gs, 256, 0, st>>>(c, p, dv, e, done, partials, ticket_shell, dot_shell);
-    return 2;
-  }
-  fd_apply_kernel<T, EPI, MODE_FULL><<<apply_grid<T>(c.nx, c.ny, c.nz, MODE_FULL), blk, 0, st>>>(
-      c, p, dv, e, done, partials, ticket_main, dot_main);
-  return 1;
+  if (dv.k27)
+    return launch_operator_k<T, EPI, true>(c, p, dv, e, done, partials, ticket_main, dot_main, ticket_shell, dot_shell,
+                                           max_blocks, st);
+  return launch_operator_k<T, EPI, false>(c, p, dv, e, done, partials, ticket_main, dot_main, ticket_shell, dot_shell,
+                                          max_blocks, st);
 }
 
 // Data term of the touched nodes with one warp per node (coarse multigrid

@@ -10,7 +10,12 @@
 //   * regularisation: re-discretised on the coarse grid -- the same stencil
 //     families with volume weights w^2 scaled by 1/2 and border-layer weights
 //     by 1/4 per level (the energy of P u_c matches in the continuum limit);
-//   * data rows: Galerkin, row_{l+1} = row_l P (at most 27 coarse columns);
+//   * data rows: Galerkin, row_{l+1} = row_l P (at most 27 coarse columns).
+//     P is exact on trilinear functions, so a row confined to one fine cell
+//     stays confined to one coarse cell; on levels >= 1 the rows confined to
+//     one cell are summed into a per-node 27-point stencil (sum of
+//     w^2 a_i a_j over the rows), evaluated inside the apply kernel from the
+//     staged neighbourhood; other rows keep the row form;
 //   * ridge^2 scaled by 8 per level;
 //   * smoother: Chebyshev polynomial of D^-1 A on [lmax/20, 1.05 lmax]
 //     (lmax by power iteration), `deg` steps pre and post -- symmetric, so the
@@ -42,6 +47,11 @@ struct MgLevel {
   int32_t *inc_row = nullptr;
   float *inc_a = nullptr;
   float *qd = nullptr;  // per-touched-node data totals (levels with long incidence lists)
+  // 27-point form of the data rows confined to one cell (levels >= 1)
+  int64_t knt = 0;
+  uint32_t *kmask = nullptr;
+  int32_t *krank = nullptr;
+  float *k27 = nullptr;
   float *dinv = nullptr;
   // vectors: b (rhs), x (solution), r (residual), d[2] (Chebyshev directions)
   float *b = nullptr, *x = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;
@@ -141,7 +151,7 @@ __global__ void __launch_bounds__(256) mg_dot_kernel(int64_t n, const float *__r
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
     l += a[g] * (w ? w[g] * b[g] : b[g]);
   double tot;
-  if (grid_sum<256>((double)l, partials, ticket, &tot)) *out = tot;
+  if (grid_sum<256, float>(l, partials, ticket, &tot)) *out = tot;
 }
 
 __global__ void mg_scale_kernel(int64_t n, const float *__restrict__ src, const float *__restrict__ w, float scale,

@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(kBlock) update_xr_kernel(int64_t n, T *__restr
     local += rn * (dinv[g] * rn);
   }
   double rz_new;
-  if (grid_sum<kBlock>((double)local, partials, ticket, &rz_new)) {
+  if (grid_sum<kBlock, T>(local, partials, ticket, &rz_new)) {
     sc->iters += 1;
     sc->beta = rz_new / rz;
     sc->rz = rz_new;
@@ -316,6 +316,10 @@ DataView<T> data_view(const ls_fd_handle *h, const T *s_rows, const T *inc_a) {
   dv.s_rows = s_rows;
   dv.qd = nullptr;
   dv.enabled = h->data.ntouched > 0;
+  dv.kmask = nullptr;
+  dv.krank = nullptr;
+  dv.k27 = nullptr;
+  dv.knt = 0;
   return dv;
 }
 
@@ -488,6 +492,107 @@ __global__ void mg_fill_hash_kernel(int64_t n, float *__restrict__ v) {
 }
 
 // device data of one level from host rows (incidence list, bit mask, FP32 copies)
+// bit mask of the marked nodes (x-fastest words) and the rank of each word's first node
+void node_mask(int64_t n, const std::vector<int64_t> &marked, std::vector<uint32_t> &mask, std::vector<int32_t> &wr) {
+  const int64_t nwords = (n + 31) / 32;
+  mask.assign(nwords, 0u);
+  wr.assign(nwords, 0);
+  for (int64_t t : marked) mask[t >> 5] |= 1u << (t & 31);
+  int32_t run = 0;
+  for (int64_t w = 0; w < nwords; ++w) {
+    wr[w] = run;
+    run += __builtin_popcount(mask[w]);
+  }
+}
+
+// Rows of a coarse level whose columns all lie in one cell (a 2 x 2 x 2 box)
+// become the 27-point per-node stencil sum_rows w^2 a_i a_j; the other rows
+// are returned in `rest` for the row form.  The stencil's centre entries go to
+// diag_out (per marked node, ascending node order).
+int mg_upload_k27(ls_fd_handle *h, MgLevel &lv, const HostRows &rows, HostRows &rest,
+                  std::vector<std::pair<int64_t, double>> &diag_out) {
+  MgHierarchy &mg = h->mg;
+  rest = HostRows{};
+  rest.width = rows.width;
+  diag_out.clear();
+  lv.knt = 0;
+  const int64_t nxy = (int64_t)lv.nx * lv.ny;
+  std::vector<std::pair<int64_t, double>> trip;  // (node * 27 + o, value)
+  for (int64_t r = 0; r < rows.nrows; ++r) {
+    int64_t cols[8];
+    double av[8];
+    int m = 0;
+    bool cell = true;
+    int lo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, hi[3] = {-1, -1, -1};
+    for (int k = 0; k < rows.width && cell; ++k) {
+      const int64_t c = rows.cols[r * rows.width + k];
+      if (c < 0) continue;
+      const int ax[3] = {(int)(c % lv.nx), (int)((c / lv.nx) % lv.ny), (int)(c / nxy)};
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = std::min(lo[d], ax[d]);
+        hi[d] = std::max(hi[d], ax[d]);
+        if (hi[d] - lo[d] > 1) cell = false;
+      }
+      if (m == 8) cell = false;  // a 2 x 2 x 2 box has 8 distinct nodes
+      if (!cell) break;
+      cols[m] = c;
+      av[m] = rows.a[r * rows.width + k];
+      ++m;
+    }
+    if (m == 0) cell = false;
+    if (!cell) {
+      rest.cols.insert(rest.cols.end(), rows.cols.begin() + r * rows.width, rows.cols.begin() + (r + 1) * rows.width);
+      rest.a.insert(rest.a.end(), rows.a.begin() + r * rows.width, rows.a.begin() + (r + 1) * rows.width);
+      rest.w2.push_back(rows.w2[r]);
+      ++rest.nrows;
+      continue;
+    }
+    const double w2 = rows.w2[r];
+    for (int u = 0; u < m; ++u)
+      for (int v = 0; v < m; ++v) {
+        const int dx = (int)(cols[v] % lv.nx) - (int)(cols[u] % lv.nx);
+        const int dy = (int)((cols[v] / lv.nx) % lv.ny) - (int)((cols[u] / lv.nx) % lv.ny);
+        const int dz = (int)(cols[v] / nxy) - (int)(cols[u] / nxy);
+        const int o = 9 * (dz + 1) + 3 * (dy + 1) + (dx + 1);
+        trip.emplace_back(cols[u] * 27 + o, w2 * av[u] * av[v]);
+      }
+  }
+  if (trip.empty()) return LS_OK;
+  std::stable_sort(trip.begin(), trip.end(), [](const std::pair<int64_t, double> &x, const std::pair<int64_t, double> &y) {
+    return x.first < y.first;
+  });
+  std::vector<int64_t> nodes;
+  std::vector<double> kv;  // 27 per node
+  for (size_t t = 0; t < trip.size(); ++t) {
+    const int64_t node = trip[t].first / 27;
+    const int o = (int)(trip[t].first % 27);
+    if (nodes.empty() || nodes.back() != node) {
+      nodes.push_back(node);
+      kv.resize(kv.size() + 27, 0.0);
+    }
+    kv[(nodes.size() - 1) * 27 + o] += trip[t].second;
+  }
+  const int64_t nt = (int64_t)nodes.size();
+  std::vector<float> k((size_t)27 * nt);
+  for (int64_t t = 0; t < nt; ++t) {
+    for (int o = 0; o < 27; ++o) k[(size_t)o * nt + t] = (float)kv[(size_t)t * 27 + o];
+    diag_out.emplace_back(nodes[t], kv[(size_t)t * 27 + 13]);
+  }
+  std::vector<uint32_t> mask;
+  std::vector<int32_t> wr;
+  node_mask(lv.n, nodes, mask, wr);
+  lv.knt = nt;
+  LS_TRY(mg_alloc(mg, &lv.kmask, mask.size()));
+  LS_TRY(mg_alloc(mg, &lv.krank, wr.size()));
+  LS_TRY(mg_alloc(mg, &lv.k27, k.size()));
+  cudaStream_t st = h->stream;
+  LS_CUDA_TRY(cudaMemcpyAsync(lv.kmask, mask.data(), mask.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(lv.krank, wr.data(), wr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(lv.k27, k.data(), k.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaStreamSynchronize(st));
+  return LS_OK;
+}
+
 int mg_upload_level(ls_fd_handle *h, MgLevel &lv, const HostRows &rows, std::vector<int64_t> &touched,
                     std::vector<double> &data_diag) {
   MgHierarchy &mg = h->mg;
@@ -523,14 +628,9 @@ int mg_upload_level(ls_fd_handle *h, MgLevel &lv, const HostRows &rows, std::vec
   }
   ptr.push_back((int64_t)inc.size());
   const int64_t nwords = (lv.n + 31) / 32;
-  std::vector<uint32_t> mask(nwords, 0u);
-  std::vector<int32_t> wr(nwords, 0);
-  for (int64_t t : touched) mask[t >> 5] |= 1u << (t & 31);
-  int32_t run = 0;
-  for (int64_t w = 0; w < nwords; ++w) {
-    wr[w] = run;
-    run += __builtin_popcount(mask[w]);
-  }
+  std::vector<uint32_t> mask;
+  std::vector<int32_t> wr;
+  node_mask(lv.n, touched, mask, wr);
   lv.nrows = rows.nrows;
   lv.width = rows.width;
   lv.ntouched = (int64_t)touched.size();
@@ -571,6 +671,10 @@ DataView<float> mg_view(const MgLevel &lv) {
   dv.s_rows = lv.s;
   dv.qd = lv.qd;
   dv.enabled = lv.ntouched > 0;
+  dv.kmask = lv.kmask;
+  dv.krank = lv.krank;
+  dv.k27 = lv.knt > 0 ? lv.k27 : nullptr;
+  dv.knt = lv.knt;
   return dv;
 }
 
@@ -798,8 +902,27 @@ int mg_build(ls_fd_handle *h, int deg) {
     LS_TRY(mg_alloc(mg, &c.d0, c.n));
     LS_TRY(mg_alloc(mg, &c.d1, c.n));
     LS_TRY(mg_alloc(mg, &c.dinv, c.n));
-    LS_TRY(mg_upload_level(h, c, rows, touched, ddiag));
-    LS_TRY(mg_level_dinv(h, c, touched, ddiag));
+    HostRows rest;
+    std::vector<std::pair<int64_t, double>> kdiag;
+    LS_TRY(mg_upload_k27(h, c, rows, rest, kdiag));
+    LS_TRY(mg_upload_level(h, c, rest, touched, ddiag));
+    // diagonal of the data term: row form plus the 27-point centre entries
+    {
+      std::vector<std::pair<int64_t, double>> all(kdiag);
+      for (size_t t = 0; t < touched.size(); ++t) all.emplace_back(touched[t], ddiag[t]);
+      std::sort(all.begin(), all.end());
+      std::vector<int64_t> tn;
+      std::vector<double> td;
+      for (const auto &e : all) {
+        if (!tn.empty() && tn.back() == e.first) {
+          td.back() += e.second;
+        } else {
+          tn.push_back(e.first);
+          td.push_back(e.second);
+        }
+      }
+      LS_TRY(mg_level_dinv(h, c, tn, td));
+    }
     mg.levels.push_back(c);
   }
   if (mg.levels.back().n > kMgMaxCoarse) return LS_OK;  // not built: Jacobi fallback
@@ -906,7 +1029,7 @@ __global__ void __launch_bounds__(kBlock) mg_update_xr_kernel(int64_t n, float *
     local += rn * (dinv[g] * rn);
   }
   double rrj;
-  if (grid_sum<kBlock>((double)local, partials, ticket, &rrj)) {
+  if (grid_sum<kBlock, float>(local, partials, ticket, &rrj)) {
     sc->iters += 1;
     sc->rrj = rrj;
     if (!isfinite(rrj)) sc->done = DONE_NAN;
@@ -925,7 +1048,7 @@ __global__ void __launch_bounds__(kBlock) mg_rz_kernel(int64_t n, const float *_
   for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x)
     local += r[g] * z[g];
   double rz;
-  if (grid_sum<kBlock>((double)local, partials, ticket, &rz)) {
+  if (grid_sum<kBlock, float>(local, partials, ticket, &rz)) {
     if (!set_only) sc->beta = rz / sc->rz;
     sc->rz = rz;
     if (!isfinite(rz)) sc->done = DONE_NAN;
@@ -1445,6 +1568,87 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
   stats->kernel_launches = h->launches - launches0;
   LS_CUDA_TRY(cudaGetLastError());
   return status;
+}
+
+extern "C" int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_levels, int *levels, void *stream) {
+  LS_ARG_CHECK(h && out && levels && reps > 0 && max_levels > 0, "bad argument");
+  LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+  *levels = 0;
+  LS_TRY(mg_build(h, 3));
+  MgHierarchy &mg = h->mg;
+  if (!mg.built) return LS_OK;
+  cudaStream_t st = h->stream;
+  const int L = std::min((int)mg.levels.size(), max_levels);
+  auto timed = [&](auto &&launch, double *ms_out) -> int {
+    launch();
+    LS_CUDA_TRY(cudaEventRecord(h->ev0, st));
+    for (int r = 0; r < reps; ++r) launch();
+    LS_CUDA_TRY(cudaEventRecord(h->ev1, st));
+    LS_CUDA_TRY(cudaEventSynchronize(h->ev1));
+    float ms = 0.0f;
+    LS_CUDA_TRY(cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    *ms_out = ms / reps;
+    return LS_OK;
+  };
+  for (int l = 0; l < L; ++l) {
+    MgLevel &lv = mg.levels[l];
+    double *o = out + (size_t)l * LS_MG_PROFILE_FIELDS;
+    for (int f = 0; f < LS_MG_PROFILE_FIELDS; ++f) o[f] = 0.0;
+    o[0] = (double)lv.n;
+    const int g = grid_for(h, lv.n);
+    fill_kernel<float><<<g, kBlock, 0, st>>>(lv.n, lv.b, 1.0f);
+    fill_kernel<float><<<g, kBlock, 0, st>>>(lv.n, lv.x, 0.0f);
+    fill_kernel<float><<<g, kBlock, 0, st>>>(lv.n, lv.r, 1.0f);
+    fill_kernel<float><<<g, kBlock, 0, st>>>(lv.n, lv.d0, 1e-3f);
+    fill_kernel<float><<<g, kBlock, 0, st>>>(lv.n, lv.d1, 1e-3f);
+    h->launches += 5;
+    if (l + 1 == (int)mg.levels.size()) {
+      LS_TRY(timed([&] {
+        mg_dense_kernel<<<(int)((lv.n * 32 + 255) / 256), 256, 0, st>>>((int)lv.n, mg.coarse_inv64, lv.b, lv.x, nullptr);
+        ++h->launches;
+      }, &o[7]));
+      continue;
+    }
+    EpiArgs<float> es{};
+    es.q = lv.d1;
+    LS_TRY(timed([&] { mg_apply<EPI_STORE>(h, lv, lv.d0, es, nullptr, st); }, &o[1]));
+    EpiArgs<float> ec{};
+    ec.x = lv.x;
+    ec.r = lv.r;
+    ec.dinv = lv.dinv;
+    ec.d_out = lv.d1;
+    ec.c1 = 0.5f;
+    ec.c2 = 1e-3f;
+    LS_TRY(timed([&] { mg_apply<EPI_CHEB>(h, lv, lv.d0, ec, nullptr, st); }, &o[2]));
+    EpiArgs<float> er{};
+    er.r = lv.r;
+    er.b = lv.b;
+    er.dinv = lv.dinv;
+    er.d_out = lv.d1;
+    er.c2 = 1e-3f;
+    LS_TRY(timed([&] { mg_apply<EPI_RESID>(h, lv, lv.x, er, nullptr, st); }, &o[3]));
+    const MgLevel &cl = mg.levels[l + 1];
+    LS_TRY(timed([&] {
+      mg_restrict_kernel<<<dim3((cl.nx + 31) / 32, (cl.ny + 7) / 8, cl.nz), dim3(32, 8), 0, st>>>(
+          lv.nx, lv.ny, lv.nz, cl.nx, cl.ny, cl.nz, lv.r, cl.b, nullptr);
+      ++h->launches;
+    }, &o[4]));
+    LS_TRY(timed([&] {
+      mg_prolong_kernel<<<dim3((lv.nx + 31) / 32, (lv.ny + 7) / 8, lv.nz), dim3(32, 8), 0, st>>>(
+          lv.nx, lv.ny, lv.nz, cl.nx, cl.ny, cl.x, lv.x, nullptr);
+      ++h->launches;
+    }, &o[5]));
+    if (lv.nrows > 0) {
+      LS_TRY(timed([&] {
+        rows_kernel<float><<<grid_for(h, lv.nrows), kBlock, 0, st>>>(lv.nrows, lv.width, lv.cols, lv.a, lv.w2, lv.d0,
+                                                                     lv.s, nullptr);
+        ++h->launches;
+      }, &o[6]));
+    }
+  }
+  *levels = L;
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
 }
 
 extern "C" int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps, ls_fd_profile *out, void *stream) {

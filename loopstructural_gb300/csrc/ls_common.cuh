@@ -60,17 +60,17 @@ __device__ __forceinline__ int linear_tid() {
   return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
 }
 
-template <int BLOCK>
-__device__ __forceinline__ double block_sum(double v, double *smem) {
+template <int BLOCK, typename V>
+__device__ __forceinline__ V block_sum(V v, V *smem) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int t = linear_tid();
   const int lane = t & 31, warp = t >> 5;
   if (lane == 0) smem[warp] = v;
   __syncthreads();
-  v = 0.0;
+  v = (V)0;
   if (warp == 0) {
-    v = (lane < BLOCK / 32) ? smem[lane] : 0.0;
+    v = (lane < BLOCK / 32) ? smem[lane] : (V)0;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   }
@@ -81,14 +81,17 @@ __device__ __forceinline__ double block_sum(double v, double *smem) {
 // Returns true in thread 0 of the last block; *total then holds the sum.
 // `tid` is the thread's linear index in its block, `bid` / `nblocks` the
 // block's linear index and the grid size (3-D grids pass their own).
-template <int BLOCK>
-__device__ __forceinline__ bool grid_sum_ex(double v, double *partials, unsigned int *ticket, double *total,
+// The block partial is formed in the value type V (FP32 block sums keep the
+// slow FP64 pipe out of FP32 kernels); partials and the final sum are FP64.
+template <int BLOCK, typename V>
+__device__ __forceinline__ bool grid_sum_ex(V v, double *partials, unsigned int *ticket, double *total,
                                             int tid, unsigned int bid, unsigned int nblocks) {
+  __shared__ V redv[BLOCK / 32];
   __shared__ double red[BLOCK / 32];
   __shared__ bool last;
-  double b = block_sum<BLOCK>(v, red);
+  const V bv = block_sum<BLOCK, V>(v, redv);
   if (tid == 0) {
-    partials[bid] = b;
+    partials[bid] = (double)bv;
     __threadfence();
     unsigned int t = atomicAdd(ticket, 1u);
     last = (t == nblocks - 1);
@@ -99,7 +102,7 @@ __device__ __forceinline__ bool grid_sum_ex(double v, double *partials, unsigned
   // last block: fixed-order sum of the partials
   double s = 0.0;
   for (int i = tid; i < (int)nblocks; i += BLOCK) s += ((volatile double *)partials)[i];
-  s = block_sum<BLOCK>(s, red);
+  s = block_sum<BLOCK, double>(s, red);
   if (tid == 0) {
     *total = s;
     *ticket = 0u;  // re-arm for the next launch
@@ -122,9 +125,9 @@ __device__ __forceinline__ bool grid_last_block(unsigned int *ticket) {
   return last && threadIdx.x == 0;
 }
 
-template <int BLOCK>
-__device__ __forceinline__ bool grid_sum(double v, double *partials, unsigned int *ticket, double *total) {
-  return grid_sum_ex<BLOCK>(v, partials, ticket, total, threadIdx.x, blockIdx.x, gridDim.x);
+template <int BLOCK, typename V = double>
+__device__ __forceinline__ bool grid_sum(V v, double *partials, unsigned int *ticket, double *total) {
+  return grid_sum_ex<BLOCK, V>(v, partials, ticket, total, threadIdx.x, blockIdx.x, gridDim.x);
 }
 
 // Two sums in one pass.
@@ -133,8 +136,8 @@ __device__ __forceinline__ bool grid_sum2(double v0, double v1, double *partials
                                           double *t0, double *t1) {
   __shared__ double red[BLOCK / 32];
   __shared__ bool last;
-  double b0 = block_sum<BLOCK>(v0, red);
-  double b1 = block_sum<BLOCK>(v1, red);
+  double b0 = block_sum<BLOCK, double>(v0, red);
+  double b1 = block_sum<BLOCK, double>(v1, red);
   if (threadIdx.x == 0) {
     partials[2 * blockIdx.x] = b0;
     partials[2 * blockIdx.x + 1] = b1;

@@ -201,6 +201,19 @@ class FdSystem:
         return x, stats
 
 
+MG_PROFILE_FIELDS = ("nodes", "apply_ms", "cheb_apply_ms", "resid_apply_ms", "restrict_ms", "prolong_ms",
+                     "rows_ms", "coarse_solve_ms")
+
+
+def profile_mg(system: "FdSystem", reps=20, max_levels=16):
+    """Device time per launch of each part of the multigrid V-cycle, per level."""
+    out = (C.c_double * (max_levels * len(MG_PROFILE_FIELDS)))()
+    nl = C.c_int(0)
+    _lib.check(system.lib.ls_fd_profile_mg(system.handle, int(reps), out, max_levels, C.byref(nl), _lib.stream_ptr()))
+    k = len(MG_PROFILE_FIELDS)
+    return [{f: out[l * k + i] for i, f in enumerate(MG_PROFILE_FIELDS)} for l in range(nl.value)]
+
+
 def profile_iteration(system: "FdSystem", precision="mixed", reps=20):
     """Device time per launch of each kernel class of one CG iteration."""
     prof = _lib.FdProfile()

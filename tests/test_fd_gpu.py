@@ -133,6 +133,30 @@ def test_regularisation_operator_matches_explicit_gram_everywhere(cells):
     system.close()
 
 
+def test_operator_on_large_thin_grid():
+    """Grids of more than 300,000 nodes with an axis under 24 nodes run the staged
+    full-grid kernel (exact shell sum at every boundary node)."""
+    cells = np.array([640, 520, 2])
+    kw = dict(dxx=1.0, dyy=0.8, dzz=1.3, dxy=0.5, dxz=0.4, dyz=0.6, dx=0.7, dy=0.9, dz=1.1,
+              cpw=0.0, gpw=0.0, npw=0.0, tpw=0.0, ipw=0.0)
+    interp = L.FiniteDifferenceInterpolator(_grid(cells, np.ones(3)))
+    interp.setup_interpolator(**kw)
+    system = interp._build_system()
+    assert system.n > 300_000
+    grid = fdo.Grid(np.zeros(3), cells, np.ones(3))
+    cs = fdo.ConstraintSet(grid.n_nodes)
+    fdo.add_regularisation(grid, cs, fdo.resolve_weights(**kw))
+    A, _ = cs.matrix()
+    x = np.random.default_rng(4).normal(size=A.shape[1])
+    N, _ = fdo.normal_equations(A, np.zeros(A.shape[0]))
+    ref = N @ x
+    got = system.apply(torch.from_numpy(x)).cpu().numpy()
+    assert np.max(np.abs(got - ref)) <= 1e-12 * np.max(np.abs(ref))
+    got32 = system.apply(torch.from_numpy(x).float()).cpu().numpy()
+    assert np.max(np.abs(got32 - ref)) <= 2e-5 * np.max(np.abs(ref))
+    system.close()
+
+
 def test_normal_operator_with_data_on_split_grid():
     """Grids of >= 24 nodes per axis run the deep-box kernel plus the boundary-shell
     kernel; the data term must land on both."""
