@@ -205,19 +205,19 @@ __device__ __forceinline__ T shell_node(const CoefT<T> &c, const PR &pr, int i, 
   return q;
 }
 
-// Output planes per block: 16 in FP32 (20 staged planes, 34.6 KB of shared
-// memory), 8 in FP64 (12 staged planes, 41.5 KB) -- both under the 48 KB static limit.
-template <typename T>
+// Output planes per block (TZ; the block stages TZ + 4 planes of 432 nodes):
+// 16 or 4 in FP32 (34.6 / 13.8 KB of shared memory; 4 on grids too small to
+// fill the GPU with 16-plane tiles), 8 in FP64 (41.5 KB).
+template <typename T, int TZ_>
 struct Tile {
-  static constexpr int TZ = sizeof(T) == 4 ? 16 : 8;
+  static constexpr int TZ = TZ_;
   static constexpr int SZ = TZ + 4;
   static constexpr int PLANE = kHY * kHX;  // 432 staged nodes per plane
 };
 
-// Operator modes: FULL evaluates every node of the grid (the boundary shell
-// through the exact branch-free sum); DEEP covers only the deep box
-// [3, n-4]^3 with the composite stencil and no branch, the shell being left to
-// fd_shell_kernel.
+// Operator modes.  FULL: every node of the grid, boundary nodes through the
+// exact shell sum.  DEEP: only the deep box [3, n-4]^3, composite stencil
+// without a branch; the boundary shell is left to fd_point_kernel.
 enum ApplyMode { MODE_FULL = 0, MODE_DEEP = 1 };
 
 // The deep box is split off when every axis has at least this many nodes.
@@ -247,12 +247,13 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // they are, so only a 5-plane window stays live in registers.
 // Returns the block's sum of the epilogue contributions (p.q for EPI_STORE)
 // through the deterministic grid reduction when `dot_out` is set.
-template <typename T, int EPI, int MODE, bool K27>
-__global__ void __launch_bounds__(kAX * kAY, MODE == MODE_DEEP ? 4 : 1) fd_apply_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv,
-                                                             EpiArgs<T> e, const int *done, double *partials,
-                                                             unsigned int *ticket, double *dot_out) {
+template <typename T, int EPI, int MODE, bool K27, int TZ_>
+__global__ void __launch_bounds__(kAX * kAY, MODE == MODE_DEEP ? 4 : 1)
+    fd_apply_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv, EpiArgs<T> e, const int *done,
+                    double *partials, unsigned int *ticket, double *dot_out) {
   if (done && *done) return;
-  constexpr int TZ = Tile<T>::TZ, SZ = Tile<T>::SZ, PLANE = Tile<T>::PLANE;
+  using TL = Tile<T, TZ_>;
+  constexpr int TZ = TL::TZ, SZ = TL::SZ, PLANE = TL::PLANE;
   __shared__ T sm[SZ][kHY][kHX];
   const int nx = c.nx, ny = c.ny, nz = c.nz;
   const int org = MODE == MODE_DEEP ? 3 : 0;  // first node of the covered box
@@ -361,9 +362,8 @@ __global__ void __launch_bounds__(kAX * kAY, MODE == MODE_DEEP ? 4 : 1) fd_apply
   }
 }
 
-template <typename T>
+template <typename T, int TZ>
 inline dim3 apply_grid(int nx, int ny, int nz, int mode) {
-  constexpr int TZ = Tile<T>::TZ;
   if (mode == MODE_DEEP) {
     nx -= 6;
     ny -= 6;
@@ -455,27 +455,43 @@ __global__ void __launch_bounds__(256) fd_point_kernel(CoefT<T> c, const T *__re
 // Grids with fewer nodes than this run the node-per-thread kernel alone.
 constexpr int64_t kPointMaxNodes = 300000;
 
+template <typename T, int EPI, int MODE, bool K27>
+inline void launch_tiles(const CoefT<T> &c, const T *p, const DataView<T> &dv, const EpiArgs<T> &e, const int *done,
+                         double *partials, unsigned int *ticket, double *dot, int sms, cudaStream_t st) {
+  const dim3 blk(kAX, kAY);
+  if constexpr (sizeof(T) == 8) {
+    fd_apply_kernel<T, EPI, MODE, K27, 8><<<apply_grid<T, 8>(c.nx, c.ny, c.nz, MODE), blk, 0, st>>>(
+        c, p, dv, e, done, partials, ticket, dot);
+  } else {
+    const dim3 g16 = apply_grid<T, 16>(c.nx, c.ny, c.nz, MODE);
+    if ((int64_t)g16.x * g16.y * g16.z >= 4 * (int64_t)sms) {
+      fd_apply_kernel<T, EPI, MODE, K27, 16><<<g16, blk, 0, st>>>(c, p, dv, e, done, partials, ticket, dot);
+    } else {
+      fd_apply_kernel<T, EPI, MODE, K27, 4><<<apply_grid<T, 4>(c.nx, c.ny, c.nz, MODE), blk, 0, st>>>(
+          c, p, dv, e, done, partials, ticket, dot);
+    }
+  }
+}
+
 template <typename T, int EPI, bool K27>
 inline int launch_operator_k(const CoefT<T> &c, const T *p, const DataView<T> &dv, const EpiArgs<T> &e,
                              const int *done, double *partials, unsigned int *ticket_main, double *dot_main,
                              unsigned int *ticket_shell, double *dot_shell, int max_blocks, cudaStream_t st) {
-  const dim3 blk(kAX, kAY);
   const int64_t n = (int64_t)c.nx * c.ny * c.nz;
+  const int sms = max_blocks / 8;
   if (n <= kPointMaxNodes) {
     const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, max_blocks));
     fd_point_kernel<T, EPI, true, K27><<<gs, 256, 0, st>>>(c, p, dv, e, done, partials, ticket_main, dot_main);
     return 1;
   }
   if (apply_split(c.nx, c.ny, c.nz)) {
-    fd_apply_kernel<T, EPI, MODE_DEEP, K27><<<apply_grid<T>(c.nx, c.ny, c.nz, MODE_DEEP), blk, 0, st>>>(
-        c, p, dv, e, done, partials, ticket_main, dot_main);
+    launch_tiles<T, EPI, MODE_DEEP, K27>(c, p, dv, e, done, partials, ticket_main, dot_main, sms, st);
     const int64_t ns = shell_count(c.nx, c.ny, c.nz);
     const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((ns + 255) / 256, max_blocks));
     fd_point_kernel<T, EPI, false, K27><<<gs, 256, 0, st>>>(c, p, dv, e, done, partials, ticket_shell, dot_shell);
     return 2;
   }
-  fd_apply_kernel<T, EPI, MODE_FULL, K27><<<apply_grid<T>(c.nx, c.ny, c.nz, MODE_FULL), blk, 0, st>>>(
-      c, p, dv, e, done, partials, ticket_main, dot_main);
+  launch_tiles<T, EPI, MODE_FULL, K27>(c, p, dv, e, done, partials, ticket_main, dot_main, sms, st);
   return 1;
 }
 

@@ -114,20 +114,25 @@ __global__ void mg_restrict_kernel(int nfx, int nfy, int nfz, int ncx, int ncy, 
   bc[((size_t)K * ncy + J) * ncx + I] = acc;
 }
 
-// x_f += P x_c (3-D launch over fine x-y, blockIdx.z = fine z)
+// x_f += P x_c (3-D launch over fine x-y, blockIdx.z = fine z).  Branch-free:
+// the 8 coarse corners of the fine node's coarse cell are always read (an
+// index past the coarse grid is clamped and weighted 0); per axis the weights
+// are (1, 0) on even fine indices and (1/2, 1/2) on odd ones.
 __global__ void mg_prolong_kernel(int nfx, int nfy, int nfz, int ncx, int ncy, const float *__restrict__ xc,
                                   float *__restrict__ xf, const int *done) {
   if (done && *done) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
   if (i >= nfx || j >= nfy || k >= nfz) return;
   const int i0 = i >> 1, j0 = j >> 1, k0 = k >> 1;
-  const int ni = (i & 1) ? 2 : 1, nj = (j & 1) ? 2 : 1, nk = (k & 1) ? 2 : 1;
-  const float w = ((i & 1) ? 0.5f : 1.f) * ((j & 1) ? 0.5f : 1.f) * ((k & 1) ? 0.5f : 1.f);
-  float acc = 0.f;
-  for (int c = 0; c < nk; ++c)
-    for (int b = 0; b < nj; ++b)
-      for (int a = 0; a < ni; ++a) acc += __ldg(xc + ((size_t)(k0 + c) * ncy + (j0 + b)) * ncx + (i0 + a));
-  xf[((size_t)k * nfy + j) * nfx + i] += w * acc;
+  const int oi = i & 1, oj = j & 1, ok = k & 1;
+  const int i1 = i0 + oi, j1 = j0 + oj;  // = i0 on even fine indices (weight 0 there)
+  const float wi1 = oi ? 0.5f : 0.f, wj1 = oj ? 0.5f : 0.f, wk1 = ok ? 0.5f : 0.f;
+  const float wi0 = 1.f - wi1, wj0 = 1.f - wj1, wk0 = 1.f - wk1;
+  const float *r00 = xc + ((size_t)k0 * ncy + j0) * ncx, *r01 = xc + ((size_t)k0 * ncy + j1) * ncx;
+  const float *r10 = xc + ((size_t)(k0 + ok) * ncy + j0) * ncx, *r11 = xc + ((size_t)(k0 + ok) * ncy + j1) * ncx;
+  const float v0 = wj0 * (wi0 * __ldg(r00 + i0) + wi1 * __ldg(r00 + i1)) + wj1 * (wi0 * __ldg(r01 + i0) + wi1 * __ldg(r01 + i1));
+  const float v1 = wj0 * (wi0 * __ldg(r10 + i0) + wi1 * __ldg(r10 + i1)) + wj1 * (wi0 * __ldg(r11 + i0) + wi1 * __ldg(r11 + i1));
+  xf[((size_t)k * nfy + j) * nfx + i] += wk0 * v0 + wk1 * v1;
 }
 
 // x = Minv b in FP64 (the coarsest operator can be ill-conditioned), one warp per row

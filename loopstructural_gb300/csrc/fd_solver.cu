@@ -1133,8 +1133,8 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
   }
   h->red_blocks = sm_count() * 8;
   {
-    const dim3 a4 = apply_grid<float>((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], MODE_FULL);
-    const dim3 a8 = apply_grid<double>((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], MODE_FULL);
+    const dim3 a4 = apply_grid<float, 4>((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], MODE_FULL);
+    const dim3 a8 = apply_grid<double, 8>((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], MODE_FULL);
     const size_t nb = std::max<size_t>({(size_t)h->red_blocks, (size_t)a4.x * a4.y * a4.z, (size_t)a8.x * a8.y * a8.z});
     if ((st = dev_alloc(&h->partials, 4 * nb)) < 0) return fail(st);
   }
