@@ -93,13 +93,16 @@ class ClockSampler:
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, index=0):
+    def __init__(self, index=0, enabled=True):
         self.index = index
+        self.enabled = enabled
         self.rows = []
         self.proc = None
         self.thread = None
 
     def __enter__(self):
+        if not self.enabled:
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -148,6 +151,31 @@ def measured_peaks():
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+def fp64_leg(args, system, grid, x_mixed, lo, hs):
+    """Plain FP64 Jacobi-CG on the GPU (the iteration of the reference's
+    column-scaled CG) to the same rtol, timed; then continued to rtol 1e-12
+    (untimed) as the tight reference for the field error of the mixed solution
+    on the 64^3 subsample of the 256^3 lattice."""
+    import torch
+
+    from loopstructural_gb300 import fd
+
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    x64, st64 = system.solve(atol=0.0, rtol=args.rtol, precision="fp64", maxiter=args.maxiter)
+    f1.record()
+    torch.cuda.synchronize()
+    fp64_s = f0.elapsed_time(f1) / 1e3
+    x64, st64t = system.solve(x=x64, atol=0.0, rtol=1e-12, precision="fp64", maxiter=args.maxiter)
+    sub_step = tuple(4 * h for h in hs)
+    v_mix, _ = fd.eval_lattice(grid, x_mixed, lo, sub_step, (64, 64, 64), gradient=False)
+    v_ref, _ = fd.eval_lattice(grid, x64, lo, sub_step, (64, 64, 64), gradient=False)
+    field_err = float(torch.linalg.norm(v_mix - v_ref) / torch.linalg.norm(v_ref))
+    coef_err = float(torch.linalg.norm(x_mixed - x64) / torch.linalg.norm(x64))
+    return fp64_s, st64, st64t, field_err, coef_err
+
+
 def gpu_arm(args, rank, world):
     import torch
 
@@ -184,13 +212,15 @@ def gpu_arm(args, rank, world):
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     stats = []
-    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0))) as clk:
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", 0)), enabled=args.clocks) as clk:
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("timed")  # lets a profiler select the timed launches
         e0.record()
         for _ in range(args.steps):
             stats.append(step())
         e1.record()
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
     barrier()
     ms = e0.elapsed_time(e1) / args.steps
     if world > 1:
@@ -202,44 +232,38 @@ def gpu_arm(args, rank, world):
     out_solve_ms = float(np.mean([s["device_ms"] for s in stats]))
     x_mixed = last["x"]
 
-    # FP64 GPU leg: plain FP64 Jacobi-CG (the iteration of the reference's
-    # column-scaled CG) to the same rtol, timed; then continued to rtol 1e-12
-    # (untimed) as the tight reference for the field error of the mixed
-    # solution on the 64^3 subsample of the 256^3 lattice
-    torch.cuda.synchronize()
-    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record()
-    x64, st64 = system.solve(atol=0.0, rtol=args.rtol, precision="fp64", maxiter=args.maxiter)
-    f1.record()
-    torch.cuda.synchronize()
-    fp64_s = f0.elapsed_time(f1) / 1e3
-    x64, st64t = system.solve(x=x64, atol=0.0, rtol=1e-12, precision="fp64", maxiter=args.maxiter)
-    sub_step = tuple(4 * h for h in hs)
-    v_mix, _ = fd.eval_lattice(grid, x_mixed, lo, sub_step, (64, 64, 64), gradient=False)
-    v_ref, _ = fd.eval_lattice(grid, x64, lo, sub_step, (64, 64, 64), gradient=False)
-    field_err = float(torch.linalg.norm(v_mix - v_ref) / torch.linalg.norm(v_ref))
-    coef_err = float(torch.linalg.norm(x_mixed - x64) / torch.linalg.norm(x64))
+    fp64_s = coef_err = field_err = None
+    st64 = st64t = {"iterations": 0, "status": -1}
+    if not args.skip_legs:
+        fp64_s, st64, st64t, field_err, coef_err = fp64_leg(args, system, grid, x_mixed, lo, hs)
 
     # dominant-kernel roofline from CUDA-event timings of each kernel class
     prof = fd.profile_iteration(system, "mixed", reps=50)
     peak, peak_kind = measured_peaks()
-    dom = "stencil" if prof["stencil_ms"] >= prof["update_ms"] else "update"
-    if dom == "stencil":
-        dom_bytes, dom_ms = prof["stencil_bytes"], prof["stencil_ms"]
-    else:
-        dom_bytes, dom_ms = 7 * 4.0 * system.n + 4 * 4.0 * system.n, prof["update_ms"]
-    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     it_gbs = prof["iteration_bytes"] / (prof["iteration_ms"] * 1e-3) / 1e9
+    # dominant kernel: the staged deep-box operator apply with the Chebyshev
+    # epilogue on the finest multigrid level (6 of the 8 finest-level applies
+    # of every iteration), timed with CUDA events on the solver's stream
+    mgp = fd.profile_mg(system, reps=50)
+    nd = int(np.prod([c + 1 - 6 for c in cells]))  # deep-box nodes [3, n-4]^3
+    dom_bytes = 28.0 * nd  # p read; x, r read + written; D^-1 read; next direction written (FP32)
+    dom_ms = mgp[0]["cheb_deep_ms"]
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "fd_apply_cheb_deep_200cubed.json")
+    if os.path.exists(tpath):
+        with open(tpath) as fh:
+            traffic = json.load(fh).get("dram_bytes_per_launch")
 
     # e2e: the public API from host arrays
-    e2e_steps = max(1, min(args.steps, 2))
-    q_host = None
+    e2e_steps = 0 if args.skip_legs else max(1, min(args.steps, 2))
     h2d = d2h = 0
     t_e2e = []
-    ax = np.linspace(0.0, 1.0, LATTICE)
-    zz, yy, xx = np.meshgrid(ax, ax, ax, indexing="ij")
-    q_host = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], axis=1)
-    del xx, yy, zz
+    if e2e_steps:
+        ax = np.linspace(0.0, 1.0, LATTICE)
+        zz, yy, xx = np.meshgrid(ax, ax, ax, indexing="ij")
+        q_host = np.stack([xx.ravel(), yy.ravel(), zz.ravel()], axis=1)
+        del xx, yy, zz
     for _ in range(e2e_steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -256,7 +280,7 @@ def gpu_arm(args, rank, world):
         h2d = val.nbytes + nrm.nbytes + 2 * q_host.nbytes
         d2h = it.c.nbytes + vv.nbytes + gg.nbytes
         del it
-    e2e_s = float(np.mean(t_e2e))
+    e2e_s = float(np.mean(t_e2e)) if t_e2e else None
 
     out = {
         "metric": METRIC,
@@ -282,17 +306,22 @@ def gpu_arm(args, rank, world):
                   "preconditioner": stats[-1]["preconditioner"], "solve_ms": float(np.mean([s["device_ms"] for s in stats])),
                   "residual": stats[-1]["residual"], "threshold": stats[-1]["threshold"],
                   "ms_per_iteration": float(np.mean([s["device_ms"] for s in stats])) / max(iters, 1)},
-        "fp64_gpu": {"solve_s": round(fp64_s, 3), "iterations": int(st64["iterations"]), "status": int(st64["status"]),
+        "fp64_gpu": {"solve_s": round(fp64_s, 3) if fp64_s else None, "iterations": int(st64["iterations"]),
+                     "status": int(st64["status"]),
                      "rtol": args.rtol, "preconditioner": "jacobi",
-                     "speedup_of_mixed_solve": round(fp64_s / (out_solve_ms / 1e3), 2),
+                     "speedup_of_mixed_solve": round(fp64_s / (out_solve_ms / 1e3), 2) if fp64_s else None,
                      "tight_reference": {"rtol": 1e-12, "extra_iterations": int(st64t["iterations"])},
                      "field_rel_error_64cubed": field_err, "coef_rel_error": coef_err},
         "jacobi_cg_iteration": {"iteration_ms": prof["iteration_ms"], "iteration_GBps": round(it_gbs, 1)},
         "kernels_ms": {k: prof[k] for k in ("stencil_ms", "data_ms", "update_ms", "iteration_ms")},
-        "roofline": {"kernel": dom, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
-                     "traffic": None},
-        "e2e": {"value": round(e2e_s, 4), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"kernel": "fd_apply_kernel<float, EPI_CHEB, MODE_DEEP> (finest level, deep box)",
+                     "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind + " (burst copy)",
+                     "algorithmic_bytes": dom_bytes, "launch_ms": dom_ms, "traffic": traffic},
+        "multigrid_levels_us": [{k: (round(v * 1e3, 1) if k.endswith("_ms") else int(v)) for k, v in lv.items()}
+                                for lv in mgp],
+        "e2e": {"value": round(e2e_s, 4) if e2e_s else None, "unit": "s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": None,
         "clocks": clk.summary(),
     }
@@ -300,7 +329,7 @@ def gpu_arm(args, rank, world):
     # CUDA-graph launch (iterations past convergence inside the last graph
     # launch return at once but are counted), plus the evaluation kernel
     out["gpu_launches"] = launches
-    if args.cpu_baseline and rank == 0:
+    if args.cpu_baseline and rank == 0 and not args.skip_legs:
         # the reference's CG is the Jacobi iteration: its count is the FP64 leg's
         out["cpu_baseline"] = cpu_baseline(int(st64["iterations"]), args.rtol)
     system.close()
@@ -391,6 +420,10 @@ def main():
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--maxiter", type=int, default=400_000)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-clocks", dest="clocks", action="store_false",
+                    help="profiling runs: no nvidia-smi clock sampler child process")
+    ap.add_argument("--skip-legs", action="store_true",
+                    help="profiling runs: skip the FP64 leg, the e2e leg and the CPU baseline")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

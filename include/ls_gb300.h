@@ -169,6 +169,15 @@ int ls_fd_apply_noalloc(const ls_fd_system *sys, const double *d_x, double *d_y,
 
 /* A^T W b (FP64) */
 int ls_fd_rhs(ls_fd_handle *h, double *d_rhs, void *stream);
+/* Replaces the right-hand side A^T W b by d_rhs (device, dof FP64) for the
+ * following solves: the adjoint solve N lambda = E^T g of a loss on evaluated
+ * values reuses the factor-free operator of the forward solve.  No
+ * counterpart in the reference (which has no adjoint). */
+int ls_fd_set_rhs(ls_fd_handle *h, const double *d_rhs, void *stream);
+/* s_r = w_r^2 (a_r . x) over the data rows (FP64; d_s has nrows entries):
+ * with x = lambda, the gradient of the loss with respect to the rows'
+ * right-hand sides b_r.  No counterpart in the reference. */
+int ls_fd_data_rows_apply(ls_fd_handle *h, const double *d_x, double *d_s, void *stream);
 /* diag(A^T W A + ridge^2 I): the squared column norms of the reference's
  * column scaling (DI:815-833) */
 int ls_fd_diagonal(ls_fd_handle *h, double *d_diag, void *stream);
@@ -212,6 +221,23 @@ typedef struct ls_solve_stats {
  * d_x (device, dof FP64) receives the solution. */
 int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d_x, ls_solve_stats *stats, void *stream);
 
+/* Does the allocations a solve with these options would do on first use
+ * (the multigrid hierarchy of a mixed multigrid solve); optional before
+ * ls_fd_solve, done by ls_fd_solve_batched for every model. */
+int ls_fd_prepare(ls_fd_handle *h, const ls_solve_opts *opts);
+
+/* Device the handle was created on. */
+int ls_fd_device(const ls_fd_handle *h);
+
+/* Solves `count` independent systems (a model ensemble) with up to
+ * `concurrency` (<= 0: 8) solves in flight, each on its handle's stream:
+ * model i solves with opts[i] into d_x[i], filling stats[i] and statuses[i]
+ * (the ls_fd_solve status).  Returns the first negative status (its message
+ * names the model), else 0.  Each result equals that of ls_fd_solve on the
+ * same handle; the reference solves its models one by one (no counterpart). */
+int ls_fd_solve_batched(ls_fd_handle *const *handles, const ls_solve_opts *opts, double *const *d_x,
+                        ls_solve_stats *stats, int64_t count, int concurrency, int *statuses);
+
 /* Per-kernel device times of one CG iteration, measured with CUDA events on
  * the handle's stream over `reps` back-to-back launches of each kernel class
  * (no counterpart in the reference, which has no device code). */
@@ -232,10 +258,12 @@ int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps, ls_fd_prof
  * level l < *levels (at most max_levels): f = 0 nodes, 1 operator apply
  * (plain), 2 apply with the Chebyshev epilogue, 3 apply with the residual
  * epilogue, 4 restriction to level l+1, 5 prolongation from level l+1,
- * 6 data rows (row form), 7 the coarsest dense solve (last level only).
+ * 6 data rows (row form), 7 the coarsest dense solve (last level only),
+ * 8 / 9 the Chebyshev apply's staged deep-box kernel / boundary-shell kernel
+ * alone (levels split into the two; 0 otherwise).
  * Returns 0 with *levels = 0 when the grid does not coarsen.  The solver
  * vectors are overwritten.  No counterpart in the reference. */
-#define LS_MG_PROFILE_FIELDS 8
+#define LS_MG_PROFILE_FIELDS 10
 int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_levels, int *levels, void *stream);
 
 /* ------------------------------------------------------------------ */
@@ -248,6 +276,15 @@ int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_levels, int
  * NULL. */
 int ls_fd_eval_points(const ls_grid3 *grid, const double *d_c, const double *d_pts, int64_t npts, int64_t ld,
                       double *d_value, double *d_grad, void *stream);
+
+/* Transpose of ls_fd_eval_points: d_out[node] += sum_i (trilinear weight of
+ * the node at point i) * d_gvalue[i] + (its shape-function gradient) .
+ * d_ggrad[3i..3i+2]; either input may be NULL; points outside the support
+ * contribute nothing.  FP64 atomics (sum order varies at the ulp level).  The
+ * adjoint of the evaluation for gradients through the solve; no counterpart
+ * in the reference. */
+int ls_fd_eval_adjoint(const ls_grid3 *grid, const double *d_pts, int64_t npts, int64_t ld, const double *d_gvalue,
+                       const double *d_ggrad, double *d_out, void *stream);
 
 /* The same on a regular lattice of points origin + step * (i, j, k),
  * i < n[0] fastest; output index i + n0*j + n0*n1*k. */

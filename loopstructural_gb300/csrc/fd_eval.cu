@@ -238,10 +238,57 @@ __global__ void __launch_bounds__(256) eval_lattice_kernel(EvalGrid g, const dou
   }
 }
 
+// Transpose of the point evaluation: out[node] += sum over the points of the
+// trilinear weight of the node times gv[i] (+ the shape-function gradient
+// times gg[i], 3 per point).  Points outside the support contribute nothing.
+// FP64 atomics: the summation order varies run to run at the ulp level.
+__global__ void eval_adjoint_kernel(EvalGrid g, const double *__restrict__ pts, int64_t n, int64_t ld,
+                                    const double *__restrict__ gv, const double *__restrict__ gg,
+                                    double *__restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double *p = pts + i * ld;
+    AxisLoc l[3];
+    bool inside = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      l[d] = locate_axis(g, d, p[d]);
+      inside &= l[d].inside;
+    }
+    if (!inside) continue;
+    const double x = l[0].l, y = l[1].l, z = l[2].l;
+    const double v = gv ? gv[i] : 0.0;
+    const double gx = gg ? gg[3 * i] / g.step[0] : 0.0, gy = gg ? gg[3 * i + 1] / g.step[1] : 0.0,
+                 gz = gg ? gg[3 * i + 2] / g.step[2] : 0.0;
+    const int64_t nx = g.n[0], nxy = g.n[0] * g.n[1];
+    const int64_t g0 = l[0].cell + nx * l[1].cell + nxy * l[2].cell;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int bx = k & 1, by = (k >> 1) & 1, bz = (k >> 2) & 1;
+      const double wx = bx ? x : 1 - x, wy = by ? y : 1 - y, wz = bz ? z : 1 - z;
+      const double dx = bx ? 1.0 : -1.0, dy = by ? 1.0 : -1.0, dz = bz ? 1.0 : -1.0;
+      const double c = v * wx * wy * wz + gx * dx * wy * wz + gy * wx * dy * wz + gz * wx * wy * dz;
+      atomicAdd(out + g0 + bx + nx * by + nxy * bz, c);
+    }
+  }
+}
+
 }  // namespace
 }  // namespace ls
 
 using namespace ls;
+
+extern "C" int ls_fd_eval_adjoint(const ls_grid3 *grid, const double *d_pts, int64_t npts, int64_t ld,
+                                  const double *d_gvalue, const double *d_ggrad, double *d_out, void *stream) {
+  LS_ARG_CHECK(grid && d_out, "NULL argument");
+  LS_ARG_CHECK(npts >= 0 && ld >= 3, "bad npts / ld");
+  if (npts == 0 || (!d_gvalue && !d_ggrad)) return LS_OK;
+  LS_ARG_CHECK(d_pts != nullptr, "NULL points");
+  EvalGrid g = make_eval_grid(*grid);
+  cudaStream_t s = as_stream(stream);
+  eval_adjoint_kernel<<<stream_grid(npts, 256), 256, 0, s>>>(g, d_pts, npts, ld, d_gvalue, d_ggrad, d_out);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
 
 extern "C" int ls_fd_eval_points(const ls_grid3 *grid, const double *d_c, const double *d_pts, int64_t npts, int64_t ld,
                                  double *d_value, double *d_grad, void *stream) {

@@ -76,6 +76,7 @@ struct ls_fd_handle {
   int64_t n = 0;
   ls::DataTerm data;
   cudaStream_t stream = nullptr;
+  int device = 0;  // device the handle's memory lives on
   // persistent vectors
   double *rhs = nullptr, *diag = nullptr, *dinv64 = nullptr;
   float *dinv32 = nullptr;
@@ -1131,6 +1132,7 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
     set_error("cudaStreamCreate failed");
     return fail(LS_ERR_CUDA);
   }
+  cudaGetDevice(&h->device);
   h->red_blocks = sm_count() * 8;
   {
     const dim3 a4 = apply_grid<float, 4>((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], MODE_FULL);
@@ -1298,11 +1300,38 @@ extern "C" int ls_fd_destroy(ls_fd_handle *h) {
 }
 
 extern "C" int64_t ls_fd_dof(const ls_fd_handle *h) { return h ? h->n : -1; }
+extern "C" int ls_fd_device(const ls_fd_handle *h) { return h ? h->device : -1; }
 
 extern "C" int ls_fd_rhs(ls_fd_handle *h, double *d_rhs, void *stream) {
   LS_ARG_CHECK(h && d_rhs, "NULL argument");
   LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
   LS_CUDA_TRY(cudaMemcpyAsync(d_rhs, h->rhs, h->n * sizeof(double), cudaMemcpyDeviceToDevice, as_stream(stream)));
+  return LS_OK;
+}
+
+extern "C" int ls_fd_set_rhs(ls_fd_handle *h, const double *d_rhs, void *stream) {
+  LS_ARG_CHECK(h && d_rhs, "NULL argument");
+  LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+  cudaStream_t hs = h->stream;
+  LS_CUDA_TRY(cudaMemcpyAsync(h->rhs, d_rhs, h->n * sizeof(double), cudaMemcpyDeviceToDevice, hs));
+  norm2_kernel<<<grid_for(h, h->n), kBlock, 0, hs>>>(h->n, h->rhs, h->dinv64, h->sc, h->partials, h->tickets + T_MISC);
+  ++h->launches;
+  LS_CUDA_TRY(cudaMemcpyAsync(h->sc_h, h->sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, hs));
+  LS_CUDA_TRY(cudaStreamSynchronize(hs));
+  h->rhs_norm2 = h->sc_h->scratch;
+  return LS_OK;
+}
+
+extern "C" int ls_fd_data_rows_apply(ls_fd_handle *h, const double *d_x, double *d_s, void *stream) {
+  LS_ARG_CHECK(h && d_x && d_s, "NULL argument");
+  LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+  const DataTerm &d = h->data;
+  if (d.nrows > 0) {
+    rows_kernel<double><<<grid_for(h, d.nrows), kBlock, 0, h->stream>>>(d.nrows, d.width, d.cols, d.a64, d.w2_64, d_x,
+                                                                        d_s, nullptr);
+    ++h->launches;
+  }
+  LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
   return LS_OK;
 }
 
@@ -1330,6 +1359,13 @@ extern "C" int ls_fd_apply_f32(ls_fd_handle *h, const float *d_x, float *d_y, vo
   launch_apply32(h, d_x, d_y, false, h->stream);
   LS_CUDA_TRY(cudaGetLastError());
   LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return LS_OK;
+}
+
+extern "C" int ls_fd_prepare(ls_fd_handle *h, const ls_solve_opts *opts) {
+  LS_ARG_CHECK(h && opts, "NULL argument");
+  if (opts->precision == LS_MIXED && opts->preconditioner == LS_PRECOND_MG && h->rhs_norm2 > 0.0)
+    LS_TRY(mg_build(h, 3));
   return LS_OK;
 }
 
@@ -1620,6 +1656,29 @@ extern "C" int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_
     ec.c1 = 0.5f;
     ec.c2 = 1e-3f;
     LS_TRY(timed([&] { mg_apply<EPI_CHEB>(h, lv, lv.d0, ec, nullptr, st); }, &o[2]));
+    if (lv.n > kPointMaxNodes && apply_split(lv.nx, lv.ny, lv.nz)) {
+      const DataView<float> dv = mg_view(lv);
+      LS_TRY(timed([&] {
+        if (dv.k27)
+          launch_tiles<float, EPI_CHEB, MODE_DEEP, true>(lv.coef, lv.d0, dv, ec, nullptr, nullptr, nullptr, nullptr,
+                                                          h->red_blocks / 8, st);
+        else
+          launch_tiles<float, EPI_CHEB, MODE_DEEP, false>(lv.coef, lv.d0, dv, ec, nullptr, nullptr, nullptr, nullptr,
+                                                           h->red_blocks / 8, st);
+        ++h->launches;
+      }, &o[8]));
+      const int64_t ns = shell_count(lv.nx, lv.ny, lv.nz);
+      const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((ns + 255) / 256, h->red_blocks));
+      LS_TRY(timed([&] {
+        if (dv.k27)
+          fd_point_kernel<float, EPI_CHEB, false, true><<<gs, 256, 0, st>>>(lv.coef, lv.d0, dv, ec, nullptr, nullptr,
+                                                                            nullptr, nullptr);
+        else
+          fd_point_kernel<float, EPI_CHEB, false, false><<<gs, 256, 0, st>>>(lv.coef, lv.d0, dv, ec, nullptr, nullptr,
+                                                                             nullptr, nullptr);
+        ++h->launches;
+      }, &o[9]));
+    }
     EpiArgs<float> er{};
     er.r = lv.r;
     er.b = lv.b;

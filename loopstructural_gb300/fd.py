@@ -176,6 +176,13 @@ class FdSystem:
     def solve(self, x=None, atol=0.0, rtol=1e-5, maxiter=None, precision="mixed", reliable_delta=0.1,
               check_every=64, preconditioner="mg"):
         """Returns (x device tensor, stats dict)."""
+        x, o = self._prepare(x, atol, rtol, maxiter, precision, reliable_delta, check_every, preconditioner)
+        st = _lib.SolveStats()
+        status = self.lib.ls_fd_solve(self.handle, C.byref(o), _lib.ptr(x), C.byref(st), _lib.stream_ptr())
+        _lib.check(status, allow_positive=True)
+        return x, _stats_dict(st)
+
+    def _prepare(self, x, atol, rtol, maxiter, precision, reliable_delta, check_every, preconditioner):
         torch = _torch()
         o = _lib.SolveOpts()
         o.precision = _lib.LS_MIXED if precision == "mixed" else _lib.LS_FP64
@@ -193,16 +200,40 @@ class FdSystem:
         if preconditioner not in ("mg", "jacobi"):
             raise ValueError(f"preconditioner must be 'mg' or 'jacobi', not {preconditioner!r}")
         o.preconditioner = _lib.LS_PRECOND_MG if preconditioner == "mg" else _lib.LS_PRECOND_JACOBI
-        st = _lib.SolveStats()
-        status = self.lib.ls_fd_solve(self.handle, C.byref(o), _lib.ptr(x), C.byref(st), _lib.stream_ptr())
-        _lib.check(status, allow_positive=True)
-        stats = {k: getattr(st, k) for k, _ in _lib.SolveStats._fields_}
-        stats["preconditioner"] = "mg" if st.preconditioner == _lib.LS_PRECOND_MG else "jacobi"
-        return x, stats
+        return x, o
+
+
+def _stats_dict(st):
+    stats = {k: getattr(st, k) for k, _ in _lib.SolveStats._fields_}
+    stats["preconditioner"] = "mg" if st.preconditioner == _lib.LS_PRECOND_MG else "jacobi"
+    return stats
+
+
+def solve_batched(systems, concurrency=8, atol=0.0, rtol=1e-5, maxiter=None, precision="mixed",
+                  reliable_delta=0.1, check_every=64, preconditioner="mg"):
+    """Solves independent systems (a model ensemble) with up to `concurrency`
+    solves in flight on the GPU; returns [(x, stats), ...] in input order."""
+    n = len(systems)
+    if n == 0:
+        return []
+    prepared = [s._prepare(None, atol, rtol, maxiter, precision, reliable_delta, check_every, preconditioner)
+                for s in systems]
+    handles = (C.c_void_p * n)(*[s.handle for s in systems])
+    opts = (_lib.SolveOpts * n)(*[o for _, o in prepared])
+    xs = (C.c_void_p * n)(*[_lib.ptr(x) for x, _ in prepared])
+    stats = (_lib.SolveStats * n)()
+    statuses = (C.c_int * n)()
+    _torch().cuda.current_stream().synchronize()
+    _lib.check(systems[0].lib.ls_fd_solve_batched(handles, opts, xs, stats, n, int(concurrency), statuses))
+    out = []
+    for i, (x, _) in enumerate(prepared):
+        _lib.check(statuses[i], allow_positive=True)
+        out.append((x, _stats_dict(stats[i])))
+    return out
 
 
 MG_PROFILE_FIELDS = ("nodes", "apply_ms", "cheb_apply_ms", "resid_apply_ms", "restrict_ms", "prolong_ms",
-                     "rows_ms", "coarse_solve_ms")
+                     "rows_ms", "coarse_solve_ms", "cheb_deep_ms", "cheb_shell_ms")
 
 
 def profile_mg(system: "FdSystem", reps=20, max_levels=16):
