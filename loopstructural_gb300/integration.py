@@ -4,12 +4,12 @@
     from loopstructural_gb300.integration import gpu_interpolator_classes, register
     register(li)   # FINITE_DIFFERENCE now builds GPU interpolators
 
-``gpu_interpolator_classes(li)`` returns a subclass of the reference's own
-``FiniteDifferenceInterpolator`` that keeps every setter, getter, weight
-dictionary, bounding-box projection and serialisation method of the reference
-and overrides only the hot path, delegating to the GB300 engine:
+``gpu_interpolator_classes(li)`` returns subclasses of the reference's own
+``FiniteDifferenceInterpolator`` and ``P1Interpolator`` that keep every setter,
+getter, weight dictionary, bounding-box projection and serialisation method of
+the reference and override only the hot path, delegating to the GB300 engine:
 
-  setup_interpolator     (_finite_difference_interpolator.py:132-224)
+  setup_interpolator     (_finite_difference_interpolator.py:132-224, _p1interpolator.py:180-246)
   solve_system           (_discrete_interpolator.py:1221-1319)
   _evaluate_value_local / _evaluate_gradient_local (_discrete_interpolator.py:1342-1379)
 
@@ -22,30 +22,35 @@ from types import SimpleNamespace
 
 import numpy as np
 
-from . import interpolators, supports
+from . import interpolators, p1, supports
 
 
-def _grid_of(support):
-    return supports.StructuredGrid(origin=np.asarray(support.origin, dtype=float),
-                                   nsteps_cells=np.asarray(support.nsteps_cells, dtype=int),
-                                   step_vector=np.asarray(support.step_vector, dtype=float))
+def _grid_of(support, cls=supports.StructuredGrid):
+    return cls(origin=np.asarray(support.origin, dtype=float),
+               nsteps_cells=np.asarray(support.nsteps_cells, dtype=int),
+               step_vector=np.asarray(support.step_vector, dtype=float))
+
+
+def _engine_for(obj, support_cls, engine_cls):
+    eng = getattr(obj, "_gb300_engine", None)
+    grid = _grid_of(obj.support, support_cls)
+    if eng is None or eng.support.n_nodes != grid.n_nodes or not np.array_equal(
+            eng.support.origin, grid.origin) or not np.array_equal(eng.support.step_vector, grid.step_vector):
+        eng = engine_cls(grid)
+        obj._gb300_engine = eng
+    return eng
 
 
 def gpu_interpolator_classes(li):
-    """Subclasses of the reference interpolators with the GPU hot path."""
+    """Subclasses of the reference interpolators with the GPU hot path:
+    (FiniteDifferenceInterpolator, P1Interpolator)."""
     base = li.FiniteDifferenceInterpolator
 
     class GpuFiniteDifferenceInterpolator(base):
         """Reference FiniteDifferenceInterpolator with GB300 assembly, solve and evaluation."""
 
         def _engine(self):
-            eng = getattr(self, "_gb300_engine", None)
-            grid = _grid_of(self.support)
-            if eng is None or eng.support.n_nodes != grid.n_nodes or not np.array_equal(
-                    eng.support.origin, grid.origin) or not np.array_equal(eng.support.step_vector, grid.step_vector):
-                eng = interpolators.FiniteDifferenceInterpolator(grid)
-                self._gb300_engine = eng
-            return eng
+            return _engine_for(self, supports.StructuredGrid, interpolators.FiniteDifferenceInterpolator)
 
         def setup_interpolator(self, **kwargs):
             eng = self._engine()
@@ -94,11 +99,47 @@ def gpu_interpolator_classes(li):
             self._sync_engine_c(eng)
             return eng._evaluate_gradient_local(np.asarray(locations, dtype=float))
 
-    return (GpuFiniteDifferenceInterpolator,)
+    class GpuP1Interpolator(_p1_mixin(GpuFiniteDifferenceInterpolator), li.P1Interpolator):
+        """Reference P1Interpolator with GB300 face rows, point rows, solve and evaluation."""
+
+        def _engine(self):
+            return _engine_for(self, supports.TetMesh, p1.P1Interpolator)
+
+    return GpuFiniteDifferenceInterpolator, GpuP1Interpolator
+
+
+def _p1_mixin(fd_cls):
+    """The engine-delegating methods of the FD subclass, for the P1 subclass
+    (same delegation; the P1 engine keeps no regularisation families)."""
+
+    class _Delegate:
+        solve_system = fd_cls.solve_system
+        _sync_engine_c = fd_cls._sync_engine_c
+        _evaluate_value_local = fd_cls._evaluate_value_local
+        _evaluate_gradient_local = fd_cls._evaluate_gradient_local
+
+        def setup_interpolator(self, **kwargs):
+            eng = self._engine()
+            eng.data = {k: np.array(v, dtype=float) for k, v in self.data.items()}
+            eng.interpolation_weights = dict(self.interpolation_weights)
+            eng.ridge_factor = self.ridge_factor
+            eng.add_ridge_regulatisation = self.add_ridge_regulatisation
+            eng.setup_interpolator(**kwargs)
+            self.interpolation_weights = dict(eng.interpolation_weights)
+            self.constraints = {}
+            for name, fam in eng.constraints.items():
+                self.constraints[name] = {"matrix": SimpleNamespace(shape=(fam.n_rows, self.dof)), "b": None,
+                                          "w": fam.w.cpu().numpy()}
+            self.up_to_date = False
+            return self.finalize_setup_diagnostics_report()
+
+    return _Delegate
 
 
 def register(li):
-    """Point the reference factory's FINITE_DIFFERENCE entry at the GPU class."""
-    (gpu_fd,) = gpu_interpolator_classes(li)
+    """Point the reference factory's FINITE_DIFFERENCE and PIECEWISE_LINEAR
+    entries at the GPU classes."""
+    gpu_fd, gpu_p1 = gpu_interpolator_classes(li)
     li.interpolator_map[li.InterpolatorType.FINITE_DIFFERENCE] = gpu_fd
-    return gpu_fd
+    li.interpolator_map[li.InterpolatorType.PIECEWISE_LINEAR] = gpu_p1
+    return gpu_fd, gpu_p1

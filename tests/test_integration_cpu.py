@@ -37,9 +37,11 @@ def test_factory_builds_gpu_subclass(li):
 
     from loopstructural_gb300 import integration
 
-    saved = li.interpolator_map[li.InterpolatorType.FINITE_DIFFERENCE]
+    saved = dict(li.interpolator_map)
     try:
-        gpu_cls = integration.register(li)
+        gpu_cls, gpu_p1 = integration.register(li)
+        assert issubclass(gpu_p1, li.P1Interpolator)
+        assert li.interpolator_map[li.InterpolatorType.PIECEWISE_LINEAR] is gpu_p1
         assert issubclass(gpu_cls, li.FiniteDifferenceInterpolator)
         bb = BoundingBox(origin=np.zeros(3), maximum=np.ones(3))
         interp = li.InterpolatorFactory.create_interpolator("FDI", boundingbox=bb, nelements=1000)
@@ -49,7 +51,8 @@ def test_factory_builds_gpu_subclass(li):
         assert interp.get_value_constraints().shape == (2, 5)
         assert interp.interpolation_weights["npw"] == 10.0
     finally:
-        li.interpolator_map[li.InterpolatorType.FINITE_DIFFERENCE] = saved
+        li.interpolator_map.clear()
+        li.interpolator_map.update(saved)
 
 
 def test_gpu_subclass_fails_loudly_without_gpu(li):
@@ -60,9 +63,27 @@ def test_gpu_subclass_fails_loudly_without_gpu(li):
 
     if torch.cuda.is_available():
         pytest.skip("a GPU is visible")
-    (gpu_cls,) = integration.gpu_interpolator_classes(li)
+    gpu_cls, _ = integration.gpu_interpolator_classes(li)
     grid = li.StructuredGrid(origin=np.zeros(3), nsteps=np.array([5, 5, 5]), step_vector=np.ones(3) * 0.2)
     interp = gpu_cls(grid)
     interp.set_value_constraints(np.array([[0.5, 0.5, 0.5, 1.0]]))
     with pytest.raises(L.ExtensionUnavailable):
         interp.setup_interpolator(regularisation=0.1)
+
+
+def test_gpu_p1_subclass_keeps_reference_api_and_fails_loudly_without_gpu(li):
+    import torch
+
+    import loopstructural_gb300 as L
+    from loopstructural_gb300 import integration
+
+    _, gpu_p1 = integration.gpu_interpolator_classes(li)
+    mesh = li.TetMesh(origin=np.zeros(3), nsteps_cells=np.array([3, 3, 3]), step_vector=np.ones(3) / 3)
+    interp = gpu_p1(mesh)
+    assert interp.interpolation_weights["cgw"] == 0.1
+    interp.set_value_constraints(np.array([[0.5, 0.5, 0.5, 1.0]]))
+    assert interp.get_value_constraints().shape == (1, 5)
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    with pytest.raises(L.ExtensionUnavailable):
+        interp.setup_interpolator(cgw=0.1)
