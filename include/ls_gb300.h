@@ -264,6 +264,12 @@ int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps, ls_fd_prof
  * Returns 0 with *levels = 0 when the grid does not coarsen.  The solver
  * vectors are overwritten.  No counterpart in the reference. */
 #define LS_MG_PROFILE_FIELDS 10
+
+/* y = A_l x with the FP32 operator of multigrid level l (0 = the system's
+ * own grid; l+1 has n_l/2+1 nodes per axis), building the hierarchy if
+ * needed; *h_nodes receives the level's node count (pass NULL vectors to only
+ * query it).  A diagnostic of the preconditioner; no reference counterpart. */
+int ls_fd_mg_apply_level(ls_fd_handle *h, int level, const float *d_x, float *d_y, int64_t *h_nodes, void *stream);
 int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_levels, int *levels, void *stream);
 
 /* ------------------------------------------------------------------ */

@@ -7,9 +7,11 @@
 // sitting on fine node 2J (the coarse grid may reach one fine cell past an
 // even-sized fine grid).  Prolongation P is trilinear (weights 1 and 1/2 per
 // axis), restriction is P^T.
-//   * regularisation: re-discretised on the coarse grid -- the same stencil
-//     families with volume weights w^2 scaled by 1/2 and border-layer weights
-//     by 1/4 per level (the energy of P u_c matches in the continuum limit);
+//   * regularisation: Galerkin on the first coarse level (P^T N_reg P as a
+//     sum of tensor products of 1-D banded matrices, fd_galerkin.cuh);
+//     re-discretised below it -- the same stencil families with volume
+//     weights w^2 scaled by 1/2 and border-layer weights by 1/4 per level
+//     (the energy of P u_c matches in the continuum limit);
 //   * data rows: Galerkin, row_{l+1} = row_l P (at most 27 coarse columns).
 //     P is exact on trilinear functions, so a row confined to one fine cell
 //     stays confined to one coarse cell; on levels >= 1 the rows confined to
@@ -26,6 +28,7 @@
 #include <vector>
 
 #include "fd_apply.cuh"
+#include "fd_galerkin.cuh"
 #include "ls_common.cuh"
 
 namespace ls {
@@ -53,6 +56,9 @@ struct MgLevel {
   int32_t *krank = nullptr;
   float *k27 = nullptr;
   float *dinv = nullptr;
+  // Galerkin regularisation operator (first coarse level)
+  bool g1 = false;
+  G1Op g1op{};
   // vectors: b (rhs), x (solution), r (residual), d[2] (Chebyshev directions)
   float *b = nullptr, *x = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;
   bool owns_bx = true;

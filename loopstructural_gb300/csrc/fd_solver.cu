@@ -425,6 +425,10 @@ int mg_alloc(MgHierarchy &mg, P **ptr, size_t count) {
   return LS_OK;
 }
 
+}  // namespace
+int ensure_host_rows(ls_fd_handle *h);
+namespace {
+
 // Galerkin coarsening of data rows: row_c = row_f P (trilinear P, weights 1 / 1/2 per axis)
 HostRows galerkin_rows(const HostRows &f, int nfx, int nfy, int ncx, int ncy) {
   HostRows c;
@@ -692,8 +696,11 @@ void mg_apply(ls_fd_handle *h, const MgLevel &lv, const float *p, const EpiArgs<
         lv.ntouched, lv.inc_ptr, lv.inc_row, lv.inc_a, lv.s, lv.qd, done);
     ++h->launches;
   }
-  h->launches += launch_operator<float, EPI>(lv.coef, p, mg_view(lv), e, done, nullptr, nullptr, nullptr, nullptr,
-                                             nullptr, h->red_blocks, st);
+  if (lv.g1)
+    h->launches += launch_g1<EPI>(lv.g1op, p, mg_view(lv), e, done, h->red_blocks / 8, st);
+  else
+    h->launches += launch_operator<float, EPI>(lv.coef, p, mg_view(lv), e, done, nullptr, nullptr, nullptr, nullptr,
+                                               nullptr, h->red_blocks, st);
 }
 
 int mg_read_scalar(ls_fd_handle *h, double *dev, double *out) {
@@ -808,7 +815,10 @@ int mg_level_dinv(ls_fd_handle *h, MgLevel &lv, const std::vector<int64_t> &touc
     LS_CUDA_TRY(cudaMemcpyAsync(dd, data_diag.data(), data_diag.size() * sizeof(double), cudaMemcpyHostToDevice, st));
   }
   const int g = grid_for(h, lv.n);
-  diag_stencil_kernel<<<g, kBlock, 0, st>>>(lv.coef64, diag);
+  if (lv.g1)
+    g1_diag_kernel<<<g, kBlock, 0, st>>>(lv.g1op, diag);
+  else
+    diag_stencil_kernel<<<g, kBlock, 0, st>>>(lv.coef64, diag);
   ++h->launches;
   if (!touched.empty()) {
     mg_diag_finish_kernel<<<grid_for(h, (int64_t)touched.size()), kBlock, 0, st>>>(lv.n, diag, (int64_t)touched.size(), dt, dd);
@@ -839,6 +849,106 @@ StencilCoef coarsen_coef(const StencilCoef &f, int nx, int ny, int nz) {
   c.zz_bdr = nz >= 3 ? f.zz_bdr * 0.25 : 0.0;
   c.ridge2 *= 8.0;
   return c;
+}
+
+// 1-D banded coarse matrices P^T X P of the Galerkin operator along one axis
+// (nf fine nodes, nc = nf/2 + 1 coarse nodes): out[kind][J][d + 2] for
+// offsets d = -2..2 (0 past the ends).
+void g1_tables_1d(int nf, int nc, std::vector<double> &out) {
+  out.assign((size_t)G1_KINDS * nc * 5, 0.0);
+  auto pw = [&](int i, int J) -> double {  // trilinear prolongation weight P[i][J]
+    const int d = i - 2 * J;
+    return d == 0 ? 1.0 : (d == 1 || d == -1) ? 0.5 : 0.0;
+  };
+  auto interior = [&](int c) { return (c >= 1 && c <= nf - 2) ? 1.0 : 0.0; };
+  auto border = [&](int c) { return (double)((c == 1) + (c == nf - 2)); };
+  // X[i][j] for each kind: sum over row centres c of m(c) D[c][i] D[c][j]
+  auto X = [&](int kind, int i, int j) -> double {
+    if (kind == G1_MI) return i == j ? interior(i) : 0.0;
+    if (kind == G1_M0) return i == j ? 1.0 : 0.0;
+    double acc = 0.0;
+    for (int c = std::max(i, j) - 1; c <= std::min(i, j) + 1; ++c) {
+      if (c < 0 || c >= nf) continue;
+      const double m = kind == G1_D2B ? border(c) : interior(c);
+      if (m == 0.0) continue;
+      auto tap = [&](int node) -> double {
+        const int o = node - c;
+        if (kind == G1_D1I) return o == -1 ? -1.0 : o == 1 ? 1.0 : 0.0;
+        return o == 0 ? -2.0 : (o == 1 || o == -1) ? 1.0 : 0.0;
+      };
+      acc += m * tap(i) * tap(j);
+    }
+    return acc;
+  };
+  for (int kind = 0; kind < G1_KINDS; ++kind)
+    for (int J = 0; J < nc; ++J)
+      for (int d = -2; d <= 2; ++d) {
+        const int K = J + d;
+        if (K < 0 || K >= nc) continue;
+        double v = 0.0;
+        for (int i = 2 * J - 1; i <= 2 * J + 1; ++i) {
+          if (i < 0 || i >= nf) continue;
+          for (int j = 2 * K - 1; j <= 2 * K + 1; ++j) {
+            if (j < 0 || j >= nf) continue;
+            v += pw(i, J) * X(kind, i, j) * pw(j, K);
+          }
+        }
+        out[((size_t)kind * nc + J) * 5 + d + 2] = v;
+      }
+}
+
+// the Galerkin regularisation operator of the first coarse level c of fine level f
+int mg_build_g1(ls_fd_handle *h, MgHierarchy &mg, const MgLevel &f, MgLevel &c) {
+  G1Op &g = c.g1op;
+  g.nx = c.nx;
+  g.ny = c.ny;
+  g.nz = c.nz;
+  const StencilCoef &k = f.coef64;
+  const double w[kG1Families] = {k.xx_int, k.yy_int, k.zz_int, k.xy, k.xz, k.yz, k.xx_bdr, k.yy_bdr, k.zz_bdr,
+                                 k.ridge2};
+  for (int fm = 0; fm < kG1Families; ++fm) g.w[fm] = (float)w[fm];
+  const int nf[3] = {f.nx, f.ny, f.nz}, nc[3] = {c.nx, c.ny, c.nz};
+  double irow[3][G1_KINDS][5];
+  for (int a = 0; a < 3; ++a) {
+    std::vector<double> t;
+    g1_tables_1d(nf[a], nc[a], t);
+    const int mid = nc[a] / 2;
+    auto same = [&](int J) {
+      for (int kind = 0; kind < G1_KINDS; ++kind)
+        for (int d = 0; d < 5; ++d) {
+          const double x = t[((size_t)kind * nc[a] + J) * 5 + d], y = t[((size_t)kind * nc[a] + mid) * 5 + d];
+          if (fabs(x - y) > 1e-12 * (fabs(y) + 1.0)) return false;
+        }
+      return true;
+    };
+    int lo = mid, hi = mid;
+    while (lo - 1 >= 2 && same(lo - 1)) --lo;
+    while (hi + 1 <= nc[a] - 3 && same(hi + 1)) ++hi;
+    if (!same(mid) || nc[a] < 5) {
+      lo = 1;
+      hi = 0;  // no interior: every node through the tables
+    }
+    g.lo[a] = lo;
+    g.hi[a] = hi;
+    for (int kind = 0; kind < G1_KINDS; ++kind)
+      for (int d = 0; d < 5; ++d) irow[a][kind][d] = t[((size_t)kind * nc[a] + mid) * 5 + d];
+    std::vector<float> t32(t.begin(), t.end());
+    float *dt = nullptr;
+    LS_TRY(mg_alloc(mg, &dt, t32.size()));
+    LS_CUDA_TRY(cudaMemcpyAsync(dt, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    g.t[a] = dt;
+  }
+  for (int m = 0; m < 3; ++m)
+    for (int dy = 0; dy < 5; ++dy)
+      for (int dx = 0; dx < 5; ++dx) {
+        double acc = 0.0;
+        for (int fm = 0; fm < kG1Families; ++fm)
+          acc += w[fm] * irow[0][g1_kind(fm, 0)][dx] * irow[1][g1_kind(fm, 1)][dy] * irow[2][g1_kind(fm, 2)][m + 2];
+        g.c[m][dy][dx] = (float)acc;
+      }
+  LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  c.g1 = true;
+  return LS_OK;
 }
 
 constexpr int64_t kMgMaxCoarse = 1000;  // largest dense coarsest level
@@ -877,6 +987,7 @@ int mg_build(ls_fd_handle *h, int deg) {
   LS_TRY(mg_alloc(mg, &L0.d0, L0.n));
   LS_TRY(mg_alloc(mg, &L0.d1, L0.n));
   mg.levels.push_back(L0);
+  LS_TRY(ensure_host_rows(h));
   HostRows rows;
   rows.nrows = h->data.nrows;
   rows.width = h->h_width;
@@ -894,6 +1005,7 @@ int mg_build(ls_fd_handle *h, int deg) {
     c.n = (int64_t)c.nx * c.ny * c.nz;
     c.coef64 = coarsen_coef(f.coef64, c.nx, c.ny, c.nz);
     c.coef = coef_as<float>(c.coef64);
+    if (mg.levels.size() == 1) LS_TRY(mg_build_g1(h, mg, f, c));
     if (rows.nrows > 0) rows = galerkin_rows(rows, f.nx, f.ny, c.nx, c.ny);
     std::vector<int64_t> touched;
     std::vector<double> ddiag;
@@ -1102,6 +1214,260 @@ int mg_restart(ls_fd_handle *h, bool reset_p) {
 
 using namespace ls;
 
+namespace ls {
+namespace {
+
+// ---- data-term setup on the device -----------------------------------------
+// Per data entry: column check, int32 column, FP32 coefficient, node count.
+__global__ void data_entries_kernel(int64_t ne, int64_t n, const int64_t *__restrict__ idc, const double *__restrict__ a,
+                                    int32_t *__restrict__ cols, float *__restrict__ a32, int32_t *__restrict__ count,
+                                    int *__restrict__ bad) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = idc[e];
+    const bool ok = c < n;
+    if (!ok) atomicExch(bad, 1);
+    cols[e] = (c < 0 || !ok) ? -1 : (int32_t)c;
+    a32[e] = (float)a[e];
+    if (c >= 0 && ok) atomicAdd(count + c, 1);
+  }
+}
+
+__global__ void data_rows_setup_kernel(int64_t nrows, const double *__restrict__ w, const double *__restrict__ b,
+                                       double *__restrict__ w2_64, float *__restrict__ w2_32, double *__restrict__ bc) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
+    const double w2 = w[r] * w[r];
+    w2_64[r] = w2;
+    w2_32[r] = (float)w2;
+    bc[r] = b[r];
+  }
+}
+
+// exclusive scan of int32 counts into int64 offsets (one block; setup time)
+__global__ void __launch_bounds__(1024) setup_scan_kernel(const int32_t *__restrict__ cnt, int64_t n,
+                                                          int64_t *__restrict__ off, int64_t *__restrict__ total) {
+  __shared__ int64_t warp_tot[32];
+  __shared__ int64_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t base = 0; base < n; base += 1024) {
+    const int64_t i = base + threadIdx.x;
+    const int64_t v = (i < n) ? cnt[i] : 0;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int64_t t = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      warp_tot[lane] = t;
+    }
+    __syncthreads();
+    const int64_t excl = x - v + (warp > 0 ? warp_tot[warp - 1] : 0) + carry;
+    if (i < n) off[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+// entry e goes to the next free slot of its node's segment (any order)
+__global__ void data_fill_kernel(int64_t ne, const int32_t *__restrict__ cols, const int64_t *__restrict__ start,
+                                 int32_t *__restrict__ fill, int64_t *__restrict__ ent) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = cols[e];
+    if (c >= 0) ent[start[c] + atomicAdd(fill + c, 1)] = e;
+  }
+}
+
+// each node's segment sorted by entry index (= row order), then the row
+// index and coefficients of every incidence
+__global__ void data_sort_kernel(int64_t n, const int64_t *__restrict__ start, int64_t *__restrict__ ent, int width,
+                                 const double *__restrict__ a, int32_t *__restrict__ inc_row,
+                                 double *__restrict__ inc_a64, float *__restrict__ inc_a32) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t s0 = start[g], s1 = start[g + 1];
+    for (int64_t i = s0 + 1; i < s1; ++i) {
+      const int64_t v = ent[i];
+      int64_t k = i - 1;
+      while (k >= s0 && ent[k] > v) {
+        ent[k + 1] = ent[k];
+        --k;
+      }
+      ent[k + 1] = v;
+    }
+    for (int64_t i = s0; i < s1; ++i) {
+      const int64_t e = ent[i];
+      inc_row[i] = (int32_t)(e / width);
+      inc_a64[i] = a[e];
+      inc_a32[i] = (float)a[e];
+    }
+  }
+}
+
+// mask word w = nodes 32w .. 32w+31 with incidences; popcount per word
+__global__ void data_mask_kernel(int64_t n, int64_t nwords, const int32_t *__restrict__ count,
+                                 uint32_t *__restrict__ mask, int32_t *__restrict__ wcount) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g - lane < nwords * 32;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t word = __ballot_sync(0xffffffffu, g < n && count[g] > 0);
+    if (lane == 0) {
+      mask[g >> 5] = word;
+      wcount[g >> 5] = __popc(word);
+    }
+  }
+}
+
+__global__ void data_touched_kernel(int64_t n, const uint32_t *__restrict__ mask, const int64_t *__restrict__ wrank64,
+                                    const int64_t *__restrict__ start, int32_t *__restrict__ word_rank,
+                                    int64_t *__restrict__ touched, int64_t *__restrict__ inc_ptr) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t w = g >> 5;
+    const uint32_t word = mask[w], bit = 1u << (g & 31);
+    if ((g & 31) == 0) word_rank[w] = (int32_t)wrank64[w];
+    if (!(word & bit)) continue;
+    const int64_t rank = wrank64[w] + __popc(word & (bit - 1u));
+    touched[rank] = g;
+    inc_ptr[rank] = start[g];
+  }
+}
+
+}  // namespace
+
+// Device copies of the data rows and the node -> row incidence list (CSR over
+// the touched nodes in node order, each node's entries in row order), built
+// on the device: counts, scan, fill, per-node sort, mask and ranks.
+int setup_data_term(ls_fd_handle *h, const ls_fd_system *sys, int64_t ne) {
+  DataTerm &d = h->data;
+  const int64_t n = h->n;
+  const int64_t nwords = (n + 31) / 32;
+  cudaStream_t hs = h->stream;
+  LS_TRY(dev_alloc(&d.cols, ne));
+  LS_TRY(dev_alloc(&d.a64, ne));
+  LS_TRY(dev_alloc(&d.a32, ne));
+  LS_TRY(dev_alloc(&d.w2_64, d.nrows));
+  LS_TRY(dev_alloc(&d.w2_32, d.nrows));
+  LS_TRY(dev_alloc(&d.b, d.nrows));
+  LS_TRY(dev_alloc(&h->s64, d.nrows));
+  LS_TRY(dev_alloc(&h->s32, d.nrows));
+  LS_TRY(dev_alloc(&d.mask, nwords));
+  LS_TRY(dev_alloc(&d.word_rank, nwords));
+  int32_t *count = nullptr, *fill = nullptr, *wcount = nullptr;
+  int64_t *start = nullptr, *ent = nullptr, *wrank = nullptr, *totals = nullptr;
+  int *bad = nullptr;
+  auto release = [&]() {
+    cudaFree(count);
+    cudaFree(fill);
+    cudaFree(wcount);
+    cudaFree(start);
+    cudaFree(ent);
+    cudaFree(wrank);
+    cudaFree(totals);
+    cudaFree(bad);
+  };
+  int st = LS_OK;
+  if ((st = dev_alloc(&count, n)) < 0 || (st = dev_alloc(&fill, n)) < 0 || (st = dev_alloc(&wcount, nwords)) < 0 ||
+      (st = dev_alloc(&start, n + 1)) < 0 || (st = dev_alloc(&wrank, nwords + 1)) < 0 ||
+      (st = dev_alloc(&totals, 2)) < 0 || (st = dev_alloc(&bad, 1)) < 0) {
+    release();
+    return st;
+  }
+  cudaMemsetAsync(count, 0, n * sizeof(int32_t), hs);
+  cudaMemsetAsync(fill, 0, n * sizeof(int32_t), hs);
+  cudaMemsetAsync(bad, 0, sizeof(int), hs);
+  if (ne > 0) {
+    data_entries_kernel<<<grid_for(h, ne), kBlock, 0, hs>>>(ne, n, sys->d_idc, sys->d_a, d.cols, d.a32, count, bad);
+    ++h->launches;
+    cudaMemcpyAsync(d.a64, sys->d_a, ne * sizeof(double), cudaMemcpyDeviceToDevice, hs);
+    data_rows_setup_kernel<<<grid_for(h, d.nrows), kBlock, 0, hs>>>(d.nrows, sys->d_w, sys->d_b, d.w2_64, d.w2_32, d.b);
+    ++h->launches;
+  }
+  setup_scan_kernel<<<1, 1024, 0, hs>>>(count, n, start, totals);
+  ++h->launches;
+  int64_t ni = 0;
+  int hbad = 0;
+  if (cudaMemcpyAsync(&ni, totals, sizeof(int64_t), cudaMemcpyDeviceToHost, hs) != cudaSuccess ||
+      cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, hs) != cudaSuccess ||
+      cudaStreamSynchronize(hs) != cudaSuccess) {
+    release();
+    set_error("data-row setup failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return LS_ERR_CUDA;
+  }
+  if (hbad) {
+    release();
+    set_error("a data-row column is out of range (dof %lld)", (long long)n);
+    return LS_ERR_ARG;
+  }
+  cudaMemcpyAsync(start + n, &ni, sizeof(int64_t), cudaMemcpyHostToDevice, hs);
+  if ((st = dev_alloc(&ent, ni)) < 0 || (st = dev_alloc(&d.inc_row, ni)) < 0 || (st = dev_alloc(&d.inc_a64, ni)) < 0 ||
+      (st = dev_alloc(&d.inc_a32, ni)) < 0) {
+    release();
+    return st;
+  }
+  if (ne > 0) {
+    data_fill_kernel<<<grid_for(h, ne), kBlock, 0, hs>>>(ne, d.cols, start, fill, ent);
+    ++h->launches;
+  }
+  data_sort_kernel<<<grid_for(h, n), kBlock, 0, hs>>>(n, start, ent, d.width > 0 ? d.width : 1, d.a64, d.inc_row,
+                                                       d.inc_a64, d.inc_a32);
+  data_mask_kernel<<<grid_for(h, nwords * 32), kBlock, 0, hs>>>(n, nwords, count, d.mask, wcount);
+  setup_scan_kernel<<<1, 1024, 0, hs>>>(wcount, nwords, wrank, totals + 1);
+  h->launches += 3;
+  int64_t nt = 0;
+  if (cudaMemcpyAsync(&nt, totals + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, hs) != cudaSuccess ||
+      cudaStreamSynchronize(hs) != cudaSuccess) {
+    release();
+    set_error("data-row setup failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return LS_ERR_CUDA;
+  }
+  d.ntouched = nt;
+  if ((st = dev_alloc(&d.touched, nt)) < 0 || (st = dev_alloc(&d.inc_ptr, nt + 1)) < 0) {
+    release();
+    return st;
+  }
+  data_touched_kernel<<<grid_for(h, n), kBlock, 0, hs>>>(n, d.mask, wrank, start, d.word_rank, d.touched, d.inc_ptr);
+  ++h->launches;
+  cudaMemcpyAsync(d.inc_ptr + nt, &ni, sizeof(int64_t), cudaMemcpyHostToDevice, hs);
+  const cudaError_t e = cudaStreamSynchronize(hs);
+  release();
+  if (e != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+    set_error("data-row setup kernels failed: %s", cudaGetErrorString(e));
+    return LS_ERR_CUDA;
+  }
+  h->h_width = d.width;
+  return LS_OK;
+}
+
+// host copy of the data rows, for the Galerkin coarsening of the multigrid
+int ensure_host_rows(ls_fd_handle *h) {
+  const DataTerm &d = h->data;
+  const int64_t ne = d.nrows * d.width;
+  if ((int64_t)h->h_idc.size() == ne && (int64_t)h->h_w2.size() == d.nrows) return LS_OK;
+  std::vector<int32_t> cols(ne);
+  h->h_idc.resize(ne);
+  h->h_a.resize(ne);
+  h->h_w2.resize(d.nrows);
+  if (ne > 0) {
+    LS_CUDA_TRY(cudaMemcpy(cols.data(), d.cols, ne * sizeof(int32_t), cudaMemcpyDeviceToHost));
+    LS_CUDA_TRY(cudaMemcpy(h->h_a.data(), d.a64, ne * sizeof(double), cudaMemcpyDeviceToHost));
+    LS_CUDA_TRY(cudaMemcpy(h->h_w2.data(), d.w2_64, d.nrows * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  for (int64_t e = 0; e < ne; ++e) h->h_idc[e] = cols[e];
+  return LS_OK;
+}
+
+}  // namespace ls
+
 extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *stream) {
   LS_ARG_CHECK(sys != nullptr && out != nullptr, "NULL argument");
   *out = nullptr;
@@ -1161,97 +1527,8 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
   d.nrows = sys->nrows;
   d.width = sys->nrows > 0 ? sys->width : 0;
   const int64_t ne = d.nrows * d.width;
-  std::vector<int64_t> idc(ne);
-  std::vector<double> av(ne), wv(d.nrows), bv(d.nrows);
-  if (ne > 0) {
-    if (cudaMemcpy(idc.data(), sys->d_idc, ne * sizeof(int64_t), cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(av.data(), sys->d_a, ne * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(wv.data(), sys->d_w, d.nrows * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess ||
-        cudaMemcpy(bv.data(), sys->d_b, d.nrows * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
-      set_error("copying data rows failed");
-      return fail(LS_ERR_CUDA);
-    }
-  }
-  std::vector<int32_t> cols(ne);
-  std::vector<std::pair<int64_t, int64_t>> inc;  // (node, entry)
-  inc.reserve(ne);
-  for (int64_t e = 0; e < ne; ++e) {
-    const int64_t c = idc[e];
-    if (c >= n) {
-      set_error("data-row column %lld out of range (dof %lld)", (long long)c, (long long)n);
-      return fail(LS_ERR_ARG);
-    }
-    cols[e] = c < 0 ? -1 : (int32_t)c;
-    if (c >= 0) inc.emplace_back(c, e);
-  }
-  std::stable_sort(inc.begin(), inc.end(),
-                   [](const std::pair<int64_t, int64_t> &x, const std::pair<int64_t, int64_t> &y) { return x.first < y.first; });
-  std::vector<int64_t> touched, ptr;
-  std::vector<int32_t> irow;
-  std::vector<double> ia64;
-  std::vector<float> ia32, a32(ne), w2_32(d.nrows);
-  std::vector<double> w2_64(d.nrows);
-  for (size_t t = 0; t < inc.size(); ++t) {
-    if (t == 0 || inc[t].first != inc[t - 1].first) {
-      touched.push_back(inc[t].first);
-      ptr.push_back((int64_t)t);
-    }
-    irow.push_back((int32_t)(inc[t].second / d.width));
-    ia64.push_back(av[inc[t].second]);
-    ia32.push_back((float)av[inc[t].second]);
-  }
-  ptr.push_back((int64_t)inc.size());
-  for (int64_t e = 0; e < ne; ++e) a32[e] = (float)av[e];
-  for (int64_t r = 0; r < d.nrows; ++r) {
-    w2_64[r] = wv[r] * wv[r];
-    w2_32[r] = (float)w2_64[r];
-  }
-  h->h_idc = idc;
-  h->h_a = av;
-  h->h_w2 = w2_64;
-  h->h_width = d.width;
-  d.ntouched = (int64_t)touched.size();
-  const int64_t ni = (int64_t)inc.size();
-  const int64_t nwords = (n + 31) / 32;
-  std::vector<uint32_t> mask(nwords, 0u);
-  std::vector<int32_t> word_rank(nwords, 0);
-  for (int64_t t : touched) mask[t >> 5] |= 1u << (t & 31);
-  {
-    int32_t run = 0;
-    for (int64_t w = 0; w < nwords; ++w) {
-      word_rank[w] = run;
-      run += __builtin_popcount(mask[w]);
-    }
-  }
-  if ((st = dev_alloc(&d.cols, ne)) < 0 || (st = dev_alloc(&d.a64, ne)) < 0 || (st = dev_alloc(&d.a32, ne)) < 0 ||
-      (st = dev_alloc(&d.w2_64, d.nrows)) < 0 || (st = dev_alloc(&d.w2_32, d.nrows)) < 0 ||
-      (st = dev_alloc(&d.b, d.nrows)) < 0 || (st = dev_alloc(&d.touched, d.ntouched)) < 0 ||
-      (st = dev_alloc(&d.inc_ptr, d.ntouched + 1)) < 0 || (st = dev_alloc(&d.inc_row, ni)) < 0 ||
-      (st = dev_alloc(&d.inc_a64, ni)) < 0 || (st = dev_alloc(&d.inc_a32, ni)) < 0 ||
-      (st = dev_alloc(&h->s64, d.nrows)) < 0 || (st = dev_alloc(&h->s32, d.nrows)) < 0 ||
-      (st = dev_alloc(&d.mask, nwords)) < 0 || (st = dev_alloc(&d.word_rank, nwords)) < 0)
-    return fail(st);
+  if ((st = setup_data_term(h, sys, ne)) < 0) return fail(st);
   cudaStream_t hs = h->stream;
-#define UP(dst, src, cnt)                                                                                        \
-  if ((cnt) > 0 && cudaMemcpyAsync(dst, (src).data(), (cnt) * sizeof((src)[0]), cudaMemcpyHostToDevice, hs) != \
-                       cudaSuccess) {                                                                            \
-    set_error("upload failed");                                                                                  \
-    return fail(LS_ERR_CUDA);                                                                                    \
-  }
-  UP(d.cols, cols, ne);
-  UP(d.a64, av, ne);
-  UP(d.a32, a32, ne);
-  UP(d.w2_64, w2_64, d.nrows);
-  UP(d.w2_32, w2_32, d.nrows);
-  UP(d.b, bv, d.nrows);
-  UP(d.touched, touched, d.ntouched);
-  UP(d.inc_ptr, ptr, d.ntouched + 1);
-  UP(d.inc_row, irow, ni);
-  UP(d.inc_a64, ia64, ni);
-  UP(d.inc_a32, ia32, ni);
-  UP(d.mask, mask, nwords);
-  UP(d.word_rank, word_rank, nwords);
-#undef UP
   // ---- rhs, diagonal, inverse diagonal ----
   const int gn = grid_for(h, n);
   cudaMemsetAsync(h->rhs, 0, n * sizeof(double), hs);
@@ -1606,6 +1883,26 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
   return status;
 }
 
+extern "C" int ls_fd_mg_apply_level(ls_fd_handle *h, int level, const float *d_x, float *d_y, int64_t *h_nodes,
+                                    void *stream) {
+  LS_ARG_CHECK(h && h_nodes, "NULL argument");
+  LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+  LS_TRY(mg_build(h, 3));
+  MgHierarchy &mg = h->mg;
+  LS_ARG_CHECK(mg.built, "the grid does not coarsen");
+  LS_ARG_CHECK(level >= 0 && level < (int)mg.levels.size(), "no such level");
+  MgLevel &lv = mg.levels[level];
+  *h_nodes = lv.n;
+  if (!d_x || !d_y) return LS_OK;
+  LS_ARG_CHECK(level + 1 < (int)mg.levels.size(), "the coarsest level has no apply");
+  EpiArgs<float> e{};
+  e.q = d_y;
+  mg_apply<EPI_STORE>(h, lv, d_x, e, nullptr, h->stream);
+  LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
+
 extern "C" int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_levels, int *levels, void *stream) {
   LS_ARG_CHECK(h && out && levels && reps > 0 && max_levels > 0, "bad argument");
   LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
@@ -1656,7 +1953,7 @@ extern "C" int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_
     ec.c1 = 0.5f;
     ec.c2 = 1e-3f;
     LS_TRY(timed([&] { mg_apply<EPI_CHEB>(h, lv, lv.d0, ec, nullptr, st); }, &o[2]));
-    if (lv.n > kPointMaxNodes && apply_split(lv.nx, lv.ny, lv.nz)) {
+    if (!lv.g1 && lv.n > kPointMaxNodes && apply_split(lv.nx, lv.ny, lv.nz)) {
       const DataView<float> dv = mg_view(lv);
       LS_TRY(timed([&] {
         if (dv.k27)

@@ -245,6 +245,21 @@ def profile_mg(system: "FdSystem", reps=20, max_levels=16):
     return [{f: out[l * k + i] for i, f in enumerate(MG_PROFILE_FIELDS)} for l in range(nl.value)]
 
 
+def mg_apply_level(system: "FdSystem", level: int, x=None):
+    """(nodes, A_level x): the FP32 operator of a multigrid level (diagnostic)."""
+    torch = _torch()
+    nodes = C.c_int64(0)
+    _lib.check(system.lib.ls_fd_mg_apply_level(system.handle, int(level), None, None, C.byref(nodes),
+                                               _lib.stream_ptr()))
+    if x is None:
+        return nodes.value, None
+    x = x.to(device=system.dev, dtype=torch.float32).contiguous()
+    y = torch.empty_like(x)
+    _lib.check(system.lib.ls_fd_mg_apply_level(system.handle, int(level), _lib.ptr(x), _lib.ptr(y), C.byref(nodes),
+                                               _lib.stream_ptr()))
+    return nodes.value, y
+
+
 def profile_iteration(system: "FdSystem", precision="mixed", reps=20):
     """Device time per launch of each kernel class of one CG iteration."""
     prof = _lib.FdProfile()

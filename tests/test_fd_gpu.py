@@ -324,3 +324,46 @@ def test_multigrid_falls_back_to_jacobi_on_thin_grids():
     assert interp.solve_system("cg", solver_kwargs={"rtol": 1e-10, "preconditioner": "mg"})
     t = interp.get_last_solve_timing()
     assert t["preconditioner"] == "jacobi" and t["status"] == 0
+
+
+def _prolong_1d(nf):
+    nc = nf // 2 + 1
+    P = np.zeros((nf, nc))
+    for i in range(nf):
+        if i % 2 == 0:
+            P[i, i // 2] = 1.0
+        else:
+            P[i, i // 2] = P[i, i // 2 + 1] = 0.5
+    return P
+
+
+@pytest.mark.parametrize("cells", [(24, 23, 26), (30, 31, 29)])
+def test_first_coarse_level_is_galerkin(cells):
+    """Multigrid level 1 applies P^T N P exactly (regularisation by the
+    tensor-product Galerkin operator, data rows by the 27-point form)."""
+    cells = np.array(cells)
+    rng = np.random.default_rng(9)
+    vp = rng.uniform(0, 1, size=(300, 3))
+    val = np.column_stack([vp, vp[:, 2], np.ones(300)])
+    npnt = rng.uniform(0, 1, size=(60, 3))
+    nrm = np.column_stack([npnt, rng.normal(size=(60, 3)), np.ones(60)])
+    setup = dict(regularisation=0.1, cpw=1.0, npw=1.0)
+    interp = L.FiniteDifferenceInterpolator(_grid(cells))
+    interp.set_value_constraints(val)
+    interp.set_normal_constraints(nrm)
+    interp.setup_interpolator(**setup)
+    system = interp._build_system()
+    grid = fdo.Grid(np.zeros(3), cells, 1.0 / cells.astype(float))
+    A, _ = fdo.assemble(grid, {"value": val, "normal": nrm}, fdo.resolve_weights(**setup)).matrix()
+    N, _ = fdo.normal_equations(A, np.zeros(A.shape[0]))
+    nf = cells + 1
+    Px, Py, Pz = (_prolong_1d(n) for n in nf)
+    P = sparse.csr_matrix(np.kron(np.kron(Pz, Py), Px))
+    G = (P.T @ N @ P).tocsr()
+    nodes, _ = fd.mg_apply_level(system, 1)
+    assert nodes == G.shape[0]
+    x = np.random.default_rng(1).normal(size=nodes)
+    _, y = fd.mg_apply_level(system, 1, torch.from_numpy(x))
+    ref = G @ x
+    assert np.max(np.abs(y.cpu().numpy() - ref)) <= 2e-5 * np.max(np.abs(ref))
+    system.close()
