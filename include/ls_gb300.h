@@ -259,8 +259,8 @@ int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps, ls_fd_prof
  * (plain), 2 apply with the Chebyshev epilogue, 3 apply with the residual
  * epilogue, 4 restriction to level l+1, 5 prolongation from level l+1,
  * 6 data rows (row form), 7 the coarsest dense solve (last level only),
- * 8 / 9 the Chebyshev apply's staged deep-box kernel / boundary-shell kernel
- * alone (levels split into the two; 0 otherwise).
+ * 8 / 9 the Chebyshev apply's staged interior kernel / boundary kernel alone
+ * (levels whose operator is split into the two; 0 otherwise).
  * Returns 0 with *levels = 0 when the grid does not coarsen.  The solver
  * vectors are overwritten.  No counterpart in the reference. */
 #define LS_MG_PROFILE_FIELDS 10

@@ -1,5 +1,5 @@
-// Galerkin coarse operator of the FD regularisation, G = P^T N_reg P, for
-// the first coarse multigrid level.
+// Galerkin coarse operators of the FD regularisation, G_l = P^T G_{l-1} P
+// (G_0 = N_reg), for the coarse multigrid levels.
 //
 // Every regularisation family is a tensor product of per-axis operators: the
 // row stencil ((1,-2,1), (-1,0,1) or the identity), the row-existence mask of
@@ -14,12 +14,17 @@
 //     xx: D2I MI MI   yy: MI D2I MI   zz: MI MI D2I
 //     xy: D1I D1I MI  xz: D1I MI D1I  yz: MI D1I D1I
 //     x-border: D2B M0 M0  (y, z alike)   ridge: M0 M0 M0.
-// Away from the faces every 1-D row equals the interior row, so G is a
-// constant, symmetric 125-point stencil there (staged-tile kernel); the
-// nodes near a face evaluate the tensor-product sum directly (node-per-
-// thread kernel).  The rediscretised operator the other levels use weights
-// the border layers much more than G does (P annihilates second differences
-// centred on odd fine nodes), which slows the V-cycle's convergence.
+// Coarsening keeps this form: each 1-D table becomes P^T T P (still
+// bandwidth 2).  Away from the faces every 1-D row equals the interior row, so
+// G is a constant, symmetric 125-point stencil there (staged-tile kernel); the
+// nodes near a face (two per side) evaluate the tensor-product sum from the
+// tables (node-per-thread kernel).  Levels of at most kG1ExplicitMax nodes
+// store every node's explicit 125-point stencil (evaluated from the tables at
+// setup) and run one node-per-thread kernel: one launch, no staging, which
+// is what small grids are bound by.  A rediscretised coarse operator would weight the border
+// layers much more than G does (P annihilates second differences centred on
+// odd fine nodes); at 200^3 the Galerkin hierarchy needs 137 instead of 213
+// iterations to rtol 1e-10.
 #pragma once
 
 #include "fd_apply.cuh"
@@ -28,6 +33,8 @@ namespace ls {
 
 enum G1Kind { G1_D2I = 0, G1_D1I = 1, G1_MI = 2, G1_D2B = 3, G1_M0 = 4, G1_KINDS = 5 };
 constexpr int kG1Families = 10;
+constexpr int64_t kG1ExplicitMax = 200000;
+constexpr int kG1MaxBand = 6;  // face stencils kept for up to 3 band rows per side
 
 struct G1Op {
   int nx, ny, nz;
@@ -35,6 +42,11 @@ struct G1Op {
   const float *t[3];                 // per axis: [kind][index][5] (offsets -2..2)
   float w[kG1Families];              // family weights
   float c[3][5][5];                  // interior stencil c(|dz|, dy, dx); c(-dz) = c(dz)
+  const float *shell_coef;           // small levels: 125 x n explicit stencils of every node
+  // face nodes (one axis in its boundary band): the stencil depends only on
+  // that axis' band row -- face_coef[(axis * kG1MaxBand + row) * 125 + o],
+  // row = index (low side) or kG1MaxBand/2 + (n - 1 - index) (high side)
+  const float *face_coef;
 };
 
 // 1-D kinds of family f along axis a
@@ -201,11 +213,37 @@ __global__ void __launch_bounds__(kAX * kAY, 4) g1_apply_kernel(G1Op g, const fl
   }
 }
 
-// Nodes outside the interior box, one thread per node.
-template <int EPI, bool K27>
+// The explicit 125-point stencils of the nodes outside the interior box
+// (setup): coef[o][s], o = 25 (dz+2) + 5 (dy+2) + (dx+2).
+__global__ void g1_coef_kernel(G1Op g, float *__restrict__ coef) {
+  const int64_t ns = box_shell_count(g);
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns; s += (int64_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    box_shell_index(g, s, i, j, k);
+    for (int o = 0; o < 125; ++o) {
+      const int dz = o / 25 - 2, dy = (o / 5) % 5 - 2, dx = o % 5 - 2;
+      double acc = 0.0;
+      for (int f = 0; f < kG1Families; ++f)
+        acc += (double)g.w[f] * g.t[0][((size_t)g1_kind(f, 0) * g.nx + i) * 5 + dx + 2] *
+               g.t[1][((size_t)g1_kind(f, 1) * g.ny + j) * 5 + dy + 2] *
+               g.t[2][((size_t)g1_kind(f, 2) * g.nz + k) * 5 + dz + 2];
+      coef[(size_t)o * ns + s] = (float)acc;
+    }
+  }
+}
+
+// Nodes outside the interior box, one thread per node: explicit stencils
+// (EXPLICIT, small levels whose every node is stored) or the tensor-product
+// sum from the tables.
+template <int EPI, bool K27, bool EXPLICIT>
 __global__ void __launch_bounds__(256) g1_shell_kernel(G1Op g, const float *__restrict__ p, DataView<float> dv,
                                                        EpiArgs<float> e, const int *done) {
   if (done && *done) return;
+  __shared__ float fc[EXPLICIT ? 1 : 3 * kG1MaxBand * 125];
+  if (!EXPLICIT) {
+    for (int t = threadIdx.x; t < 3 * kG1MaxBand * 125; t += blockDim.x) fc[t] = __ldg(g.face_coef + t);
+    __syncthreads();
+  }
   const int nx = g.nx, ny = g.ny, nz = g.nz;
   const int64_t ns = box_shell_count(g);
   for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < ns; s += (int64_t)gridDim.x * blockDim.x) {
@@ -224,7 +262,34 @@ __global__ void __launch_bounds__(256) g1_shell_kernel(G1Op g, const float *__re
       const bool ok = (vz >> (dz + 2)) & (vy >> (dy + 2)) & (vx >> (dx + 2)) & 1u;
       return ok ? __ldg(p + (gi + dz * sxy + dy * nx + dx)) : 0.f;
     };
-    float q = g1_node(g, i, j, k, pr);
+    float q = 0.f;
+    if (EXPLICIT) {
+#pragma unroll
+      for (int o = 0; o < 125; ++o)
+        q += __ldg(g.shell_coef + (size_t)o * ns + s) * pr(o / 25 - 2, (o / 5) % 5 - 2, o % 5 - 2);
+    } else {
+      // axes in their boundary band and the band row of each
+      const int ax[3] = {i, j, k}, an[3] = {nx, ny, nz};
+      int nb = 0, axis = 0, row = 0;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const int x = ax[a];
+        if (x < g.lo[a] || x > g.hi[a]) {
+          ++nb;
+          axis = a;
+          row = x < g.lo[a] ? x : kG1MaxBand / 2 + (an[a] - 1 - x);
+        }
+      }
+      if (nb == 1 && (row % (kG1MaxBand / 2)) < kG1MaxBand / 2 &&
+          (row < kG1MaxBand / 2 ? row < g.lo[axis] : an[axis] - 1 - (row - kG1MaxBand / 2) > g.hi[axis]) &&
+          (row < kG1MaxBand / 2 ? g.lo[axis] <= kG1MaxBand / 2 : an[axis] - 1 - g.hi[axis] <= kG1MaxBand / 2)) {
+        const float *c = fc + (axis * kG1MaxBand + row) * 125;
+#pragma unroll
+        for (int o = 0; o < 125; ++o) q += c[o] * pr(o / 25 - 2, (o / 5) % 5 - 2, o % 5 - 2);
+      } else {
+        q = g1_node(g, i, j, k, pr);
+      }
+    }
     if (dv.enabled) q += data_term<float>(dv, gi);
     if (K27) q += k27_term<float>(dv, gi, pr);
     epilogue<float, EPI>(e, gi, __ldg(p + gi), q);
@@ -246,12 +311,13 @@ __global__ void g1_diag_kernel(G1Op g, double *__restrict__ diag) {
   }
 }
 
+// parts: bit 0 the interior kernel, bit 1 the boundary kernel
 template <int EPI, bool K27>
 inline int launch_g1_k(const G1Op &g, const float *p, const DataView<float> &dv, const EpiArgs<float> &e,
-                       const int *done, int sms, cudaStream_t st) {
+                       const int *done, int sms, cudaStream_t st, int parts = 3) {
   int launches = 0;
   const int bx = g.hi[0] - g.lo[0] + 1, by = g.hi[1] - g.lo[1] + 1, bz = g.hi[2] - g.lo[2] + 1;
-  if (bx > 0 && by > 0 && bz > 0) {
+  if ((parts & 1) && bx > 0 && by > 0 && bz > 0) {
     const dim3 blk(kAX, kAY);
     const dim3 g16((bx + kAX - 1) / kAX, (by + kAY - 1) / kAY, (bz + 15) / 16);
     if ((int64_t)g16.x * g16.y * g16.z >= 4 * (int64_t)sms) {
@@ -263,9 +329,12 @@ inline int launch_g1_k(const G1Op &g, const float *p, const DataView<float> &dv,
     ++launches;
   }
   const int64_t ns = box_shell_count(g);
-  if (ns > 0) {
+  if ((parts & 2) && ns > 0) {
     const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((ns + 255) / 256, 8 * (int64_t)sms));
-    g1_shell_kernel<EPI, K27><<<gs, 256, 0, st>>>(g, p, dv, e, done);
+    if (g.shell_coef)
+      g1_shell_kernel<EPI, K27, true><<<gs, 256, 0, st>>>(g, p, dv, e, done);
+    else
+      g1_shell_kernel<EPI, K27, false><<<gs, 256, 0, st>>>(g, p, dv, e, done);
     ++launches;
   }
   return launches;
@@ -274,9 +343,9 @@ inline int launch_g1_k(const G1Op &g, const float *p, const DataView<float> &dv,
 // q = (G + data term) p with an epilogue; returns the number of launches
 template <int EPI>
 inline int launch_g1(const G1Op &g, const float *p, const DataView<float> &dv, const EpiArgs<float> &e,
-                     const int *done, int sms, cudaStream_t st) {
-  if (dv.k27) return launch_g1_k<EPI, true>(g, p, dv, e, done, sms, st);
-  return launch_g1_k<EPI, false>(g, p, dv, e, done, sms, st);
+                     const int *done, int sms, cudaStream_t st, int parts = 3) {
+  if (dv.k27) return launch_g1_k<EPI, true>(g, p, dv, e, done, sms, st, parts);
+  return launch_g1_k<EPI, false>(g, p, dv, e, done, sms, st, parts);
 }
 
 }  // namespace ls

@@ -7,11 +7,9 @@
 // sitting on fine node 2J (the coarse grid may reach one fine cell past an
 // even-sized fine grid).  Prolongation P is trilinear (weights 1 and 1/2 per
 // axis), restriction is P^T.
-//   * regularisation: Galerkin on the first coarse level (P^T N_reg P as a
-//     sum of tensor products of 1-D banded matrices, fd_galerkin.cuh);
-//     re-discretised below it -- the same stencil families with volume
-//     weights w^2 scaled by 1/2 and border-layer weights by 1/4 per level
-//     (the energy of P u_c matches in the continuum limit);
+//   * regularisation: Galerkin, P^T A_l P, on every coarse level -- a sum of
+//     tensor products of 1-D banded matrices (fd_galerkin.cuh), coarsened
+//     axis by axis;
 //   * data rows: Galerkin, row_{l+1} = row_l P (at most 27 coarse columns).
 //     P is exact on trilinear functions, so a row confined to one fine cell
 //     stays confined to one coarse cell; on levels >= 1 the rows confined to
@@ -59,6 +57,7 @@ struct MgLevel {
   // Galerkin regularisation operator (first coarse level)
   bool g1 = false;
   G1Op g1op{};
+  std::vector<double> g1host[3];  // the 1-D tables (FP64), for coarsening to the next level
   // vectors: b (rhs), x (solution), r (residual), d[2] (Chebyshev directions)
   float *b = nullptr, *x = nullptr, *r = nullptr, *d0 = nullptr, *d1 = nullptr;
   bool owns_bx = true;

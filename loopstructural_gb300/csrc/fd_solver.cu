@@ -897,21 +897,50 @@ void g1_tables_1d(int nf, int nc, std::vector<double> &out) {
       }
 }
 
-// the Galerkin regularisation operator of the first coarse level c of fine level f
+// P^T T P of banded 1-D tables T (nf nodes) onto nc = nf/2 + 1 coarse nodes
+void g1_tables_coarsen(const std::vector<double> &tf, int nf, int nc, std::vector<double> &out) {
+  out.assign((size_t)G1_KINDS * nc * 5, 0.0);
+  auto pw = [&](int i, int J) -> double {
+    const int d = i - 2 * J;
+    return d == 0 ? 1.0 : (d == 1 || d == -1) ? 0.5 : 0.0;
+  };
+  for (int kind = 0; kind < G1_KINDS; ++kind)
+    for (int J = 0; J < nc; ++J)
+      for (int d = -2; d <= 2; ++d) {
+        const int K = J + d;
+        if (K < 0 || K >= nc) continue;
+        double v = 0.0;
+        for (int i = 2 * J - 1; i <= 2 * J + 1; ++i) {
+          if (i < 0 || i >= nf) continue;
+          for (int j = 2 * K - 1; j <= 2 * K + 1; ++j) {
+            if (j < 0 || j >= nf || j - i < -2 || j - i > 2) continue;
+            v += pw(i, J) * tf[((size_t)kind * nf + i) * 5 + (j - i) + 2] * pw(j, K);
+          }
+        }
+        out[((size_t)kind * nc + J) * 5 + d + 2] = v;
+      }
+}
+
+// the Galerkin regularisation operator of coarse level c of fine level f
+// (tables from the fine stencil for the first coarse level, else by
+// coarsening the fine level's tables)
 int mg_build_g1(ls_fd_handle *h, MgHierarchy &mg, const MgLevel &f, MgLevel &c) {
   G1Op &g = c.g1op;
   g.nx = c.nx;
   g.ny = c.ny;
   g.nz = c.nz;
-  const StencilCoef &k = f.coef64;
+  const StencilCoef &k = mg.levels[0].coef64;  // G_l = P^T G_{l-1} P keeps the fine weights
   const double w[kG1Families] = {k.xx_int, k.yy_int, k.zz_int, k.xy, k.xz, k.yz, k.xx_bdr, k.yy_bdr, k.zz_bdr,
                                  k.ridge2};
   for (int fm = 0; fm < kG1Families; ++fm) g.w[fm] = (float)w[fm];
   const int nf[3] = {f.nx, f.ny, f.nz}, nc[3] = {c.nx, c.ny, c.nz};
   double irow[3][G1_KINDS][5];
   for (int a = 0; a < 3; ++a) {
-    std::vector<double> t;
-    g1_tables_1d(nf[a], nc[a], t);
+    std::vector<double> &t = c.g1host[a];
+    if (f.g1)
+      g1_tables_coarsen(f.g1host[a], nf[a], nc[a], t);
+    else
+      g1_tables_1d(nf[a], nc[a], t);
     const int mid = nc[a] / 2;
     auto same = [&](int J) {
       for (int kind = 0; kind < G1_KINDS; ++kind)
@@ -946,7 +975,50 @@ int mg_build_g1(ls_fd_handle *h, MgHierarchy &mg, const MgLevel &f, MgLevel &c) 
           acc += w[fm] * irow[0][g1_kind(fm, 0)][dx] * irow[1][g1_kind(fm, 1)][dy] * irow[2][g1_kind(fm, 2)][m + 2];
         g.c[m][dy][dx] = (float)acc;
       }
+  // face stencils: one axis in its band (rows differ), the other two interior
+  {
+    std::vector<float> fcv((size_t)3 * kG1MaxBand * 125, 0.f);
+    for (int a = 0; a < 3; ++a)
+      for (int row = 0; row < kG1MaxBand; ++row) {
+        const int half = kG1MaxBand / 2;
+        const int idx = row < half ? row : nc[a] - 1 - (row - half);
+        const bool band = row < half ? (idx < g.lo[a] && g.lo[a] <= half) : (idx > g.hi[a] && nc[a] - 1 - g.hi[a] <= half);
+        if (!band || idx < 0 || idx >= nc[a]) continue;
+        const std::vector<double> &t = c.g1host[a];
+        for (int o = 0; o < 125; ++o) {
+          const int d[3] = {o % 5, (o / 5) % 5, o / 25};  // dx, dy, dz (+2)
+          double acc = 0.0;
+          for (int fm = 0; fm < kG1Families; ++fm) {
+            double prod = w[fm];
+            for (int b = 0; b < 3; ++b) {
+              const int kind = g1_kind(fm, b);
+              prod *= b == a ? t[((size_t)kind * nc[a] + idx) * 5 + d[b]] : irow[b][kind][d[b]];
+            }
+            acc += prod;
+          }
+          fcv[((size_t)a * kG1MaxBand + row) * 125 + o] = (float)acc;
+        }
+      }
+    float *dfc = nullptr;
+    LS_TRY(mg_alloc(mg, &dfc, fcv.size()));
+    LS_CUDA_TRY(cudaMemcpyAsync(dfc, fcv.data(), fcv.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    g.face_coef = dfc;
+  }
+  // small levels: every node's explicit stencil, one node-per-thread kernel
+  g.shell_coef = nullptr;
+  if (c.n <= kG1ExplicitMax) {
+    for (int a = 0; a < 3; ++a) {
+      g.lo[a] = 1;
+      g.hi[a] = 0;
+    }
+    float *coef = nullptr;
+    LS_TRY(mg_alloc(mg, &coef, (size_t)125 * c.n));
+    g1_coef_kernel<<<grid_for(h, c.n), kBlock, 0, h->stream>>>(g, coef);
+    ++h->launches;
+    g.shell_coef = coef;
+  }
   LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  LS_CUDA_TRY(cudaGetLastError());
   c.g1 = true;
   return LS_OK;
 }
@@ -1005,7 +1077,7 @@ int mg_build(ls_fd_handle *h, int deg) {
     c.n = (int64_t)c.nx * c.ny * c.nz;
     c.coef64 = coarsen_coef(f.coef64, c.nx, c.ny, c.nz);
     c.coef = coef_as<float>(c.coef64);
-    if (mg.levels.size() == 1) LS_TRY(mg_build_g1(h, mg, f, c));
+    LS_TRY(mg_build_g1(h, mg, f, c));
     if (rows.nrows > 0) rows = galerkin_rows(rows, f.nx, f.ny, c.nx, c.ny);
     std::vector<int64_t> touched;
     std::vector<double> ddiag;
@@ -1953,7 +2025,13 @@ extern "C" int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_
     ec.c1 = 0.5f;
     ec.c2 = 1e-3f;
     LS_TRY(timed([&] { mg_apply<EPI_CHEB>(h, lv, lv.d0, ec, nullptr, st); }, &o[2]));
-    if (!lv.g1 && lv.n > kPointMaxNodes && apply_split(lv.nx, lv.ny, lv.nz)) {
+    if (lv.g1) {
+      const DataView<float> dv = mg_view(lv);
+      LS_TRY(timed([&] { h->launches += launch_g1<EPI_CHEB>(lv.g1op, lv.d0, dv, ec, nullptr, h->red_blocks / 8, st, 1); },
+                   &o[8]));
+      LS_TRY(timed([&] { h->launches += launch_g1<EPI_CHEB>(lv.g1op, lv.d0, dv, ec, nullptr, h->red_blocks / 8, st, 2); },
+                   &o[9]));
+    } else if (lv.n > kPointMaxNodes && apply_split(lv.nx, lv.ny, lv.nz)) {
       const DataView<float> dv = mg_view(lv);
       LS_TRY(timed([&] {
         if (dv.k27)
