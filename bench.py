@@ -411,6 +411,119 @@ def reference_arm(args, rank, world):
     }
 
 
+# ---------------------------------------------------------------------------
+# secondary workloads (their own JSON line; not the headline metric)
+# ---------------------------------------------------------------------------
+def ensemble_models(count=256, seed=0):
+    """Ensemble of independent layered-field models: n in {32,48,64,80,96}^3
+    nodes, 500-5000 values, 100-1000 normals, thickness scale s ~ U[0.5, 2]
+    (f = z/s + ...), normal noise sigma 0.05."""
+    import loopstructural_gb300 as L
+
+    rng = np.random.default_rng(seed)
+    models = []
+    for _ in range(count):
+        n = int(rng.choice([32, 48, 64, 80, 96]))
+        s = rng.uniform(0.5, 2.0)
+        nv, nn = int(rng.integers(500, 5001)), int(rng.integers(100, 1001))
+        vp = rng.uniform(0, 1, size=(nv, 3))
+        val = np.column_stack([vp, vp[:, 2] / s + 0.1 * np.sin(2 * np.pi * vp[:, 0]), np.ones(nv)])
+        npnt = rng.uniform(0, 1, size=(nn, 3))
+        g = np.column_stack([0.2 * np.pi * np.cos(2 * np.pi * npnt[:, 0]), np.zeros(nn), np.full(nn, 1.0 / s)])
+        g /= np.linalg.norm(g, axis=1)[:, None]
+        g += rng.normal(0, 0.05, size=g.shape)
+        cells = np.array([n - 1] * 3)
+        models.append({"grid": L.StructuredGrid(origin=np.zeros(3), nsteps=cells, step_vector=1.0 / cells),
+                       "value": val, "normal": np.column_stack([npnt, g, np.ones(nn)]),
+                       "setup": {"regularisation": 0.1, "cpw": 1.0, "npw": 1.0}})
+    return models
+
+
+def ensemble_arm(args):
+    import torch
+
+    import loopstructural_gb300 as L
+    from loopstructural_gb300.ensemble import FdEnsemble
+
+    L.build()
+    models = ensemble_models(args.models)
+    kw = {"rtol": args.rtol, "atol": 0.0, "precision": "mixed"}
+    ens = FdEnsemble(models[:8])
+    ens.solve(concurrency=args.concurrency, solver_kwargs=kw)  # warm-up (module load, graphs)
+    ens.close()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ens = FdEnsemble(models)
+    t1 = time.perf_counter()
+    stats = ens.solve(concurrency=args.concurrency, solver_kwargs=kw)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    dof = sum(int(np.prod(m["grid"].nsteps)) for m in models)
+    out = {"metric": "ensemble FD models solved per second (setup + batched mixed multigrid solve)",
+           "impl": "gb300", "value": round(len(models) / (t2 - t0), 2), "unit": "models/s", "n_gpus": 1,
+           "higher_is_better": True, "data": "synthetic (seeded layered fields, per-model thickness scale)",
+           "config": {"workload": "%d models, n in {32,48,64,80,96}^3, 500-5000 values, 100-1000 normals, "
+                                  "rtol %g, %d concurrent solves" % (len(models), args.rtol, args.concurrency),
+                      "total_dof": dof},
+           "setup_s": round(t1 - t0, 3), "solve_s": round(t2 - t1, 3),
+           "iterations_mean": float(np.mean([s["iterations"] for s in stats])),
+           "all_converged": all(s["status"] == 0 for s in stats)}
+    ens.close()
+    return out
+
+
+def adjoint_arm(args):
+    """128^3 FD, 5,000 values + 1,000 normals; loss = mean (u(q) - f(q))^2 over
+    10,000 held-out points; gradient w.r.t. the values by the adjoint, checked
+    by central differences on 64 random components."""
+    import torch
+
+    import loopstructural_gb300 as L
+    from loopstructural_gb300.adjoint import ValueFieldAdjoint
+
+    L.build()
+    cells, val, nrm = make_workload(n_nodes=128, n_value=5000, n_normal=1000, sigma=NORMAL_SIGMA)
+    grid = L.StructuredGrid(origin=np.zeros(3), nsteps=cells, step_vector=1.0 / cells)
+    interp = L.FiniteDifferenceInterpolator(grid)
+    interp.set_value_constraints(val)
+    interp.set_normal_constraints(nrm)
+    interp.setup_interpolator(regularisation=REGULARISATION, cpw=1.0, npw=1.0)
+    q = np.random.default_rng(7).uniform(0, 1, size=(10_000, 3))
+    f = ValueFieldAdjoint(interp, q, precision="mixed", rtol=1e-13)
+    t = torch.tensor(field(q), device="cuda", dtype=torch.float64)
+    v0 = torch.tensor(val[:, 3], device="cuda", dtype=torch.float64)
+    v = v0.clone().requires_grad_(True)
+    ((f(v) - t) ** 2).mean().backward()  # warm-up
+    v = v0.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    loss = ((f(v) - t) ** 2).mean()
+    loss.backward()
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    grad = v.grad.clone()
+    rng = np.random.default_rng(11)
+    h = 1e-3  # the loss is quadratic in v: central differences are exact for any h
+    errs = []
+    for i in rng.choice(val.shape[0], size=64, replace=False):
+        e = torch.zeros_like(v0)
+        e[i] = h
+        lp = float(((f.solve_field(v0 + e)[1] - t) ** 2).mean())
+        lm = float(((f.solve_field(v0 - e)[1] - t) ** 2).mean())
+        errs.append(abs((lp - lm) / (2 * h) - float(grad[i])))
+    scale = float(grad.abs().max())
+    f.close()
+    return {"metric": "adjoint gradient of a field misfit w.r.t. value constraints (forward + adjoint solve)",
+            "impl": "gb300", "value": round(t_grad, 4), "unit": "s", "higher_is_better": False,
+            "data": "synthetic (seeded faulted layered field)",
+            "config": {"workload": "FD 128^3, 5000 values + 1000 normals, loss over 10000 held-out points, "
+                                   "mixed multigrid solves to rtol 1e-13"},
+            "fd_check": {"components": 64, "step": h, "max_abs_error": max(errs),
+                         "max_rel_error": max(errs) / scale, "grad_max": scale},
+            "solves": {k: {"iterations": int(st["iterations"]), "device_ms": st["device_ms"]}
+                       for k, st in f.last_stats.items()}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -424,9 +537,18 @@ def main():
                     help="profiling runs: no nvidia-smi clock sampler child process")
     ap.add_argument("--skip-legs", action="store_true",
                     help="profiling runs: skip the FP64 leg, the e2e leg and the CPU baseline")
+    ap.add_argument("--workload", default="headline", choices=["headline", "ensemble", "adjoint"],
+                    help="secondary workloads print their own line (ensembles, adjoint gradient)")
+    ap.add_argument("--models", type=int, default=256)
+    ap.add_argument("--concurrency", type=int, default=16)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    if args.workload != "headline":
+        out = ensemble_arm(args) if args.workload == "ensemble" else adjoint_arm(args)
+        if rank == 0:
+            print(json.dumps(out))
+        return
     if args.impl == "reference":
         out = reference_arm(args, rank, world)
     else:
