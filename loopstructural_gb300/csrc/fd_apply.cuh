@@ -206,8 +206,12 @@ __device__ __forceinline__ T shell_node(const CoefT<T> &c, const PR &pr, int i, 
 }
 
 // Output planes per block (TZ; the block stages TZ + 4 planes of 432 nodes):
-// 16 or 4 in FP32 (34.6 / 13.8 KB of shared memory; 4 on grids too small to
-// fill the GPU with 16-plane tiles), 8 in FP64 (41.5 KB).
+// 8 or 4 in FP32 (20.8 / 13.8 KB of shared memory; 4 on grids too small to
+// fill the GPU with 8-plane tiles), 8 in FP64 (41.5 KB).  Deeper FP32 tiles
+// stage fewer halo planes but their fully unrolled plane loop outgrows the
+// instruction cache and spills under the 4-blocks-per-SM register budget
+// (measured: 16-plane tiles 95 us, 8-plane tiles 80 us per Chebyshev apply
+// at 200^3).
 template <typename T, int TZ_>
 struct Tile {
   static constexpr int TZ = TZ_;
@@ -463,9 +467,9 @@ inline void launch_tiles(const CoefT<T> &c, const T *p, const DataView<T> &dv, c
     fd_apply_kernel<T, EPI, MODE, K27, 8><<<apply_grid<T, 8>(c.nx, c.ny, c.nz, MODE), blk, 0, st>>>(
         c, p, dv, e, done, partials, ticket, dot);
   } else {
-    const dim3 g16 = apply_grid<T, 16>(c.nx, c.ny, c.nz, MODE);
-    if ((int64_t)g16.x * g16.y * g16.z >= 4 * (int64_t)sms) {
-      fd_apply_kernel<T, EPI, MODE, K27, 16><<<g16, blk, 0, st>>>(c, p, dv, e, done, partials, ticket, dot);
+    const dim3 g8 = apply_grid<T, 8>(c.nx, c.ny, c.nz, MODE);
+    if ((int64_t)g8.x * g8.y * g8.z >= 4 * (int64_t)sms) {
+      fd_apply_kernel<T, EPI, MODE, K27, 8><<<g8, blk, 0, st>>>(c, p, dv, e, done, partials, ticket, dot);
     } else {
       fd_apply_kernel<T, EPI, MODE, K27, 4><<<apply_grid<T, 4>(c.nx, c.ny, c.nz, MODE), blk, 0, st>>>(
           c, p, dv, e, done, partials, ticket, dot);
