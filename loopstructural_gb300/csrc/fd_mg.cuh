@@ -53,6 +53,8 @@ struct MgLevel {
   uint32_t *kmask = nullptr;
   int32_t *krank = nullptr;
   float *k27 = nullptr;
+  std::vector<float> k27host;      // host copy ([27][knt]) and the nodes, for the coarsest dense matrix
+  std::vector<int64_t> k27nodes;
   float *dinv = nullptr;
   // Galerkin regularisation operator (first coarse level)
   bool g1 = false;

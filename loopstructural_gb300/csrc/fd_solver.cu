@@ -522,7 +522,11 @@ int mg_upload_k27(ls_fd_handle *h, MgLevel &lv, const HostRows &rows, HostRows &
   diag_out.clear();
   lv.knt = 0;
   const int64_t nxy = (int64_t)lv.nx * lv.ny;
-  std::vector<std::pair<int64_t, double>> trip;  // (node * 27 + o, value)
+  // pass 1: classify the rows; mark the nodes of the cell rows
+  std::vector<int32_t> slot(lv.n, -1);
+  std::vector<int64_t> ccol;  // 8 per cell row (-1 padding)
+  std::vector<double> cval;   // w^2-free coefficients, 8 per cell row
+  std::vector<double> cw2;
   for (int64_t r = 0; r < rows.nrows; ++r) {
     int64_t cols[8];
     double av[8];
@@ -552,37 +556,46 @@ int mg_upload_k27(ls_fd_handle *h, MgLevel &lv, const HostRows &rows, HostRows &
       ++rest.nrows;
       continue;
     }
-    const double w2 = rows.w2[r];
-    for (int u = 0; u < m; ++u)
-      for (int v = 0; v < m; ++v) {
-        const int dx = (int)(cols[v] % lv.nx) - (int)(cols[u] % lv.nx);
-        const int dy = (int)((cols[v] / lv.nx) % lv.ny) - (int)((cols[u] / lv.nx) % lv.ny);
-        const int dz = (int)(cols[v] / nxy) - (int)(cols[u] / nxy);
-        const int o = 9 * (dz + 1) + 3 * (dy + 1) + (dx + 1);
-        trip.emplace_back(cols[u] * 27 + o, w2 * av[u] * av[v]);
-      }
-  }
-  if (trip.empty()) return LS_OK;
-  std::stable_sort(trip.begin(), trip.end(), [](const std::pair<int64_t, double> &x, const std::pair<int64_t, double> &y) {
-    return x.first < y.first;
-  });
-  std::vector<int64_t> nodes;
-  std::vector<double> kv;  // 27 per node
-  for (size_t t = 0; t < trip.size(); ++t) {
-    const int64_t node = trip[t].first / 27;
-    const int o = (int)(trip[t].first % 27);
-    if (nodes.empty() || nodes.back() != node) {
-      nodes.push_back(node);
-      kv.resize(kv.size() + 27, 0.0);
+    for (int u = 0; u < 8; ++u) {
+      ccol.push_back(u < m ? cols[u] : -1);
+      cval.push_back(u < m ? av[u] : 0.0);
+      if (u < m) slot[cols[u]] = 0;
     }
-    kv[(nodes.size() - 1) * 27 + o] += trip[t].second;
+    cw2.push_back(rows.w2[r]);
   }
+  if (cw2.empty()) return LS_OK;
+  // slots in ascending node order
+  std::vector<int64_t> nodes;
+  for (int64_t g = 0; g < lv.n; ++g)
+    if (slot[g] == 0) {
+      slot[g] = (int32_t)nodes.size();
+      nodes.push_back(g);
+    }
+  // pass 2: sum w^2 a_u a_v per (node, offset), rows in order
   const int64_t nt = (int64_t)nodes.size();
+  std::vector<double> kv((size_t)27 * nt, 0.0);
+  for (size_t r = 0; r < cw2.size(); ++r) {
+    const int64_t *cols = &ccol[8 * r];
+    const double *av = &cval[8 * r];
+    for (int u = 0; u < 8; ++u) {
+      if (cols[u] < 0) continue;
+      const int ux = (int)(cols[u] % lv.nx), uy = (int)((cols[u] / lv.nx) % lv.ny), uz = (int)(cols[u] / nxy);
+      double *row = &kv[(size_t)slot[cols[u]] * 27];
+      for (int v = 0; v < 8; ++v) {
+        if (cols[v] < 0) continue;
+        const int dx = (int)(cols[v] % lv.nx) - ux, dy = (int)((cols[v] / lv.nx) % lv.ny) - uy,
+                  dz = (int)(cols[v] / nxy) - uz;
+        row[9 * (dz + 1) + 3 * (dy + 1) + (dx + 1)] += cw2[r] * av[u] * av[v];
+      }
+    }
+  }
   std::vector<float> k((size_t)27 * nt);
   for (int64_t t = 0; t < nt; ++t) {
     for (int o = 0; o < 27; ++o) k[(size_t)o * nt + t] = (float)kv[(size_t)t * 27 + o];
     diag_out.emplace_back(nodes[t], kv[(size_t)t * 27 + 13]);
   }
+  lv.k27host = k;
+  lv.k27nodes = nodes;
   std::vector<uint32_t> mask;
   std::vector<int32_t> wr;
   node_mask(lv.n, nodes, mask, wr);
@@ -746,18 +759,37 @@ int mg_coarse_inverse(ls_fd_handle *h, MgLevel &lv) {
   MgHierarchy &mg = h->mg;
   cudaStream_t st = h->stream;
   const int nc = (int)lv.n;
-  std::vector<double> A((size_t)nc * nc);
-  std::vector<float> col(nc);
-  const float one = 1.0f;
-  for (int j = 0; j < nc; ++j) {
-    LS_CUDA_TRY(cudaMemsetAsync(lv.d0, 0, nc * sizeof(float), st));
-    LS_CUDA_TRY(cudaMemcpyAsync(lv.d0 + j, &one, sizeof(float), cudaMemcpyHostToDevice, st));
-    EpiArgs<float> e{};
-    e.q = lv.d1;
-    mg_apply<EPI_STORE>(h, lv, lv.d0, e, nullptr, st);
-    LS_CUDA_TRY(cudaMemcpyAsync(col.data(), lv.d1, nc * sizeof(float), cudaMemcpyDeviceToHost, st));
-    LS_CUDA_TRY(cudaStreamSynchronize(st));
-    for (int i = 0; i < nc; ++i) A[(size_t)i * nc + j] = col[i];
+  std::vector<double> A((size_t)nc * nc, 0.0);
+  if (lv.g1 && lv.g1op.shell_coef && lv.nrows == 0) {
+    // the level's explicit stencils (every node of a small Galerkin level) and
+    // its 27-point data term: the matrix without a single operator apply
+    std::vector<float> coef((size_t)125 * nc);
+    LS_CUDA_TRY(cudaMemcpy(coef.data(), lv.g1op.shell_coef, coef.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    const int nx = lv.nx, ny = lv.ny, nz = lv.nz;
+    auto put = [&](int i, int dx, int dy, int dz, double v) {
+      const int x = i % nx, y = (i / nx) % ny, z = i / (nx * ny);
+      if (x + dx < 0 || x + dx >= nx || y + dy < 0 || y + dy >= ny || z + dz < 0 || z + dz >= nz) return;
+      A[(size_t)i * nc + (i + dz * nx * ny + dy * nx + dx)] += v;
+    };
+    for (int i = 0; i < nc; ++i)
+      for (int o = 0; o < 125; ++o) put(i, o % 5 - 2, (o / 5) % 5 - 2, o / 25 - 2, coef[(size_t)o * nc + i]);
+    const int64_t nt = (int64_t)lv.k27nodes.size();
+    for (int64_t t = 0; t < nt; ++t)
+      for (int o = 0; o < 27; ++o)
+        put((int)lv.k27nodes[t], o % 3 - 1, (o / 3) % 3 - 1, o / 9 - 1, lv.k27host[(size_t)o * nt + t]);
+  } else {
+    std::vector<float> col(nc);
+    const float one = 1.0f;
+    for (int j = 0; j < nc; ++j) {
+      LS_CUDA_TRY(cudaMemsetAsync(lv.d0, 0, nc * sizeof(float), st));
+      LS_CUDA_TRY(cudaMemcpyAsync(lv.d0 + j, &one, sizeof(float), cudaMemcpyHostToDevice, st));
+      EpiArgs<float> e{};
+      e.q = lv.d1;
+      mg_apply<EPI_STORE>(h, lv, lv.d0, e, nullptr, st);
+      LS_CUDA_TRY(cudaMemcpyAsync(col.data(), lv.d1, nc * sizeof(float), cudaMemcpyDeviceToHost, st));
+      LS_CUDA_TRY(cudaStreamSynchronize(st));
+      for (int i = 0; i < nc; ++i) A[(size_t)i * nc + j] = col[i];
+    }
   }
   // symmetrise (the FP32 apply is symmetric up to rounding)
   for (int i = 0; i < nc; ++i)
@@ -1023,7 +1055,9 @@ int mg_build_g1(ls_fd_handle *h, MgHierarchy &mg, const MgLevel &f, MgLevel &c) 
   return LS_OK;
 }
 
-constexpr int64_t kMgMaxCoarse = 1000;  // largest dense coarsest level
+constexpr int64_t kMgMaxCoarse = 1000;       // largest dense coarsest level
+constexpr int64_t kMgMaxCoarseSmall = 200;   // ... for grids below kMgSmallGrid nodes
+constexpr int64_t kMgSmallGrid = 2000000;
 
 // Builds the hierarchy; returns LS_OK with mg.built == false when the grid
 // cannot be coarsened to a dense-solvable size (the solve then uses Jacobi).
@@ -1068,7 +1102,10 @@ int mg_build(ls_fd_handle *h, int deg) {
   rows.w2 = h->h_w2;
   for (;;) {
     const MgLevel &f = mg.levels.back();
-    if (f.n <= kMgMaxCoarse) break;
+    // the dense coarsest solve costs O(n^3) to set up: grids too small for an
+    // extra level's per-iteration cost to matter coarsen further
+    const int64_t coarsest = h->n < kMgSmallGrid ? kMgMaxCoarseSmall : kMgMaxCoarse;
+    if (f.n <= coarsest) break;
     if (f.nx < 5 || f.ny < 5 || f.nz < 5) break;
     MgLevel c;
     c.nx = f.nx / 2 + 1;

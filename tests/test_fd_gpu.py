@@ -366,7 +366,7 @@ def test_coarse_levels_are_galerkin(cells):
         level += 1
         nodes, _ = fd.mg_apply_level(system, level)
         assert nodes == G.shape[0]
-        if nodes <= 1000:  # the coarsest level is solved densely, not applied
+        if nodes <= 200:  # the coarsest level (of grids this small) is solved densely, not applied
             break
         x = np.random.default_rng(level).normal(size=nodes)
         _, y = fd.mg_apply_level(system, level, torch.from_numpy(x))
