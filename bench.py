@@ -524,6 +524,27 @@ def adjoint_arm(args):
                        for k, st in f.last_stats.items()}}
 
 
+def mgprofile_arm(args):
+    """Per-level device times of the multigrid V-cycle parts on the headline
+    system (the profiling entry used for kernel captures)."""
+    import loopstructural_gb300 as L
+    from loopstructural_gb300 import fd
+
+    L.build()
+    cells, val, nrm = make_workload()
+    grid = L.StructuredGrid(origin=np.zeros(3), nsteps=cells, step_vector=1.0 / cells)
+    interp = L.FiniteDifferenceInterpolator(grid)
+    interp.set_value_constraints(val)
+    interp.set_normal_constraints(nrm)
+    interp.setup_interpolator(regularisation=REGULARISATION, cpw=1.0, npw=1.0)
+    system = interp._build_system()
+    levels = fd.profile_mg(system, reps=args.steps)
+    system.close()
+    return {"metric": "multigrid V-cycle part times per level (us)", "impl": "gb300",
+            "levels": [{k: (round(v * 1e3, 1) if k.endswith("_ms") else int(v)) for k, v in lv.items()}
+                       for lv in levels]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -537,15 +558,17 @@ def main():
                     help="profiling runs: no nvidia-smi clock sampler child process")
     ap.add_argument("--skip-legs", action="store_true",
                     help="profiling runs: skip the FP64 leg, the e2e leg and the CPU baseline")
-    ap.add_argument("--workload", default="headline", choices=["headline", "ensemble", "adjoint"],
-                    help="secondary workloads print their own line (ensembles, adjoint gradient)")
+    ap.add_argument("--workload", default="headline", choices=["headline", "ensemble", "adjoint", "mgprofile"],
+                    help="secondary workloads print their own line (ensembles, adjoint gradient, per-level "
+                         "multigrid kernel times)")
     ap.add_argument("--models", type=int, default=256)
     ap.add_argument("--concurrency", type=int, default=16)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.workload != "headline":
-        out = ensemble_arm(args) if args.workload == "ensemble" else adjoint_arm(args)
+        arms = {"ensemble": ensemble_arm, "adjoint": adjoint_arm, "mgprofile": mgprofile_arm}
+        out = arms[args.workload](args)
         if rank == 0:
             print(json.dumps(out))
         return

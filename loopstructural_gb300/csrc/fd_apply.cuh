@@ -319,8 +319,8 @@ __global__ void __launch_bounds__(kAX * kAY, MODE == MODE_DEEP ? 4 : 1)
     EpiIn<T> pre[TZ];
 #pragma unroll
     for (int hz = 0; hz < SZ; ++hz) {
-      // epilogue operands of output plane hz - 2, two planes ahead of their use
-      if (hz >= 2 && hz - 2 < TZ && z0 + hz - 2 < ze) pre[hz - 2] = epi_load<T, EPI>(e, (z0 + hz - 2) * sxy + gcol);
+      // epilogue operands of output plane hz - 1, three planes ahead of their use
+      if (hz >= 1 && hz - 1 < TZ && z0 + hz - 1 < ze) pre[hz - 1] = epi_load<T, EPI>(e, (z0 + hz - 1) * sxy + gcol);
       const T(&pl)[kHY][kHX] = sm[hz];
       const T p0 = pl[hy][hx];
       P[hz] = p0;
