@@ -319,9 +319,9 @@ inline int launch_g1_k(const G1Op &g, const float *p, const DataView<float> &dv,
   const int bx = g.hi[0] - g.lo[0] + 1, by = g.hi[1] - g.lo[1] + 1, bz = g.hi[2] - g.lo[2] + 1;
   if ((parts & 1) && bx > 0 && by > 0 && bz > 0) {
     const dim3 blk(kAX, kAY);
-    const dim3 g16((bx + kAX - 1) / kAX, (by + kAY - 1) / kAY, (bz + 15) / 16);
-    if ((int64_t)g16.x * g16.y * g16.z >= 4 * (int64_t)sms) {
-      g1_apply_kernel<EPI, K27, 16><<<g16, blk, 0, st>>>(g, p, dv, e, done);
+    const dim3 g8((bx + kAX - 1) / kAX, (by + kAY - 1) / kAY, (bz + 7) / 8);
+    if ((int64_t)g8.x * g8.y * g8.z >= 4 * (int64_t)sms) {
+      g1_apply_kernel<EPI, K27, 8><<<g8, blk, 0, st>>>(g, p, dv, e, done);
     } else {
       const dim3 g4((bx + kAX - 1) / kAX, (by + kAY - 1) / kAY, (bz + 3) / 4);
       g1_apply_kernel<EPI, K27, 4><<<g4, blk, 0, st>>>(g, p, dv, e, done);
