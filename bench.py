@@ -139,6 +139,33 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
+def max_over_ranks(value, world, device="cuda"):
+    """The largest of the ranks' values (the job's time for a time-like metric)."""
+    if world <= 1:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(value, world, device="cuda"):
+    if world <= 1:
+        return value
+    import torch
+
+    t = torch.tensor([float(value)], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+    return float(t.item())
+
+
+def shard(items, rank, world):
+    """Round-robin partition of independent work units (ensemble models) over
+    ranks: no data-path collective, weak scaling by unit."""
+    return list(items)[rank::world]
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -222,11 +249,7 @@ def gpu_arm(args, rank, world):
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_pop()
     barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, "cuda")
     iters = int(np.mean([s["iterations"] for s in stats]))
     launches = int(sum(s["kernel_launches"] for s in stats))
     out_solve_ms = float(np.mean([s["device_ms"] for s in stats]))
@@ -458,14 +481,15 @@ def ensemble_models(count=256, seed=0):
     return models
 
 
-def ensemble_arm(args):
+def ensemble_arm(args, rank=0, world=1):
     import torch
 
     import loopstructural_gb300 as L
     from loopstructural_gb300.ensemble import FdEnsemble
 
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     L.build()
-    models = ensemble_models(args.models)
+    models = shard(ensemble_models(args.models), rank, world)
     kw = {"rtol": args.rtol, "atol": 0.0, "precision": "mixed"}
     ens = FdEnsemble(models[:8])
     ens.solve(concurrency=args.concurrency, solver_kwargs=kw)  # warm-up (module load, graphs)
@@ -477,12 +501,17 @@ def ensemble_arm(args):
     stats = ens.solve(concurrency=args.concurrency, solver_kwargs=kw)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    dof = sum(int(np.prod(m["grid"].nsteps)) for m in models)
+    if world > 1:
+        torch.distributed.barrier()
+    total_models = int(sum_over_ranks(len(models), world))
+    t_job = max_over_ranks(t2 - t0, world)
+    dof = int(sum_over_ranks(sum(int(np.prod(m["grid"].nsteps)) for m in models), world))
     out = {"metric": "ensemble FD models solved per second (setup + batched mixed multigrid solve)",
-           "impl": "gb300", "value": round(len(models) / (t2 - t0), 2), "unit": "models/s", "n_gpus": 1,
+           "impl": "gb300", "value": round(total_models / t_job, 2), "unit": "models/s", "n_gpus": world,
+           "scaling": "weak (models sharded over ranks, no data-path collective)",
            "higher_is_better": True, "data": "synthetic (seeded layered fields, per-model thickness scale)",
            "config": {"workload": "%d models, n in {32,48,64,80,96}^3, 500-5000 values, 100-1000 normals, "
-                                  "rtol %g, %d concurrent solves" % (len(models), args.rtol, args.concurrency),
+                                  "rtol %g, %d concurrent solves per GPU" % (total_models, args.rtol, args.concurrency),
                       "total_dof": dof},
            "setup_s": round(t1 - t0, 3), "solve_s": round(t2 - t1, 3),
            "iterations_mean": float(np.mean([s["iterations"] for s in stats])),
@@ -586,8 +615,15 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.workload != "headline":
-        arms = {"ensemble": ensemble_arm, "adjoint": adjoint_arm, "mgprofile": mgprofile_arm}
-        out = arms[args.workload](args)
+        if args.workload == "ensemble":
+            if world > 1:
+                import torch
+
+                torch.distributed.init_process_group("nccl")
+            out = ensemble_arm(args, rank, world)
+        else:
+            arms = {"adjoint": adjoint_arm, "mgprofile": mgprofile_arm}
+            out = arms[args.workload](args) if rank == 0 else None
         if rank == 0:
             print(json.dumps(out))
         return
