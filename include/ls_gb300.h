@@ -201,6 +201,7 @@ typedef struct ls_solve_opts {
   double reliable_delta;  /* mixed: refresh the FP64 residual once ||S r|| fell by this factor (<=0: 0.1) */
   int32_t check_every;    /* iterations per device batch between host checks (<=0: 64) */
   int32_t preconditioner; /* ls_preconditioner */
+  int32_t mg_degree;      /* multigrid: Chebyshev smoothing steps before and after the coarse correction (<=0: 3) */
 } ls_solve_opts;
 
 typedef struct ls_solve_stats {

@@ -79,7 +79,7 @@ class SolveOpts(C.Structure):
     _fields_ = [
         ("precision", C.c_int32), ("use_x0", C.c_int32), ("atol", C.c_double), ("rtol", C.c_double),
         ("maxiter", C.c_int64), ("reliable_delta", C.c_double), ("check_every", C.c_int32),
-        ("preconditioner", C.c_int32),
+        ("preconditioner", C.c_int32), ("mg_degree", C.c_int32),
     ]
 
 

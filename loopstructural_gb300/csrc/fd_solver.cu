@@ -1055,6 +1055,28 @@ int mg_build_g1(ls_fd_handle *h, MgHierarchy &mg, const MgLevel &f, MgLevel &c) 
   return LS_OK;
 }
 
+constexpr int kMgDefaultDegree = 3;
+
+// Chebyshev step coefficients of degree `deg` on [lmax/20, 1.05 lmax] (every level but the coarsest)
+void mg_set_degree(MgHierarchy &mg, int deg) {
+  mg.deg = deg;
+  for (size_t l = 0; l + 1 < mg.levels.size(); ++l) {
+    MgLevel &lv = mg.levels[l];
+    const double lmax = 1.05 * lv.lmax, lmin = lv.lmax / 20.0;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    lv.inv_theta = (float)(1.0 / theta);
+    lv.c1.assign(deg, 0.f);
+    lv.c2.assign(deg, 0.f);
+    for (int k = 0; k < deg; ++k) {
+      const double rn = 1.0 / (2.0 * sigma - rho);
+      lv.c1[k] = (float)(rn * rho);
+      lv.c2[k] = (float)(2.0 * rn / delta);
+      rho = rn;
+    }
+  }
+}
+
 constexpr int64_t kMgMaxCoarse = 1000;       // largest dense coarsest level
 constexpr int64_t kMgMaxCoarseSmall = 200;   // ... for grids below kMgSmallGrid nodes
 constexpr int64_t kMgSmallGrid = 2000000;
@@ -1152,20 +1174,9 @@ int mg_build(ls_fd_handle *h, int deg) {
     MgLevel &lv = mg.levels[l];
     float est = 1.0f;
     LS_TRY(mg_lambda_max(h, lv, &est));
-    const double lmax = 1.05 * est, lmin = est / 20.0;
-    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
-    double rho = 1.0 / sigma;
     lv.lmax = est;
-    lv.inv_theta = (float)(1.0 / theta);
-    lv.c1.resize(deg);
-    lv.c2.resize(deg);
-    for (int k = 0; k < deg; ++k) {
-      const double rn = 1.0 / (2.0 * sigma - rho);
-      lv.c1[k] = (float)(rn * rho);
-      lv.c2[k] = (float)(2.0 * rn / delta);
-      rho = rn;
-    }
   }
+  mg_set_degree(mg, deg);
   LS_TRY(mg_coarse_inverse(h, mg.levels.back()));
   mg.built = true;
   return LS_OK;
@@ -1751,7 +1762,7 @@ extern "C" int ls_fd_apply_f32(ls_fd_handle *h, const float *d_x, float *d_y, vo
 extern "C" int ls_fd_prepare(ls_fd_handle *h, const ls_solve_opts *opts) {
   LS_ARG_CHECK(h && opts, "NULL argument");
   if (opts->precision == LS_MIXED && opts->preconditioner == LS_PRECOND_MG && h->rhs_norm2 > 0.0)
-    LS_TRY(mg_build(h, 3));
+    LS_TRY(mg_build(h, opts->mg_degree > 0 ? opts->mg_degree : kMgDefaultDegree));
   return LS_OK;
 }
 
@@ -1776,8 +1787,14 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
 
   bool use_mg = false;
   if (opts->precision == LS_MIXED && opts->preconditioner == LS_PRECOND_MG && bnorm > 0.0) {
-    LS_TRY(mg_build(h, 3));
+    const int deg = opts->mg_degree > 0 ? opts->mg_degree : kMgDefaultDegree;
+    LS_TRY(mg_build(h, deg));
     use_mg = h->mg.built;
+    if (use_mg && h->mg.deg != deg) {  // another smoother degree: new coefficients, new graph
+      mg_set_degree(h->mg, deg);
+      if (h->gmg) cudaGraphExecDestroy(h->gmg);
+      h->gmg = nullptr;
+    }
   }
   LS_CUDA_TRY(cudaEventRecord(h->ev0, st));
   if (opts->use_x0)
@@ -1996,7 +2013,7 @@ extern "C" int ls_fd_mg_apply_level(ls_fd_handle *h, int level, const float *d_x
                                     void *stream) {
   LS_ARG_CHECK(h && h_nodes, "NULL argument");
   LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
-  LS_TRY(mg_build(h, 3));
+  LS_TRY(mg_build(h, kMgDefaultDegree));
   MgHierarchy &mg = h->mg;
   LS_ARG_CHECK(mg.built, "the grid does not coarsen");
   LS_ARG_CHECK(level >= 0 && level < (int)mg.levels.size(), "no such level");
@@ -2016,7 +2033,7 @@ extern "C" int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_
   LS_ARG_CHECK(h && out && levels && reps > 0 && max_levels > 0, "bad argument");
   LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
   *levels = 0;
-  LS_TRY(mg_build(h, 3));
+  LS_TRY(mg_build(h, kMgDefaultDegree));
   MgHierarchy &mg = h->mg;
   if (!mg.built) return LS_OK;
   cudaStream_t st = h->stream;

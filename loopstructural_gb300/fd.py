@@ -174,9 +174,10 @@ class FdSystem:
         return y
 
     def solve(self, x=None, atol=0.0, rtol=1e-5, maxiter=None, precision="mixed", reliable_delta=0.1,
-              check_every=64, preconditioner="mg"):
+              check_every=64, preconditioner="mg", mg_degree=0):
         """Returns (x device tensor, stats dict)."""
         x, o = self._prepare(x, atol, rtol, maxiter, precision, reliable_delta, check_every, preconditioner)
+        o.mg_degree = int(mg_degree)
         st = _lib.SolveStats()
         status = self.lib.ls_fd_solve(self.handle, C.byref(o), _lib.ptr(x), C.byref(st), _lib.stream_ptr())
         _lib.check(status, allow_positive=True)
