@@ -1,6 +1,7 @@
 // Batched solves of independent FD systems (model ensembles): host worker
-// threads each take the next handle and run its solve on the handle's own
-// stream, so up to `concurrency` solves overlap on the GPU.  The solves are
+// threads each take the next handle and run its setup, then (after every
+// setup is done) its solve on the handle's own stream, so up to `concurrency`
+// models overlap on the GPU.  The solves are
 // independent (per-handle workspaces, thread-local errors and graph capture),
 // so results equal those of the same solves run one after another.
 #include <algorithm>
@@ -18,33 +19,40 @@ extern "C" int ls_fd_solve_batched(ls_fd_handle *const *handles, const ls_solve_
   if (count == 0) return LS_OK;
   LS_ARG_CHECK(handles && opts && d_x && stats && statuses, "NULL argument");
   for (int64_t i = 0; i < count; ++i) LS_ARG_CHECK(handles[i] && d_x[i], "NULL handle or solution pointer");
-  // every allocation (multigrid hierarchies) happens here, one model after
-  // another, so that no allocator call overlaps another thread's graph capture
-  for (int64_t i = 0; i < count; ++i) {
-    cudaSetDevice(ls_fd_device(handles[i]));
-    const int st = ls_fd_prepare(handles[i], &opts[i]);
-    if (st < 0) {
-      const std::string msg = ls_last_error();
-      ls::set_error("model %lld: %s", (long long)i, msg.c_str());
-      return st;
-    }
-  }
   const int workers = (int)std::max<int64_t>(1, std::min<int64_t>(concurrency > 0 ? concurrency : 8, count));
-  std::atomic<int64_t> next{0};
   std::vector<std::string> errors(count);
-  auto work = [&]() {
-    for (;;) {
-      const int64_t i = next.fetch_add(1);
-      if (i >= count) break;
-      cudaSetDevice(ls_fd_device(handles[i]));
-      statuses[i] = ls_fd_solve(handles[i], &opts[i], d_x[i], &stats[i], nullptr);
-      if (statuses[i] < 0) errors[i] = ls_last_error();
-    }
+  // runs fn(i) for every model on `workers` threads, each on the model's device
+  auto parallel = [&](auto &&fn) {
+    std::atomic<int64_t> next{0};
+    auto work = [&]() {
+      for (;;) {
+        const int64_t i = next.fetch_add(1);
+        if (i >= count) break;
+        cudaSetDevice(ls_fd_device(handles[i]));
+        fn(i);
+      }
+    };
+    std::vector<std::thread> pool;
+    pool.reserve(workers);
+    for (int t = 0; t < workers; ++t) pool.emplace_back(work);
+    for (auto &t : pool) t.join();
   };
-  std::vector<std::thread> pool;
-  pool.reserve(workers);
-  for (int t = 0; t < workers; ++t) pool.emplace_back(work);
-  for (auto &t : pool) t.join();
+  // phase 1: every allocation (multigrid hierarchies) -- no graph is being
+  // captured yet, so allocator calls cannot disturb a capture
+  parallel([&](int64_t i) {
+    statuses[i] = ls_fd_prepare(handles[i], &opts[i]);
+    if (statuses[i] < 0) errors[i] = ls_last_error();
+  });
+  for (int64_t i = 0; i < count; ++i)
+    if (statuses[i] < 0) {
+      ls::set_error("model %lld: %s", (long long)i, errors[i].c_str());
+      return statuses[i];
+    }
+  // phase 2: the solves (graph captures and replays on per-model streams)
+  parallel([&](int64_t i) {
+    statuses[i] = ls_fd_solve(handles[i], &opts[i], d_x[i], &stats[i], nullptr);
+    if (statuses[i] < 0) errors[i] = ls_last_error();
+  });
   for (int64_t i = 0; i < count; ++i)
     if (statuses[i] < 0) {
       ls::set_error("model %lld: %s", (long long)i, errors[i].c_str());
