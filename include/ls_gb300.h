@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define LS_ABI_VERSION 1
+#define LS_ABI_VERSION 2
 
 typedef enum ls_status {
   LS_OK = 0,
@@ -69,7 +69,8 @@ typedef enum ls_row_kind {
   LS_ROWS_VALUE = 0,    /* FD:236-269 add_value_constraints: 1 row/point, w = weight*point_w */
   LS_ROWS_NORM = 1,     /* FD:403-476 add_norm_constraints: 3 rows/point (norm_0..2), w = weight/3*point_w */
   LS_ROWS_GRADIENT = 2, /* FD:342-401 add_gradient_constraints: 2 rows/point (strike, dip), w = weight */
-  LS_ROWS_TANGENT = 3   /* FD:478-539 add_gradient_orthogonal_constraints: 1 row/point, w = weight */
+  LS_ROWS_TANGENT = 3,  /* FD:478-539 add_gradient_orthogonal_constraints: 1 row/point, w = weight */
+  LS_ROWS_ORTHOGONAL = 4 /* FD:478-539 with a target: columns x y z vx vy vz b, 1 row/point, w = weight */
 } ls_row_kind;
 
 /* Point-constraint rows on a StructuredGrid.  Replaces the per-family
@@ -87,6 +88,19 @@ typedef enum ls_row_kind {
 int ls_fd_point_rows(const ls_grid3 *grid, int kind, const double *d_pts, int64_t npts, int64_t ld,
                      double weight, int64_t *d_idc, double *d_a, double *d_b, double *d_w,
                      int64_t *h_count, int32_t *h_nan, void *stream);
+
+/* Directional regularisation weights of FD:1207-1337
+ * minimise_directional_gradient_change(w, vector): for every interior node m
+ * (1 <= i, j, k <= n - 2) and family f in (dxx, dyy, dzz, dxy, dxz, dyz),
+ * rw = weight * c_f(v_m), c = (vx^2, vy^2, vz^2, 2 vx vy, 2 vx vz, 2 vy vz);
+ * a row with |rw| > 0 adds s_f^2 rw^2 to d_omega[f * dof + m] (s_f^2 = 1/6 for
+ * dxx..dzz, 1/4 for the cross families: the squared row normalisation of
+ * DI:361-366).  d_vec: dof x ld FP64 (vx, vy, vz first), the direction at
+ * every node in node order; d_omega (6 x dof) accumulates over calls (zero it
+ * first).  h_counts (6 int64, may be NULL): the rows of each family the
+ * reference would add (FD:1320-1335 drops the others). */
+int ls_fd_directional_weights(const ls_grid3 *grid, const double *d_vec, int64_t ld, double weight,
+                              double *d_omega, int64_t *h_counts, void *stream);
 
 /* Interface pair rows (FD:297-340 add_interface_constraints): row p is
  * [trilinear(i), -trilinear(j)] over 16 columns for d_pairs[p] = (i, j), both
@@ -136,6 +150,10 @@ typedef struct ls_fd_system {
   const double *d_a; /* normalised coefficients */
   const double *d_b; /* normalised right-hand side */
   const double *d_w; /* row weights (W = w^2) */
+  /* directional regularisation (FD:1207-1337), or NULL: 6 x dof FP64 weights,
+   * family-major (dxx, dyy, dzz, dxy, dxz, dyz), as accumulated by
+   * ls_fd_directional_weights; the handle keeps its own copy */
+  const double *d_dir;
 } ls_fd_system;
 
 typedef struct ls_fd_handle ls_fd_handle;
@@ -156,7 +174,7 @@ int ls_fd_apply_f32(ls_fd_handle *h, const float *d_x, float *d_y, void *stream)
  * (one FP64 value per data row plus reduction partials) in a static device
  * array of LS_NOALLOC_SCRATCH_DOUBLES doubles (~8.4 MB per GPU that loads the
  * library, held until the process exits).  Limits: sys->nrows <=
- * LS_NOALLOC_MAX_ROWS, else LS_ERR_ARG.  Computes d_y = N d_x (FP64) and, when
+ * LS_NOALLOC_MAX_ROWS and sys->d_dir == NULL, else LS_ERR_ARG.  Computes d_y = N d_x (FP64) and, when
  * h_xNx is not NULL, x.Nx (written to host memory after a stream sync).  The
  * first call on a device resolves the array's device address
  * (cudaGetSymbolAddress), so make that first call before any stream capture.
@@ -314,6 +332,12 @@ int ls_p1_face_count(const ls_grid3 *mesh, int64_t *h_faces);
  * the shared nodes (the normal's orientation); it does not change A^T W A. */
 int ls_p1_face_rows(const ls_grid3 *mesh, double weight, int64_t *d_pairs, int64_t *d_shared, int64_t *d_idc,
                     double *d_a, double *d_b, double *d_w, void *stream);
+
+/* Directional face rows (P1:172-178 -> P1:115-166 with `vector`): the rows of
+ * ls_p1_face_rows with the face normal replaced by d_vec[f] (F x 3 FP64, one
+ * direction per face in the same face order), normalised, b = 0, w = weight. */
+int ls_p1_face_rows_directional(const ls_grid3 *mesh, double weight, const double *d_vec, int64_t *d_idc,
+                                double *d_a, double *d_b, double *d_w, void *stream);
 
 /* Containing tetrahedron (-1 outside) and barycentric coordinates of points
  * (T:274-365: last containing tet of the 5 candidates wins; strict inside). */

@@ -10,6 +10,7 @@ from ._lib import ExtensionUnavailable, LsError
 from .constraints import ValidationError
 from .interpolators import FiniteDifferenceInterpolator
 from .p1 import P1Interpolator, PiecewiseLinearInterpolator
+from .regularisation import DirectionalRegularisation, RegularisationConfig
 from .supports import StructuredGrid, TetMesh
 
 __all__ = [
@@ -17,6 +18,8 @@ __all__ = [
     "P1Interpolator",
     "PiecewiseLinearInterpolator",
     "StructuredGrid",
+    "DirectionalRegularisation",
+    "RegularisationConfig",
     "TetMesh",
     "ValidationError",
     "ExtensionUnavailable",

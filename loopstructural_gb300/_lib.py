@@ -17,12 +17,15 @@ LS_NOT_CONVERGED = 1
 LS_NAN = 2
 LS_BREAKDOWN = 3
 LS_FP64 = 0
+ABI_VERSION = 2  # LS_ABI_VERSION of include/ls_gb300.h
 LS_MIXED = 1
 LS_PRECOND_JACOBI = 0
 LS_PRECOND_MG = 1
 NOALLOC_MAX_ROWS = 1048576
 
-ROWS_VALUE, ROWS_NORM, ROWS_GRADIENT, ROWS_TANGENT = 0, 1, 2, 3
+ROWS_VALUE, ROWS_NORM, ROWS_GRADIENT, ROWS_TANGENT, ROWS_ORTHOGONAL = 0, 1, 2, 3, 4
+# directional regularisation weight planes (ls_fd_directional_weights)
+DIRECTIONAL_FAMILIES = ("dxx", "dyy", "dzz", "dxy", "dxz", "dyz")
 REG_FAMILIES = (
     "dxy", "dyz", "dxz", "dxx", "dyy", "dzz",
     "dx_lower", "dx_upper", "dy_lower", "dy_upper", "dz_lower", "dz_upper",
@@ -31,12 +34,13 @@ REG_FAMILIES = (
 # every symbol include/ls_gb300.h declares
 EXPORTS = (
     "ls_last_error", "ls_abi_version",
-    "ls_fd_point_rows", "ls_fd_pair_rows", "ls_fd_reg_shape", "ls_fd_reg_rows",
+    "ls_fd_point_rows", "ls_fd_pair_rows", "ls_fd_reg_shape", "ls_fd_reg_rows", "ls_fd_directional_weights",
     "ls_fd_create", "ls_fd_destroy", "ls_fd_dof", "ls_fd_apply", "ls_fd_apply_f32", "ls_fd_apply_noalloc", "ls_fd_rhs",
     "ls_fd_diagonal", "ls_fd_solve", "ls_fd_profile_iteration", "ls_fd_profile_mg", "ls_fd_eval_points", "ls_fd_eval_lattice",
     "ls_fd_eval_adjoint", "ls_fd_set_rhs", "ls_fd_data_rows_apply", "ls_fd_device", "ls_fd_prepare", "ls_fd_solve_batched",
     "ls_fd_mg_apply_level",
-    "ls_p1_face_count", "ls_p1_face_rows", "ls_p1_locate", "ls_p1_point_rows", "ls_p1_eval_points",
+    "ls_p1_face_count", "ls_p1_face_rows", "ls_p1_face_rows_directional", "ls_p1_locate", "ls_p1_point_rows",
+    "ls_p1_eval_points",
 )
 
 
@@ -72,6 +76,7 @@ class FdSystem(C.Structure):
         ("ridge", C.c_double),
         ("nrows", C.c_int64), ("width", C.c_int32),
         ("d_idc", C.c_void_p), ("d_a", C.c_void_p), ("d_b", C.c_void_p), ("d_w", C.c_void_p),
+        ("d_dir", C.c_void_p),
     ]
 
 
@@ -108,6 +113,8 @@ _SIGS = {
     "ls_fd_pair_rows": (C.c_int, [C.POINTER(Grid3), _P, C.c_int64, _P, C.c_int64, C.c_double, _P, _P, _P, _P, _P]),
     "ls_fd_reg_shape": (C.c_int, [C.POINTER(Grid3), C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     "ls_fd_reg_rows": (C.c_int, [C.POINTER(Grid3), C.c_int, _P, _P]),
+    "ls_fd_directional_weights": (C.c_int, [C.POINTER(Grid3), _P, C.c_int64, C.c_double, _P,
+                                            C.POINTER(C.c_int64), _P]),
     "ls_fd_create": (C.c_int, [C.POINTER(FdSystem), C.POINTER(_P), _P]),
     "ls_fd_destroy": (C.c_int, [_P]),
     "ls_fd_dof": (C.c_int64, [_P]),
@@ -132,6 +139,7 @@ _SIGS = {
                                      C.POINTER(C.c_int64 * 3), _P, _P, _P]),
     "ls_p1_face_count": (C.c_int, [C.POINTER(Grid3), C.POINTER(C.c_int64)]),
     "ls_p1_face_rows": (C.c_int, [C.POINTER(Grid3), C.c_double, _P, _P, _P, _P, _P, _P, _P]),
+    "ls_p1_face_rows_directional": (C.c_int, [C.POINTER(Grid3), C.c_double, _P, _P, _P, _P, _P, _P]),
     "ls_p1_locate": (C.c_int, [C.POINTER(Grid3), _P, C.c_int64, C.c_int64, _P, _P, _P]),
     "ls_p1_point_rows": (C.c_int, [C.POINTER(Grid3), C.c_int, _P, C.c_int64, C.c_int64, C.c_double, _P, _P, _P, _P,
                                    C.POINTER(C.c_int64), _P]),
@@ -157,6 +165,8 @@ def load(build_if_missing: bool = False):
             fn = getattr(lib, name)
             fn.restype = res
             fn.argtypes = args
+        if lib.ls_abi_version() != ABI_VERSION:
+            raise ExtensionUnavailable(f"{path} has ABI {lib.ls_abi_version()}, this binding needs {ABI_VERSION}; rebuild it")
         _lib = lib
         return lib
 

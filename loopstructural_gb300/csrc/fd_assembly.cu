@@ -261,7 +261,7 @@ __global__ void point_rows_kernel(GridArgs g, const double *__restrict__ pts, in
       normalise8(ad, b1);
       store_row(s, idc, as, b0, weight, d_idc, d_a, d_b, d_w, nan_flag);
       store_row(n + s, idc, ad, b1, weight, d_idc, d_a, d_b, d_w, nan_flag);
-    } else {  // LS_ROWS_TANGENT, FD:478-539
+    } else {  // LS_ROWS_TANGENT / LS_ROWS_ORTHOGONAL, FD:478-539
       double T[3][8];
       element_gradient(l, g.step, T);
       double v[3] = {p[3], p[4], p[5]};
@@ -277,7 +277,7 @@ __global__ void point_rows_kernel(GridArgs g, const double *__restrict__ pts, in
       double a[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) a[k] = (v[0] * T[0][k] + v[1] * T[1][k]) + v[2] * T[2][k];
-      double b = 0.0;
+      double b = (KIND == LS_ROWS_ORTHOGONAL) ? p[6] : 0.0;  // FD:535 b_ = zeros + b
       normalise8(a, b);
       store_row(s, idc, a, b, weight, d_idc, d_a, d_b, d_w, nan_flag);
     }
@@ -400,6 +400,39 @@ __global__ void reg_rows_kernel(int64_t nx, int64_t ny, int64_t nz, int fam, int
   }
 }
 
+// Directional regularisation weights (FD:1207-1337): at every interior node m
+// (1 <= i, j, k <= n - 2, the centres of the interior families) the row
+// weights rw_f = w * c_f(v(m)), c = (vx^2, vy^2, vz^2, 2 vx vy, 2 vx vz,
+// 2 vy vz) in the reference's evaluation order; rows with |rw| > 0 (not zero,
+// not NaN) add s_f^2 rw^2 to omega[f][m] (s_f^2 = 1/6 for dxx/dyy/dzz, whose
+// normalised taps are (1, -2, 1)/sqrt(6); 1/4 for the cross families, whose
+// normalised taps are +-1/2) and count as a row of family f.
+__global__ void dir_weights_kernel(int nx, int ny, int nz, const double *__restrict__ vec, int64_t ld, double w,
+                                   double *__restrict__ omega, unsigned long long *__restrict__ counts) {
+  const int64_t n = (int64_t)nx * ny * nz;
+  unsigned long long cnt[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(g / ((int64_t)nx * ny));
+    const int rem = (int)(g - (int64_t)k * nx * ny);
+    const int j = rem / nx, i = rem - j * nx;
+    if (i < 1 || i > nx - 2 || j < 1 || j > ny - 2 || k < 1 || k > nz - 2) continue;
+    const double vx = vec[g * ld], vy = vec[g * ld + 1], vz = vec[g * ld + 2];
+    const double c[6] = {vx * vx, vy * vy, vz * vz, 2.0 * vx * vy, 2.0 * vx * vz, 2.0 * vy * vz};
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      const double rw = w * c[f];
+      if (fabs(rw) > 0.0) {
+        omega[f * n + g] += (f < 3 ? 1.0 / 6.0 : 0.25) * (rw * rw);
+        ++cnt[f];
+      }
+    }
+  }
+  if (counts)
+#pragma unroll
+    for (int f = 0; f < 6; ++f)
+      if (cnt[f]) atomicAdd(counts + f, cnt[f]);
+}
+
 int check_grid(const ls_grid3 *g) {
   LS_ARG_CHECK(g != nullptr, "grid is NULL");
   for (int d = 0; d < 3; ++d) {
@@ -418,9 +451,9 @@ extern "C" int ls_fd_point_rows(const ls_grid3 *grid, int kind, const double *d_
                                 double weight, int64_t *d_idc, double *d_a, double *d_b, double *d_w,
                                 int64_t *h_count, int32_t *h_nan, void *stream) {
   LS_TRY(check_grid(grid));
-  LS_ARG_CHECK(kind >= LS_ROWS_VALUE && kind <= LS_ROWS_TANGENT, "unknown row kind");
+  LS_ARG_CHECK(kind >= LS_ROWS_VALUE && kind <= LS_ROWS_ORTHOGONAL, "unknown row kind");
   LS_ARG_CHECK(npts >= 0, "npts < 0");
-  const int64_t min_ld = (kind == LS_ROWS_VALUE) ? 5 : 6;
+  const int64_t min_ld = (kind == LS_ROWS_VALUE) ? 5 : (kind == LS_ROWS_ORTHOGONAL ? 7 : 6);
   LS_ARG_CHECK(ld >= min_ld, "ld too small for the row kind");
   LS_ARG_CHECK(h_count != nullptr && h_nan != nullptr, "h_count / h_nan NULL");
   *h_count = 0;
@@ -451,8 +484,11 @@ extern "C" int ls_fd_point_rows(const ls_grid3 *grid, int kind, const double *d_
     case LS_ROWS_GRADIENT:
       point_rows_kernel<LS_ROWS_GRADIENT><<<grd, blk, 0, s>>>(g, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w, nanf);
       break;
-    default:
+    case LS_ROWS_TANGENT:
       point_rows_kernel<LS_ROWS_TANGENT><<<grd, blk, 0, s>>>(g, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w, nanf);
+      break;
+    default:
+      point_rows_kernel<LS_ROWS_ORTHOGONAL><<<grd, blk, 0, s>>>(g, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w, nanf);
       break;
   }
   LS_CUDA_TRY(cudaGetLastError());
@@ -500,5 +536,28 @@ extern "C" int ls_fd_reg_rows(const ls_grid3 *grid, int family, int64_t *d_idc, 
   reg_rows_kernel<<<stream_grid(sh.rows, 256), 256, 0, s>>>(grid->nsteps[0], grid->nsteps[1], grid->nsteps[2], family,
                                                           sh.rows, d_idc);
   LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
+
+extern "C" int ls_fd_directional_weights(const ls_grid3 *grid, const double *d_vec, int64_t ld, double weight,
+                                         double *d_omega, int64_t *h_counts, void *stream) {
+  LS_TRY(check_grid(grid));
+  LS_ARG_CHECK(ld >= 3, "ld < 3");
+  LS_ARG_CHECK(d_vec != nullptr && d_omega != nullptr, "NULL device buffer");
+  const int64_t n = grid->nsteps[0] * grid->nsteps[1] * grid->nsteps[2];
+  LS_ARG_CHECK(n < (int64_t)2000000000, "grid too large");
+  cudaStream_t s = as_stream(stream);
+  unsigned long long *cnt = nullptr;
+  LS_CUDA_TRY(cudaMallocAsync((void **)&cnt, 6 * sizeof(unsigned long long), s));
+  LS_CUDA_TRY(cudaMemsetAsync(cnt, 0, 6 * sizeof(unsigned long long), s));
+  dir_weights_kernel<<<stream_grid(n, 256), 256, 0, s>>>((int)grid->nsteps[0], (int)grid->nsteps[1],
+                                                        (int)grid->nsteps[2], d_vec, ld, weight, d_omega, cnt);
+  LS_CUDA_TRY(cudaGetLastError());
+  unsigned long long host[6] = {0, 0, 0, 0, 0, 0};
+  LS_CUDA_TRY(cudaMemcpyAsync(host, cnt, sizeof(host), cudaMemcpyDeviceToHost, s));
+  LS_CUDA_TRY(cudaFreeAsync(cnt, s));
+  LS_CUDA_TRY(cudaStreamSynchronize(s));
+  if (h_counts)
+    for (int f = 0; f < 6; ++f) h_counts[f] = (int64_t)host[f];
   return LS_OK;
 }

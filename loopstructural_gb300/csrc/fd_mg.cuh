@@ -56,6 +56,13 @@ struct MgLevel {
   std::vector<float> k27host;      // host copy ([27][knt]) and the nodes, for the coarsest dense matrix
   std::vector<int64_t> k27nodes;
   float *dinv = nullptr;
+  // directional regularisation weights (6 x n, family-major; level 0: the
+  // handle's, coarse levels: restricted) and the scratch for the isotropic
+  // part of an apply that the directional kernel completes
+  float *dir = nullptr;
+  float *dq = nullptr;
+  // coarse levels: row mass of the averaged weights and their square roots
+  float *dmass = nullptr, *dsw = nullptr;
   // Galerkin regularisation operator (first coarse level)
   bool g1 = false;
   G1Op g1op{};
@@ -72,6 +79,7 @@ struct MgLevel {
 struct MgHierarchy {
   std::vector<MgLevel> levels;
   double *coarse_inv64 = nullptr;  // dense inverse of the coarsest operator (FP64), row-major
+  float *dir_u = nullptr, *dir_v = nullptr;  // 6 x n(level 1) scratch of the coarse directional passes
   int deg = 3;
   bool built = false;
   std::vector<void *> allocations;

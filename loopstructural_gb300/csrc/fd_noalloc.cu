@@ -117,6 +117,7 @@ extern "C" int ls_fd_apply_noalloc(const ls_fd_system *sys, const double *d_x, d
   const int64_t n = g.nsteps[0] * g.nsteps[1] * g.nsteps[2];
   LS_ARG_CHECK(n < (int64_t)2000000000, "grid too large");
   LS_ARG_CHECK(sys->nrows >= 0, "nrows < 0");
+  LS_ARG_CHECK(sys->d_dir == nullptr, "directional regularisation needs a handle; use ls_fd_create + ls_fd_apply");
   if (sys->nrows > kMaxRows) {
     ls::set_error("ls_fd_apply_noalloc: %lld data rows exceed the static scratch limit of %lld rows "
                   "(LS_NOALLOC_MAX_ROWS); use ls_fd_create + ls_fd_apply", (long long)sys->nrows,

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "fd_apply.cuh"
+#include "fd_directional.cuh"
 #include "fd_mg.cuh"
 #include "fd_stencil.cuh"
 #include "ls_common.cuh"
@@ -34,6 +35,7 @@ struct CgScalars {
   double rz;       // r . z of the current residual
   double pq_s;     // p . (stencil part of N p)
   double pq_d;     // p . (data part of N p)
+  double pq_x;     // p . (directional part of N p; 0 without directional terms)
   double beta;
   double thresh2;  // stopping threshold squared (on r . z)
   double rrj;      // r . D^-1 r of the current FP32 residual (MG stopping test)
@@ -100,6 +102,9 @@ struct ls_fd_handle {
   // multigrid preconditioner (built on first use)
   ls::MgHierarchy mg;
   float *z32 = nullptr;                 // preconditioned residual
+  // directional regularisation weights (6 x n, family-major; null without)
+  double *dir64 = nullptr;
+  float *dir32 = nullptr;
   std::vector<int64_t> h_idc;           // host copy of the data rows (Galerkin coarsening)
   std::vector<double> h_a, h_w2;
   int h_width = 0;
@@ -128,7 +133,17 @@ int done_to_status(int d) {
   }
 }
 
-enum Ticket { T_STENCIL = 0, T_DATA = 1, T_UPDATE = 2, T_REFRESH = 3, T_MISC = 4, T_PUPD = 5, T_SHELL = 6, T_COUNT = 7 };
+enum Ticket {
+  T_STENCIL = 0,
+  T_DATA = 1,
+  T_UPDATE = 2,
+  T_REFRESH = 3,
+  T_MISC = 4,
+  T_PUPD = 5,
+  T_SHELL = 6,
+  T_DIR = 7,
+  T_COUNT = 8
+};
 
 // ---------------------------------------------------------------------------
 // kernels
@@ -145,7 +160,7 @@ __global__ void __launch_bounds__(kBlock) update_xr_kernel(int64_t n, T *__restr
                                                            const T *__restrict__ dinv, CgScalars *sc,
                                                            double *partials, unsigned int *ticket) {
   if (sc->done) return;
-  const double pq = sc->pq_s + sc->pq_d;
+  const double pq = sc->pq_s + sc->pq_d + sc->pq_x;
   const double rz = sc->rz;
   const double alpha_d = rz / pq;
   if (!sc->profile && (!(pq > 0.0) || !isfinite(alpha_d))) {
@@ -307,6 +322,14 @@ int grid_for(const ls_fd_handle *h, int64_t n) {
 }
 
 template <typename T>
+const T *dir_weights(const ls_fd_handle *h) {
+  if constexpr (sizeof(T) == 8)
+    return h->dir64;
+  else
+    return h->dir32;
+}
+
+template <typename T>
 DataView<T> data_view(const ls_fd_handle *h, const T *s_rows, const T *inc_a) {
   DataView<T> dv;
   dv.mask = h->data.mask;
@@ -340,6 +363,12 @@ void launch_apply(ls_fd_handle *h, const T *p, T *q, T *s, const T *a, const T *
   h->launches += launch_operator<T, EPI_STORE>(coef_as<T>(h->coef), p, data_view<T>(h, s, ia), e, done, h->partials,
                                                h->tickets + T_STENCIL, &h->sc->pq_s, h->tickets + T_SHELL,
                                                &h->sc->pq_d, h->red_blocks, st);
+  if (h->dir64) {  // q += D^T W D p in place; its share of p.q lands in pq_x
+    const DirView<T> dv{(int)h->grid.nsteps[0], (int)h->grid.nsteps[1], (int)h->grid.nsteps[2], dir_weights<T>(h)};
+    dir_apply_kernel<T, EPI_STORE><<<grid_for(h, h->n), 256, 0, st>>>(dv, p, q, e, done, h->partials,
+                                                                     h->tickets + T_DIR, &h->sc->pq_x);
+    ++h->launches;
+  }
 }
 
 void launch_apply64(ls_fd_handle *h, const double *p, double *q, bool check_done, cudaStream_t st) {
@@ -696,6 +725,16 @@ DataView<float> mg_view(const MgLevel &lv) {
   return dv;
 }
 
+DirCoarse dir_coarse(const MgLevel &lv) {
+  DirCoarse dc;
+  dc.nx = lv.nx;
+  dc.ny = lv.ny;
+  dc.nz = lv.nz;
+  for (int a = 0; a < 3; ++a) dc.t[a] = lv.g1op.t[a];
+  dc.sw = lv.dsw;
+  return dc;
+}
+
 // q = A_l p on level l (rows + fused apply with an epilogue)
 template <int EPI>
 void mg_apply(ls_fd_handle *h, const MgLevel &lv, const float *p, const EpiArgs<float> &e, const int *done,
@@ -708,6 +747,30 @@ void mg_apply(ls_fd_handle *h, const MgLevel &lv, const float *p, const EpiArgs<
     data_nodes_warp_kernel<float><<<std::max<int64_t>(1, std::min<int64_t>((lv.ntouched * 32 + 255) / 256, 8 * sm_count())), 256, 0, st>>>(
         lv.ntouched, lv.inc_ptr, lv.inc_row, lv.inc_a, lv.s, lv.qd, done);
     ++h->launches;
+  }
+  if (lv.dir) {
+    // isotropic part stored to dq, then the directional kernel adds its term
+    // and runs the epilogue
+    EpiArgs<float> es{};
+    es.q = lv.dq;
+    if (lv.g1)
+      h->launches += launch_g1<EPI_STORE>(lv.g1op, p, mg_view(lv), es, done, h->red_blocks / 8, st);
+    else
+      h->launches += launch_operator<float, EPI_STORE>(lv.coef, p, mg_view(lv), es, done, nullptr, nullptr, nullptr,
+                                                       nullptr, nullptr, h->red_blocks, st);
+    if (lv.dsw) {  // coarse level: S G S in three passes
+      const DirCoarse dc = dir_coarse(lv);
+      const int g = grid_for(h, lv.n);
+      dir_coarse_x_kernel<<<g, 256, 0, st>>>(dc, p, h->mg.dir_u, done);
+      dir_coarse_y_kernel<<<g, 256, 0, st>>>(dc, h->mg.dir_u, h->mg.dir_v, done);
+      dir_coarse_z_kernel<EPI><<<g, 256, 0, st>>>(dc, h->mg.dir_v, p, lv.dq, e, done);
+      h->launches += 3;
+    } else {  // finest level: the exact term
+      const DirView<float> dv{lv.nx, lv.ny, lv.nz, lv.dir};
+      dir_apply_kernel<float, EPI><<<grid_for(h, lv.n), 256, 0, st>>>(dv, p, lv.dq, e, done, nullptr, nullptr, nullptr);
+      ++h->launches;
+    }
+    return;
   }
   if (lv.g1)
     h->launches += launch_g1<EPI>(lv.g1op, p, mg_view(lv), e, done, h->red_blocks / 8, st);
@@ -777,6 +840,28 @@ int mg_coarse_inverse(ls_fd_handle *h, MgLevel &lv) {
     for (int64_t t = 0; t < nt; ++t)
       for (int o = 0; o < 27; ++o)
         put((int)lv.k27nodes[t], o % 3 - 1, (o / 3) % 3 - 1, o / 9 - 1, lv.k27host[(size_t)o * nt + t]);
+    if (lv.dsw) {
+      // sum_f S_f (Tx_f (x) Ty_f (x) Tz_f) S_f from the FP64 tables
+      std::vector<float> sw((size_t)kDirFamilies * nc);
+      LS_CUDA_TRY(cudaMemcpy(sw.data(), lv.dsw, sw.size() * sizeof(float), cudaMemcpyDeviceToHost));
+      const int nn[3] = {nx, ny, nz};
+      auto tab = [&](int a, int f, int idx, int o) { return lv.g1host[a][((size_t)g1_kind(f, a) * nn[a] + idx) * 5 + o + 2]; };
+      for (int g = 0; g < nc; ++g) {
+        const int x = g % nx, y = (g / nx) % ny, z = g / (nx * ny);
+        for (int f = 0; f < kDirFamilies; ++f) {
+          const double sg = sw[(size_t)f * nc + g];
+          if (sg == 0.0) continue;
+          for (int dz = -2; dz <= 2; ++dz)
+            for (int dy = -2; dy <= 2; ++dy)
+              for (int dx = -2; dx <= 2; ++dx) {
+                if (x + dx < 0 || x + dx >= nx || y + dy < 0 || y + dy >= ny || z + dz < 0 || z + dz >= nz) continue;
+                const int g2 = g + dz * nx * ny + dy * nx + dx;
+                const double t = tab(0, f, x, dx) * tab(1, f, y, dy) * tab(2, f, z, dz);
+                if (t != 0.0) A[(size_t)g * nc + g2] += sg * t * sw[(size_t)f * nc + g2];
+              }
+        }
+      }
+    }
   } else {
     std::vector<float> col(nc);
     const float one = 1.0f;
@@ -852,6 +937,10 @@ int mg_level_dinv(ls_fd_handle *h, MgLevel &lv, const std::vector<int64_t> &touc
   else
     diag_stencil_kernel<<<g, kBlock, 0, st>>>(lv.coef64, diag);
   ++h->launches;
+  if (lv.dsw) {
+    dir_coarse_diag_kernel<<<g, kBlock, 0, st>>>(dir_coarse(lv), lv.dir, diag);
+    ++h->launches;
+  }
   if (!touched.empty()) {
     mg_diag_finish_kernel<<<grid_for(h, (int64_t)touched.size()), kBlock, 0, st>>>(lv.n, diag, (int64_t)touched.size(), dt, dd);
     ++h->launches;
@@ -1107,6 +1196,8 @@ int mg_build(ls_fd_handle *h, int deg) {
   L0.inc_row = h->data.inc_row;
   L0.inc_a = h->data.inc_a32;
   L0.dinv = h->dinv32;
+  L0.dir = h->dir32;
+  if (L0.dir) LS_TRY(mg_alloc(mg, &L0.dq, L0.n));
   L0.owns_bx = false;
   L0.b = h->r32;
   if (!h->z32) LS_TRY(dev_alloc(&h->z32, h->n));
@@ -1146,6 +1237,19 @@ int mg_build(ls_fd_handle *h, int deg) {
     LS_TRY(mg_alloc(mg, &c.d0, c.n));
     LS_TRY(mg_alloc(mg, &c.d1, c.n));
     LS_TRY(mg_alloc(mg, &c.dinv, c.n));
+    if (f.dir) {
+      LS_TRY(mg_alloc(mg, &c.dir, (size_t)kDirFamilies * c.n));
+      LS_TRY(mg_alloc(mg, &c.dsw, (size_t)kDirFamilies * c.n));
+      LS_TRY(mg_alloc(mg, &c.dmass, c.n));
+      LS_TRY(mg_alloc(mg, &c.dq, c.n));
+      if (!mg.dir_u) {  // the first coarse level is the largest
+        LS_TRY(mg_alloc(mg, &mg.dir_u, (size_t)kDirFamilies * c.n));
+        LS_TRY(mg_alloc(mg, &mg.dir_v, (size_t)kDirFamilies * c.n));
+      }
+      dir_average_kernel<<<grid_for(h, c.n), kBlock, 0, h->stream>>>(f.nx, f.ny, f.nz, f.dir, f.dmass, c.nx, c.ny,
+                                                                      c.nz, c.dir, c.dmass, c.dsw);
+      ++h->launches;
+    }
     HostRows rest;
     std::vector<std::pair<int64_t, double>> kdiag;
     LS_TRY(mg_upload_k27(h, c, rows, rest, kdiag));
@@ -1247,7 +1351,7 @@ __global__ void __launch_bounds__(kBlock) mg_update_xr_kernel(int64_t n, float *
                                                               const float *__restrict__ dinv, CgScalars *sc,
                                                               double *partials, unsigned int *ticket) {
   if (sc->done) return;
-  const double pq = sc->pq_s + sc->pq_d;
+  const double pq = sc->pq_s + sc->pq_d + sc->pq_x;
   const double alpha_d = sc->rz / pq;
   if (!(pq > 0.0) || !isfinite(alpha_d)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) sc->done = isfinite(pq) ? DONE_BREAKDOWN : DONE_NAN;
@@ -1649,11 +1753,28 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
   const int64_t ne = d.nrows * d.width;
   if ((st = setup_data_term(h, sys, ne)) < 0) return fail(st);
   cudaStream_t hs = h->stream;
+  // ---- directional regularisation weights: FP64 copy and FP32 copy ----
+  if (sys->d_dir) {
+    const int64_t nd = (int64_t)kDirFamilies * n;
+    if ((st = dev_alloc(&h->dir64, nd)) < 0) return fail(st);
+    if ((st = dev_alloc(&h->dir32, nd)) < 0) return fail(st);
+    if (cudaMemcpyAsync(h->dir64, sys->d_dir, nd * sizeof(double), cudaMemcpyDeviceToDevice, hs) != cudaSuccess) {
+      set_error("copy of the directional weights failed");
+      return fail(LS_ERR_CUDA);
+    }
+    dir_to_f32_kernel<<<grid_for(h, nd), kBlock, 0, hs>>>(nd, h->dir64, h->dir32);
+    ++h->launches;
+  }
   // ---- rhs, diagonal, inverse diagonal ----
   const int gn = grid_for(h, n);
   cudaMemsetAsync(h->rhs, 0, n * sizeof(double), hs);
   diag_stencil_kernel<<<gn, kBlock, 0, hs>>>(h->coef, h->diag);
   ++h->launches;
+  if (h->dir64) {
+    const DirView<double> dv{(int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], h->dir64};
+    dir_diag_kernel<double><<<gn, kBlock, 0, hs>>>(dv, h->diag);
+    ++h->launches;
+  }
   if (d.ntouched > 0) {
     data_node_setup_kernel<<<grid_for(h, d.ntouched), kBlock, 0, hs>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row,
                                                                        d.inc_a64, d.w2_64, d.b, h->diag, h->rhs);
@@ -1685,7 +1806,7 @@ extern "C" int ls_fd_destroy(ls_fd_handle *h) {
   void *ptrs[] = {h->rhs, h->diag, h->dinv64, h->dinv32, h->x64, h->r64, h->p64, h->q64, h->s64, h->x32, h->r32,
                   h->p32, h->q32, h->s32, h->sc, h->partials, h->tickets, h->data.cols, h->data.a64, h->data.a32,
                   h->data.w2_64, h->data.w2_32, h->data.b, h->data.touched, h->data.inc_ptr, h->data.inc_row,
-                  h->data.inc_a64, h->data.inc_a32, h->data.mask, h->data.word_rank};
+                  h->data.inc_a64, h->data.inc_a32, h->data.mask, h->data.word_rank, h->dir64, h->dir32};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->sc_h) cudaFreeHost(h->sc_h);
@@ -1818,7 +1939,7 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
     }
     const long long iters0 = iters;
     s.rz = s.rz32;
-    s.pq_s = s.pq_d = 0.0;
+    s.pq_s = s.pq_d = s.pq_x = 0.0;
     s.thresh2 = thresh * thresh;
     s.iters = iters0;
     s.maxiter = maxiter;
@@ -1884,7 +2005,7 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
     LS_TRY(refresh(h, opts->use_x0 != 0, nullptr, nullptr));  // r64, p64 = D^-1 r64, rz64
     LS_TRY(read_scalars(h));
     s.rz = s.rz64;
-    s.pq_s = s.pq_d = 0.0;
+    s.pq_s = s.pq_d = s.pq_x = 0.0;
     s.thresh2 = thresh * thresh;
     s.iters = 0;
     s.maxiter = maxiter;
@@ -1916,7 +2037,7 @@ extern "C" int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d
       LS_TRY(write_scalars(h));
       LS_TRY(mg_restart(h, true));
       LS_TRY(read_scalars(h));
-      s.pq_s = s.pq_d = 0.0;
+      s.pq_s = s.pq_d = s.pq_x = 0.0;
       s.thresh2 = thresh * thresh;
       s.iters = 0;
       s.maxiter = maxiter;

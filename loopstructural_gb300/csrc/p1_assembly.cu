@@ -217,10 +217,13 @@ __device__ __forceinline__ double norm8(const double a[8]) {
   return sqrt(0.0 + r);
 }
 
-// faces of tet i and their rows (P1:115-166): const = [n . grad_i, -n . grad_j]
+// faces of tet i and their rows (P1:115-166): const = [n . grad_i, -n . grad_j],
+// n the face normal, or vec[face] when given (P1:129-130, the directional
+// regularisation of P1:172-178)
 __global__ void face_rows_kernel(MeshArgs m, int64_t ntet, const int64_t *__restrict__ off, double weight,
-                                 int64_t *__restrict__ pairs, int64_t *__restrict__ shared, int64_t *__restrict__ idc,
-                                 double *__restrict__ a, double *__restrict__ b, double *__restrict__ w) {
+                                 const double *__restrict__ vec, int64_t *__restrict__ pairs,
+                                 int64_t *__restrict__ shared, int64_t *__restrict__ idc, double *__restrict__ a,
+                                 double *__restrict__ b, double *__restrict__ w) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntet; t += (int64_t)gridDim.x * blockDim.x) {
     int64_t nb[4];
     tet_neighbours(m, t, nb);
@@ -276,8 +279,12 @@ __global__ void face_rows_kernel(MeshArgs m, int64_t ntet, const int64_t *__rest
       }
       const double v1[3] = {P[1][0] - P[0][0], P[1][1] - P[0][1], P[1][2] - P[0][2]};
       const double v2[3] = {P[2][0] - P[0][0], P[2][1] - P[0][1], P[2][2] - P[0][2]};
-      const double nrm[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2],
-                             v1[0] * v2[1] - v1[1] * v2[0]};
+      double nrm[3] = {v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2], v1[0] * v2[1] - v1[1] * v2[0]};
+      if (vec) {
+        nrm[0] = vec[3 * f];
+        nrm[1] = vec[3 * f + 1];
+        nrm[2] = vec[3 * f + 2];
+      }
       double row[8];
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
@@ -514,8 +521,9 @@ extern "C" int ls_p1_face_count(const ls_grid3 *mesh, int64_t *h_faces) {
   return LS_OK;
 }
 
-extern "C" int ls_p1_face_rows(const ls_grid3 *mesh, double weight, int64_t *d_pairs, int64_t *d_shared,
-                               int64_t *d_idc, double *d_a, double *d_b, double *d_w, void *stream) {
+namespace {
+int face_rows(const ls_grid3 *mesh, double weight, const double *d_vec, int64_t *d_pairs, int64_t *d_shared,
+              int64_t *d_idc, double *d_a, double *d_b, double *d_w, void *stream) {
   LS_TRY(check_mesh(mesh));
   LS_ARG_CHECK(d_idc && d_a && d_b && d_w, "NULL device buffer");
   const MeshArgs m = make_mesh_args(*mesh);
@@ -527,11 +535,24 @@ extern "C" int ls_p1_face_rows(const ls_grid3 *mesh, double weight, int64_t *d_p
   LS_CUDA_TRY(cudaMallocAsync((void **)&off, (ntet + 1) * sizeof(int64_t), s));
   face_count_kernel<<<stream_grid(ntet, 256), 256, 0, s>>>(m, ntet, cnt);
   scan_counts_kernel<<<1, 1024, 0, s>>>(cnt, ntet, off, off + ntet);
-  face_rows_kernel<<<stream_grid(ntet, 128), 128, 0, s>>>(m, ntet, off, weight, d_pairs, d_shared, d_idc, d_a, d_b, d_w);
+  face_rows_kernel<<<stream_grid(ntet, 128), 128, 0, s>>>(m, ntet, off, weight, d_vec, d_pairs, d_shared, d_idc, d_a,
+                                                         d_b, d_w);
   LS_CUDA_TRY(cudaGetLastError());
   LS_CUDA_TRY(cudaFreeAsync(cnt, s));
   LS_CUDA_TRY(cudaFreeAsync(off, s));
   return LS_OK;
+}
+}  // namespace
+
+extern "C" int ls_p1_face_rows(const ls_grid3 *mesh, double weight, int64_t *d_pairs, int64_t *d_shared,
+                               int64_t *d_idc, double *d_a, double *d_b, double *d_w, void *stream) {
+  return face_rows(mesh, weight, nullptr, d_pairs, d_shared, d_idc, d_a, d_b, d_w, stream);
+}
+
+extern "C" int ls_p1_face_rows_directional(const ls_grid3 *mesh, double weight, const double *d_vec, int64_t *d_idc,
+                                           double *d_a, double *d_b, double *d_w, void *stream) {
+  LS_ARG_CHECK(d_vec != nullptr, "NULL direction buffer");
+  return face_rows(mesh, weight, d_vec, nullptr, nullptr, d_idc, d_a, d_b, d_w, stream);
 }
 
 extern "C" int ls_p1_locate(const ls_grid3 *mesh, const double *d_pts, int64_t npts, int64_t ld, int64_t *d_tet,

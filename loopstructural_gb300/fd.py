@@ -36,7 +36,8 @@ def point_rows(support, kind: int, pts: np.ndarray, weight: float):
     lib = _lib.load()
     pts = np.ascontiguousarray(pts, dtype=np.float64)
     npts, ld = pts.shape
-    fam = {_lib.ROWS_VALUE: 1, _lib.ROWS_NORM: 3, _lib.ROWS_GRADIENT: 2, _lib.ROWS_TANGENT: 1}[kind]
+    fam = {_lib.ROWS_VALUE: 1, _lib.ROWS_NORM: 3, _lib.ROWS_GRADIENT: 2, _lib.ROWS_TANGENT: 1,
+           _lib.ROWS_ORTHOGONAL: 1}[kind]
     d_pts = torch.from_numpy(pts).to(dev)
     idc = torch.empty((fam * npts, 8), dtype=torch.int64, device=dev)
     a = torch.empty((fam * npts, 8), dtype=torch.float64, device=dev)
@@ -74,6 +75,20 @@ def pair_rows(support, pts: np.ndarray, pairs: np.ndarray, weight: float):
     return idc, a, b, w
 
 
+def directional_weights(support, vector: np.ndarray, weight: float, omega):
+    """Adds one directional term's weights to ``omega`` (6 x dof FP64 device
+    tensor, family-major) on the GPU; returns the row count of each family
+    (dxx, dyy, dzz, dxy, dxz, dyz) the reference would add."""
+    torch = _torch()
+    lib = _lib.load()
+    vec = torch.from_numpy(np.ascontiguousarray(vector, dtype=np.float64)).to(omega.device)
+    counts = (C.c_int64 * 6)()
+    g = support.grid3()
+    _lib.check(lib.ls_fd_directional_weights(C.byref(g), _lib.ptr(vec), 3, float(weight), _lib.ptr(omega), counts,
+                                             _lib.stream_ptr()))
+    return [int(c) for c in counts]
+
+
 def reg_shape(support, family: str):
     lib = _lib.load()
     rows = C.c_int64(0)
@@ -99,7 +114,7 @@ class FdSystem:
     """Owns an ``ls_fd_handle``: the matrix-free normal equations of one
     interpolator setup."""
 
-    def __init__(self, support, reg_weights: dict, rows, ridge: float):
+    def __init__(self, support, reg_weights: dict, rows, ridge: float, directional=None):
         torch = _torch()
         self.dev = _lib.device()
         self.lib = _lib.load()
@@ -137,6 +152,7 @@ class FdSystem:
         s.d_a = _lib.ptr(self._a)
         s.d_b = _lib.ptr(self._b)
         s.d_w = _lib.ptr(self._w)
+        s.d_dir = _lib.ptr(directional) if directional is not None else None
         self.nrows = nrows
         self.handle = C.c_void_p()
         _lib.check(self.lib.ls_fd_create(C.byref(s), C.byref(self.handle), _lib.stream_ptr()))

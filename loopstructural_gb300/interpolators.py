@@ -17,6 +17,7 @@ from time import perf_counter
 import numpy as np
 
 from . import _lib, constraints, fd
+from . import regularisation as regcfg
 
 logger = logging.getLogger(__name__)
 
@@ -167,6 +168,17 @@ class _DiscreteInterpolatorBase:
         return dict(self.latest_solve_timing)
 
     # -- least squares container (DI:316-389 semantics on device rows) ------
+    @staticmethod
+    def _unique_name(name, taken):
+        """DI:374-379 name de-duplication (``name_k``)."""
+        base = name
+        while name in taken:
+            count = 0
+            if "_" in name:
+                count = int(name.split("_")[1]) + 1
+            name = base + f"_{count}"
+        return name
+
     def _add_family(self, name, idc, a, b, w):
         import torch
 
@@ -175,13 +187,48 @@ class _DiscreteInterpolatorBase:
         if bool(torch.isnan(a).any()) or bool(torch.isnan(b).any()):
             logger.warning("Constraints contain nan not adding constraints: %s", name)
             return
-        base = name
-        while name in self.constraints:
-            count = 0
-            if "_" in name:
-                count = int(name.split("_")[1]) + 1
-            name = base + f"_{count}"
+        name = self._unique_name(name, self.constraints)
         self.constraints[name] = ConstraintFamily(name, idc, a, b, w)
+
+    # -- directional regularisation (DI:395-451) ----------------------------
+    def resolve_regularisation_config(self, regularisation=None, directional_regularisation=None):
+        return regcfg.coerce_regularisation_config(regularisation=regularisation,
+                                                   directional_regularisation=directional_regularisation)
+
+    def get_regularisation_sample_points(self) -> np.ndarray:
+        raise NotImplementedError(f"{self.__class__.__name__} does not define regularisation sample points")
+
+    def _regularisation_sample_shape(self):
+        return tuple(np.asarray(self.get_regularisation_sample_points()).shape)
+
+    def _add_directional_regularisation(self, weight, vectors, name="directional regularisation"):
+        raise NotImplementedError(f"{self.__class__.__name__} does not implement directional regularisation")
+
+    def add_directional_regularisation(self, directional_regularisation):
+        """Evaluates each term's direction at the regularisation sample points
+        (when it is a callable) and adds its rows; terms of weight 0 are
+        skipped, wrongly shaped directions warn and are skipped (DI:422-451)."""
+        terms = self.resolve_regularisation_config(directional_regularisation=directional_regularisation).directional
+        if len(terms) == 0:
+            return terms
+        sample = None
+        expected = self._regularisation_sample_shape()
+        for term in terms:
+            if term.weight == 0:
+                continue
+            if callable(term.direction):
+                if sample is None:
+                    sample = np.asarray(self.get_regularisation_sample_points(), dtype=float)
+                vectors = term.direction(sample)
+            else:
+                vectors = term.direction
+            vectors = np.asarray(vectors, dtype=float)
+            if vectors.shape != expected:
+                logger.warning("%s: directional regularisation vectors must have shape %s, got %s. Skipping.",
+                               term.name, expected, vectors.shape)
+                continue
+            self._add_directional_regularisation(term.weight, vectors, name=term.name)
+        return terms
 
     def reset(self):
         self.constraints = {}
@@ -314,18 +361,27 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
         self.interface_pair_threshold = 200
         self.interface_pair_fallback = "star"
         self.regularisation_families = {}
+        self._reset_directional()
+
+    def _reset_directional(self):
+        # directional families: name -> (rows, term index, family); the terms'
+        # (weight, direction); the summed device weights (6 x dof) of the operator
+        self.directional_families = {}
+        self._dir_terms = []
+        self._dir_omega = None
+
+    def reset(self):
+        super().reset()
+        self._reset_directional()
 
     def setup_interpolator(self, **kwargs) -> SetupReport:
         self.reset()
-        reg = kwargs.get("regularisation", None)
-        if reg is not None:
-            if isinstance(reg, dict):
-                reg = reg.get("isotropic", reg.get("weight", None))
-            if reg is not None:
-                for k in self.REG_WEIGHT_KEYS:
-                    self.interpolation_weights[k] = float(reg)
-        if kwargs.get("directional_regularisation") is not None:
-            raise NotImplementedError("directional regularisation is not part of the GPU path")
+        cfg = self.resolve_regularisation_config(regularisation=kwargs.get("regularisation", None),
+                                                 directional_regularisation=kwargs.get("directional_regularisation",
+                                                                                       None))
+        if cfg.isotropic is not None:
+            for k in self.REG_WEIGHT_KEYS:
+                self.interpolation_weights[k] = cfg.isotropic
         for k, v in kwargs.items():
             self.up_to_date = False
             if k in ("regularisation", "directional_regularisation"):
@@ -343,13 +399,93 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
         self._add_point_rows(_lib.ROWS_VALUE, self.get_value_constraints(), w["cpw"], ["value"])
         self._add_point_rows(_lib.ROWS_TANGENT, self.get_tangent_constraints(), w["tpw"], ["gradient orthogonal"])
         self._add_interface_rows(w["ipw"])
-        self._add_regularisation_families()
+        self._add_regularisation_families(interior=True, borders=False)
+        self.add_directional_regularisation(cfg.directional)  # FD:222, between interior and border families
+        self._add_regularisation_families(interior=False, borders=True)
         self.setup_seconds = perf_counter() - t0
         self.up_to_date = False
         report = SetupReport({name: f.n_rows for name, f in self.constraints.items()})
         for name, (rows, _w) in self.regularisation_families.items():
             report[name] = rows
+        for name, (rows, _t, _f) in self.directional_families.items():
+            report[name] = rows
         return report
+
+    # -- directional regularisation (FD:1207-1348) ----------------------------
+    def get_regularisation_sample_points(self) -> np.ndarray:
+        return self.support.nodes
+
+    def _regularisation_sample_shape(self):
+        return (int(self.support.n_nodes), 3)
+
+    def _add_directional_regularisation(self, weight, vectors, name="directional regularisation"):
+        self.minimise_directional_gradient_change(weight, vectors, name=name)
+
+    def minimise_directional_gradient_change(self, w, vector, name="directional regularisation"):
+        """Directional second-derivative regularisation: the six interior
+        families again with row weight w * c_f(v) (c = vx², vy², vz², 2vxvy,
+        2vxvz, 2vyvz) at each interior node, rows of zero weight dropped.  The
+        rows stay matrix-free: their weights are summed per node and family
+        on the device (ls_fd_directional_weights) and the operator applies
+        sum_f D_f^T W_f D_f."""
+        import torch
+
+        n = int(self.support.n_nodes)
+        if vector is None or np.ndim(vector) != 2 or np.shape(vector) != (n, 3):
+            logger.warning("%s: vector must have shape (%d, 3), got %s.  Skipping.", name, n,
+                           None if vector is None else np.shape(vector))
+            return
+        vector = np.asarray(vector, dtype=float)
+        if self._dir_omega is None:
+            self._dir_omega = torch.zeros((len(_lib.DIRECTIONAL_FAMILIES), n), dtype=torch.float64,
+                                          device=_lib.device())
+        counts = fd.directional_weights(self.support, vector, float(w), self._dir_omega)
+        self._dir_terms.append((float(w), vector))
+        taken = set(self.constraints) | set(self.regularisation_families) | set(self.directional_families)
+        for f, op in enumerate(_lib.DIRECTIONAL_FAMILIES):
+            if counts[f] > 0:
+                fam = self._unique_name(f"{name}_{op}", taken)
+                taken.add(fam)
+                self.directional_families[fam] = (int(counts[f]), len(self._dir_terms) - 1, op)
+        self.up_to_date = False
+
+    def add_gradient_orthogonal_constraints(self, points, vectors, w=1.0, b=0, name="gradient orthogonal"):
+        """Rows grad(f) . v / |v| = b at the points (FD:478-539), normalised;
+        points outside the grid are dropped."""
+        points = np.asarray(points, dtype=float)
+        if points.shape[0] == 0:
+            return
+        vectors = np.asarray(vectors, dtype=float)
+        arr = np.empty((points.shape[0], 7))
+        arr[:, :3] = points[:, :3]
+        arr[:, 3:6] = vectors[:, :3]
+        arr[:, 6] = b
+        n, fams, _nan = fd.point_rows(self.support, _lib.ROWS_ORTHOGONAL, arr, float(w))
+        if n <= 0:
+            logger.warning("%d gradient constraints not added: outside of model bounding box", points.shape[0])
+            return
+        idc, a, bb, ww = fams[0]
+        self._add_family(name, idc, a, bb, ww)
+        self.up_to_date = False
+
+    def directional_rows(self, name):
+        """Explicit (idc, A, B, w) of a directional family as the reference
+        stores it (parity inspection): the interior family's rows with
+        w * c_f(v) at the row centre, zero-weight rows dropped."""
+        _rows, term, op = self.directional_families[name]
+        w, vec = self._dir_terms[term]
+        idc = fd.reg_rows(self.support, op).cpu().numpy()
+        nx, ny, nz = (int(v) for v in self.support.nsteps)
+        i, j, k = np.meshgrid(np.arange(1, nx - 1), np.arange(1, ny - 1), np.arange(1, nz - 1), indexing="ij")
+        centre = (i + nx * (j + ny * k)).transpose(2, 1, 0).ravel()  # ascending node index
+        vx, vy, vz = vec[centre, 0], vec[centre, 1], vec[centre, 2]
+        comp = {"dxx": vx**2, "dyy": vy**2, "dzz": vz**2, "dxy": 2.0 * vx * vy, "dxz": 2.0 * vx * vz,
+                "dyz": 2.0 * vy * vz}[op]
+        row_w = w * comp
+        keep = np.abs(row_w) > 0.0
+        vals = fd.REG_TAP_VALUES[op]
+        return {"idc": idc[keep], "A": np.tile(vals, (int(keep.sum()), 1)), "B": np.zeros(int(keep.sum())),
+                "w": row_w[keep]}
 
     def _add_point_rows(self, kind, points, weight, names):
         if points.shape[0] == 0:
@@ -395,22 +531,24 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
             idc, a, b, w = fd.pair_rows(self.support, pin, sel[pairs], weight)
             self._add_family(f"interface_{uid}", idc, a, b, w)
 
-    def _add_regularisation_families(self):
+    def _add_regularisation_families(self, interior=True, borders=True):
         """Matrix-free: record (rows, weight) per family in the reference order
-        (G:489-510 then FD:1052-1144)."""
+        (G:489-510 interior families, FD:1052-1144 borders)."""
         w = self.interpolation_weights
-        self.regularisation_families = {}
-        rw = {"dxy": w["dxy"] / 4, "dyz": w["dyz"] / 4, "dxz": w["dxz"] / 4, "dxx": w["dxx"], "dyy": w["dyy"],
-              "dzz": w["dzz"]}
-        for name, weight in rw.items():
-            rows, _ = fd.reg_shape(self.support, name)
-            if rows > 0:
-                self.regularisation_families[name] = (rows, float(weight))
-        for name, key in (("dx_lower", "dx"), ("dx_upper", "dx"), ("dy_lower", "dy"), ("dy_upper", "dy"),
-                          ("dz_lower", "dz"), ("dz_upper", "dz")):
-            rows, _ = fd.reg_shape(self.support, name)
-            if w[key] != 0 and rows > 0:
-                self.regularisation_families[name] = (rows, float(w[key]))
+        if interior:
+            self.regularisation_families = {}
+            rw = {"dxy": w["dxy"] / 4, "dyz": w["dyz"] / 4, "dxz": w["dxz"] / 4, "dxx": w["dxx"], "dyy": w["dyy"],
+                  "dzz": w["dzz"]}
+            for name, weight in rw.items():
+                rows, _ = fd.reg_shape(self.support, name)
+                if rows > 0:
+                    self.regularisation_families[name] = (rows, float(weight))
+        if borders:
+            for name, key in (("dx_lower", "dx"), ("dx_upper", "dx"), ("dy_lower", "dy"), ("dy_upper", "dy"),
+                              ("dz_lower", "dz"), ("dz_upper", "dz")):
+                rows, _ = fd.reg_shape(self.support, name)
+                if w[key] != 0 and rows > 0:
+                    self.regularisation_families[name] = (rows, float(w[key]))
 
     def regularisation_rows(self, name):
         """Explicit (idc, A, B, w) of a matrix-free family, as the reference's
@@ -432,15 +570,19 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
     def _build_system(self):
         rows = [(f.idc, f.a, f.b, f.w) for f in self.constraints.values()]
         ridge = self.ridge_factor if self.add_ridge_regulatisation else 0.0
-        return fd.FdSystem(self.support, self._reg_weights(), rows, ridge)
+        omega = self._dir_omega if self.directional_families else None
+        return fd.FdSystem(self.support, self._reg_weights(), rows, ridge, directional=omega)
 
     def _matrix_rows(self):
-        return sum(f.n_rows for f in self.constraints.values()) + sum(r for r, _ in self.regularisation_families.values())
+        return (sum(f.n_rows for f in self.constraints.values()) + sum(r for r, _ in self.regularisation_families.values())
+                + sum(r for r, _t, _f in self.directional_families.values()))
 
     def _matrix_nnz(self):
         nnz = sum(f.n_rows * f.idc.shape[1] for f in self.constraints.values())
         for name, (r, _) in self.regularisation_families.items():
             nnz += r * (4 if name in ("dxy", "dyz", "dxz") else 3)
+        for r, _t, op in self.directional_families.values():
+            nnz += r * (4 if op in ("dxy", "dyz", "dxz") else 3)
         return nnz
 
     def _evaluate_value_local(self, locations):

@@ -41,6 +41,35 @@ def face_rows(mesh, weight: float, with_topology: bool = False):
     return idc, a, b, w
 
 
+def face_rows_directional(mesh, weight: float, vectors: np.ndarray):
+    """Face rows with the normal replaced by one direction per face (F, 3)."""
+    import torch
+
+    dev = _lib.device()
+    lib = _lib.load()
+    g = mesh.grid3()
+    nf = C.c_int64(0)
+    _lib.check(lib.ls_p1_face_count(C.byref(g), C.byref(nf)))
+    F = nf.value
+    d_vec = torch.from_numpy(np.ascontiguousarray(vectors, dtype=np.float64)).to(dev)
+    idc = torch.empty((F, 8), dtype=torch.int64, device=dev)
+    a = torch.empty((F, 8), dtype=torch.float64, device=dev)
+    b = torch.empty(F, dtype=torch.float64, device=dev)
+    w = torch.empty(F, dtype=torch.float64, device=dev)
+    _lib.check(lib.ls_p1_face_rows_directional(C.byref(g), float(weight), _lib.ptr(d_vec), _lib.ptr(idc), _lib.ptr(a),
+                                               _lib.ptr(b), _lib.ptr(w), _lib.stream_ptr()))
+    return idc, a, b, w
+
+
+def face_centres(mesh):
+    """Centroid of each face's three shared nodes, in face order (P1:169-170)."""
+    shared = face_rows(mesh, 1.0, with_topology=True)[5].cpu().numpy()
+    n = np.asarray(mesh.nsteps, dtype=np.int64)
+    ijk = np.stack([shared % n[0], (shared // n[0]) % n[1], shared // (n[0] * n[1])], axis=-1)
+    coords = np.asarray(mesh.origin, dtype=float) + ijk * np.asarray(mesh.step_vector, dtype=float)
+    return coords.mean(axis=1)
+
+
 def locate(mesh, pts: np.ndarray):
     import torch
 
@@ -106,13 +135,11 @@ class P1Interpolator(_DiscreteInterpolatorBase):
 
     def setup_interpolator(self, **kwargs) -> SetupReport:
         self.reset()
-        reg = kwargs.get("regularisation", None)
-        if isinstance(reg, dict):
-            reg = reg.get("isotropic", reg.get("weight", None))
-        if reg is not None:
-            self.interpolation_weights["cgw"] = float(reg)
-        if kwargs.get("directional_regularisation") is not None:
-            raise NotImplementedError("directional regularisation is not part of the GPU path")
+        cfg = self.resolve_regularisation_config(regularisation=kwargs.get("regularisation", None),
+                                                 directional_regularisation=kwargs.get("directional_regularisation",
+                                                                                       None))
+        if cfg.isotropic is not None:
+            self.interpolation_weights["cgw"] = cfg.isotropic
         for k, v in kwargs.items():
             self.up_to_date = False
             if k in ("regularisation", "directional_regularisation"):
@@ -122,8 +149,8 @@ class P1Interpolator(_DiscreteInterpolatorBase):
             raise NotImplementedError("use_regularisation_weight_scale is not part of the GPU path")
         w = self.interpolation_weights
         if w["cgw"] > 0.0:
-            idc, a, b, ww = face_rows(self.support, w["cgw"])
-            self._add_family("edge jump", idc, a, b, ww)
+            self.minimise_edge_jumps(w["cgw"])
+        self.add_directional_regularisation(cfg.directional)  # P1:229
         # gradient constraints: no-op in the reference P1 (P1:70-71)
         normals = self.get_norm_constraints()
         if normals.shape[0] > 0:
@@ -135,6 +162,31 @@ class P1Interpolator(_DiscreteInterpolatorBase):
             raise NotImplementedError("P1 tangent constraints are not part of the GPU path")
         self.up_to_date = False
         return SetupReport({name: f.n_rows for name, f in self.constraints.items()})
+
+    # -- directional regularisation (P1:169-178) -----------------------------
+    def get_regularisation_sample_points(self) -> np.ndarray:
+        return face_centres(self.support)
+
+    def _regularisation_sample_shape(self):
+        nf = C.c_int64(0)
+        _lib.check(_lib.load().ls_p1_face_count(C.byref(self.support.grid3()), C.byref(nf)))
+        return (int(nf.value), 3)
+
+    def _add_directional_regularisation(self, weight, vectors, name="directional regularisation"):
+        self.minimise_edge_jumps(w=weight, vector=vectors, name=name)
+
+    def minimise_edge_jumps(self, w=0.1, vector_func=None, vector=None, name="edge jump"):
+        """Constant-gradient face rows (P1:115-166); ``vector`` (one row per
+        face) or ``vector_func`` (evaluated at the faces' mid-edge points,
+        P1:126-127) replaces the face normal."""
+        if vector_func is not None:
+            raise NotImplementedError("vector_func needs the reference's shared-edge points; pass vector=")
+        if vector is not None and np.shape(vector)[0] == self._regularisation_sample_shape()[0]:
+            idc, a, b, ww = face_rows_directional(self.support, w, np.asarray(vector, dtype=float))
+        else:
+            idc, a, b, ww = face_rows(self.support, w)
+        self._add_family(name, idc, a, b, ww)
+        self.up_to_date = False
 
     def _build_system(self):
         rows = [(f.idc, f.a, f.b, f.w) for f in self.constraints.values()]

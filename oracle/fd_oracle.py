@@ -387,8 +387,9 @@ def boundary_indexes(grid: Grid, axis, upper=False):  # FD:636-641
     return idx[idx[:, axis] == bi, :].T
 
 
-def add_regularisation(grid, cs, weights):
-    """Interior operators (G:489-510 order and /4 cross weights) then borders
+def add_regularisation(grid, cs, weights, directional=()):
+    """Interior operators (G:489-510 order and /4 cross weights), the
+    directional terms ((w, vector, name) triples, FD:222), then borders
     (FD:1052-1144)."""
     ops = {
         "dxy": (DXY_MASK, weights["dxy"] / 4),
@@ -403,6 +404,9 @@ def add_regularisation(grid, cs, weights):
         if idc.size == 0:
             continue
         cs.add(np.tile(vals, (idc.shape[0], 1)), np.zeros(idc.shape[0]), idc, w=w, name=name)
+    for dw, vector, dname in directional:
+        if dw != 0:
+            add_directional_regularisation(grid, cs, dw, vector, dname)
     borders = [
         (DXX_MASK, weights["dx"], "dx_lower", boundary_indexes(grid, 0, False)),
         (DXX_MASK, weights["dx"], "dx_upper", boundary_indexes(grid, 0, True)),
@@ -418,6 +422,37 @@ def add_regularisation(grid, cs, weights):
         cs.add(np.tile(vals, (idc.shape[0], 1)), np.zeros(idc.shape[0]), idc, w=w, name=name)
 
 
+DIRECTIONAL_FAMILIES = ("dxx", "dyy", "dzz", "dxy", "dxz", "dyz")  # FD:1262-1269 order
+
+
+def add_directional_regularisation(grid, cs, w, vector, name="directional regularisation"):  # FD:1207-1337
+    """The six interior second-derivative families again, row weight
+    w * c_f(v) at each interior node (c = vx², vy², vz², 2vxvy, 2vxvz, 2vyvz);
+    rows whose weight is not > 0 in magnitude (zero or NaN) are dropped, and
+    a family with no row left is not added."""
+    vector = None if vector is None else np.asarray(vector, dtype=float)
+    if vector is None or vector.ndim != 2 or vector.shape != (grid.n_nodes, 3):
+        return
+    masks = {"dxx": DXX_MASK, "dyy": DYY_MASK, "dzz": DZZ_MASK, "dxy": DXY_MASK, "dxz": DXZ_MASK, "dyz": DYZ_MASK}
+    centre = grid.neighbour_global_indexes(np.zeros((3, 1), dtype=int))
+    if centre is None or centre.size == 0:
+        return
+    rows = centre.T[:, 0].astype(int)
+    vx, vy, vz = vector[rows, 0], vector[rows, 1], vector[rows, 2]
+    comp = {"dxx": vx**2, "dyy": vy**2, "dzz": vz**2,
+            "dxy": 2.0 * vx * vy, "dxz": 2.0 * vx * vz, "dyz": 2.0 * vy * vz}
+    for op in DIRECTIONAL_FAMILIES:
+        idc, vals = family_rows(grid, masks[op])
+        if idc.size == 0:
+            continue
+        row_w = w * comp[op]
+        keep = np.abs(row_w) > 0.0
+        if not np.any(keep):
+            continue
+        A = np.tile(vals, (idc.shape[0], 1))
+        cs.add(A[keep], np.zeros(int(np.sum(keep))), idc[keep], w=row_w[keep], name=f"{name}_{op}")
+
+
 def resolve_weights(regularisation=None, **kwargs):
     """FD:159-175: isotropic ``regularisation`` sets dxx..dyz; every other
     keyword overwrites ``interpolation_weights``."""
@@ -430,7 +465,7 @@ def resolve_weights(regularisation=None, **kwargs):
     return w
 
 
-def assemble(grid: Grid, data: dict, weights: dict) -> ConstraintSet:
+def assemble(grid: Grid, data: dict, weights: dict, directional=()) -> ConstraintSet:
     """FD:209-223 ``setup_interpolator`` family order."""
     cs = ConstraintSet(grid.n_nodes)
     add_norm_constraints(grid, cs, data.get("normal", np.zeros((0, 7))), weights["npw"])
@@ -440,7 +475,7 @@ def assemble(grid: Grid, data: dict, weights: dict) -> ConstraintSet:
     if tangent.shape[0] > 0:
         add_gradient_orthogonal_constraints(grid, cs, tangent[:, :3], tangent[:, 3:6], weights["tpw"])
     add_interface_constraints(grid, cs, data.get("interface", np.zeros((0, 5))), weights["ipw"])
-    add_regularisation(grid, cs, weights)
+    add_regularisation(grid, cs, weights, directional)
     return cs
 
 

@@ -226,16 +226,26 @@ class TetMesh(Grid):
         return vals
 
 
-def minimise_edge_jumps(mesh: TetMesh, cs: ConstraintSet, w):  # P1:115-166
+def minimise_edge_jumps(mesh: TetMesh, cs: ConstraintSet, w, vector=None, name="edge jump"):  # P1:115-166
+    """``vector`` (one row per face, P1:129-130) replaces the face normal:
+    the directional regularisation of P1:172-178."""
     rel, shared = mesh.face_table()
     norm = mesh.face_normals(shared)
+    if vector is not None and np.asarray(vector).shape[0] == rel.shape[0]:
+        norm = np.asarray(vector, dtype=float)
     g = mesh.element_gradients()
     Dt = g[rel[:, 0]]
     Dn = g[rel[:, 1]]
     const = np.hstack([np.einsum("ij,ijk->ik", norm, Dt), -np.einsum("ij,ijk->ik", norm, Dn)])
     idc = np.hstack([mesh.elements[rel[:, 0]], mesh.elements[rel[:, 1]]])
-    cs.add(const, np.zeros(const.shape[0]), idc, w=w, name="edge jump")
+    cs.add(const, np.zeros(const.shape[0]), idc, w=w, name=name)
     return rel, shared
+
+
+def face_centres(mesh: TetMesh):
+    """P1:169-170 regularisation sample points: mean of the 3 shared face nodes."""
+    _rel, shared = mesh.face_table()
+    return mesh.nodes[shared].mean(axis=1)
 
 
 def add_norm_constraints(mesh: TetMesh, cs: ConstraintSet, points, w):  # P1:73-96
@@ -264,11 +274,15 @@ def resolve_weights(regularisation=None, **kwargs):  # P1:180-246
     return w
 
 
-def assemble(mesh: TetMesh, data: dict, weights: dict) -> ConstraintSet:
-    """P1:180-246 family order: edge jumps, (gradient: no-op), norm, value."""
+def assemble(mesh: TetMesh, data: dict, weights: dict, directional=()) -> ConstraintSet:
+    """P1:180-246 family order: edge jumps, directional terms ((w, vector,
+    name) triples, P1:229), (gradient: no-op), norm, value."""
     cs = ConstraintSet(mesh.n_nodes)
     if weights["cgw"] > 0.0:
         minimise_edge_jumps(mesh, cs, weights["cgw"])
+    for dw, vector, dname in directional:
+        if dw != 0:
+            minimise_edge_jumps(mesh, cs, dw, vector=vector, name=dname)
     add_norm_constraints(mesh, cs, data.get("normal", np.zeros((0, 7))), weights["npw"])
     add_value_constraints(mesh, cs, data.get("value", np.zeros((0, 5))), weights["cpw"])
     return cs

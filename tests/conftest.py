@@ -17,3 +17,11 @@ def golden():
     import numpy as np
 
     return np.load(os.path.join(ROOT, "tests", "golden", "reference_golden.npz"), allow_pickle=False)
+
+
+@pytest.fixture(scope="session")
+def dgolden():
+    """Directional-regularisation and gradient-orthogonal fixtures."""
+    import numpy as np
+
+    return np.load(os.path.join(ROOT, "tests", "golden", "directional_golden.npz"), allow_pickle=False)

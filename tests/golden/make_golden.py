@@ -3,6 +3,7 @@
 Run in a container where the reference source tree is available:
 
     python tests/golden/make_golden.py /path/to/LoopStructural
+    python tests/golden/make_golden.py /path/to/LoopStructural --directional
 
 It imports the reference's ``loop_interpolation`` / ``loop_common`` packages
 (``pyvista`` and ``yaml`` are stubbed: they are only used for VTK/YAML export)
@@ -237,6 +238,93 @@ def p1_case(li, TetMesh, name, cells, n_val, n_norm, seed, setup_kwargs, out):
         cls.add_constraints_to_least_squares = orig
 
 
+def _direction_field(p):
+    """A smoothly varying unit direction with exact zero components on part of
+    the grid (so that some directional rows have weight 0 and are skipped)."""
+    v = np.column_stack([np.cos(2.0 * p[:, 2]), 0.4 * np.sin(3.0 * p[:, 0]), 0.3 + p[:, 1]])
+    v[p[:, 0] < 0.25, 0] = 0.0
+    v[p[:, 2] > 0.8, 1] = 0.0
+    return v / np.linalg.norm(v, axis=1)[:, None]
+
+
+def fd_directional_case(li, StructuredGrid, name, cells, seed, out):
+    """Directional regularisation (FD:1207-1337) given as an array and as a
+    callable, plus a gradient-orthogonal family with a non-zero target
+    (FD:478-539) added after setup."""
+    from loop_interpolation._regularisation import DirectionalRegularisation
+
+    calls, (cls, orig) = _hook(li)
+    try:
+        rng = np.random.default_rng(seed)
+        grid = StructuredGrid(origin=np.zeros(3), nsteps=np.array(cells), step_vector=1.0 / np.array(cells, dtype=float))
+        interp = li.FiniteDifferenceInterpolator(grid)
+        vp = rng.uniform(0, 1, size=(30, 3))
+        val = np.column_stack([vp, _field(vp, fault=True), np.ones(30)])
+        interp.set_value_constraints(val)
+        npnt = rng.uniform(0, 1, size=(8, 3))
+        g = _grad(npnt)
+        nrm = np.column_stack([npnt, g / np.linalg.norm(g, axis=1)[:, None], np.ones(8)])
+        interp.set_normal_constraints(nrm)
+        nodes = np.asarray(grid.nodes)
+        v1 = _direction_field(nodes)
+
+        def v2(p):
+            return np.column_stack([np.zeros(len(p)), np.ones(len(p)), p[:, 2]])
+
+        reg = {"isotropic": 0.1,
+               "directional": [DirectionalRegularisation(weight=0.5, direction=v1, name="fold a"),
+                               {"weight": 0.2, "direction": v2, "name": "fold b"}]}
+        interp.setup_interpolator(regularisation=reg, cpw=1.0, npw=1.0)
+        op = rng.uniform(0, 1, size=(12, 3))
+        ov = rng.normal(size=(12, 3))
+        interp.add_gradient_orthogonal_constraints(op, ov.copy(), w=2.0, b=0.3, name="fold normalisation")
+        _families_to_arrays(interp, calls, f"{name}_", out)
+        out[f"{name}_cells"] = np.array(cells)
+        out[f"{name}_value_in"] = val
+        out[f"{name}_normal_in"] = nrm
+        out[f"{name}_dir_a"] = v1
+        out[f"{name}_dir_b"] = v2(nodes)
+        out[f"{name}_orth_points"] = op
+        out[f"{name}_orth_vectors"] = ov
+        out[f"{name}_c_direct"] = _solve_direct(interp)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
+def p1_directional_case(li, TetMesh, name, cells, seed, out):
+    """P1 directional regularisation (P1:115-178): edge-jump rows whose
+    normal is the given per-face vector."""
+    calls, (cls, orig) = _hook(li)
+    try:
+        rng = np.random.default_rng(seed)
+        mesh = TetMesh(origin=np.zeros(3), nsteps_cells=np.array(cells), step_vector=1.0 / np.array(cells, dtype=float))
+        interp = li.P1Interpolator(mesh)
+        vp = rng.uniform(0.05, 0.95, size=(25, 3))
+        val = np.column_stack([vp, _field(vp, fault=True), np.ones(25)])
+        interp.set_value_constraints(val)
+        centres = interp.get_regularisation_sample_points()
+        vec = _direction_field(centres)
+        interp.setup_interpolator(cgw=0.1, cpw=1.0, npw=1.0,
+                                  directional_regularisation={"weight": 0.3, "direction": vec, "name": "fold p1"})
+        _families_to_arrays(interp, calls, f"{name}_", out)
+        out[f"{name}_cells"] = np.array(cells)
+        out[f"{name}_value_in"] = val
+        out[f"{name}_dir"] = vec
+        out[f"{name}_c_direct"] = _solve_direct(interp)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
+def main_directional(root):
+    li, StructuredGrid, TetMesh = _import_reference(root)
+    out = {}
+    fd_directional_case(li, StructuredGrid, "fd_dir", (7, 6, 8), seed=3, out=out)
+    p1_directional_case(li, TetMesh, "p1_dir", (3, 4, 3), seed=4, out=out)
+    path = os.path.join(HERE, "directional_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")
+
+
 def main(root):
     li, StructuredGrid, TetMesh = _import_reference(root)
     out = {}
@@ -254,4 +342,10 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # usage: make_golden.py [reference root] [--directional]
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else "/root/reference"
+    if "--directional" in sys.argv:
+        main_directional(root)
+    else:
+        main(root)

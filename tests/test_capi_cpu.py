@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.ls_abi_version() == 1
+    assert lib.ls_abi_version() == 2
 
 
 @pytest.mark.parametrize("cells", [(5, 5, 5), (3, 4, 2), (2, 5, 6), (1, 4, 4), (8, 6, 12)])
