@@ -621,6 +621,68 @@ def p1_arm(args):
     return out
 
 
+def fold_directions(nodes):
+    """Fold-like direction fields at the nodes: across the fold (rotating with
+    x), the fold axis (y) and the axial-plane direction (their cross product)."""
+    ang = 2.0 * np.pi * nodes[:, 0]
+    across = np.column_stack([np.cos(ang), np.zeros(len(ang)), np.sin(ang)])
+    axis = np.zeros_like(across)
+    axis[:, 1] = 1.0
+    return across, np.cross(across, axis), axis
+
+
+def directional_arm(args):
+    """FD 128^3 nodes (2.1 M DOF) with directional regularisation: isotropic
+    0.01 plus three fold-like directional terms (weights 0.1 / 0.01 / 0.01, as
+    the reference's fold regularisation defaults), 5,000 values + 1,000
+    normals of the faulted field; mixed multigrid-PCG vs FP64 Jacobi-CG to the
+    same rtol, then value + gradient at 10^6 points."""
+    import torch
+
+    import loopstructural_gb300 as L
+
+    L.build()
+    n = 128
+    cells, val, nrm = make_workload(n_nodes=n, n_value=5000, n_normal=1000)
+    grid = L.StructuredGrid(origin=np.zeros(3), nsteps=cells, step_vector=1.0 / cells)
+    across, plane, axis = fold_directions(grid.nodes)
+    terms = [L.DirectionalRegularisation(0.1, across, "fold regularisation 1"),
+             L.DirectionalRegularisation(0.01, plane, "fold regularisation 2"),
+             L.DirectionalRegularisation(0.01, axis, "fold regularisation 3")]
+    out = {"metric": "FD 128^3 directional (fold) regularisation setup + solve + evaluate (s)", "impl": "gb300",
+           "unit": "s", "higher_is_better": False, "data": "synthetic (seeded faulted layered field, fold-like directions)",
+           "config": {"workload": "FD 128^3 nodes, isotropic 0.01 + 3 directional terms, 5000 values + 1000 normals, "
+                                  "mixed MG-PCG to rtol %g, 1e6-point evaluation" % args.rtol}}
+    q = np.random.default_rng(1).uniform(0, 1, size=(1_000_000, 3))
+    res = {}
+    for label, prec, pc in (("warm", "mixed", "mg"), ("mixed_mg", "mixed", "mg"), ("fp64_jacobi", "fp64", "jacobi")):
+        interp = L.FiniteDifferenceInterpolator(grid)
+        interp.set_value_constraints(val)
+        interp.set_normal_constraints(nrm)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        report = interp.setup_interpolator(regularisation={"isotropic": 0.01, "directional": terms}, cpw=1.0, npw=1.0)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        interp.solve_system("cg", solver_kwargs={"rtol": args.rtol, "atol": 0.0, "precision": prec,
+                                                 "preconditioner": pc, "maxiter": args.maxiter})
+        t2 = time.perf_counter()
+        v = interp.evaluate_value(q)
+        gr = interp.evaluate_gradient(q)
+        t3 = time.perf_counter()
+        t = interp.get_last_solve_timing()
+        res[label] = {"setup_s": round(t1 - t0, 3), "solve_s": round(t2 - t1, 3), "eval_s": round(t3 - t2, 3),
+                      "iterations": int(t["iterations"]), "status": int(t["status"]), "c": interp.c.copy()}
+        del v, gr
+    m, j = res["mixed_mg"], res["fp64_jacobi"]
+    out.update({"value": round(m["setup_s"] + m["solve_s"] + m["eval_s"], 3),
+                "mixed_mg": {k: v for k, v in m.items() if k != "c"},
+                "fp64_jacobi": {k: v for k, v in j.items() if k != "c"},
+                "coef_rel_diff_mixed_vs_fp64": float(np.linalg.norm(m["c"] - j["c"]) / np.linalg.norm(j["c"])),
+                "directional_rows": {k: int(v) for k, v in report.items() if k.startswith("fold")}})
+    return out
+
+
 def mgprofile_arm(args):
     """Per-level device times of the multigrid V-cycle parts on the headline
     system (the profiling entry used for kernel captures)."""
@@ -655,7 +717,7 @@ def main():
                     help="profiling runs: no nvidia-smi clock sampler child process")
     ap.add_argument("--skip-legs", action="store_true",
                     help="profiling runs: skip the FP64 leg, the e2e leg and the CPU baseline")
-    ap.add_argument("--workload", default="headline", choices=["headline", "ensemble", "adjoint", "p1", "mgprofile"],
+    ap.add_argument("--workload", default="headline", choices=["headline", "ensemble", "adjoint", "p1", "directional", "mgprofile"],
                     help="secondary workloads print their own line (ensembles, adjoint gradient, per-level "
                          "multigrid kernel times)")
     ap.add_argument("--models", type=int, default=256)
@@ -671,7 +733,7 @@ def main():
                 torch.distributed.init_process_group("nccl")
             out = ensemble_arm(args, rank, world)
         else:
-            arms = {"adjoint": adjoint_arm, "p1": p1_arm, "mgprofile": mgprofile_arm}
+            arms = {"adjoint": adjoint_arm, "p1": p1_arm, "directional": directional_arm, "mgprofile": mgprofile_arm}
             out = arms[args.workload](args) if rank == 0 else None
         if rank == 0:
             print(json.dumps(out))
