@@ -8,6 +8,7 @@ kernels behind the C ABI in include/ls_gb300.h.
 from . import constraints
 from ._lib import ExtensionUnavailable, LsError
 from .constraints import ValidationError
+from .fold import FDFoldInterpolator
 from .interpolators import FiniteDifferenceInterpolator
 from .p1 import P1Interpolator, PiecewiseLinearInterpolator
 from .regularisation import DirectionalRegularisation, RegularisationConfig
@@ -15,6 +16,7 @@ from .supports import StructuredGrid, TetMesh
 
 __all__ = [
     "FiniteDifferenceInterpolator",
+    "FDFoldInterpolator",
     "P1Interpolator",
     "PiecewiseLinearInterpolator",
     "StructuredGrid",

@@ -63,7 +63,12 @@ def gpu_interpolator_classes(li):
             eng.add_ridge_regulatisation = self.add_ridge_regulatisation
             eng.setup_interpolator(**kwargs)
             self.interpolation_weights = dict(eng.interpolation_weights)
-            # row counts for the reference's diagnostics report (matrix shape only)
+            self._mirror_families(eng)
+            self.up_to_date = False
+            return self.finalize_setup_diagnostics_report()
+
+        def _mirror_families(self, eng):
+            """Row counts for the reference's diagnostics report (matrix shape only)."""
             self.constraints = {}
             for name, fam in eng.constraints.items():
                 self.constraints[name] = {"matrix": SimpleNamespace(shape=(fam.n_rows, self.dof)), "b": None,
@@ -71,8 +76,29 @@ def gpu_interpolator_classes(li):
             for name, (rows, w) in eng.regularisation_families.items():
                 self.constraints[name] = {"matrix": SimpleNamespace(shape=(rows, self.dof)), "b": None,
                                           "w": np.full(rows, w)}
+            for name, (rows, _t, _f) in eng.directional_families.items():
+                self.constraints[name] = {"matrix": SimpleNamespace(shape=(rows, self.dof)), "b": None,
+                                          "w": None}
+
+        # families added after setup (fold constraints, FF:93-237) go to the engine
+        def add_gradient_orthogonal_constraints(self, points, vectors, w=1.0, b=0, name="gradient orthogonal"):
+            eng = self._engine()
+            eng.add_gradient_orthogonal_constraints(points, vectors, w=w, b=b, name=name)
+            self._mirror_families(eng)
             self.up_to_date = False
-            return self.finalize_setup_diagnostics_report()
+
+        def minimise_directional_gradient_change(self, w, vector, name="directional regularisation"):
+            eng = self._engine()
+            eng.minimise_directional_gradient_change(w, vector, name=name)
+            self._mirror_families(eng)
+            self.up_to_date = False
+
+        def add_directional_regularisation(self, directional_regularisation):
+            eng = self._engine()
+            terms = eng.add_directional_regularisation(directional_regularisation)
+            self._mirror_families(eng)
+            self.up_to_date = False
+            return terms
 
         def solve_system(self, solver=None, tol=None, solver_kwargs=None):
             eng = self._engine()
@@ -134,6 +160,21 @@ def _p1_mixin(fd_cls):
             return self.finalize_setup_diagnostics_report()
 
     return _Delegate
+
+
+def gpu_fold_interpolator_class(li):
+    """Subclass of the reference's FDFoldInterpolator (_fd_fold_interpolator.py)
+    whose base setup, fold families, solve and evaluation run on the GPU: its
+    own setup_interpolator / add_fold_constraints (reference code) call the
+    GPU FD class's setup and add_* methods through the method order."""
+    from loop_interpolation._fd_fold_interpolator import FDFoldInterpolator
+
+    gpu_fd, _ = gpu_interpolator_classes(li)
+
+    class GpuFDFoldInterpolator(FDFoldInterpolator, gpu_fd):
+        """Reference FDFoldInterpolator on the GB300 engine."""
+
+    return GpuFDFoldInterpolator
 
 
 def register(li):

@@ -453,6 +453,57 @@ def add_directional_regularisation(grid, cs, w, vector, name="directional regula
         cs.add(A[keep], np.zeros(int(np.sum(keep))), idc[keep], w=row_w[keep], name=f"{name}_{op}")
 
 
+def fold_norm_target(fold, normals, fold_norm=-1.0, dgz_alignment="warn"):
+    """_fold_norm_alignment.py:9-118: the grad . dgz target, sign-flipped under
+    'correct' when the median unit dot(dgz, normal) at the normal points is
+    below -0.2."""
+    target = float(-1.0 if fold_norm is None else fold_norm)
+    mode = "warn" if dgz_alignment is None else str(dgz_alignment).strip().lower()
+    normals = np.asarray(normals, dtype=float)
+    if mode == "none" or normals.ndim != 2 or normals.shape[0] == 0 or normals.shape[1] < 6:
+        return target
+    _, _, dgz = fold.get_deformed_orientation(normals[:, :3])
+    dgz = np.asarray(dgz, dtype=float)
+    vec = normals[:, 3:6]
+    nn, dn = np.linalg.norm(vec, axis=1), np.linalg.norm(dgz, axis=1)
+    ok = np.all(np.isfinite(vec), axis=1) & np.all(np.isfinite(dgz), axis=1) & (nn > 1e-12) & (dn > 1e-12)
+    if not np.any(ok):
+        return target
+    med = float(np.median(np.einsum("ij,ij->i", dgz[ok] / dn[ok, None], vec[ok] / nn[ok, None])))
+    if med < -0.2 and mode == "correct":
+        target *= -1.0
+    return target
+
+
+def add_fold_constraints(grid, cs, fold, normals, fold_orientation=10.0, fold_axis_w=10.0,
+                         fold_regularisation=(0.1, 0.01, 0.01), fold_normalisation=1.0, fold_norm=-1.0,
+                         dgz_alignment="warn", mask_fn=None):
+    """_fd_fold_interpolator.py:93-237 (FDFoldInterpolator.add_fold_constraints)."""
+    nodes = grid.nodes
+    deformed, axis, dgz = fold.get_deformed_orientation(nodes)
+    weight = np.ones(grid.n_nodes)
+    if mask_fn is not None:
+        weight[mask_fn(nodes)] = 0.0
+    active = weight > 0.0
+    pos = nodes[active]
+    if fold_orientation is not None:
+        add_gradient_orthogonal_constraints(grid, cs, pos, np.array(deformed)[active], fold_orientation,
+                                            name="fold orientation")
+    if fold_axis_w is not None:
+        add_gradient_orthogonal_constraints(grid, cs, pos, np.array(axis)[active], fold_axis_w, name="fold axis")
+    if fold_normalisation is not None:
+        target = fold_norm_target(fold, normals, fold_norm, dgz_alignment)
+        add_gradient_orthogonal_constraints(grid, cs, pos, np.array(dgz)[active], fold_normalisation, b=target,
+                                            name="fold normalisation")
+    if fold_regularisation is not None:
+        for w, v, name in zip(fold_regularisation, (dgz, deformed, axis),
+                              ("fold regularisation 1", "fold regularisation 2", "fold regularisation 3")):
+            v = np.asarray(v, dtype=float).copy()
+            v[~active] = 0.0
+            if w != 0:
+                add_directional_regularisation(grid, cs, w, v, name)
+
+
 def resolve_weights(regularisation=None, **kwargs):
     """FD:159-175: isotropic ``regularisation`` sets dxx..dyz; every other
     keyword overwrites ``interpolation_weights``."""

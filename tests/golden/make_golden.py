@@ -315,11 +315,64 @@ def p1_directional_case(li, TetMesh, name, cells, seed, out):
         cls.add_constraints_to_least_squares = orig
 
 
+class SyntheticFold:
+    """A fold geometry provider with the reference FoldEvent's
+    ``get_deformed_orientation(points) -> (deformed_orientation, fold_axis,
+    dgz)`` contract: the fold axis plunges gently along y, the across-fold
+    direction dgz rotates with x, the deformed orientation completes the
+    frame.  Plain numpy, so both implementations see identical vectors."""
+
+    def get_deformed_orientation(self, points):
+        p = np.asarray(points, dtype=float)
+        ang = 1.5 * np.pi * p[:, 0]
+        dgz = np.column_stack([np.sin(ang), np.zeros(len(p)), -np.cos(ang)])
+        axis = np.tile([0.0, 1.0, 0.15], (len(p), 1))
+        axis /= np.linalg.norm(axis, axis=1)[:, None]
+        deformed = np.cross(dgz, axis)
+        return deformed, axis, dgz
+
+
+def fold_case_weights():
+    """The fold_weights of the fd_fold case (shared with the tests)."""
+    return {"fold_orientation": 5.0, "fold_axis_w": 3.0, "fold_regularisation": [0.2, 0.05, 0.02],
+            "fold_normalisation": 1.5, "fold_norm": -1.0, "dgz_alignment": "correct",
+            "mask_fn": lambda p: p[:, 2] > 0.85}
+
+
+def fd_fold_case(li, StructuredGrid, name, cells, seed, out):
+    """FDFoldInterpolator (_fd_fold_interpolator.py) with a synthetic fold,
+    a node mask and dgz alignment correction."""
+    from loop_interpolation._fd_fold_interpolator import FDFoldInterpolator
+
+    calls, (cls, orig) = _hook(li)
+    try:
+        rng = np.random.default_rng(seed)
+        grid = StructuredGrid(origin=np.zeros(3), nsteps=np.array(cells), step_vector=1.0 / np.array(cells, dtype=float))
+        interp = FDFoldInterpolator(grid, fold=SyntheticFold())
+        vp = rng.uniform(0, 1, size=(25, 3))
+        val = np.column_stack([vp, _field(vp), np.ones(25)])
+        interp.set_value_constraints(val)
+        npnt = rng.uniform(0, 1, size=(10, 3))
+        g = _grad(npnt)
+        nrm = np.column_stack([npnt, g / np.linalg.norm(g, axis=1)[:, None], np.ones(10)])
+        interp.set_normal_constraints(nrm)
+        fold_weights = fold_case_weights()
+        interp.setup_interpolator(regularisation=0.05, cpw=1.0, npw=1.0, fold_weights=fold_weights)
+        _families_to_arrays(interp, calls, f"{name}_", out)
+        out[f"{name}_cells"] = np.array(cells)
+        out[f"{name}_value_in"] = val
+        out[f"{name}_normal_in"] = nrm
+        out[f"{name}_c_direct"] = _solve_direct(interp)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
 def main_directional(root):
     li, StructuredGrid, TetMesh = _import_reference(root)
     out = {}
     fd_directional_case(li, StructuredGrid, "fd_dir", (7, 6, 8), seed=3, out=out)
     p1_directional_case(li, TetMesh, "p1_dir", (3, 4, 3), seed=4, out=out)
+    fd_fold_case(li, StructuredGrid, "fd_fold", (8, 7, 9), seed=5, out=out)
     path = os.path.join(HERE, "directional_golden.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")

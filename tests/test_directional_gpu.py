@@ -22,7 +22,8 @@ from loopstructural_gb300 import _lib, fd  # noqa: E402
 from oracle import fd_oracle as fdo  # noqa: E402
 
 from test_fd_gpu import _check_operator, _csr, _grid  # noqa: E402
-from test_oracle_directional import fd_dir_case, p1_dir_case  # noqa: E402
+from test_oracle_directional import fd_dir_case, fd_fold_oracle, p1_dir_case  # noqa: E402
+from golden.make_golden import SyntheticFold, fold_case_weights  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -215,3 +216,46 @@ def test_noalloc_rejects_directional_systems():
     s.d_dir = _lib.ptr(w)
     x = torch.zeros(125, dtype=torch.float64, device=_lib.device())
     assert lib.ls_fd_apply_noalloc(C.byref(s), _lib.ptr(x), _lib.ptr(x), None, None) == -1
+
+
+def _fold_interp(g):
+    cells = g["fd_fold_cells"]
+    interp = L.FDFoldInterpolator(_grid(cells), fold=SyntheticFold())
+    interp.set_value_constraints(g["fd_fold_value_in"])
+    interp.set_normal_constraints(g["fd_fold_normal_in"])
+    report = interp.setup_interpolator(regularisation=0.05, cpw=1.0, npw=1.0, fold_weights=fold_case_weights())
+    return interp, report
+
+
+def test_fd_fold_interpolator_matches_reference(dgolden):
+    interp, report = _fold_interp(dgolden)
+    names = [str(s) for s in dgolden["fd_fold_family_names"]]
+    assert set(report) == set(names)
+    for nm in names:
+        got = _rows(interp, nm)
+        np.testing.assert_array_equal(got["idc"], dgolden[f"fd_fold_fam_{nm}_idc"], err_msg=nm)
+        m = _csr(got["idc"], got["A"], interp.dof)
+        np.testing.assert_allclose(m.data, dgolden[f"fd_fold_fam_{nm}_data"], rtol=1e-15, atol=1e-15, err_msg=nm)
+        np.testing.assert_allclose(got["B"], dgolden[f"fd_fold_fam_{nm}_b"], rtol=1e-15, atol=1e-15, err_msg=nm)
+        np.testing.assert_allclose(got["w"], dgolden[f"fd_fold_fam_{nm}_w"], rtol=1e-15, atol=0, err_msg=nm)
+        assert report[nm] == got["idc"].shape[0], nm
+    system = interp._build_system()
+    _g, cs = fd_fold_oracle(dgolden)
+    A, _b = cs.matrix()
+    _check_operator(system, A, x_seed=9)
+    system.close()
+    for prec, pc, tol in (("mixed", "mg", 1e-8), ("fp64", "jacobi", 1e-6)):
+        assert interp.solve_system("cg", solver_kwargs={"rtol": 1e-14, "atol": 0.0, "precision": prec,
+                                                        "preconditioner": pc, "maxiter": 400000})
+        ref = dgolden["fd_fold_c_direct"]
+        err = np.linalg.norm(interp.c - ref) / np.linalg.norm(ref)
+        assert err <= tol, (prec, err, interp.get_last_solve_timing())
+
+
+def test_fd_fold_needs_a_fold():
+    interp = L.FDFoldInterpolator(_grid((4, 4, 4)))
+    with pytest.raises(RuntimeError):
+        interp.setup_interpolator()
+    interp.fold = SyntheticFold()
+    with pytest.raises(ValueError):
+        interp.setup_interpolator(fold_weights={"dgz_alignment": "sideways"})

@@ -87,3 +87,28 @@ def test_gpu_p1_subclass_keeps_reference_api_and_fails_loudly_without_gpu(li):
         pytest.skip("a GPU is visible")
     with pytest.raises(L.ExtensionUnavailable):
         interp.setup_interpolator(cgw=0.1)
+
+
+def test_gpu_fold_subclass_routes_fold_families_to_the_engine(li):
+    import torch
+
+    import loopstructural_gb300 as L
+    from loopstructural_gb300 import integration
+
+    gpu_fold = integration.gpu_fold_interpolator_class(li)
+    from loop_interpolation._fd_fold_interpolator import FDFoldInterpolator
+
+    assert issubclass(gpu_fold, FDFoldInterpolator)
+    gpu_fd = gpu_fold.__mro__[2]
+    # the reference fold code reaches the GPU setup and add_* methods
+    for meth in ("setup_interpolator", "add_gradient_orthogonal_constraints", "add_directional_regularisation",
+                 "solve_system", "_evaluate_value_local"):
+        assert getattr(gpu_fold, meth) is getattr(FDFoldInterpolator, meth) or meth in gpu_fd.__dict__, meth
+    assert gpu_fold.add_gradient_orthogonal_constraints is gpu_fd.add_gradient_orthogonal_constraints
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    grid = li.StructuredGrid(origin=np.zeros(3), nsteps=np.array([5, 5, 5]), step_vector=np.ones(3) * 0.2)
+    interp = gpu_fold(grid, fold=object())
+    interp.set_value_constraints(np.array([[0.5, 0.5, 0.5, 1.0]]))
+    with pytest.raises(L.ExtensionUnavailable):
+        interp.setup_interpolator(regularisation=0.1)

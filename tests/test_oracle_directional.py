@@ -6,7 +6,7 @@ import numpy as np
 from oracle import fd_oracle as fdo
 from oracle import p1_oracle as p1o
 
-from golden.make_golden import _direction_field
+from golden.make_golden import SyntheticFold, _direction_field, fold_case_weights
 from test_oracle_golden import _check_families
 
 
@@ -56,3 +56,21 @@ def test_p1_directional_families_match_reference(dgolden):
     c = fdo.solve_direct(A, b)
     ref = dgolden["p1_dir_c_direct"]
     assert np.linalg.norm(c - ref) <= 1e-9 * np.linalg.norm(ref)
+
+
+def fd_fold_oracle(g):
+    cells = g["fd_fold_cells"]
+    grid = fdo.Grid(np.zeros(3), cells, 1.0 / cells.astype(float))
+    data = {"value": g["fd_fold_value_in"], "normal": g["fd_fold_normal_in"]}
+    cs = fdo.assemble(grid, data, fdo.resolve_weights(regularisation=0.05, cpw=1.0, npw=1.0))
+    fdo.add_fold_constraints(grid, cs, SyntheticFold(), g["fd_fold_normal_in"], **fold_case_weights())
+    return grid, cs
+
+
+def test_fd_fold_families_and_solution_match_reference(dgolden):
+    grid, cs = fd_fold_oracle(dgolden)
+    _check_families(dgolden, "fd_fold_", cs, grid.n_nodes)
+    A, b = cs.matrix()
+    c = fdo.solve_direct(A, b)
+    ref = dgolden["fd_fold_c_direct"]
+    assert np.linalg.norm(c - ref) <= 1e-10 * np.linalg.norm(ref)
