@@ -683,6 +683,40 @@ def directional_arm(args):
     return out
 
 
+def isosurface_arm(args):
+    """Isosurface extraction (marching tetrahedra on the grid nodes) at 256^3
+    nodes: three levels of the faulted layered field, node values resident on
+    the device; device time of classify + scans + emit per surface."""
+    import torch
+
+    import loopstructural_gb300 as L
+    from loopstructural_gb300 import fd
+
+    L.build()
+    n = 256
+    grid = L.StructuredGrid(origin=np.zeros(3), nsteps=np.array([n - 1] * 3), step_vector=np.ones(3) / (n - 1))
+    x = np.arange(n) / (n - 1)
+    zz, yy, xx = np.meshgrid(x, x, x, indexing="ij")
+    pts = np.column_stack([xx.ravel(), yy.ravel(), zz.ravel()])
+    vals = torch.from_numpy(field(pts)).cuda()
+    levels = (0.3, 0.5, 0.7)
+    for lv in levels:  # warm-up
+        fd.isosurface(grid, vals, lv)
+    torch.cuda.synchronize()
+    out = {"metric": "isosurface extraction at 256^3 nodes (ms per surface)", "impl": "gb300", "unit": "ms",
+           "higher_is_better": False, "data": "synthetic (faulted layered field on the nodes)",
+           "config": {"workload": "256^3 nodes (16.8 M), levels 0.3/0.5/0.7, vertices + normals + triangles to host"}}
+    per = []
+    for lv in levels:
+        t0 = time.perf_counter()
+        verts, tris, _n = fd.isosurface(grid, vals, lv)
+        per.append({"level": lv, "ms": round((time.perf_counter() - t0) * 1e3, 2), "vertices": int(verts.shape[0]),
+                    "triangles": int(tris.shape[0])})
+    out["surfaces"] = per
+    out["value"] = round(float(np.mean([p["ms"] for p in per])), 2)
+    return out
+
+
 def mgprofile_arm(args):
     """Per-level device times of the multigrid V-cycle parts on the headline
     system (the profiling entry used for kernel captures)."""
@@ -717,7 +751,7 @@ def main():
                     help="profiling runs: no nvidia-smi clock sampler child process")
     ap.add_argument("--skip-legs", action="store_true",
                     help="profiling runs: skip the FP64 leg, the e2e leg and the CPU baseline")
-    ap.add_argument("--workload", default="headline", choices=["headline", "ensemble", "adjoint", "p1", "directional", "mgprofile"],
+    ap.add_argument("--workload", default="headline", choices=["headline", "ensemble", "adjoint", "p1", "directional", "isosurface", "mgprofile"],
                     help="secondary workloads print their own line (ensembles, adjoint gradient, per-level "
                          "multigrid kernel times)")
     ap.add_argument("--models", type=int, default=256)
@@ -733,7 +767,8 @@ def main():
                 torch.distributed.init_process_group("nccl")
             out = ensemble_arm(args, rank, world)
         else:
-            arms = {"adjoint": adjoint_arm, "p1": p1_arm, "directional": directional_arm, "mgprofile": mgprofile_arm}
+            arms = {"adjoint": adjoint_arm, "p1": p1_arm, "directional": directional_arm,
+                    "isosurface": isosurface_arm, "mgprofile": mgprofile_arm}
             out = arms[args.workload](args) if rank == 0 else None
         if rank == 0:
             print(json.dumps(out))

@@ -356,6 +356,27 @@ int ls_p1_point_rows(const ls_grid3 *mesh, int kind, const double *d_pts, int64_
 int ls_p1_eval_points(const ls_grid3 *mesh, const double *d_c, const double *d_pts, int64_t npts, int64_t ld,
                       double *d_value, double *d_grad, void *stream);
 
+/* ------------------------------------------------------------------ */
+/* Isosurfaces of a solved FD field (DI:1395-1405 surfaces(value))      */
+/* ------------------------------------------------------------------ */
+
+/* The level set {f = iso} of the node values d_values (one per grid node,
+ * node order i + nx (j + ny k)) under the piecewise-linear interpolant on the
+ * Freudenthal triangulation of the cells (6 tetrahedra per cell along the
+ * main diagonal): one vertex per crossing edge (shared by all its
+ * triangles), triangles wound with their normal towards increasing f.  The
+ * reference contours the same node values with VTK's marching cubes.
+ * ls_iso_extract classifies the cells and returns the vertex and triangle
+ * counts (host, after a stream sync); ls_iso_copy writes d_verts (V x 3
+ * FP64 coordinates), d_normals (V x 3, unit gradient direction; may be NULL)
+ * and d_tris (T x 3 int64 vertex indices); d_values must stay valid until
+ * ls_iso_copy has run.  NaN node values exclude their edges and cells. */
+typedef struct ls_iso ls_iso;
+int ls_iso_extract(const ls_grid3 *grid, const double *d_values, double iso, ls_iso **out, int64_t *h_nverts,
+                   int64_t *h_ntris, void *stream);
+int ls_iso_copy(ls_iso *h, double *d_verts, double *d_normals, int64_t *d_tris, void *stream);
+int ls_iso_destroy(ls_iso *h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -321,3 +321,26 @@ def eval_lattice(support, c_dev, origin, step, counts, value=True, gradient=True
     _lib.check(lib.ls_fd_eval_lattice(C.byref(g), _lib.ptr(c_dev), C.byref(o3), C.byref(s3), C.byref(n3), _lib.ptr(v),
                                       _lib.ptr(gr), _lib.stream_ptr()))
     return v, gr
+
+
+def isosurface(support, values, iso: float, normals: bool = True):
+    """Level set {f = iso} of node values on a StructuredGrid (GPU): returns
+    (vertices (V, 3), triangles (T, 3) int64, normals (V, 3) or None) as host
+    arrays.  ``values`` is a device tensor of one value per node."""
+    torch = _torch()
+    lib = _lib.load()
+    values = values.to(dtype=torch.float64).contiguous()
+    g = support.grid3()
+    h = C.c_void_p()
+    nv, nt = C.c_int64(0), C.c_int64(0)
+    _lib.check(lib.ls_iso_extract(C.byref(g), _lib.ptr(values), float(iso), C.byref(h), C.byref(nv), C.byref(nt),
+                                  _lib.stream_ptr()))
+    try:
+        verts = torch.empty((nv.value, 3), dtype=torch.float64, device=values.device)
+        nrm = torch.empty((nv.value, 3), dtype=torch.float64, device=values.device) if normals else None
+        tris = torch.empty((nt.value, 3), dtype=torch.int64, device=values.device)
+        _lib.check(lib.ls_iso_copy(h, _lib.ptr(verts), _lib.ptr(nrm), _lib.ptr(tris), _lib.stream_ptr()))
+        out = (verts.cpu().numpy(), tris.cpu().numpy(), nrm.cpu().numpy() if normals else None)
+    finally:
+        lib.ls_iso_destroy(h)
+    return out

@@ -599,6 +599,25 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
             return np.zeros((0, 3))
         return fd.eval_points(self.support, self._c_device(), loc, value=False, gradient=True)[1]
 
+    def surfaces(self, value, name="surface", **kwargs):
+        """Isosurface(s) of the solved field on the grid nodes (DI:1395-1405):
+        a list with one Surface per isovalue that the field crosses (an empty
+        list when it crosses none).  ``value`` is a number or a sequence."""
+        from .surface import Surface
+
+        self.update()
+        values = np.atleast_1d(np.asarray(value, dtype=float))
+        out = []
+        for v in values:
+            verts, tris, nrm = fd.isosurface(self.support, self._c_device(), float(v))
+            if verts.shape[0] == 0:
+                continue
+            if self.bounding_box is not None and hasattr(self.bounding_box, "reproject"):
+                verts = self.bounding_box.reproject(verts)
+            out.append(Surface(vertices=verts, triangles=tris, normals=nrm, name=name,
+                               values=np.full(verts.shape[0], float(v))))
+        return out
+
     def evaluate_lattice(self, origin, step, counts, value=True, gradient=True):
         """Dense-lattice evaluation on the device (K7 lattice kernel); returns
         device tensors (value (Q,), gradient (Q, 3)), i fastest."""
