@@ -24,7 +24,8 @@
 // tetrahedron with 1 or 3 vertices above iso gives one triangle, with 2 a
 // quadrilateral split in two; triangles are wound so that their normal points
 // towards increasing f.  Vertex normals: the central-difference node
-// gradients interpolated along the edge, normalised.
+// gradients interpolated along the edge, normalised (one-sided next to NaN
+// nodes; the edge direction where no gradient is left).
 //
 // Passes: classify (node masks, per-cell triangle counts), two exclusive
 // scans (3-phase, multi-block), emit.
@@ -221,17 +222,26 @@ struct EmitArgs {
   int64_t *tris;    // T x 3
 };
 
-// index-space gradient at node (i, j, k): central differences, one-sided on faces
+// gradient at node (i, j, k): central differences, one-sided on faces and
+// next to NaN nodes, 0 along an axis with no finite pair
 __device__ void node_gradient(const EmitArgs &a, int i, int j, int k, double g[3]) {
   const int nx = a.gr.nx, ny = a.gr.ny, nz = a.gr.nz;
   const int c[3] = {i, j, k}, lim[3] = {nx, ny, nz};
   const int64_t st[3] = {1, nx, (int64_t)nx * ny};
   const int64_t p = i + (int64_t)nx * (j + (int64_t)ny * k);
+  const double fp = a.f[p];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    const int lo = c[d] > 0 ? -1 : 0, hi = c[d] + 1 < lim[d] ? 1 : 0;
-    const double span = (double)(hi - lo);
-    g[d] = span > 0 ? (a.f[p + hi * st[d]] - a.f[p + lo * st[d]]) / (span * a.gr.h[d]) : 0.0;
+    const double fm = c[d] > 0 ? a.f[p - st[d]] : NAN;
+    const double fq = c[d] + 1 < lim[d] ? a.f[p + st[d]] : NAN;
+    double v = 0.0;
+    if (!isnan(fm) && !isnan(fq))
+      v = (fq - fm) / (2.0 * a.gr.h[d]);
+    else if (!isnan(fq) && !isnan(fp))
+      v = (fq - fp) / a.gr.h[d];
+    else if (!isnan(fm) && !isnan(fp))
+      v = (fp - fm) / a.gr.h[d];
+    g[d] = v;
   }
 }
 
@@ -272,7 +282,14 @@ __global__ void iso_emit_kernel(EmitArgs a) {
             nv[c] = g0[c] + t * (g1[c] - g0[c]);
             len += nv[c] * nv[c];
           }
-          len = len > 0.0 ? 1.0 / sqrt(len) : 0.0;
+          if (!(len > 0.0)) {  // no usable node gradient: the edge direction, towards increasing f
+            const double s = f1 > f0 ? 1.0 : -1.0;
+            nv[0] = s * di / a.gr.h[0];
+            nv[1] = s * dj / a.gr.h[1];
+            nv[2] = s * dk / a.gr.h[2];
+            len = nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2];
+          }
+          len = 1.0 / sqrt(len);
 #pragma unroll
           for (int c = 0; c < 3; ++c) a.normals[3 * vid + c] = nv[c] * len;
         }
