@@ -31,27 +31,34 @@ struct DirView {
 
 constexpr int kDirFamilies = 6;
 
-// (sum_f D_f^T W_f D_f p) at node (i, j, k)
+// (sum_f D_f^T W_f D_f p) at node (i, j, k).  The 25 distinct p values the
+// 21 rows around the node touch (offsets within 2 along each axis and the
+// (+-2, +-2) corners of the three planes) are loaded once (0 outside the
+// grid: they only meet rows whose centre is not interior, whose weight is 0).
 template <typename T>
 __device__ __forceinline__ T dir_node(const DirView<T> &d, const T *__restrict__ p, int i, int j, int k) {
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int64_t n = (int64_t)nx * ny * nz;
   const int g = (k * ny + j) * nx + i;
   const int st[3] = {1, nx, nx * ny};
+  const int c[3] = {i, j, k}, lim[3] = {nx, ny, nz};
+  auto inb = [&](int a, int off) { return c[a] + off >= 0 && c[a] + off < lim[a]; };
   // is the row centre (i, j, k) + (a0, a1, a2) an interior node?
   auto interior = [&](int a0, int a1, int a2) {
     return (i + a0 >= 1) & (i + a0 <= nx - 2) & (j + a1 >= 1) & (j + a1 <= ny - 2) & (k + a2 >= 1) & (k + a2 <= nz - 2);
   };
+  const T pc = __ldg(p + g);
   T acc = 0;
 #pragma unroll
   for (int f = 0; f < 3; ++f) {
-    const int s = st[f];
+    T v[5];
+#pragma unroll
+    for (int o = -2; o <= 2; ++o) v[o + 2] = o == 0 ? pc : (inb(f, o) ? __ldg(p + g + o * st[f]) : (T)0);
 #pragma unroll
     for (int t = -1; t <= 1; ++t) {  // node g is tap t of the row centred at m = g - t e_f
       if (interior(f == 0 ? -t : 0, f == 1 ? -t : 0, f == 2 ? -t : 0)) {
-        const int m = g - t * s;
-        const T D = __ldg(p + m - s) - (T)2 * __ldg(p + m) + __ldg(p + m + s);
-        acc += (t == 0 ? (T)-2 : (T)1) * __ldg(d.w + f * n + m) * D;
+        const T D = v[1 - t] - (T)2 * v[2 - t] + v[3 - t];
+        acc += (t == 0 ? (T)-2 : (T)1) * __ldg(d.w + f * n + (g - t * st[f])) * D;
       }
     }
   }
@@ -59,15 +66,26 @@ __device__ __forceinline__ T dir_node(const DirView<T> &d, const T *__restrict__
   for (int f = 3; f < 6; ++f) {
     const int u = (f == 5) ? 1 : 0, v = (f == 3) ? 1 : 2;
     const int su = st[u], sv = st[v];
+    T q[3][3];  // q[a][b] = p at (2a - 2) e_u + (2b - 2) e_v
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = 0; b < 3; ++b) {
+        const int ou = 2 * a - 2, ov = 2 * b - 2;
+        q[a][b] = (ou == 0 && ov == 0) ? pc
+                                       : ((inb(u, ou) && inb(v, ov)) ? __ldg(p + g + ou * su + ov * sv) : (T)0);
+      }
 #pragma unroll
     for (int du = -1; du <= 1; du += 2)
 #pragma unroll
       for (int dv = -1; dv <= 1; dv += 2) {  // node g is tap (du, dv) of the row centred at g - du e_u - dv e_v
         const int a0 = (u == 0 ? -du : 0), a1 = (u == 1 ? -du : 0) + (v == 1 ? -dv : 0), a2 = (v == 2 ? -dv : 0);
         if (interior(a0, a1, a2)) {
-          const int m = g - du * su - dv * sv;
-          const T D = __ldg(p + m + su + sv) - __ldg(p + m + su - sv) - __ldg(p + m - su + sv) + __ldg(p + m - su - sv);
-          acc += (T)(du * dv) * __ldg(d.w + f * n + m) * D;
+          // the row centre sits at (-du, -dv); its taps at (-du +- 1, -dv +- 1)
+          // are q[(3 - du) / 2 or (1 - du) / 2][(3 - dv) / 2 or (1 - dv) / 2]
+          const int ap = (3 - du) / 2, am = (1 - du) / 2, bp = (3 - dv) / 2, bm = (1 - dv) / 2;
+          const T D = q[ap][bp] - q[ap][bm] - q[am][bp] + q[am][bm];
+          acc += (T)(du * dv) * __ldg(d.w + f * n + (g - du * su - dv * sv)) * D;
         }
       }
   }
