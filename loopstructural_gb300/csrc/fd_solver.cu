@@ -779,6 +779,20 @@ void mg_apply(ls_fd_handle *h, const MgLevel &lv, const float *p, const EpiArgs<
                                                nullptr, h->red_blocks, st);
 }
 
+// one Gauss-Jordan step on the augmented nc x 2nc matrix: row c divided by
+// the pivot, every other row r minus in[r][c] times the new row c
+__global__ void mg_gj_step_kernel(int nc, int c, double tiny, const double *__restrict__ in, double *__restrict__ out) {
+  const int w = 2 * nc;
+  double piv = in[(size_t)c * w + c];
+  if (fabs(piv) < tiny) piv = piv < 0.0 ? -tiny : tiny;
+  const int64_t total = (int64_t)nc * w;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t / w), k = (int)(t - (int64_t)r * w);
+    const double rowc = in[(size_t)c * w + k] / piv;
+    out[t] = (r == c) ? rowc : in[t] - in[(size_t)r * w + c] * rowc;
+  }
+}
+
 int mg_read_scalar(ls_fd_handle *h, double *dev, double *out) {
   LS_CUDA_TRY(cudaMemcpyAsync(out, dev, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -817,7 +831,8 @@ int mg_lambda_max(ls_fd_handle *h, MgLevel &lv, float *lmax_out) {
   return LS_OK;
 }
 
-// dense inverse of the coarsest operator (Gauss-Jordan with partial pivoting, FP64)
+// dense inverse of the coarsest operator (FP64): assembled on the host,
+// inverted by Gauss-Jordan on the GPU
 int mg_coarse_inverse(ls_fd_handle *h, MgLevel &lv) {
   MgHierarchy &mg = h->mg;
   cudaStream_t st = h->stream;
@@ -882,39 +897,35 @@ int mg_coarse_inverse(ls_fd_handle *h, MgLevel &lv) {
       const double m = 0.5 * (A[(size_t)i * nc + j] + A[(size_t)j * nc + i]);
       A[(size_t)i * nc + j] = A[(size_t)j * nc + i] = m;
     }
-  std::vector<double> inv((size_t)nc * nc, 0.0);
-  for (int i = 0; i < nc; ++i) inv[(size_t)i * nc + i] = 1.0;
+  // Gauss-Jordan on the GPU: [A | I] -> [I | A^-1], one launch per pivot,
+  // ping-pong buffers (every element of step c reads row c and column c of
+  // the previous matrix).  No pivoting: the coarsest operator is symmetric
+  // positive definite (Galerkin products of SPD operators plus the ridge); a
+  // vanishing pivot is replaced by +-1e-14 max|diag| as a guard.
   double maxdiag = 0.0;
   for (int i = 0; i < nc; ++i) maxdiag = std::max(maxdiag, fabs(A[(size_t)i * nc + i]));
-  for (int c = 0; c < nc; ++c) {
-    int piv = c;
-    for (int r = c + 1; r < nc; ++r)
-      if (fabs(A[(size_t)r * nc + c]) > fabs(A[(size_t)piv * nc + c])) piv = r;
-    if (piv != c)
-      for (int k = 0; k < nc; ++k) {
-        std::swap(A[(size_t)c * nc + k], A[(size_t)piv * nc + k]);
-        std::swap(inv[(size_t)c * nc + k], inv[(size_t)piv * nc + k]);
-      }
-    double d = A[(size_t)c * nc + c];
-    if (fabs(d) < 1e-14 * maxdiag) d = (d < 0 ? -1.0 : 1.0) * 1e-14 * maxdiag;  // guard a singular pivot
-    const double id = 1.0 / d;
-    for (int k = 0; k < nc; ++k) {
-      A[(size_t)c * nc + k] *= id;
-      inv[(size_t)c * nc + k] *= id;
-    }
-    for (int r = 0; r < nc; ++r) {
-      if (r == c) continue;
-      const double f = A[(size_t)r * nc + c];
-      if (f == 0.0) continue;
-      for (int k = 0; k < nc; ++k) {
-        A[(size_t)r * nc + k] -= f * A[(size_t)c * nc + k];
-        inv[(size_t)r * nc + k] -= f * inv[(size_t)c * nc + k];
-      }
-    }
+  const int w = 2 * nc;
+  std::vector<double> aug((size_t)nc * w, 0.0);
+  for (int i = 0; i < nc; ++i) {
+    std::copy(A.begin() + (size_t)i * nc, A.begin() + (size_t)(i + 1) * nc, aug.begin() + (size_t)i * w);
+    aug[(size_t)i * w + nc + i] = 1.0;
   }
+  double *buf[2] = {nullptr, nullptr};
+  LS_TRY(dev_alloc(&buf[0], (size_t)nc * w));
+  LS_TRY(dev_alloc(&buf[1], (size_t)nc * w));
+  LS_CUDA_TRY(cudaMemcpyAsync(buf[0], aug.data(), aug.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  const int gs = (int)std::min<int64_t>(((int64_t)nc * w + 255) / 256, 8 * sm_count());
+  for (int c = 0; c < nc; ++c) {
+    mg_gj_step_kernel<<<gs, 256, 0, st>>>(nc, c, 1e-14 * maxdiag, buf[c & 1], buf[(c + 1) & 1]);
+    ++h->launches;
+  }
+  LS_CUDA_TRY(cudaGetLastError());
   LS_TRY(mg_alloc(mg, &mg.coarse_inv64, (size_t)nc * nc));
-  LS_CUDA_TRY(cudaMemcpyAsync(mg.coarse_inv64, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpy2DAsync(mg.coarse_inv64, nc * sizeof(double), buf[nc & 1] + nc, w * sizeof(double),
+                                nc * sizeof(double), nc, cudaMemcpyDeviceToDevice, st));
   LS_CUDA_TRY(cudaStreamSynchronize(st));
+  cudaFree(buf[0]);
+  cudaFree(buf[1]);
   return LS_OK;
 }
 
