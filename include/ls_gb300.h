@@ -243,6 +243,12 @@ int ls_fd_solve(ls_fd_handle *h, const ls_solve_opts *opts, double *d_x, ls_solv
 /* Does the allocations a solve with these options would do on first use
  * (the multigrid hierarchy of a mixed multigrid solve); optional before
  * ls_fd_solve, done by ls_fd_solve_batched for every model. */
+/* Host wall time (ms) of the multigrid setup phases of the handle's last
+ * build (no counterpart in the reference): host copy of the data rows,
+ * regularisation tables, data-row coarsening, data-term upload, diagonals,
+ * eigenvalue estimates, coarsest inverse, total.  Returns the number of
+ * values written (<= n, at most 8); zeros before a multigrid build. */
+int ls_fd_setup_profile(const ls_fd_handle *h, double *h_out, int n);
 int ls_fd_prepare(ls_fd_handle *h, const ls_solve_opts *opts);
 
 /* Device the handle was created on. */

@@ -83,6 +83,10 @@ struct MgHierarchy {
   int deg = 3;
   bool built = false;
   std::vector<void *> allocations;
+  // host wall time (ms) of the setup phases, each ended by a stream sync:
+  // host rows, regularisation tables, data-row coarsening, data-term upload,
+  // diagonals, eigenvalue estimates, coarsest inverse, total
+  double setup_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 // ---------------------------------------------------------------------------

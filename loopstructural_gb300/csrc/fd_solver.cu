@@ -16,6 +16,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <chrono>
 #include <vector>
 
 #include "fd_apply.cuh"
@@ -1187,6 +1188,17 @@ int mg_build(ls_fd_handle *h, int deg) {
   MgHierarchy &mg = h->mg;
   if (mg.built || !mg.levels.empty()) return LS_OK;  // built, or tried and not applicable
   mg.deg = deg;
+  using clock = std::chrono::steady_clock;
+  const auto t_start = clock::now();
+  auto t_phase = t_start;
+  // adds the time since the last mark (after a stream sync) to setup phase `ph`
+  auto mark = [&](int ph) -> int {
+    LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+    const auto now = clock::now();
+    mg.setup_ms[ph] += std::chrono::duration<double, std::milli>(now - t_phase).count();
+    t_phase = now;
+    return LS_OK;
+  };
   MgLevel L0;
   L0.nx = (int)h->grid.nsteps[0];
   L0.ny = (int)h->grid.nsteps[1];
@@ -1218,6 +1230,7 @@ int mg_build(ls_fd_handle *h, int deg) {
   LS_TRY(mg_alloc(mg, &L0.d1, L0.n));
   mg.levels.push_back(L0);
   LS_TRY(ensure_host_rows(h));
+  LS_TRY(mark(0));
   HostRows rows;
   rows.nrows = h->data.nrows;
   rows.width = h->h_width;
@@ -1239,7 +1252,9 @@ int mg_build(ls_fd_handle *h, int deg) {
     c.coef64 = coarsen_coef(f.coef64, c.nx, c.ny, c.nz);
     c.coef = coef_as<float>(c.coef64);
     LS_TRY(mg_build_g1(h, mg, f, c));
+    LS_TRY(mark(1));
     if (rows.nrows > 0) rows = galerkin_rows(rows, f.nx, f.ny, c.nx, c.ny);
+    LS_TRY(mark(2));
     std::vector<int64_t> touched;
     std::vector<double> ddiag;
     LS_TRY(mg_alloc(mg, &c.b, c.n));
@@ -1265,6 +1280,7 @@ int mg_build(ls_fd_handle *h, int deg) {
     std::vector<std::pair<int64_t, double>> kdiag;
     LS_TRY(mg_upload_k27(h, c, rows, rest, kdiag));
     LS_TRY(mg_upload_level(h, c, rest, touched, ddiag));
+    LS_TRY(mark(3));
     // diagonal of the data term: row form plus the 27-point centre entries
     {
       std::vector<std::pair<int64_t, double>> all(kdiag);
@@ -1282,6 +1298,7 @@ int mg_build(ls_fd_handle *h, int deg) {
       }
       LS_TRY(mg_level_dinv(h, c, tn, td));
     }
+    LS_TRY(mark(4));
     mg.levels.push_back(c);
   }
   if (mg.levels.back().n > kMgMaxCoarse) return LS_OK;  // not built: Jacobi fallback
@@ -1291,8 +1308,11 @@ int mg_build(ls_fd_handle *h, int deg) {
     LS_TRY(mg_lambda_max(h, lv, &est));
     lv.lmax = est;
   }
+  LS_TRY(mark(5));
   mg_set_degree(mg, deg);
   LS_TRY(mg_coarse_inverse(h, mg.levels.back()));
+  LS_TRY(mark(6));
+  mg.setup_ms[7] = std::chrono::duration<double, std::milli>(clock::now() - t_start).count();
   mg.built = true;
   return LS_OK;
 }
@@ -1889,6 +1909,13 @@ extern "C" int ls_fd_apply_f32(ls_fd_handle *h, const float *d_x, float *d_y, vo
   LS_CUDA_TRY(cudaGetLastError());
   LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
   return LS_OK;
+}
+
+extern "C" int ls_fd_setup_profile(const ls_fd_handle *h, double *h_out, int n) {
+  LS_ARG_CHECK(h && h_out, "NULL argument");
+  const int k = std::min(n, 8);
+  for (int i = 0; i < k; ++i) h_out[i] = h->mg.setup_ms[i];
+  return k;
 }
 
 extern "C" int ls_fd_prepare(ls_fd_handle *h, const ls_solve_opts *opts) {

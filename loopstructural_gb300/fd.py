@@ -262,6 +262,17 @@ def profile_mg(system: "FdSystem", reps=20, max_levels=16):
     return [{f: out[l * k + i] for i, f in enumerate(MG_PROFILE_FIELDS)} for l in range(nl.value)]
 
 
+MG_SETUP_PHASES = ("host_rows", "tables", "row_coarsening", "data_upload", "diagonals", "eigenvalues",
+                   "coarse_inverse", "total")
+
+
+def setup_profile(system: "FdSystem"):
+    """Host wall time (ms) of the multigrid setup phases of the last build."""
+    out = (C.c_double * 8)()
+    k = _lib.check(system.lib.ls_fd_setup_profile(system.handle, out, 8), allow_positive=True)
+    return {MG_SETUP_PHASES[i]: out[i] for i in range(k)}
+
+
 def mg_apply_level(system: "FdSystem", level: int, x=None):
     """(nodes, A_level x): the FP32 operator of a multigrid level (diagnostic)."""
     torch = _torch()
