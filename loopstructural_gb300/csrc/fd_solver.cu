@@ -22,6 +22,7 @@
 #include "fd_apply.cuh"
 #include "fd_directional.cuh"
 #include "fd_mg.cuh"
+#include "fd_mg_cells.cuh"
 #include "fd_stencil.cuh"
 #include "ls_common.cuh"
 
@@ -540,43 +541,73 @@ void node_mask(int64_t n, const std::vector<int64_t> &marked, std::vector<uint32
   }
 }
 
-// Rows of a coarse level whose columns all lie in one cell (a 2 x 2 x 2 box)
-// become the 27-point per-node stencil sum_rows w^2 a_i a_j; the other rows
-// are returned in `rest` for the row form.  The stencil's centre entries go to
-// diag_out (per marked node, ascending node order).
-int mg_upload_k27(ls_fd_handle *h, MgLevel &lv, const HostRows &rows, HostRows &rest,
-                  std::vector<std::pair<int64_t, double>> &diag_out) {
-  MgHierarchy &mg = h->mg;
+// exclusive scan of int32 counts into int64 offsets (one block; setup time)
+__global__ void __launch_bounds__(1024) setup_scan_kernel(const int32_t *__restrict__ cnt, int64_t n,
+                                                          int64_t *__restrict__ off, int64_t *__restrict__ total) {
+  __shared__ int64_t warp_tot[32];
+  __shared__ int64_t carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t base = 0; base < n; base += 1024) {
+    const int64_t i = base + threadIdx.x;
+    const int64_t v = (i < n) ? cnt[i] : 0;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      int64_t t = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, t, o);
+        if (lane >= o) t += y;
+      }
+      warp_tot[lane] = t;
+    }
+    __syncthreads();
+    const int64_t excl = x - v + (warp > 0 ? warp_tot[warp - 1] : 0) + carry;
+    if (i < n) off[i] = excl;
+    __syncthreads();
+    if (threadIdx.x == 1023) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+// Splits the finest level's data rows into cell rows -- columns within one
+// 2 x 2 x 2 box, every point row -- uploaded as (cell, 8 corner coefficients,
+// w^2) for the device path of fd_mg_cells.cuh, and the other rows (interface
+// pairs spanning two cells), kept in row form.
+int mg_split_rows(ls_fd_handle *h, const HostRows &rows, int nx, int ny, int nz, CellRows &cr, HostRows &rest) {
   rest = HostRows{};
   rest.width = rows.width;
-  diag_out.clear();
-  lv.knt = 0;
-  const int64_t nxy = (int64_t)lv.nx * lv.ny;
-  // pass 1: classify the rows; mark the nodes of the cell rows
-  std::vector<int32_t> slot(lv.n, -1);
-  std::vector<int64_t> ccol;  // 8 per cell row (-1 padding)
-  std::vector<double> cval;   // w^2-free coefficients, 8 per cell row
-  std::vector<double> cw2;
+  const int64_t nxy = (int64_t)nx * ny;
+  const int lim[3] = {nx, ny, nz};
+  std::vector<int32_t> cc[3];
+  std::vector<double> cv, cw2;
   for (int64_t r = 0; r < rows.nrows; ++r) {
-    int64_t cols[8];
-    double av[8];
+    int xyz[64][3];
+    double av[64];
     int m = 0;
-    bool cell = true;
+    bool cell = rows.width <= 64;
     int lo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, hi[3] = {-1, -1, -1};
     for (int k = 0; k < rows.width && cell; ++k) {
       const int64_t c = rows.cols[r * rows.width + k];
       if (c < 0) continue;
-      const int ax[3] = {(int)(c % lv.nx), (int)((c / lv.nx) % lv.ny), (int)(c / nxy)};
+      const int z = (int)(c / nxy), rem = (int)(c - (int64_t)z * nxy), y = rem / nx, x = rem - y * nx;
+      const int ax[3] = {x, y, z};
       for (int d = 0; d < 3; ++d) {
+        xyz[m][d] = ax[d];
         lo[d] = std::min(lo[d], ax[d]);
         hi[d] = std::max(hi[d], ax[d]);
         if (hi[d] - lo[d] > 1) cell = false;
       }
-      if (m == 8) cell = false;  // a 2 x 2 x 2 box has 8 distinct nodes
-      if (!cell) break;
-      cols[m] = c;
-      av[m] = rows.a[r * rows.width + k];
-      ++m;
+      av[m++] = rows.a[r * rows.width + k];
     }
     if (m == 0) cell = false;
     if (!cell) {
@@ -586,58 +617,99 @@ int mg_upload_k27(ls_fd_handle *h, MgLevel &lv, const HostRows &rows, HostRows &
       ++rest.nrows;
       continue;
     }
-    for (int u = 0; u < 8; ++u) {
-      ccol.push_back(u < m ? cols[u] : -1);
-      cval.push_back(u < m ? av[u] : 0.0);
-      if (u < m) slot[cols[u]] = 0;
-    }
+    int base[3];
+    for (int d = 0; d < 3; ++d) base[d] = std::min(lo[d], lim[d] - 2);  // a box on the upper face ends there
+    double c8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int e = 0; e < m; ++e)
+      c8[(xyz[e][0] - base[0]) | ((xyz[e][1] - base[1]) << 1) | ((xyz[e][2] - base[2]) << 2)] += av[e];
+    for (int d = 0; d < 3; ++d) cc[d].push_back(base[d]);
+    cv.insert(cv.end(), c8, c8 + 8);
     cw2.push_back(rows.w2[r]);
   }
-  if (cw2.empty()) return LS_OK;
-  // slots in ascending node order
-  std::vector<int64_t> nodes;
-  for (int64_t g = 0; g < lv.n; ++g)
-    if (slot[g] == 0) {
-      slot[g] = (int32_t)nodes.size();
-      nodes.push_back(g);
-    }
-  // pass 2: sum w^2 a_u a_v per (node, offset), rows in order
-  const int64_t nt = (int64_t)nodes.size();
-  std::vector<double> kv((size_t)27 * nt, 0.0);
-  for (size_t r = 0; r < cw2.size(); ++r) {
-    const int64_t *cols = &ccol[8 * r];
-    const double *av = &cval[8 * r];
-    for (int u = 0; u < 8; ++u) {
-      if (cols[u] < 0) continue;
-      const int ux = (int)(cols[u] % lv.nx), uy = (int)((cols[u] / lv.nx) % lv.ny), uz = (int)(cols[u] / nxy);
-      double *row = &kv[(size_t)slot[cols[u]] * 27];
-      for (int v = 0; v < 8; ++v) {
-        if (cols[v] < 0) continue;
-        const int dx = (int)(cols[v] % lv.nx) - ux, dy = (int)((cols[v] / lv.nx) % lv.ny) - uy,
-                  dz = (int)(cols[v] / nxy) - uz;
-        row[9 * (dz + 1) + 3 * (dy + 1) + (dx + 1)] += cw2[r] * av[u] * av[v];
-      }
-    }
-  }
-  std::vector<float> k((size_t)27 * nt);
-  for (int64_t t = 0; t < nt; ++t) {
-    for (int o = 0; o < 27; ++o) k[(size_t)o * nt + t] = (float)kv[(size_t)t * 27 + o];
-    diag_out.emplace_back(nodes[t], kv[(size_t)t * 27 + 13]);
-  }
-  lv.k27host = k;
-  lv.k27nodes = nodes;
-  std::vector<uint32_t> mask;
-  std::vector<int32_t> wr;
-  node_mask(lv.n, nodes, mask, wr);
-  lv.knt = nt;
-  LS_TRY(mg_alloc(mg, &lv.kmask, mask.size()));
-  LS_TRY(mg_alloc(mg, &lv.krank, wr.size()));
-  LS_TRY(mg_alloc(mg, &lv.k27, k.size()));
+  cr.nrows = (int64_t)cw2.size();
+  if (cr.nrows == 0) return LS_OK;
+  LS_TRY(dev_alloc(&cr.ci, cr.nrows));
+  LS_TRY(dev_alloc(&cr.cj, cr.nrows));
+  LS_TRY(dev_alloc(&cr.ck, cr.nrows));
+  LS_TRY(dev_alloc(&cr.c, 8 * cr.nrows));
+  LS_TRY(dev_alloc(&cr.w2, cr.nrows));
   cudaStream_t st = h->stream;
-  LS_CUDA_TRY(cudaMemcpyAsync(lv.kmask, mask.data(), mask.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
-  LS_CUDA_TRY(cudaMemcpyAsync(lv.krank, wr.data(), wr.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-  LS_CUDA_TRY(cudaMemcpyAsync(lv.k27, k.data(), k.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(cr.ci, cc[0].data(), cr.nrows * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(cr.cj, cc[1].data(), cr.nrows * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(cr.ck, cc[2].data(), cr.nrows * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(cr.c, cv.data(), 8 * cr.nrows * sizeof(double), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(cr.w2, cw2.data(), cr.nrows * sizeof(double), cudaMemcpyHostToDevice, st));
   LS_CUDA_TRY(cudaStreamSynchronize(st));
+  return LS_OK;
+}
+
+void free_cell_rows(CellRows &cr) {
+  void *p[] = {cr.ci, cr.cj, cr.ck, cr.c, cr.w2};
+  for (void *q : p)
+    if (q) cudaFree(q);
+  cr = CellRows{};
+}
+
+// The level's 27-point form of its (already coarsened) cell rows: buckets of
+// rows per cell, the marked nodes, then one gather per marked node.
+int mg_cells_k27(ls_fd_handle *h, MgLevel &lv, const CellRows &cr) {
+  MgHierarchy &mg = h->mg;
+  cudaStream_t st = h->stream;
+  const int cx = lv.nx - 1, cy = lv.ny - 1, cz = lv.nz - 1;
+  const int64_t ncells = (int64_t)cx * cy * cz, nwords = (lv.n + 31) / 32;
+  int32_t *cnt = nullptr, *fill = nullptr, *bucket = nullptr, *wcount = nullptr;
+  int64_t *off = nullptr, *wrank = nullptr, *tot = nullptr;
+  LS_CUDA_TRY(cudaMallocAsync((void **)&cnt, ncells * sizeof(int32_t), st));
+  LS_CUDA_TRY(cudaMallocAsync((void **)&fill, ncells * sizeof(int32_t), st));
+  LS_CUDA_TRY(cudaMallocAsync((void **)&bucket, cr.nrows * sizeof(int32_t), st));
+  LS_CUDA_TRY(cudaMallocAsync((void **)&wcount, nwords * sizeof(int32_t), st));
+  LS_CUDA_TRY(cudaMallocAsync((void **)&off, (ncells + 1) * sizeof(int64_t), st));
+  LS_CUDA_TRY(cudaMallocAsync((void **)&wrank, (nwords + 1) * sizeof(int64_t), st));
+  LS_CUDA_TRY(cudaMallocAsync((void **)&tot, 2 * sizeof(int64_t), st));
+  LS_CUDA_TRY(cudaMemsetAsync(cnt, 0, ncells * sizeof(int32_t), st));
+  LS_CUDA_TRY(cudaMemsetAsync(fill, 0, ncells * sizeof(int32_t), st));
+  const int gr = grid_for(h, cr.nrows);
+  cell_count_kernel<<<gr, kBlock, 0, st>>>(cr.nrows, cr.ci, cr.cj, cr.ck, cx, cy, cnt);
+  setup_scan_kernel<<<1, 1024, 0, st>>>(cnt, ncells, off, tot);
+  LS_CUDA_TRY(cudaMemcpyAsync(off + ncells, &cr.nrows, sizeof(int64_t), cudaMemcpyHostToDevice, st));
+  cell_fill_kernel<<<gr, kBlock, 0, st>>>(cr.nrows, cr.ci, cr.cj, cr.ck, cx, cy, off, fill, bucket);
+  cell_sort_kernel<<<grid_for(h, ncells), kBlock, 0, st>>>(ncells, off, bucket);
+  LS_TRY(mg_alloc(mg, &lv.kmask, nwords));
+  LS_TRY(mg_alloc(mg, &lv.krank, nwords));
+  cell_touch_kernel<<<grid_for(h, nwords * 32), kBlock, 0, st>>>(lv.nx, lv.ny, lv.nz, cnt, lv.kmask, wcount);
+  setup_scan_kernel<<<1, 1024, 0, st>>>(wcount, nwords, wrank, tot + 1);
+  h->launches += 6;
+  int64_t knt = 0;
+  LS_CUDA_TRY(cudaMemcpyAsync(&knt, tot + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  LS_CUDA_TRY(cudaStreamSynchronize(st));
+  lv.knt = knt;
+  if (knt > 0) {
+    LS_TRY(mg_alloc(mg, &lv.k27, (size_t)27 * knt));
+    cell_k27_kernel<<<grid_for(h, lv.n), kBlock, 0, st>>>(lv.nx, lv.ny, lv.nz, lv.kmask, wrank, off, bucket, cr.c,
+                                                          cr.w2, knt, lv.k27, lv.krank);
+    ++h->launches;
+  }
+  LS_CUDA_TRY(cudaGetLastError());
+  void *tmp[] = {cnt, fill, bucket, wcount, off, wrank, tot};
+  for (void *q : tmp) LS_CUDA_TRY(cudaFreeAsync(q, st));
+  LS_CUDA_TRY(cudaStreamSynchronize(st));
+  return LS_OK;
+}
+
+// host copies of the coarsest level's 27-point form (dense coarsest matrix)
+int mg_k27_to_host(MgLevel &lv, cudaStream_t st) {
+  lv.k27host.clear();
+  lv.k27nodes.clear();
+  if (lv.knt == 0) return LS_OK;
+  const int64_t nwords = (lv.n + 31) / 32;
+  std::vector<uint32_t> mask(nwords);
+  lv.k27host.resize((size_t)27 * lv.knt);
+  LS_CUDA_TRY(cudaMemcpyAsync(mask.data(), lv.kmask, nwords * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(lv.k27host.data(), lv.k27, lv.k27host.size() * sizeof(float), cudaMemcpyDeviceToHost,
+                              st));
+  LS_CUDA_TRY(cudaStreamSynchronize(st));
+  for (int64_t g = 0; g < lv.n; ++g)
+    if (mask[g >> 5] & (1u << (g & 31))) lv.k27nodes.push_back(g);
   return LS_OK;
 }
 
@@ -953,6 +1025,10 @@ int mg_level_dinv(ls_fd_handle *h, MgLevel &lv, const std::vector<int64_t> &touc
     dir_coarse_diag_kernel<<<g, kBlock, 0, st>>>(dir_coarse(lv), lv.dir, diag);
     ++h->launches;
   }
+  if (lv.knt > 0) {
+    k27_diag_kernel<<<g, kBlock, 0, st>>>(lv.n, lv.kmask, lv.krank, lv.k27, lv.knt, diag);
+    ++h->launches;
+  }
   if (!touched.empty()) {
     mg_diag_finish_kernel<<<grid_for(h, (int64_t)touched.size()), kBlock, 0, st>>>(lv.n, diag, (int64_t)touched.size(), dt, dd);
     ++h->launches;
@@ -1230,13 +1306,26 @@ int mg_build(ls_fd_handle *h, int deg) {
   LS_TRY(mg_alloc(mg, &L0.d1, L0.n));
   mg.levels.push_back(L0);
   LS_TRY(ensure_host_rows(h));
-  LS_TRY(mark(0));
   HostRows rows;
-  rows.nrows = h->data.nrows;
-  rows.width = h->h_width;
-  rows.cols = h->h_idc;
-  rows.a = h->h_a;
-  rows.w2 = h->h_w2;
+  CellRows cells;
+  {
+    HostRows all;
+    all.nrows = h->data.nrows;
+    all.width = h->h_width;
+    all.cols = h->h_idc;
+    all.a = h->h_a;
+    all.w2 = h->h_w2;
+    const int st_split = mg_split_rows(h, all, L0.nx, L0.ny, L0.nz, cells, rows);
+    if (st_split < 0) {
+      free_cell_rows(cells);
+      return st_split;
+    }
+  }
+  struct CellRowsGuard {
+    CellRows &c;
+    ~CellRowsGuard() { free_cell_rows(c); }
+  } cells_guard{cells};
+  LS_TRY(mark(0));
   for (;;) {
     const MgLevel &f = mg.levels.back();
     // the dense coarsest solve costs O(n^3) to set up: grids too small for an
@@ -1254,6 +1343,11 @@ int mg_build(ls_fd_handle *h, int deg) {
     LS_TRY(mg_build_g1(h, mg, f, c));
     LS_TRY(mark(1));
     if (rows.nrows > 0) rows = galerkin_rows(rows, f.nx, f.ny, c.nx, c.ny);
+    if (cells.nrows > 0) {
+      cell_coarsen_kernel<<<grid_for(h, cells.nrows), kBlock, 0, h->stream>>>(cells.nrows, cells.ci, cells.cj, cells.ck,
+                                                                             cells.c);
+      ++h->launches;
+    }
     LS_TRY(mark(2));
     std::vector<int64_t> touched;
     std::vector<double> ddiag;
@@ -1276,28 +1370,13 @@ int mg_build(ls_fd_handle *h, int deg) {
                                                                       c.nz, c.dir, c.dmass, c.dsw);
       ++h->launches;
     }
-    HostRows rest;
-    std::vector<std::pair<int64_t, double>> kdiag;
-    LS_TRY(mg_upload_k27(h, c, rows, rest, kdiag));
-    LS_TRY(mg_upload_level(h, c, rest, touched, ddiag));
+    c.knt = 0;
+    if (cells.nrows > 0) LS_TRY(mg_cells_k27(h, c, cells));
+    LS_TRY(mg_upload_level(h, c, rows, touched, ddiag));
     LS_TRY(mark(3));
-    // diagonal of the data term: row form plus the 27-point centre entries
-    {
-      std::vector<std::pair<int64_t, double>> all(kdiag);
-      for (size_t t = 0; t < touched.size(); ++t) all.emplace_back(touched[t], ddiag[t]);
-      std::sort(all.begin(), all.end());
-      std::vector<int64_t> tn;
-      std::vector<double> td;
-      for (const auto &e : all) {
-        if (!tn.empty() && tn.back() == e.first) {
-          td.back() += e.second;
-        } else {
-          tn.push_back(e.first);
-          td.push_back(e.second);
-        }
-      }
-      LS_TRY(mg_level_dinv(h, c, tn, td));
-    }
+    // diagonal: regularisation, the row-form data term (touched / ddiag) and
+    // the 27-point centre entries (added on the device)
+    LS_TRY(mg_level_dinv(h, c, touched, ddiag));
     LS_TRY(mark(4));
     mg.levels.push_back(c);
   }
@@ -1310,6 +1389,7 @@ int mg_build(ls_fd_handle *h, int deg) {
   }
   LS_TRY(mark(5));
   mg_set_degree(mg, deg);
+  LS_TRY(mg_k27_to_host(mg.levels.back(), h->stream));
   LS_TRY(mg_coarse_inverse(h, mg.levels.back()));
   LS_TRY(mark(6));
   mg.setup_ms[7] = std::chrono::duration<double, std::milli>(clock::now() - t_start).count();
@@ -1497,43 +1577,6 @@ __global__ void data_rows_setup_kernel(int64_t nrows, const double *__restrict__
   }
 }
 
-// exclusive scan of int32 counts into int64 offsets (one block; setup time)
-__global__ void __launch_bounds__(1024) setup_scan_kernel(const int32_t *__restrict__ cnt, int64_t n,
-                                                          int64_t *__restrict__ off, int64_t *__restrict__ total) {
-  __shared__ int64_t warp_tot[32];
-  __shared__ int64_t carry;
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int64_t base = 0; base < n; base += 1024) {
-    const int64_t i = base + threadIdx.x;
-    const int64_t v = (i < n) ? cnt[i] : 0;
-    int64_t x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) warp_tot[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      int64_t t = warp_tot[lane];
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int64_t y = __shfl_up_sync(0xffffffffu, t, o);
-        if (lane >= o) t += y;
-      }
-      warp_tot[lane] = t;
-    }
-    __syncthreads();
-    const int64_t excl = x - v + (warp > 0 ? warp_tot[warp - 1] : 0) + carry;
-    if (i < n) off[i] = excl;
-    __syncthreads();
-    if (threadIdx.x == 1023) carry = excl + v;
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) *total = carry;
-}
 
 // entry e goes to the next free slot of its node's segment (any order)
 __global__ void data_fill_kernel(int64_t ne, const int32_t *__restrict__ cols, const int64_t *__restrict__ start,
