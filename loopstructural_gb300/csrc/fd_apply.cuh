@@ -20,6 +20,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cassert>
 
 #include "fd_stencil.cuh"
 #include "ls_common.cuh"
@@ -251,7 +252,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // they are, so only a 5-plane window stays live in registers.
 // Returns the block's sum of the epilogue contributions (p.q for EPI_STORE)
 // through the deterministic grid reduction when `dot_out` is set.
-template <typename T, int EPI, int MODE, bool K27, int TZ_>
+template <typename T, int EPI, int MODE, int TZ_>
 __global__ void __launch_bounds__(kAX * kAY, MODE == MODE_DEEP ? 4 : 1)
     fd_apply_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv, EpiArgs<T> e, const int *done,
                     double *partials, unsigned int *ticket, double *dot_out) {
@@ -271,15 +272,14 @@ __global__ void __launch_bounds__(kAX * kAY, MODE == MODE_DEEP ? 4 : 1)
   const int gcol = j * nx + i;
   // mask words of the column's output nodes, loaded before the staging burst
   // and reduced to one bit per output plane while it is in flight
-  uint32_t mw[TZ], kw[TZ];
+  uint32_t mw[TZ];
 #pragma unroll
   for (int oz = 0; oz < TZ; ++oz) {
     const int g = (z0 + oz) * sxy + gcol;
     const bool ok = col_in & (z0 + oz < ze);
     mw[oz] = (dv.enabled && ok) ? __ldg(dv.mask + (g >> 5)) : 0u;
-    kw[oz] = (K27 && ok) ? __ldg(dv.kmask + (g >> 5)) : 0u;
   }
-  uint32_t dbits = 0u, kbits = 0u;
+  uint32_t dbits = 0u;
   // ---- stage the tile ----
   {
     int off[2];
@@ -307,7 +307,6 @@ __global__ void __launch_bounds__(kAX * kAY, MODE == MODE_DEEP ? 4 : 1)
   for (int oz = 0; oz < TZ; ++oz) {
     const int g = (z0 + oz) * sxy + gcol;
     dbits |= ((mw[oz] >> (g & 31)) & 1u) << oz;
-    if (K27) kbits |= ((kw[oz] >> (g & 31)) & 1u) << oz;
   }
   cp_async_wait_all();
   __syncthreads();
@@ -349,10 +348,6 @@ __global__ void __launch_bounds__(kAX * kAY, MODE == MODE_DEEP ? 4 : 1)
             q = shell_node<T>(c, pr, i, j, z);
           }
           if ((dbits >> oz) & 1u) q += data_term<T>(dv, g);
-          if (K27 && ((kbits >> oz) & 1u)) {
-            auto pk = [&](int dz, int dy, int dx) -> T { return sm[ho + dz][hy + dy][hx + dx]; };
-            q += k27_term<T>(dv, g, pk);
-          }
           local += epi_store<T, EPI>(e, g, P[ho], q, pre[oz]);
         }
       }
@@ -413,7 +408,7 @@ __device__ __forceinline__ void shell_node_index(int64_t s, int nx, int ny, int 
 // from L1/L2), with the data term and the epilogue: the boundary shell of a
 // split grid (ALL = false), or every node of a small grid (ALL = true), where
 // a thread per node exposes more parallelism than the staged tiles.
-template <typename T, int EPI, bool ALL, bool K27>
+template <typename T, int EPI, bool ALL>
 __global__ void __launch_bounds__(256) fd_point_kernel(CoefT<T> c, const T *__restrict__ p, DataView<T> dv,
                                                        EpiArgs<T> e, const int *done, double *partials,
                                                        unsigned int *ticket, double *dot_out) {
@@ -447,7 +442,6 @@ __global__ void __launch_bounds__(256) fd_point_kernel(CoefT<T> c, const T *__re
     };
     T q = shell_node<T>(c, pr, i, j, k);
     if (dv.enabled) q += data_term<T>(dv, g);
-    if (K27) q += k27_term<T>(dv, g, pr);
     local += epilogue<T, EPI>(e, g, __ldg(p + g), q);
   }
   if (dot_out) {
@@ -459,25 +453,25 @@ __global__ void __launch_bounds__(256) fd_point_kernel(CoefT<T> c, const T *__re
 // Grids with fewer nodes than this run the node-per-thread kernel alone.
 constexpr int64_t kPointMaxNodes = 300000;
 
-template <typename T, int EPI, int MODE, bool K27>
+template <typename T, int EPI, int MODE>
 inline void launch_tiles(const CoefT<T> &c, const T *p, const DataView<T> &dv, const EpiArgs<T> &e, const int *done,
                          double *partials, unsigned int *ticket, double *dot, int sms, cudaStream_t st) {
   const dim3 blk(kAX, kAY);
   if constexpr (sizeof(T) == 8) {
-    fd_apply_kernel<T, EPI, MODE, K27, 8><<<apply_grid<T, 8>(c.nx, c.ny, c.nz, MODE), blk, 0, st>>>(
+    fd_apply_kernel<T, EPI, MODE, 8><<<apply_grid<T, 8>(c.nx, c.ny, c.nz, MODE), blk, 0, st>>>(
         c, p, dv, e, done, partials, ticket, dot);
   } else {
     const dim3 g8 = apply_grid<T, 8>(c.nx, c.ny, c.nz, MODE);
     if ((int64_t)g8.x * g8.y * g8.z >= 4 * (int64_t)sms) {
-      fd_apply_kernel<T, EPI, MODE, K27, 8><<<g8, blk, 0, st>>>(c, p, dv, e, done, partials, ticket, dot);
+      fd_apply_kernel<T, EPI, MODE, 8><<<g8, blk, 0, st>>>(c, p, dv, e, done, partials, ticket, dot);
     } else {
-      fd_apply_kernel<T, EPI, MODE, K27, 4><<<apply_grid<T, 4>(c.nx, c.ny, c.nz, MODE), blk, 0, st>>>(
+      fd_apply_kernel<T, EPI, MODE, 4><<<apply_grid<T, 4>(c.nx, c.ny, c.nz, MODE), blk, 0, st>>>(
           c, p, dv, e, done, partials, ticket, dot);
     }
   }
 }
 
-template <typename T, int EPI, bool K27>
+template <typename T, int EPI>
 inline int launch_operator_k(const CoefT<T> &c, const T *p, const DataView<T> &dv, const EpiArgs<T> &e,
                              const int *done, double *partials, unsigned int *ticket_main, double *dot_main,
                              unsigned int *ticket_shell, double *dot_shell, int max_blocks, cudaStream_t st) {
@@ -485,17 +479,17 @@ inline int launch_operator_k(const CoefT<T> &c, const T *p, const DataView<T> &d
   const int sms = max_blocks / 8;
   if (n <= kPointMaxNodes) {
     const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, max_blocks));
-    fd_point_kernel<T, EPI, true, K27><<<gs, 256, 0, st>>>(c, p, dv, e, done, partials, ticket_main, dot_main);
+    fd_point_kernel<T, EPI, true><<<gs, 256, 0, st>>>(c, p, dv, e, done, partials, ticket_main, dot_main);
     return 1;
   }
   if (apply_split(c.nx, c.ny, c.nz)) {
-    launch_tiles<T, EPI, MODE_DEEP, K27>(c, p, dv, e, done, partials, ticket_main, dot_main, sms, st);
+    launch_tiles<T, EPI, MODE_DEEP>(c, p, dv, e, done, partials, ticket_main, dot_main, sms, st);
     const int64_t ns = shell_count(c.nx, c.ny, c.nz);
     const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((ns + 255) / 256, max_blocks));
-    fd_point_kernel<T, EPI, false, K27><<<gs, 256, 0, st>>>(c, p, dv, e, done, partials, ticket_shell, dot_shell);
+    fd_point_kernel<T, EPI, false><<<gs, 256, 0, st>>>(c, p, dv, e, done, partials, ticket_shell, dot_shell);
     return 2;
   }
-  launch_tiles<T, EPI, MODE_FULL, K27>(c, p, dv, e, done, partials, ticket_main, dot_main, sms, st);
+  launch_tiles<T, EPI, MODE_FULL>(c, p, dv, e, done, partials, ticket_main, dot_main, sms, st);
   return 1;
 }
 
@@ -503,16 +497,15 @@ inline int launch_operator_k(const CoefT<T> &c, const T *p, const DataView<T> &d
 // small grids; the deep-box kernel plus the shell kernel on split grids; else
 // one staged full-grid kernel.  The epilogue sums land in dot_main (full grid
 // / deep box) and dot_shell (shell; untouched otherwise).  Returns the number
-// of kernels launched.
+// of kernels launched.  Used on the finest level, whose data rows are in row
+// form (the coarse levels' 27-point form is applied by fd_galerkin.cuh).
 template <typename T, int EPI>
 inline int launch_operator(const CoefT<T> &c, const T *p, const DataView<T> &dv, const EpiArgs<T> &e, const int *done,
                            double *partials, unsigned int *ticket_main, double *dot_main, unsigned int *ticket_shell,
                            double *dot_shell, int max_blocks, cudaStream_t st) {
-  if (dv.k27)
-    return launch_operator_k<T, EPI, true>(c, p, dv, e, done, partials, ticket_main, dot_main, ticket_shell, dot_shell,
-                                           max_blocks, st);
-  return launch_operator_k<T, EPI, false>(c, p, dv, e, done, partials, ticket_main, dot_main, ticket_shell, dot_shell,
-                                          max_blocks, st);
+  assert(dv.k27 == nullptr);  // the 27-point data form exists on Galerkin levels only (fd_galerkin.cuh)
+  return launch_operator_k<T, EPI>(c, p, dv, e, done, partials, ticket_main, dot_main, ticket_shell, dot_shell,
+                                   max_blocks, st);
 }
 
 // Data term of the touched nodes with one warp per node (coarse multigrid

@@ -2290,23 +2290,15 @@ extern "C" int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_
     } else if (lv.n > kPointMaxNodes && apply_split(lv.nx, lv.ny, lv.nz)) {
       const DataView<float> dv = mg_view(lv);
       LS_TRY(timed([&] {
-        if (dv.k27)
-          launch_tiles<float, EPI_CHEB, MODE_DEEP, true>(lv.coef, lv.d0, dv, ec, nullptr, nullptr, nullptr, nullptr,
-                                                          h->red_blocks / 8, st);
-        else
-          launch_tiles<float, EPI_CHEB, MODE_DEEP, false>(lv.coef, lv.d0, dv, ec, nullptr, nullptr, nullptr, nullptr,
-                                                           h->red_blocks / 8, st);
+        launch_tiles<float, EPI_CHEB, MODE_DEEP>(lv.coef, lv.d0, dv, ec, nullptr, nullptr, nullptr, nullptr,
+                                                 h->red_blocks / 8, st);
         ++h->launches;
       }, &o[8]));
       const int64_t ns = shell_count(lv.nx, lv.ny, lv.nz);
       const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((ns + 255) / 256, h->red_blocks));
       LS_TRY(timed([&] {
-        if (dv.k27)
-          fd_point_kernel<float, EPI_CHEB, false, true><<<gs, 256, 0, st>>>(lv.coef, lv.d0, dv, ec, nullptr, nullptr,
-                                                                            nullptr, nullptr);
-        else
-          fd_point_kernel<float, EPI_CHEB, false, false><<<gs, 256, 0, st>>>(lv.coef, lv.d0, dv, ec, nullptr, nullptr,
-                                                                             nullptr, nullptr);
+        fd_point_kernel<float, EPI_CHEB, false><<<gs, 256, 0, st>>>(lv.coef, lv.d0, dv, ec, nullptr, nullptr, nullptr,
+                                                                    nullptr);
         ++h->launches;
       }, &o[9]));
     }
