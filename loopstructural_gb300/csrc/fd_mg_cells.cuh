@@ -11,9 +11,11 @@
 // Their normal-equations block is w^2 c c^T on the cell's corners.  A node's
 // 27-point stencil (offset o = 9 (dz + 1) + 3 (dy + 1) + (dx + 1)) sums it over
 // the node's 8 cells in a fixed order and, within a cell, over the cell's rows
-// in row order (rows bucketed per cell by a count / scan / fill / per-cell
-// sort), so the result does not depend on thread scheduling -- no float
-// atomics.
+// in array order, so the result does not depend on thread scheduling -- no
+// float atomics.  The rows are sorted once, on the finest level, by the Morton
+// code of their cell; coarsening a cell drops the last 3 bits of its code, so
+// on every level the rows of a cell stay one contiguous run of the array
+// (cell_segments_kernel finds the runs; nothing is sorted per level).
 #pragma once
 
 #include "ls_common.cuh"
@@ -64,41 +66,20 @@ __global__ void cell_coarsen_kernel(int64_t nrows, int32_t *__restrict__ ci, int
   }
 }
 
-__global__ void cell_count_kernel(int64_t nrows, const int32_t *__restrict__ ci, const int32_t *__restrict__ cj,
-                                  const int32_t *__restrict__ ck, int cx, int cy, int32_t *__restrict__ cnt) {
-  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x)
-    atomicAdd(cnt + cell_index(ci[r], cj[r], ck[r], cx, cy), 1);
-}
-
-// row r goes to the next free slot of its cell's bucket (any order; sorted next)
-__global__ void cell_fill_kernel(int64_t nrows, const int32_t *__restrict__ ci, const int32_t *__restrict__ cj,
-                                 const int32_t *__restrict__ ck, int cx, int cy, const int64_t *__restrict__ off,
-                                 int32_t *__restrict__ fill, int32_t *__restrict__ bucket) {
+// [start, end) of each cell's run of rows (cells without rows keep 0, 0)
+__global__ void cell_segments_kernel(int64_t nrows, const int32_t *__restrict__ ci, const int32_t *__restrict__ cj,
+                                     const int32_t *__restrict__ ck, int cx, int cy, int64_t *__restrict__ start,
+                                     int64_t *__restrict__ end) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
     const int64_t cell = cell_index(ci[r], cj[r], ck[r], cx, cy);
-    bucket[off[cell] + atomicAdd(fill + cell, 1)] = (int32_t)r;
-  }
-}
-
-// each cell's bucket in row order
-__global__ void cell_sort_kernel(int64_t ncells, const int64_t *__restrict__ off, int32_t *__restrict__ bucket) {
-  for (int64_t cell = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; cell < ncells;
-       cell += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t s0 = off[cell], s1 = off[cell + 1];
-    for (int64_t i = s0 + 1; i < s1; ++i) {
-      const int32_t v = bucket[i];
-      int64_t k = i - 1;
-      while (k >= s0 && bucket[k] > v) {
-        bucket[k + 1] = bucket[k];
-        --k;
-      }
-      bucket[k + 1] = v;
-    }
+    if (r == 0 || cell_index(ci[r - 1], cj[r - 1], ck[r - 1], cx, cy) != cell) start[cell] = r;
+    if (r == nrows - 1 || cell_index(ci[r + 1], cj[r + 1], ck[r + 1], cx, cy) != cell) end[cell] = r + 1;
   }
 }
 
 // bit per node: does any of its (up to 8) cells hold rows?  Word counts for the ranks.
-__global__ void cell_touch_kernel(int nx, int ny, int nz, const int32_t *__restrict__ cnt, uint32_t *__restrict__ mask,
+__global__ void cell_touch_kernel(int nx, int ny, int nz, const int64_t *__restrict__ start,
+                                  const int64_t *__restrict__ end, uint32_t *__restrict__ mask,
                                   int32_t *__restrict__ wcount) {
   const int64_t n = (int64_t)nx * ny * nz, nwords = (n + 31) / 32;
   const int lane = threadIdx.x & 31;
@@ -113,7 +94,10 @@ __global__ void cell_touch_kernel(int nx, int ny, int nz, const int32_t *__restr
 #pragma unroll
       for (int b = 0; b < 8; ++b) {
         const int ii = i - (b & 1), jj = j - ((b >> 1) & 1), kk = k - ((b >> 2) & 1);
-        if (ii >= 0 && jj >= 0 && kk >= 0 && ii < cx && jj < cy && kk < cz) t |= cnt[cell_index(ii, jj, kk, cx, cy)] > 0;
+        if (ii >= 0 && jj >= 0 && kk >= 0 && ii < cx && jj < cy && kk < cz) {
+          const int64_t cell = cell_index(ii, jj, kk, cx, cy);
+          t |= end[cell] > start[cell];
+        }
       }
     }
     const uint32_t word = __ballot_sync(0xffffffffu, t);
@@ -127,8 +111,8 @@ __global__ void cell_touch_kernel(int nx, int ny, int nz, const int32_t *__restr
 // the 27-point stencils of the marked nodes ([27][knt], rank order) and the
 // per-word ranks
 __global__ void cell_k27_kernel(int nx, int ny, int nz, const uint32_t *__restrict__ mask,
-                                const int64_t *__restrict__ wrank64, const int64_t *__restrict__ off,
-                                const int32_t *__restrict__ bucket, const double *__restrict__ c,
+                                const int64_t *__restrict__ wrank64, const int64_t *__restrict__ start,
+                                const int64_t *__restrict__ end, const double *__restrict__ c,
                                 const double *__restrict__ w2, int64_t knt, float *__restrict__ k27,
                                 int32_t *__restrict__ krank) {
   const int64_t n = (int64_t)nx * ny * nz;
@@ -150,8 +134,7 @@ __global__ void cell_k27_kernel(int nx, int ny, int nz, const uint32_t *__restri
       const int ii = i - (b & 1), jj = j - ((b >> 1) & 1), kk = k - ((b >> 2) & 1);
       if (ii < 0 || jj < 0 || kk < 0 || ii >= cx || jj >= cy || kk >= cz) continue;
       const int64_t cell = cell_index(ii, jj, kk, cx, cy);
-      for (int64_t s = off[cell]; s < off[cell + 1]; ++s) {
-        const int32_t r = bucket[s];
+      for (int64_t r = start[cell]; r < end[cell]; ++r) {
         const double wb = w2[r] * c[8 * (int64_t)r + b];
 #pragma unroll
         for (int q = 0; q < 8; ++q) {

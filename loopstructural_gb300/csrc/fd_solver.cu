@@ -628,6 +628,35 @@ int mg_split_rows(ls_fd_handle *h, const HostRows &rows, int nx, int ny, int nz,
   }
   cr.nrows = (int64_t)cw2.size();
   if (cr.nrows == 0) return LS_OK;
+  // rows sorted (stably) by the Morton code of their cell: a coarse cell's
+  // code is the fine code >> 3, so each cell's rows stay contiguous on every level
+  {
+    auto spread = [](uint64_t v) {
+      uint64_t x = v & 0x1fffffULL;
+      x = (x | x << 32) & 0x1f00000000ffffULL;
+      x = (x | x << 16) & 0x1f0000ff0000ffULL;
+      x = (x | x << 8) & 0x100f00f00f00f00fULL;
+      x = (x | x << 4) & 0x10c30c30c30c30c3ULL;
+      x = (x | x << 2) & 0x1249249249249249ULL;
+      return x;
+    };
+    std::vector<std::pair<uint64_t, int64_t>> key((size_t)cr.nrows);
+    for (int64_t r = 0; r < cr.nrows; ++r)
+      key[r] = {spread((uint64_t)cc[0][r]) | spread((uint64_t)cc[1][r]) << 1 | spread((uint64_t)cc[2][r]) << 2, r};
+    std::sort(key.begin(), key.end());  // (code, row): ties keep row order
+    std::vector<int32_t> sc[3];
+    std::vector<double> sv((size_t)8 * cr.nrows), sw((size_t)cr.nrows);
+    for (int d = 0; d < 3; ++d) sc[d].resize((size_t)cr.nrows);
+    for (int64_t t = 0; t < cr.nrows; ++t) {
+      const int64_t r = key[t].second;
+      for (int d = 0; d < 3; ++d) sc[d][t] = cc[d][r];
+      std::copy(cv.begin() + 8 * r, cv.begin() + 8 * r + 8, sv.begin() + 8 * t);
+      sw[t] = cw2[r];
+    }
+    for (int d = 0; d < 3; ++d) cc[d].swap(sc[d]);
+    cv.swap(sv);
+    cw2.swap(sw);
+  }
   LS_TRY(dev_alloc(&cr.ci, cr.nrows));
   LS_TRY(dev_alloc(&cr.cj, cr.nrows));
   LS_TRY(dev_alloc(&cr.ck, cr.nrows));
@@ -650,47 +679,40 @@ void free_cell_rows(CellRows &cr) {
   cr = CellRows{};
 }
 
-// The level's 27-point form of its (already coarsened) cell rows: buckets of
+// The level's 27-point form of its (already coarsened) cell rows: the runs of
 // rows per cell, the marked nodes, then one gather per marked node.
 int mg_cells_k27(ls_fd_handle *h, MgLevel &lv, const CellRows &cr) {
   MgHierarchy &mg = h->mg;
   cudaStream_t st = h->stream;
   const int cx = lv.nx - 1, cy = lv.ny - 1, cz = lv.nz - 1;
   const int64_t ncells = (int64_t)cx * cy * cz, nwords = (lv.n + 31) / 32;
-  int32_t *cnt = nullptr, *fill = nullptr, *bucket = nullptr, *wcount = nullptr;
-  int64_t *off = nullptr, *wrank = nullptr, *tot = nullptr;
-  LS_CUDA_TRY(cudaMallocAsync((void **)&cnt, ncells * sizeof(int32_t), st));
-  LS_CUDA_TRY(cudaMallocAsync((void **)&fill, ncells * sizeof(int32_t), st));
-  LS_CUDA_TRY(cudaMallocAsync((void **)&bucket, cr.nrows * sizeof(int32_t), st));
+  int32_t *wcount = nullptr;
+  int64_t *start = nullptr, *end = nullptr, *wrank = nullptr, *tot = nullptr;
+  LS_CUDA_TRY(cudaMallocAsync((void **)&start, ncells * sizeof(int64_t), st));
+  LS_CUDA_TRY(cudaMallocAsync((void **)&end, ncells * sizeof(int64_t), st));
   LS_CUDA_TRY(cudaMallocAsync((void **)&wcount, nwords * sizeof(int32_t), st));
-  LS_CUDA_TRY(cudaMallocAsync((void **)&off, (ncells + 1) * sizeof(int64_t), st));
   LS_CUDA_TRY(cudaMallocAsync((void **)&wrank, (nwords + 1) * sizeof(int64_t), st));
-  LS_CUDA_TRY(cudaMallocAsync((void **)&tot, 2 * sizeof(int64_t), st));
-  LS_CUDA_TRY(cudaMemsetAsync(cnt, 0, ncells * sizeof(int32_t), st));
-  LS_CUDA_TRY(cudaMemsetAsync(fill, 0, ncells * sizeof(int32_t), st));
-  const int gr = grid_for(h, cr.nrows);
-  cell_count_kernel<<<gr, kBlock, 0, st>>>(cr.nrows, cr.ci, cr.cj, cr.ck, cx, cy, cnt);
-  setup_scan_kernel<<<1, 1024, 0, st>>>(cnt, ncells, off, tot);
-  LS_CUDA_TRY(cudaMemcpyAsync(off + ncells, &cr.nrows, sizeof(int64_t), cudaMemcpyHostToDevice, st));
-  cell_fill_kernel<<<gr, kBlock, 0, st>>>(cr.nrows, cr.ci, cr.cj, cr.ck, cx, cy, off, fill, bucket);
-  cell_sort_kernel<<<grid_for(h, ncells), kBlock, 0, st>>>(ncells, off, bucket);
+  LS_CUDA_TRY(cudaMallocAsync((void **)&tot, sizeof(int64_t), st));
+  LS_CUDA_TRY(cudaMemsetAsync(start, 0, ncells * sizeof(int64_t), st));
+  LS_CUDA_TRY(cudaMemsetAsync(end, 0, ncells * sizeof(int64_t), st));
+  cell_segments_kernel<<<grid_for(h, cr.nrows), kBlock, 0, st>>>(cr.nrows, cr.ci, cr.cj, cr.ck, cx, cy, start, end);
   LS_TRY(mg_alloc(mg, &lv.kmask, nwords));
   LS_TRY(mg_alloc(mg, &lv.krank, nwords));
-  cell_touch_kernel<<<grid_for(h, nwords * 32), kBlock, 0, st>>>(lv.nx, lv.ny, lv.nz, cnt, lv.kmask, wcount);
-  setup_scan_kernel<<<1, 1024, 0, st>>>(wcount, nwords, wrank, tot + 1);
-  h->launches += 6;
+  cell_touch_kernel<<<grid_for(h, nwords * 32), kBlock, 0, st>>>(lv.nx, lv.ny, lv.nz, start, end, lv.kmask, wcount);
+  setup_scan_kernel<<<1, 1024, 0, st>>>(wcount, nwords, wrank, tot);
+  h->launches += 3;
   int64_t knt = 0;
-  LS_CUDA_TRY(cudaMemcpyAsync(&knt, tot + 1, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(&knt, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   LS_CUDA_TRY(cudaStreamSynchronize(st));
   lv.knt = knt;
   if (knt > 0) {
     LS_TRY(mg_alloc(mg, &lv.k27, (size_t)27 * knt));
-    cell_k27_kernel<<<grid_for(h, lv.n), kBlock, 0, st>>>(lv.nx, lv.ny, lv.nz, lv.kmask, wrank, off, bucket, cr.c,
+    cell_k27_kernel<<<grid_for(h, lv.n), kBlock, 0, st>>>(lv.nx, lv.ny, lv.nz, lv.kmask, wrank, start, end, cr.c,
                                                           cr.w2, knt, lv.k27, lv.krank);
     ++h->launches;
   }
   LS_CUDA_TRY(cudaGetLastError());
-  void *tmp[] = {cnt, fill, bucket, wcount, off, wrank, tot};
+  void *tmp[] = {start, end, wcount, wrank, tot};
   for (void *q : tmp) LS_CUDA_TRY(cudaFreeAsync(q, st));
   LS_CUDA_TRY(cudaStreamSynchronize(st));
   return LS_OK;
