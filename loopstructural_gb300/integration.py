@@ -125,6 +125,15 @@ def gpu_interpolator_classes(li):
             self._sync_engine_c(eng)
             return eng._evaluate_gradient_local(np.asarray(locations, dtype=float))
 
+        def surfaces(self, value, **kwargs):
+            """Isosurfaces of the solved field on the GPU (the reference
+            contours through pyvista, _discrete_interpolator.py:1395-1405);
+            returns loopstructural_gb300 Surface objects."""
+            self.update()
+            eng = self._engine()
+            self._sync_engine_c(eng)
+            return eng.surfaces(value, **kwargs)
+
     class GpuP1Interpolator(_p1_mixin(GpuFiniteDifferenceInterpolator), li.P1Interpolator):
         """Reference P1Interpolator with GB300 face rows, point rows, solve and evaluation."""
 

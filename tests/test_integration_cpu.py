@@ -69,6 +69,10 @@ def test_gpu_subclass_fails_loudly_without_gpu(li):
     interp.set_value_constraints(np.array([[0.5, 0.5, 0.5, 1.0]]))
     with pytest.raises(L.ExtensionUnavailable):
         interp.setup_interpolator(regularisation=0.1)
+    # surfaces go to the engine (the reference's own contours through pyvista)
+    assert gpu_cls.surfaces is not li.FiniteDifferenceInterpolator.surfaces
+    with pytest.raises(L.ExtensionUnavailable):
+        interp.surfaces(0.5)
 
 
 def test_gpu_p1_subclass_keeps_reference_api_and_fails_loudly_without_gpu(li):
