@@ -23,6 +23,7 @@
 #include "fd_directional.cuh"
 #include "fd_mg.cuh"
 #include "fd_mg_cells.cuh"
+#include "mg_rows_host.hpp"
 #include "fd_stencil.cuh"
 #include "ls_common.cuh"
 
@@ -441,13 +442,6 @@ int refresh(ls_fd_handle *h, bool have_x, float *r32, float *p32) {
 // ---------------------------------------------------------------------------
 // multigrid: hierarchy construction and the V-cycle launch sequence
 // ---------------------------------------------------------------------------
-struct HostRows {
-  int64_t nrows = 0;
-  int width = 0;
-  std::vector<int64_t> cols;  // nrows * width, -1 = padding
-  std::vector<double> a;
-  std::vector<double> w2;
-};
 
 template <typename P>
 int mg_alloc(MgHierarchy &mg, P **ptr, size_t count) {
@@ -584,90 +578,21 @@ __global__ void __launch_bounds__(1024) setup_scan_kernel(const int32_t *__restr
 // w^2) for the device path of fd_mg_cells.cuh, and the other rows (interface
 // pairs spanning two cells), kept in row form.
 int mg_split_rows(ls_fd_handle *h, const HostRows &rows, int nx, int ny, int nz, CellRows &cr, HostRows &rest) {
-  rest = HostRows{};
-  rest.width = rows.width;
-  const int64_t nxy = (int64_t)nx * ny;
-  const int lim[3] = {nx, ny, nz};
-  std::vector<int32_t> cc[3];
-  std::vector<double> cv, cw2;
-  for (int64_t r = 0; r < rows.nrows; ++r) {
-    int xyz[64][3];
-    double av[64];
-    int m = 0;
-    bool cell = rows.width <= 64;
-    int lo[3] = {INT32_MAX, INT32_MAX, INT32_MAX}, hi[3] = {-1, -1, -1};
-    for (int k = 0; k < rows.width && cell; ++k) {
-      const int64_t c = rows.cols[r * rows.width + k];
-      if (c < 0) continue;
-      const int z = (int)(c / nxy), rem = (int)(c - (int64_t)z * nxy), y = rem / nx, x = rem - y * nx;
-      const int ax[3] = {x, y, z};
-      for (int d = 0; d < 3; ++d) {
-        xyz[m][d] = ax[d];
-        lo[d] = std::min(lo[d], ax[d]);
-        hi[d] = std::max(hi[d], ax[d]);
-        if (hi[d] - lo[d] > 1) cell = false;
-      }
-      av[m++] = rows.a[r * rows.width + k];
-    }
-    if (m == 0) cell = false;
-    if (!cell) {
-      rest.cols.insert(rest.cols.end(), rows.cols.begin() + r * rows.width, rows.cols.begin() + (r + 1) * rows.width);
-      rest.a.insert(rest.a.end(), rows.a.begin() + r * rows.width, rows.a.begin() + (r + 1) * rows.width);
-      rest.w2.push_back(rows.w2[r]);
-      ++rest.nrows;
-      continue;
-    }
-    int base[3];
-    for (int d = 0; d < 3; ++d) base[d] = std::min(lo[d], lim[d] - 2);  // a box on the upper face ends there
-    double c8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    for (int e = 0; e < m; ++e)
-      c8[(xyz[e][0] - base[0]) | ((xyz[e][1] - base[1]) << 1) | ((xyz[e][2] - base[2]) << 2)] += av[e];
-    for (int d = 0; d < 3; ++d) cc[d].push_back(base[d]);
-    cv.insert(cv.end(), c8, c8 + 8);
-    cw2.push_back(rows.w2[r]);
-  }
-  cr.nrows = (int64_t)cw2.size();
+  CellRowsHost hc;
+  split_cell_rows(rows, nx, ny, nz, hc, rest);
+  cr.nrows = hc.nrows();
   if (cr.nrows == 0) return LS_OK;
-  // rows sorted (stably) by the Morton code of their cell: a coarse cell's
-  // code is the fine code >> 3, so each cell's rows stay contiguous on every level
-  {
-    auto spread = [](uint64_t v) {
-      uint64_t x = v & 0x1fffffULL;
-      x = (x | x << 32) & 0x1f00000000ffffULL;
-      x = (x | x << 16) & 0x1f0000ff0000ffULL;
-      x = (x | x << 8) & 0x100f00f00f00f00fULL;
-      x = (x | x << 4) & 0x10c30c30c30c30c3ULL;
-      x = (x | x << 2) & 0x1249249249249249ULL;
-      return x;
-    };
-    std::vector<std::pair<uint64_t, int64_t>> key((size_t)cr.nrows);
-    for (int64_t r = 0; r < cr.nrows; ++r)
-      key[r] = {spread((uint64_t)cc[0][r]) | spread((uint64_t)cc[1][r]) << 1 | spread((uint64_t)cc[2][r]) << 2, r};
-    std::sort(key.begin(), key.end());  // (code, row): ties keep row order
-    std::vector<int32_t> sc[3];
-    std::vector<double> sv((size_t)8 * cr.nrows), sw((size_t)cr.nrows);
-    for (int d = 0; d < 3; ++d) sc[d].resize((size_t)cr.nrows);
-    for (int64_t t = 0; t < cr.nrows; ++t) {
-      const int64_t r = key[t].second;
-      for (int d = 0; d < 3; ++d) sc[d][t] = cc[d][r];
-      std::copy(cv.begin() + 8 * r, cv.begin() + 8 * r + 8, sv.begin() + 8 * t);
-      sw[t] = cw2[r];
-    }
-    for (int d = 0; d < 3; ++d) cc[d].swap(sc[d]);
-    cv.swap(sv);
-    cw2.swap(sw);
-  }
   LS_TRY(dev_alloc(&cr.ci, cr.nrows));
   LS_TRY(dev_alloc(&cr.cj, cr.nrows));
   LS_TRY(dev_alloc(&cr.ck, cr.nrows));
   LS_TRY(dev_alloc(&cr.c, 8 * cr.nrows));
   LS_TRY(dev_alloc(&cr.w2, cr.nrows));
   cudaStream_t st = h->stream;
-  LS_CUDA_TRY(cudaMemcpyAsync(cr.ci, cc[0].data(), cr.nrows * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-  LS_CUDA_TRY(cudaMemcpyAsync(cr.cj, cc[1].data(), cr.nrows * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-  LS_CUDA_TRY(cudaMemcpyAsync(cr.ck, cc[2].data(), cr.nrows * sizeof(int32_t), cudaMemcpyHostToDevice, st));
-  LS_CUDA_TRY(cudaMemcpyAsync(cr.c, cv.data(), 8 * cr.nrows * sizeof(double), cudaMemcpyHostToDevice, st));
-  LS_CUDA_TRY(cudaMemcpyAsync(cr.w2, cw2.data(), cr.nrows * sizeof(double), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(cr.ci, hc.ci.data(), cr.nrows * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(cr.cj, hc.cj.data(), cr.nrows * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(cr.ck, hc.ck.data(), cr.nrows * sizeof(int32_t), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(cr.c, hc.c.data(), 8 * cr.nrows * sizeof(double), cudaMemcpyHostToDevice, st));
+  LS_CUDA_TRY(cudaMemcpyAsync(cr.w2, hc.w2.data(), cr.nrows * sizeof(double), cudaMemcpyHostToDevice, st));
   LS_CUDA_TRY(cudaStreamSynchronize(st));
   return LS_OK;
 }
