@@ -57,3 +57,25 @@ def test_no_crossing_and_nan_cells():
     full = iso.isosurface(v, (n, n, n), np.zeros(3), np.full(3, h), 1.1)
     part = iso.isosurface(v2, (n, n, n), np.zeros(3), np.full(3, h), 1.1)
     assert 0 < part.shape[0] < full.shape[0]
+
+
+def test_isosurfacer_value_and_name_rules():
+    """LoopIsosurfacer.fit's isovalue / name rules (LoopStructural/utils/_surface.py:96-133)."""
+    import pytest
+
+    from loopstructural_gb300 import surface as S
+
+    v = np.array([0.0, np.nan, 2.0])
+    assert S.isovalues_for(None, v) == [1.0]
+    assert S.isovalues_for(0.5, v) == [0.5]
+    assert S.isovalues_for(0, v) == [0.0]
+    assert S.isovalues_for([0.2, 0.3], v) == [0.2, 0.3]
+    np.testing.assert_allclose(S.isovalues_for(3, v), [0.1, 1.0, 1.9])
+    with pytest.raises(ValueError):
+        S.isovalues_for(-2, v)
+    assert S.surface_names(None, 2) == (["surface", "surface"], False)
+    assert S.surface_names("top", 1) == (["top"], True)
+    assert S.surface_names("top", 2) == (["top", "top"], False)
+    assert S.surface_names(["a", "b"], 2) == (["a", "b"], True)
+    with pytest.raises(ValueError):
+        S.LoopIsosurfacer(object())

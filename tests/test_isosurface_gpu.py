@@ -79,3 +79,28 @@ def test_interpolator_surfaces():
         v = interp.evaluate_value(s.vertices)
         assert np.max(np.abs(v - level)) < 0.02
         assert abs(s.area - 1.0) < 0.2  # a near-horizontal layer across the unit box
+
+
+def test_isosurfacer_on_a_callable():
+    """LoopIsosurfacer (utils/_surface.py API) samples the callable on the box's
+    regular grid and extracts each level with the GPU kernel."""
+    from types import SimpleNamespace
+
+    from loopstructural_gb300.surface import LoopIsosurfacer
+
+    box = SimpleNamespace(origin=np.array([-1.0, -1.0, -1.0]), maximum=np.array([1.0, 1.0, 1.0]),
+                          nsteps=np.array([21, 17, 19]))
+
+    def fn(p):
+        return np.sum(p * p, axis=1)
+
+    surfs = LoopIsosurfacer(box, callable=fn).fit([0.25, 0.64, 9.0], name="shell")
+    assert [s.name for s in surfs] == ["shell_0.25", "shell_0.64"]
+    for s, level in zip(surfs, (0.25, 0.64)):
+        grid = L.StructuredGrid(origin=box.origin, nsteps=box.nsteps - 1,
+                                step_vector=(box.maximum - box.origin) / (box.nsteps - 1))
+        ref = iso.isosurface(fn(grid.nodes), grid.nsteps, grid.origin, grid.step_vector, level)
+        assert s.triangles.shape[0] == ref.shape[0]
+        r = np.linalg.norm(s.vertices, axis=1)
+        assert np.max(np.abs(r - np.sqrt(level))) < 0.05
+        assert np.all(s.values == level)
