@@ -22,6 +22,13 @@ host arrays (constraints set, assembled, solved, evaluated at host points,
 results copied back).  `--impl reference` times the CPU oracle port of the
 reference's default path (explicit assembly + column-scaled scipy CG) on a
 bounded sample and extrapolates to the same workload.
+
+Secondary workloads print their own line (`--workload NAME`): `ensemble`
+(256 FD models solved concurrently), `adjoint` (gradient of a field misfit
+with respect to the value constraints at 128^3), `p1` (TetMesh 128^3),
+`directional` (fold-like directional regularisation at 128^3), `fold`
+(FDFoldInterpolator at 128^3), `isosurface` (256^3 nodes), `mgprofile`
+(per-level multigrid kernel times, the entry used for kernel captures).
 """
 from __future__ import annotations
 
