@@ -40,6 +40,38 @@ class ConstraintFamily:
                 "w": self.w.cpu().numpy()}
 
 
+def normalise_rows(A, B, idc, w=1.0, name="undefined"):
+    """DI:316-389 add_constraints_to_least_squares on host arrays: shape checks
+    (an error logged and None returned when A and idc differ), 3-D blocks
+    flattened (an array w tiled), NaN rows -> warning and None, rows divided
+    by their L2 norm (B with them), w broadcast.  Returns (A, B, idc, w)."""
+    A = np.array(A, dtype=float)
+    B = np.array(B, dtype=float)
+    idc = np.array(idc)
+    if A.shape != idc.shape:
+        logger.error("Cannot add constraints: A and indexes have different shape : %s", name)
+        return None
+    if A.ndim > 2:
+        if isinstance(w, np.ndarray):
+            w = np.tile(w, (A.shape[1]))
+        A = A.reshape((A.shape[0] * A.shape[1], A.shape[2]))
+        idc = idc.reshape((idc.shape[0] * idc.shape[1], idc.shape[2]))
+        B = B.reshape(A.shape[0])
+    if np.any(np.isnan(idc)) or np.any(np.isnan(A)) or np.any(np.isnan(B)):
+        logger.warning("Constraints contain nan not adding constraints: %s", name)
+        return None
+    length = np.linalg.norm(A, axis=1)
+    B[length > 0] /= length[length > 0]
+    A[length > 0, :] /= length[length > 0, None]
+    if isinstance(w, (float, int)):
+        w = np.ones(A.shape[0]) * w
+    if not isinstance(w, np.ndarray):
+        raise TypeError("w must be a numpy array")
+    if w.shape[0] != A.shape[0]:
+        raise ValueError("Weight array does not match number of constraints")
+    return A, B.reshape(-1), idc.astype(np.int64), np.asarray(w, dtype=float)
+
+
 class SetupReport(dict):
     """Row counts per constraint family (the reference returns a
     ConstraintDiagnosticsReport with the same information)."""
@@ -57,6 +89,7 @@ class _DiscreteInterpolatorBase:
         self.interpolation_weights = {}
         self.latest_solve_timing = {}
         self.constraints: dict[str, ConstraintFamily] = {}
+        self.family_order: list[str] = []
         self.up_to_date = False
         self._c = np.zeros(self.support.n_nodes)
         self._c_dev = None
@@ -187,8 +220,83 @@ class _DiscreteInterpolatorBase:
         if bool(torch.isnan(a).any()) or bool(torch.isnan(b).any()):
             logger.warning("Constraints contain nan not adding constraints: %s", name)
             return
-        name = self._unique_name(name, self.constraints)
+        name = self._unique_name(name, self._taken_names())
         self.constraints[name] = ConstraintFamily(name, idc, a, b, w)
+        self.family_order.append(name)
+
+    def _taken_names(self):
+        taken = set(self.constraints)
+        taken |= set(getattr(self, "regularisation_families", {}))
+        taken |= set(getattr(self, "directional_families", {}))
+        return taken
+
+    def add_constraints_to_least_squares(self, A, B, idc, w=1.0, name="undefined"):
+        """Adds a constraint family from host arrays (DI:316-389): rows of
+        coefficients A over columns idc with targets B and weights w, row
+        normalised; the family joins the next solve."""
+        import torch
+
+        out = normalise_rows(A, B, idc, w, name)
+        if out is None:
+            return
+        A, B, idc, w = out
+        if idc.size and (idc.min() < 0 or idc.max() >= self.dof):
+            raise ValueError("constraint column index out of range")
+        dev = _lib.device()
+        self._add_family(name, torch.from_numpy(idc).to(dev), torch.from_numpy(A).to(dev),
+                         torch.from_numpy(B).to(dev), torch.from_numpy(w).to(dev))
+        self.up_to_date = False
+
+    def clear_constraints(self):
+        """Drops every constraint family (DI:297-304)."""
+        self.constraints = {}
+        if hasattr(self, "regularisation_families"):
+            self.regularisation_families = {}
+        if hasattr(self, "_reset_directional"):
+            self._reset_directional()
+        self.family_order = []
+        self._release_system()
+
+    def _family_rows(self, name):
+        """(idc, A, B, w) host arrays of any family, in the reference's form."""
+        if name in self.constraints:
+            return self.constraints[name].numpy()
+        if name in getattr(self, "directional_families", {}):
+            return self.directional_rows(name)
+        return self.regularisation_rows(name)
+
+    def calculate_residual_for_constraints(self):
+        """A c - B of every family (DI:453-465), by family name."""
+        c = np.asarray(self.c, dtype=float)
+        out = {}
+        for name in self.family_order:
+            f = self._family_rows(name)
+            idc = f["idc"]
+            vals = np.where(idc >= 0, c[np.clip(idc, 0, None)], 0.0)
+            out[name] = np.einsum("ij,ij->i", f["A"], vals) - f["B"].reshape(-1)
+        return out
+
+    def build_matrix(self):
+        """The explicit weighted system (DI:684-755): every family's rows times
+        its weights, stacked in the order the families were added, as a CSR
+        matrix and right-hand side (no ridge; the solve adds it)."""
+        from scipy import sparse
+
+        mats, bs = [], []
+        for name in self.family_order:
+            f = self._family_rows(name)
+            n, k = f["A"].shape
+            if n == 0:
+                continue
+            keep = f["idc"].reshape(-1) >= 0
+            rows = np.repeat(np.arange(n), k)[keep]
+            m = sparse.coo_matrix((f["A"].reshape(-1)[keep], (rows, f["idc"].reshape(-1)[keep])),
+                                  shape=(n, self.dof)).tocsr()
+            mats.append(m.multiply(f["w"][:, None]).tocsr())
+            bs.append(f["B"].reshape(-1) * f["w"])
+        if not mats:
+            return sparse.csr_matrix((0, self.dof)), np.zeros(0)
+        return sparse.vstack(mats).tocsr(), np.hstack(bs)
 
     # -- directional regularisation (DI:395-451) ----------------------------
     def resolve_regularisation_config(self, regularisation=None, directional_regularisation=None):
@@ -232,6 +340,7 @@ class _DiscreteInterpolatorBase:
 
     def reset(self):
         self.constraints = {}
+        self.family_order = []
         self._release_system()
 
     def _release_system(self):
@@ -246,9 +355,40 @@ class _DiscreteInterpolatorBase:
         return bool(self.up_to_date)
 
     # -- solve (DI:1221-1319, SS:48-72) ---------------------------------------
+    def _solve_with_callable(self, solver):
+        """A custom solver on the explicit system (DI:1283-1313 with
+        SS:32-45): build_matrix, the ridge rows and the column scaling S of
+        the reference's preprocessing, c = S solver(A S, b)."""
+        from scipy import sparse
+
+        started = perf_counter()
+        A, b = self.build_matrix()
+        t0 = perf_counter()
+        if self.add_ridge_regulatisation:
+            A = sparse.vstack([A, sparse.eye(A.shape[1]) * self.ridge_factor]).tocsr()
+            b = np.hstack([b, np.zeros(A.shape[1])])
+        S = None
+        if self.apply_scaling_matrix:
+            norms = sparse.linalg.norm(A, axis=0)
+            scale = np.ones(A.shape[1])
+            scale[norms > 0] = 1.0 / norms[norms > 0]
+            S = sparse.diags(scale)
+            A = A @ S
+        t1 = perf_counter()
+        logger.warning("Using custom solver")
+        c = np.asarray(solver(A.tocsr(), b))
+        t2 = perf_counter()
+        self._c = np.asarray(S @ c if S is not None else c, dtype=float)
+        self._c_dev = None
+        self.up_to_date = True
+        self.latest_solve_timing = {"solver": "callable", "backend": "host", "assembly_seconds": t0 - started,
+                                    "preprocess_seconds": t1 - t0, "solve_seconds": t2 - t1,
+                                    "matrix_rows": int(A.shape[0]), "matrix_cols": int(A.shape[1]),
+                                    "matrix_nnz": int(A.nnz), "total_seconds": perf_counter() - started,
+                                    "up_to_date": True}
+        return True
+
     def _solver_options(self, solver, tol, solver_kwargs):
-        if callable(solver):
-            raise NotImplementedError("custom solver callables need an explicit matrix; use solver='cg'")
         if solver not in ("cg", "lsmr", "admm", None):
             logger.warning("Unknown solver %s using cg. Available solvers are cg, lsmr, admm", solver)
             solver = "cg"
@@ -290,6 +430,8 @@ class _DiscreteInterpolatorBase:
     def solve_system(self, solver=None, tol=None, solver_kwargs=None) -> bool:
         import torch
 
+        if callable(solver):
+            return self._solve_with_callable(solver)
         solve_started = perf_counter()
         self._c = np.full(self.support.n_nodes, np.nan)
         self._c_dev = None
@@ -372,6 +514,7 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
 
     def reset(self):
         super().reset()
+        self.regularisation_families = {}
         self._reset_directional()
 
     def setup_interpolator(self, **kwargs) -> SetupReport:
@@ -447,6 +590,7 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
                 fam = self._unique_name(f"{name}_{op}", taken)
                 taken.add(fam)
                 self.directional_families[fam] = (int(counts[f]), len(self._dir_terms) - 1, op)
+                self.family_order.append(fam)
         self.up_to_date = False
 
     def add_gradient_orthogonal_constraints(self, points, vectors, w=1.0, b=0, name="gradient orthogonal"):
@@ -543,12 +687,14 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
                 rows, _ = fd.reg_shape(self.support, name)
                 if rows > 0:
                     self.regularisation_families[name] = (rows, float(weight))
+                    self.family_order.append(name)
         if borders:
             for name, key in (("dx_lower", "dx"), ("dx_upper", "dx"), ("dy_lower", "dy"), ("dy_upper", "dy"),
                               ("dz_lower", "dz"), ("dz_upper", "dz")):
                 rows, _ = fd.reg_shape(self.support, name)
                 if w[key] != 0 and rows > 0:
                     self.regularisation_families[name] = (rows, float(w[key]))
+                    self.family_order.append(name)
 
     def regularisation_rows(self, name):
         """Explicit (idc, A, B, w) of a matrix-free family, as the reference's

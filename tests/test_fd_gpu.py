@@ -373,3 +373,24 @@ def test_coarse_levels_are_galerkin(cells):
         ref = G @ x
         assert np.max(np.abs(y.cpu().numpy() - ref)) <= 2e-5 * np.max(np.abs(ref)), level
     system.close()
+
+
+@pytest.mark.parametrize("name", ["fd_small", "fd_cfg1_20"])
+def test_build_matrix_and_custom_solver_match_reference(golden, name):
+    """The explicit system (DI:684-755) in the reference's family order, and a
+    custom solver callable on it (DI:1283-1313)."""
+    from scipy.sparse.linalg import spsolve
+
+    interp = _interp(golden, name)
+    _g, cs = _oracle_system(golden, name)
+    assert interp.family_order == [str(s) for s in golden[f"{name}_family_names"]]
+    A, b = interp.build_matrix()
+    Ar, br = cs.matrix()
+    assert A.shape == Ar.shape
+    assert abs(A - Ar).max() <= 1e-15 * abs(Ar).max()
+    np.testing.assert_allclose(b, br, rtol=1e-15, atol=1e-15 * np.max(np.abs(br)))
+    assert interp.solve_system(lambda M, rhs: spsolve((M.T @ M).tocsc(), M.T @ rhs))
+    ref = golden[f"{name}_c_direct"]
+    assert np.linalg.norm(interp.c - ref) <= 1e-8 * np.linalg.norm(ref)
+    res = interp.calculate_residual_for_constraints()
+    assert set(res) == set(cs.families)
