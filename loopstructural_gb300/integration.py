@@ -100,6 +100,28 @@ def gpu_interpolator_classes(li):
             self.up_to_date = False
             return terms
 
+        # the explicit-matrix API works on the engine's families
+        def add_constraints_to_least_squares(self, A, B, idc, w=1.0, name="undefined"):
+            eng = self._engine()
+            eng.add_constraints_to_least_squares(A, B, idc, w=w, name=name)
+            self._mirror_families(eng)
+            self.up_to_date = False
+
+        def build_matrix(self):
+            return self._engine().build_matrix()
+
+        def calculate_residual_for_constraints(self):
+            eng = self._engine()
+            eng.c = np.array(self.c, dtype=float)
+            return eng.calculate_residual_for_constraints()
+
+        def clear_constraints(self):
+            eng = self._engine()
+            eng.clear_constraints()
+            self._mirror_families(eng)
+            self.ineq_constraints = {}
+            self.equal_constraints = {}
+
         def solve_system(self, solver=None, tol=None, solver_kwargs=None):
             eng = self._engine()
             ok = eng.solve_system(solver, tol, solver_kwargs)

@@ -71,6 +71,11 @@ def test_gpu_subclass_fails_loudly_without_gpu(li):
         interp.setup_interpolator(regularisation=0.1)
     # surfaces go to the engine (the reference's own contours through pyvista)
     assert gpu_cls.surfaces is not li.FiniteDifferenceInterpolator.surfaces
+    # so do the explicit-matrix methods (a family added through the reference's
+    # own method would otherwise never reach the GPU solve)
+    for meth in ("add_constraints_to_least_squares", "build_matrix", "calculate_residual_for_constraints",
+                 "clear_constraints"):
+        assert meth in gpu_cls.__dict__, meth
     with pytest.raises(L.ExtensionUnavailable):
         interp.surfaces(0.5)
 
