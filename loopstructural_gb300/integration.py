@@ -73,10 +73,10 @@ def gpu_interpolator_classes(li):
             for name, fam in eng.constraints.items():
                 self.constraints[name] = {"matrix": SimpleNamespace(shape=(fam.n_rows, self.dof)), "b": None,
                                           "w": fam.w.cpu().numpy()}
-            for name, (rows, w) in eng.regularisation_families.items():
+            for name, (rows, w) in getattr(eng, "regularisation_families", {}).items():
                 self.constraints[name] = {"matrix": SimpleNamespace(shape=(rows, self.dof)), "b": None,
                                           "w": np.full(rows, w)}
-            for name, (rows, _t, _f) in eng.directional_families.items():
+            for name, (rows, _t, _f) in getattr(eng, "directional_families", {}).items():
                 self.constraints[name] = {"matrix": SimpleNamespace(shape=(rows, self.dof)), "b": None,
                                           "w": None}
 
@@ -174,6 +174,11 @@ def _p1_mixin(fd_cls):
         _sync_engine_c = fd_cls._sync_engine_c
         _evaluate_value_local = fd_cls._evaluate_value_local
         _evaluate_gradient_local = fd_cls._evaluate_gradient_local
+        _mirror_families = fd_cls._mirror_families
+        add_constraints_to_least_squares = fd_cls.add_constraints_to_least_squares
+        build_matrix = fd_cls.build_matrix
+        calculate_residual_for_constraints = fd_cls.calculate_residual_for_constraints
+        clear_constraints = fd_cls.clear_constraints
 
         def setup_interpolator(self, **kwargs):
             eng = self._engine()
