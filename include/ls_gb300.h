@@ -168,19 +168,24 @@ int ls_fd_apply(ls_fd_handle *h, const double *d_x, double *d_y, void *stream);
 /* the same operator in FP32 (the inner-iteration kernel of the mixed solve) */
 int ls_fd_apply_f32(ls_fd_handle *h, const float *d_x, float *d_y, void *stream);
 /* No-allocation variant of ls_fd_apply (no counterpart in the reference, which
- * has no device code).  For callers that cannot call cudaMalloc -- inside a CUDA
- * stream capture, or under a framework that owns all device memory -- it takes
- * the system description directly (no handle) and keeps its private scratch
- * (one FP64 value per data row plus reduction partials) in a static device
- * array of LS_NOALLOC_SCRATCH_DOUBLES doubles (~8.4 MB per GPU that loads the
- * library, held until the process exits).  Limits: sys->nrows <=
- * LS_NOALLOC_MAX_ROWS and sys->d_dir == NULL, else LS_ERR_ARG.  Computes d_y = N d_x (FP64) and, when
- * h_xNx is not NULL, x.Nx (written to host memory after a stream sync).  The
- * first call on a device resolves the array's device address
- * (cudaGetSymbolAddress), so make that first call before any stream capture.
- * Every call shares the one array: calls that overlap on the GPU race and must
- * be serialised by the caller.  The data-row scatter uses FP64 atomics, so the
- * result can differ from ls_fd_apply in the last bits. */
+ * has no device code).  For callers that cannot call cudaMalloc -- a host
+ * framework that owns all device memory through its own pool, or a plugin
+ * running under a fixed device-memory budget -- it takes the system
+ * description directly (no handle) and keeps its private scratch (one FP64
+ * value per data row plus reduction partials) in a static device array of
+ * LS_NOALLOC_SCRATCH_DOUBLES doubles (~8.4 MB per GPU that loads the library,
+ * held until the process exits).  Limits: sys->nrows <= LS_NOALLOC_MAX_ROWS,
+ * sys->d_dir == NULL and at most 524,280 nodes along y, else LS_ERR_ARG.
+ * Computes d_y = N d_x (FP64).  When h_xNx is not NULL it also writes x.Nx to
+ * host memory, which copies to the host and synchronises `stream` before
+ * returning; pass NULL for a call that only enqueues work.  Data-row columns
+ * must be < dof: out-of-range columns are skipped, and reported as LS_ERR_ARG
+ * when h_xNx is not NULL.  The first call on a device resolves the array's
+ * device address (cudaGetSymbolAddress), so make that first call before any
+ * stream capture.  Every call shares the one array, which keeps the last
+ * call's contents: calls that overlap on the GPU race and must be serialised
+ * by the caller.  The data-row scatter uses FP64 atomics, so the result can
+ * differ from ls_fd_apply in the last bits. */
 #define LS_NOALLOC_MAX_ROWS 1048576
 #define LS_NOALLOC_SCRATCH_DOUBLES (LS_NOALLOC_MAX_ROWS + 4096 + 8)
 int ls_fd_apply_noalloc(const ls_fd_system *sys, const double *d_x, double *d_y, double *h_xNx, void *stream);

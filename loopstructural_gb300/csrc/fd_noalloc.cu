@@ -1,10 +1,10 @@
 // ls_fd_apply_noalloc: the FP64 normal-operator apply for callers that cannot
 // allocate device memory.
 //
-// Who needs it: code that runs where cudaMalloc is off limits -- inside a CUDA
-// stream capture (allocation calls are not capturable), under a host framework
-// that owns all device memory through its own pool and forbids side
-// allocations, or in a latency-critical loop that must not touch the driver's
+// Who needs it: code running where cudaMalloc is off limits -- a host
+// framework that owns all device memory through its own pool and forbids side
+// allocations, a plugin loaded into a process with a fixed device-memory
+// budget, or a latency-critical loop that must not enter the driver's
 // allocator.  Those callers still own every input and output buffer; what they
 // cannot provide is the operator's private scratch (one FP64 value per data
 // row, plus the reduction partials of the optional x.Nx dot product).
@@ -12,13 +12,18 @@
 // The scratch is a file-scope static __device__ array of LS_NOALLOC_SCRATCH_DOUBLES
 // doubles (8.4 MB) that every GPU which loads this library holds until the
 // process exits.  It caps the data rows at LS_NOALLOC_MAX_ROWS; larger systems
-// are rejected with LS_ERR_ARG.  All calls share the one array: calls that
-// overlap on the GPU (different streams, or different host threads) race on
-// it and must be serialised by the caller.  The data-row scatter uses FP64
-// atomics, so results may differ from ls_fd_apply in the last bits.
+// are rejected with LS_ERR_ARG.  All calls share the one array and it keeps
+// the last call's contents: calls that overlap on the GPU (different streams,
+// or different host threads) race on it and must be serialised by the caller.
+// The data-row scatter uses FP64 atomics, so results may differ from
+// ls_fd_apply in the last bits.  Data-row columns must be < dof: a column
+// outside the grid is skipped by the kernels and raises a flag word in the
+// scratch, which the call reports as LS_ERR_ARG when it reads x.Nx back.
 #include <math.h>
+#include <string.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "fd_stencil.cuh"
 #include "ls_common.cuh"
@@ -30,14 +35,15 @@ constexpr int kNoallocBlock = kNoallocTX * kNoallocTY;
 constexpr int64_t kMaxRows = LS_NOALLOC_MAX_ROWS;
 constexpr int kMaxBlocks = 4096;
 // layout: [0, kMaxRows) per-row products | [kMaxRows, +kMaxBlocks) partials |
-//         ticket word | dot result
+//         ticket word | dot result | bad-column flag
 constexpr int64_t kScratchDoubles = kMaxRows + kMaxBlocks + 8;
 static_assert(kScratchDoubles == LS_NOALLOC_SCRATCH_DOUBLES, "scratch size mismatch");
 
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
 // device address of g_noalloc_scratch per device, resolved once per device
-double *g_scratch_ptr[64] = {nullptr};
+// (every thread that resolves it stores the same address)
+std::atomic<double *> g_scratch_ptr[64];
 
 __global__ void __launch_bounds__(kNoallocBlock) noalloc_stencil_kernel(ls::CoefT<double> c,
                                                                         const double *__restrict__ x,
@@ -52,27 +58,33 @@ __global__ void __launch_bounds__(kNoallocBlock) noalloc_stencil_kernel(ls::Coef
 }
 
 // s_r = w_r^2 (a_r . x) into the scratch
-__global__ void noalloc_rows_kernel(int64_t nrows, int width, const int64_t *__restrict__ idc,
+// (a column >= n is skipped and raises *bad)
+__global__ void noalloc_rows_kernel(int64_t nrows, int width, int64_t n, const int64_t *__restrict__ idc,
                                     const double *__restrict__ a, const double *__restrict__ w,
-                                    const double *__restrict__ x, double *__restrict__ s) {
+                                    const double *__restrict__ x, double *__restrict__ s, unsigned int *bad) {
   for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nrows; r += (int64_t)gridDim.x * blockDim.x) {
     double acc = 0.0;
     for (int k = 0; k < width; ++k) {
       const int64_t col = idc[r * width + k];
-      if (col >= 0) acc += a[r * width + k] * x[col];
+      if (col >= n) {
+        *bad = 1u;
+      } else if (col >= 0) {
+        acc += a[r * width + k] * x[col];
+      }
     }
     s[r] = w[r] * w[r] * acc;
   }
 }
 
 // y[col] += a_rk s_r
-__global__ void noalloc_scatter_kernel(int64_t nrows, int width, const int64_t *__restrict__ idc,
+// (columns outside [0, n) are skipped; the rows kernel has flagged them)
+__global__ void noalloc_scatter_kernel(int64_t nrows, int width, int64_t n, const int64_t *__restrict__ idc,
                                        const double *__restrict__ a, const double *__restrict__ s,
                                        double *__restrict__ y) {
   const int64_t ne = nrows * width;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t col = idc[e];
-    if (col >= 0) atomicAdd(y + col, a[e] * s[e / width]);
+    if (col >= 0 && col < n) atomicAdd(y + col, a[e] * s[e / width]);
   }
 }
 
@@ -95,12 +107,14 @@ int scratch_for_current_device(double **out) {
     ls::set_error("device ordinal %d out of range", dev);
     return LS_ERR_ARG;
   }
-  if (g_scratch_ptr[dev] == nullptr) {
+  double *cached = g_scratch_ptr[dev].load(std::memory_order_relaxed);
+  if (cached == nullptr) {
     void *p = nullptr;
     LS_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_scratch_ptr[dev] = static_cast<double *>(p);
+    cached = static_cast<double *>(p);
+    g_scratch_ptr[dev].store(cached, std::memory_order_relaxed);
   }
-  *out = g_scratch_ptr[dev];
+  *out = cached;
   return LS_OK;
 }
 
@@ -132,25 +146,37 @@ extern "C" int ls_fd_apply_noalloc(const ls_fd_system *sys, const double *d_x, d
   const ls::StencilCoef c64 = ls::make_stencil_coef(g, sys->w_dxx, sys->w_dyy, sys->w_dzz, sys->w_dxy, sys->w_dyz,
                                                   sys->w_dxz, sys->w_dx, sys->w_dy, sys->w_dz, sys->ridge);
   const int gx = (int)((g.nsteps[0] + kNoallocTX - 1) / kNoallocTX);
-  const int gy = (int)((g.nsteps[1] + kNoallocTY - 1) / kNoallocTY);
+  const int64_t gy = (g.nsteps[1] + kNoallocTY - 1) / kNoallocTY;
+  LS_ARG_CHECK(gy <= 65535, "ls_fd_apply_noalloc: the y axis is limited to 524,280 nodes");
   const int gz = (int)std::min<int64_t>(g.nsteps[2], 64);
-  noalloc_stencil_kernel<<<dim3(gx, gy, gz), dim3(kNoallocTX, kNoallocTY), 0, s>>>(ls::coef_as<double>(c64), d_x, d_y);
+  double *partials = scratch + kMaxRows;
+  unsigned int *ticket = reinterpret_cast<unsigned int *>(scratch + kMaxRows + kMaxBlocks);
+  double *out = scratch + kMaxRows + kMaxBlocks + 1;  // out[0] = x.Nx, out[1] = bad-column flag word
+  unsigned int *bad = reinterpret_cast<unsigned int *>(out + 1);
+  // the ticket and the flag must start at zero; the scratch keeps whatever the last call left
+  LS_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(double), s));
+  LS_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(double), s));
+  noalloc_stencil_kernel<<<dim3(gx, (int)gy, gz), dim3(kNoallocTX, kNoallocTY), 0, s>>>(ls::coef_as<double>(c64), d_x,
+                                                                                         d_y);
   if (sys->nrows > 0) {
-    noalloc_rows_kernel<<<ls::stream_grid(sys->nrows, 256), 256, 0, s>>>(sys->nrows, sys->width, sys->d_idc, sys->d_a,
-                                                                         sys->d_w, d_x, scratch);
+    noalloc_rows_kernel<<<ls::stream_grid(sys->nrows, 256), 256, 0, s>>>(sys->nrows, sys->width, n, sys->d_idc,
+                                                                         sys->d_a, sys->d_w, d_x, scratch, bad);
     noalloc_scatter_kernel<<<ls::stream_grid(sys->nrows * sys->width, 256), 256, 0, s>>>(
-        sys->nrows, sys->width, sys->d_idc, sys->d_a, scratch, d_y);
+        sys->nrows, sys->width, n, sys->d_idc, sys->d_a, scratch, d_y);
   }
   if (h_xNx != nullptr) {
-    double *partials = scratch + kMaxRows;
-    unsigned int *ticket = reinterpret_cast<unsigned int *>(scratch + kMaxRows + kMaxBlocks);
-    double *out = scratch + kMaxRows + kMaxBlocks + 1;
-    // the ticket must start at zero; the scratch keeps whatever the last call left
-    LS_CUDA_TRY(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));
     const int nb = std::min(ls::stream_grid(n, 256), kMaxBlocks);
     noalloc_dot_kernel<<<nb, 256, 0, s>>>(n, d_x, d_y, partials, ticket, out);
-    LS_CUDA_TRY(cudaMemcpyAsync(h_xNx, out, sizeof(double), cudaMemcpyDeviceToHost, s));
+    double back[2] = {0.0, 0.0};
+    LS_CUDA_TRY(cudaMemcpyAsync(back, out, sizeof(back), cudaMemcpyDeviceToHost, s));
     LS_CUDA_TRY(cudaStreamSynchronize(s));
+    unsigned int flag = 0;
+    memcpy(&flag, &back[1], sizeof(flag));
+    if (flag != 0) {
+      ls::set_error("ls_fd_apply_noalloc: a data-row column is outside [0, dof); those entries were skipped");
+      return LS_ERR_ARG;
+    }
+    *h_xNx = back[0];
   }
   LS_CUDA_TRY(cudaGetLastError());
   return LS_OK;

@@ -25,50 +25,54 @@ _DEFAULT = object()
 _ALIGNMENT_MODES = {"none", "warn", "correct"}
 
 
+def _dgz_normal_agreement(fold, normals):
+    """Median cosine between the fold's dgz direction and the normal vectors
+    of the normal constraints (rows x y z nx ny nz ...), over the rows where
+    both are finite and non-zero; None when it cannot be measured (no usable
+    rows, or a fold that cannot evaluate dgz at the points)."""
+    table = np.asarray(normals, dtype=float)
+    if table.ndim != 2 or table.shape[1] < 6 or len(table) == 0:
+        return None
+    try:
+        dgz = np.asarray(fold.get_deformed_orientation(table[:, :3])[2], dtype=float)
+    except (AttributeError, TypeError, ValueError, RuntimeError) as exc:
+        logger.warning("dgz could not be evaluated at the normal constraints (%s); fold_norm left as given.", exc)
+        return None
+    if dgz.ndim != 2 or dgz.shape[1] != 3:
+        logger.warning("dgz has shape %s, expected (n, 3); fold_norm left as given.", getattr(dgz, "shape", None))
+        return None
+    rows = min(len(dgz), len(table))
+    if rows != len(dgz) or rows != len(table):
+        logger.warning("dgz has %d rows and the normals %d; comparing the first %d.", len(dgz), len(table), rows)
+    a, b = dgz[:rows], table[:rows, 3:6]
+    la, lb = np.linalg.norm(a, axis=1), np.linalg.norm(b, axis=1)
+    usable = np.isfinite(a).all(axis=1) & np.isfinite(b).all(axis=1) & (la > 1e-12) & (lb > 1e-12)
+    if not usable.any():
+        return None
+    cosines = np.sum(a[usable] * b[usable], axis=1) / (la[usable] * lb[usable])
+    return float(np.median(cosines))
+
+
 def resolve_fold_norm_target(*, fold, normal_constraints, fold_norm, dgz_alignment, default_fold_norm=-1.0):
-    """Target of grad(f) . dgz (FN:9-118): ``fold_norm`` (default -1), its sign
-    flipped under ``dgz_alignment='correct'`` when dgz points against the
-    normal constraints (median unit dot product below -0.2); ``'warn'`` only
-    logs, ``'none'`` skips the check."""
+    """Target of grad(f) . dgz for the fold-normalisation rows (FN:9-118).
+
+    It is ``fold_norm`` (``default_fold_norm`` when None).  With
+    ``dgz_alignment`` 'warn' (the default) or 'correct', the fold's dgz is
+    compared with the normal constraints: a median cosine below -0.2 means dgz
+    points against the data, which is logged, and under 'correct' the target's
+    sign is flipped.  'none' skips the comparison; any other mode raises
+    ValueError."""
     target = float(default_fold_norm if fold_norm is None else fold_norm)
     mode = "warn" if dgz_alignment is None else str(dgz_alignment).strip().lower()
     if mode not in _ALIGNMENT_MODES:
         raise ValueError(f"dgz_alignment must be one of {{{', '.join(sorted(_ALIGNMENT_MODES))}}}, got {dgz_alignment!r}")
-    if mode == "none":
+    agreement = None if mode == "none" else _dgz_normal_agreement(fold, normal_constraints)
+    if agreement is None or agreement >= -0.2:
         return target
-    normals = np.asarray(normal_constraints, dtype=float)
-    if normals.ndim != 2 or normals.shape[0] == 0 or normals.shape[1] < 6:
-        return target
-    vec = normals[:, 3:6]
-    try:
-        _, _, dgz = fold.get_deformed_orientation(normals[:, :3])
-    except (AttributeError, TypeError, ValueError, RuntimeError) as exc:
-        logger.warning("Could not evaluate dgz for alignment check (%s).", exc)
-        return target
-    dgz = np.asarray(dgz, dtype=float)
-    if dgz.ndim != 2 or dgz.shape[1] != vec.shape[1]:
-        logger.warning("Skipping dgz alignment check due to unexpected dgz shape %s.", getattr(dgz, "shape", None))
-        return target
-    if dgz.shape[0] != vec.shape[0]:
-        n = min(dgz.shape[0], vec.shape[0])
-        logger.warning("dgz alignment check received mismatched rows (dgz=%d, normals=%d); using first %d.",
-                       dgz.shape[0], vec.shape[0], n)
-        if n == 0:
-            return target
-        dgz, vec = dgz[:n], vec[:n]
-    nn = np.linalg.norm(vec, axis=1)
-    dn = np.linalg.norm(dgz, axis=1)
-    ok = np.all(np.isfinite(vec), axis=1) & np.all(np.isfinite(dgz), axis=1) & (nn > 1e-12) & (dn > 1e-12)
-    if not np.any(ok):
-        return target
-    med = float(np.median(np.einsum("ij,ij->i", dgz[ok] / dn[ok, None], vec[ok] / nn[ok, None])))
-    if med < -0.2:
-        logger.warning("Detected dgz opposite to normal constraints (median dot %.3f). "
-                       "fold_norm may need sign inversion.", med)
-        if mode == "correct":
-            target *= -1.0
-            logger.warning("Auto-correcting fold_norm sign to %.3f using dgz_alignment='correct'.", target)
-    return target
+    flipped = mode == "correct"
+    logger.warning("dgz points opposite to the normal constraints (median cosine %.3f); %s", agreement,
+                   f"fold_norm sign flipped to {-target:.3f}." if flipped else "fold_norm may need the opposite sign.")
+    return -target if flipped else target
 
 
 class FDFoldInterpolator(FiniteDifferenceInterpolator):

@@ -40,36 +40,52 @@ class ConstraintFamily:
                 "w": self.w.cpu().numpy()}
 
 
-def normalise_rows(A, B, idc, w=1.0, name="undefined"):
-    """DI:316-389 add_constraints_to_least_squares on host arrays: shape checks
-    (an error logged and None returned when A and idc differ), 3-D blocks
-    flattened (an array w tiled), NaN rows -> warning and None, rows divided
-    by their L2 norm (B with them), w broadcast.  Returns (A, B, idc, w)."""
-    A = np.array(A, dtype=float)
-    B = np.array(B, dtype=float)
-    idc = np.array(idc)
-    if A.shape != idc.shape:
-        logger.error("Cannot add constraints: A and indexes have different shape : %s", name)
-        return None
-    if A.ndim > 2:
-        if isinstance(w, np.ndarray):
-            w = np.tile(w, (A.shape[1]))
-        A = A.reshape((A.shape[0] * A.shape[1], A.shape[2]))
-        idc = idc.reshape((idc.shape[0] * idc.shape[1], idc.shape[2]))
-        B = B.reshape(A.shape[0])
-    if np.any(np.isnan(idc)) or np.any(np.isnan(A)) or np.any(np.isnan(B)):
-        logger.warning("Constraints contain nan not adding constraints: %s", name)
-        return None
-    length = np.linalg.norm(A, axis=1)
-    B[length > 0] /= length[length > 0]
-    A[length > 0, :] /= length[length > 0, None]
+def _row_weights(w, nrows):
+    """Per-row weights: a Python number is broadcast; anything else must be an
+    array of one weight per row (TypeError / ValueError otherwise, the
+    reference's exceptions)."""
     if isinstance(w, (float, int)):
-        w = np.ones(A.shape[0]) * w
+        return np.full(nrows, float(w))
     if not isinstance(w, np.ndarray):
         raise TypeError("w must be a numpy array")
-    if w.shape[0] != A.shape[0]:
+    if w.shape[0] != nrows:
         raise ValueError("Weight array does not match number of constraints")
-    return A, B.reshape(-1), idc.astype(np.int64), np.asarray(w, dtype=float)
+    return np.asarray(w, dtype=float)
+
+
+def normalise_rows(A, B, idc, w=1.0, name="undefined"):
+    """The row preparation of DI:316-389 add_constraints_to_least_squares on
+    host arrays; returns (A, B, idc, w) as 2-D rows, or None when the family is
+    dropped.
+
+    * A and idc must have the same shape (else an error is logged, None).
+    * A 3-D block (points x rows-per-point x columns) becomes point-major rows;
+      an array w is then repeated once per row of a point, as the reference
+      does (``np.tile``), so callers pass per-row weights that way.
+    * A NaN anywhere in A, B or idc drops the family with a warning.
+    * Every row with a non-zero L2 norm is divided by it, B with it.
+    * w: see ``_row_weights``."""
+    coef = np.array(A, dtype=float)
+    cols = np.array(idc)
+    if coef.shape != cols.shape:
+        logger.error("Cannot add constraints: A and indexes have different shape : %s", name)
+        return None
+    rhs = np.array(B, dtype=float)
+    if coef.ndim > 2:
+        per_point = coef.shape[1]
+        coef = coef.reshape(-1, coef.shape[-1])
+        cols = cols.reshape(coef.shape)
+        rhs = rhs.reshape(len(coef))
+        if isinstance(w, np.ndarray):
+            w = np.tile(w, per_point)
+    if any(np.isnan(arr).any() for arr in (cols, coef, rhs)):
+        logger.warning("Constraints contain nan not adding constraints: %s", name)
+        return None
+    norms = np.linalg.norm(coef, axis=1)
+    scaled = norms > 0
+    coef[scaled] /= norms[scaled, None]
+    rhs[scaled] /= norms[scaled]
+    return coef, rhs.reshape(-1), cols.astype(np.int64), _row_weights(w, len(coef))
 
 
 class SetupReport(dict):

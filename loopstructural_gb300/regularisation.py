@@ -1,103 +1,150 @@
 """Regularisation configuration: an isotropic weight plus directional terms.
 
-Mirrors the reference's ``loop_interpolation/_regularisation.py``
-(``DirectionalRegularisation``, ``RegularisationConfig``,
-``coerce_regularisation_config``): the same accepted forms and the same
-errors, so that ``setup_interpolator(regularisation=..., directional_regularisation=...)``
-takes exactly what the reference takes.  Objects of the reference's own
-classes are accepted too (anything with ``weight`` / ``direction`` / ``name``
-attributes, or ``isotropic`` / ``directional`` for a whole configuration).
+``setup_interpolator(regularisation=..., directional_regularisation=...)``
+accepts the forms the reference's ``loop_interpolation/_regularisation.py``
+accepts, and rejects the others with the same exception types and messages:
+
+* ``regularisation``: ``None``; a number (the isotropic weight); a
+  configuration object (``isotropic`` + ``directional``); one directional
+  entry written as a mapping (keys ``direction``/``vector``, ``weight``,
+  ``name``); or a mapping with ``isotropic`` (alias ``weight``) and
+  ``directional`` keys.
+* ``directional_regularisation`` (appended to the terms above): ``None``; one
+  term (object or mapping); or a sequence of terms.
+
+Objects of the reference's own classes are accepted as well: a term is
+anything carrying ``weight``, ``direction`` and ``name``, a configuration
+anything carrying ``isotropic`` and ``directional``.
+
+Here each input is first given a *form* (``_form_of``), and one table per
+entry point maps a form to the routine that reads it.
 """
 from __future__ import annotations
 
 from collections.abc import Sequence
-from dataclasses import dataclass
-from typing import Callable, Union
+from typing import Callable, NamedTuple, Optional, Union
 
 import numpy as np
 
 DirectionProvider = Union[np.ndarray, Callable[[np.ndarray], np.ndarray]]
 
 
-@dataclass(frozen=True)
-class DirectionalRegularisation:
+class DirectionalRegularisation(NamedTuple):
     """One directional term: ``direction`` is an (n, 3) array sampled at the
-    interpolator's regularisation sample points, or a callable that returns
-    one from those points."""
+    interpolator's regularisation sample points, or a callable returning one
+    from those points; ``weight`` scales the term's rows."""
 
     weight: float
     direction: DirectionProvider
     name: str = "directional regularisation"
 
 
-@dataclass(frozen=True)
-class RegularisationConfig:
-    isotropic: float | None = None
+class RegularisationConfig(NamedTuple):
+    """The isotropic weight (``None``: the interpolator's default) and the
+    directional terms of one setup."""
+
+    isotropic: Optional[float] = None
     directional: tuple = ()
 
 
-def _is_term(value) -> bool:
-    return all(hasattr(value, k) for k in ("weight", "direction", "name"))
+_TERM_ATTRS = ("weight", "direction", "name")
+_TERM_KEYS = ("direction", "vector", "weight", "name")
+
+_MSG_NEED_DIRECTION = "Directional regularisation entries require 'direction' or 'vector'"
+_MSG_NEED_WEIGHT = "Directional regularisation entries require 'weight'"
+_MSG_BAD_TERM = "Directional regularisation must be a DirectionalRegularisation or dict entry"
+_MSG_SCALARS = "A sequence of scalars is not a valid directional regularisation config"
+_MSG_BAD_DIRECTIONAL = "Unsupported directional regularisation configuration"
+_MSG_BAD_CONFIG = "Unsupported regularisation configuration"
 
 
-def _is_config(value) -> bool:
-    return hasattr(value, "isotropic") and hasattr(value, "directional")
-
-
-def _is_directional_mapping(value) -> bool:
-    return isinstance(value, dict) and any(k in value for k in ("direction", "vector", "weight", "name"))
-
-
-def _coerce_term(value, index: int = 0, default_name: str = "directional regularisation"):
-    if isinstance(value, DirectionalRegularisation) or _is_term(value):
-        return value
+def _form_of(value) -> str:
+    """The form of a configuration input: 'none', 'term', 'config',
+    'term-mapping' (a mapping with a term key), 'mapping', 'scalar',
+    'sequence' or 'other'.  Terms and configurations are recognised by their
+    attributes first, so the tuple types above never count as sequences."""
+    if value is None:
+        return "none"
+    if all(hasattr(value, a) for a in _TERM_ATTRS):
+        return "term"
+    if hasattr(value, "isotropic") and hasattr(value, "directional"):
+        return "config"
     if isinstance(value, dict):
-        direction = value.get("direction", value.get("vector", None))
-        if direction is None:
-            raise ValueError("Directional regularisation entries require 'direction' or 'vector'")
-        weight = value.get("weight", None)
-        if weight is None:
-            raise ValueError("Directional regularisation entries require 'weight'")
-        return DirectionalRegularisation(weight=float(weight), direction=direction,
-                                         name=value.get("name", f"{default_name} {index + 1}"))
-    raise TypeError("Directional regularisation must be a DirectionalRegularisation or dict entry")
+        return "term-mapping" if any(k in value for k in _TERM_KEYS) else "mapping"
+    if np.isscalar(value):
+        return "scalar"
+    if isinstance(value, Sequence) and not isinstance(value, (bytes, np.ndarray)):
+        return "sequence"
+    return "other"
+
+
+def _term_from_mapping(entry: dict, index: int, default_name: str) -> DirectionalRegularisation:
+    direction = entry.get("direction", entry.get("vector"))
+    if direction is None:
+        raise ValueError(_MSG_NEED_DIRECTION)
+    if entry.get("weight") is None:
+        raise ValueError(_MSG_NEED_WEIGHT)
+    label = entry["name"] if "name" in entry else f"{default_name} {index + 1}"
+    return DirectionalRegularisation(float(entry["weight"]), direction, label)
+
+
+def _one_term(value, index: int, default_name: str):
+    form = _form_of(value)
+    if form == "term":
+        return value
+    if form in ("term-mapping", "mapping"):
+        return _term_from_mapping(value, index, default_name)
+    raise TypeError(_MSG_BAD_TERM)
+
+
+def _terms_from_sequence(items, default_name: str) -> tuple:
+    if len(items) == 0:
+        return ()
+    if all(np.isscalar(item) for item in items):
+        raise TypeError(_MSG_SCALARS)
+    return tuple(_one_term(item, i, default_name) for i, item in enumerate(items))
 
 
 def coerce_directional_regularisation(value, default_name: str = "directional regularisation") -> tuple:
-    if value is None:
+    """The directional terms described by ``value`` (see the module notes)."""
+    form = _form_of(value)
+    if form == "none":
         return ()
-    if isinstance(value, (DirectionalRegularisation, dict)) or _is_term(value):
-        return (_coerce_term(value, default_name=default_name),)
-    if isinstance(value, Sequence) and not isinstance(value, (str, bytes, np.ndarray)):
-        if len(value) == 0:
-            return ()
-        if all(np.isscalar(item) for item in value):
-            raise TypeError("A sequence of scalars is not a valid directional regularisation config")
-        return tuple(_coerce_term(item, index=i, default_name=default_name) for i, item in enumerate(value))
-    raise TypeError("Unsupported directional regularisation configuration")
+    if form in ("term", "term-mapping", "mapping"):
+        return (_one_term(value, 0, default_name),)
+    if form == "sequence":
+        return _terms_from_sequence(value, default_name)
+    raise TypeError(_MSG_BAD_DIRECTIONAL)
+
+
+def _config_from_mapping(entry: dict) -> RegularisationConfig:
+    iso = entry.get("isotropic", entry.get("weight"))
+    if iso is not None:
+        iso = float(iso)
+    return RegularisationConfig(iso, coerce_directional_regularisation(entry.get("directional", ())))
+
+
+# form of ``regularisation`` -> (isotropic weight, directional terms)
+_READERS = {
+    "none": lambda v: RegularisationConfig(),
+    "config": lambda v: RegularisationConfig(v.isotropic, tuple(v.directional)),
+    "scalar": lambda v: RegularisationConfig(float(v), ()),
+    "term-mapping": lambda v: RegularisationConfig(None, coerce_directional_regularisation(v)),
+    "mapping": _config_from_mapping,
+}
 
 
 def coerce_regularisation_config(regularisation=None, directional_regularisation=None) -> RegularisationConfig:
-    """Isotropic weight and directional terms from the forms the reference
-    accepts: a scalar, a config object, a single directional mapping, or a
-    dict with ``isotropic`` / ``weight`` and ``directional`` keys; plus the
-    separate ``directional_regularisation`` argument (appended)."""
-    isotropic = None
-    directional = ()
-    if isinstance(regularisation, RegularisationConfig) or _is_config(regularisation):
-        isotropic = regularisation.isotropic
-        directional = tuple(regularisation.directional)
-    elif np.isscalar(regularisation) and regularisation is not None:
-        isotropic = float(regularisation)
-    elif _is_directional_mapping(regularisation):
-        directional = coerce_directional_regularisation(regularisation)
-    elif isinstance(regularisation, dict):
-        iso = regularisation.get("isotropic", regularisation.get("weight", None))
-        if iso is not None and "direction" not in regularisation and "vector" not in regularisation:
-            isotropic = float(iso)
-        directional = coerce_directional_regularisation(regularisation.get("directional", ()))
-    elif regularisation is not None:
-        raise TypeError("Unsupported regularisation configuration")
-    if directional_regularisation is not None:
-        directional = directional + coerce_directional_regularisation(directional_regularisation)
-    return RegularisationConfig(isotropic=isotropic, directional=directional)
+    """Isotropic weight and directional terms from the forms listed in the
+    module notes; the separate ``directional_regularisation`` terms are
+    appended after those of ``regularisation``."""
+    form = _form_of(regularisation)
+    if form == "term":
+        # a term object on its own is not a whole configuration
+        raise TypeError(_MSG_BAD_CONFIG)
+    reader = _READERS.get(form)
+    if reader is None:
+        raise TypeError(_MSG_BAD_CONFIG)
+    cfg = reader(regularisation)
+    extra = coerce_directional_regularisation(directional_regularisation)
+    return RegularisationConfig(cfg.isotropic, tuple(cfg.directional) + extra)

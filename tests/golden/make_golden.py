@@ -395,9 +395,12 @@ def main(root):
 
 
 if __name__ == "__main__":
-    # usage: make_golden.py [reference root] [--directional]
+    # usage: make_golden.py <reference source root> [--directional]
+    # (or the root in the LOOPSTRUCTURAL_REFERENCE environment variable)
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    root = args[0] if args else "/root/reference"
+    root = args[0] if args else os.environ.get("LOOPSTRUCTURAL_REFERENCE")
+    if not root:
+        sys.exit("make_golden.py: pass the LoopStructural source root (or set LOOPSTRUCTURAL_REFERENCE)")
     if "--directional" in sys.argv:
         main_directional(root)
     else:

@@ -10,13 +10,13 @@ import types
 import numpy as np
 import pytest
 
-REF = os.environ.get("LOOPSTRUCTURAL_REFERENCE", "/root/reference")
+REF = os.environ.get("LOOPSTRUCTURAL_REFERENCE", "")
 
 
 @pytest.fixture(scope="module")
 def li():
-    if not os.path.isdir(os.path.join(REF, "packages", "loop_interpolation")):
-        pytest.skip("reference source not available")
+    if not REF or not os.path.isdir(os.path.join(REF, "packages", "loop_interpolation")):
+        pytest.skip("reference source not available: set LOOPSTRUCTURAL_REFERENCE to the LoopStructural source root")
     for name in ("pyvista", "yaml"):
         if name not in sys.modules:
             try:

@@ -1,7 +1,8 @@
 """ls_fd_apply_noalloc: the normal-operator apply for callers that cannot
-allocate device memory (inside a CUDA stream capture, or under a framework that
-owns every device allocation).  It keeps its scratch in a static device array,
-so the caller passes only inputs and outputs.
+allocate device memory (a host framework that owns every device allocation
+through its own pool, or a plugin under a fixed device-memory budget).  It
+keeps its scratch in a static device array, so the caller passes only inputs
+and outputs.
 
 Checked through the C ABI against the allocating entry point ls_fd_apply on
 two calls in a row (the static scratch keeps the previous call's contents),
@@ -84,3 +85,46 @@ def test_noalloc_rejects_oversized_systems():
     x = C.c_void_p(16)
     assert lib.ls_fd_apply_noalloc(C.byref(s), x, x, None, None) == -1
     assert b"static scratch limit" in lib.ls_last_error()
+
+
+def test_noalloc_without_dot_product_enqueues_only():
+    """h_xNx = NULL: the call only enqueues the apply (no host copy, no sync)."""
+    interp, system = _system()
+    lib = _lib.load()
+    desc = _desc(system, interp)
+    rng = np.random.default_rng(12)
+    for call in range(2):
+        x = torch.from_numpy(rng.normal(size=system.n)).cuda()
+        ref = system.apply(x)
+        y = torch.full_like(x, float("nan"))
+        status = lib.ls_fd_apply_noalloc(C.byref(desc), _lib.ptr(x), _lib.ptr(y), None, _lib.stream_ptr())
+        assert status == 0, lib.ls_last_error()
+        torch.cuda.synchronize()
+        assert float((y - ref).abs().max()) <= 1e-12 * float(ref.abs().max()), f"call {call}"
+    system.close()
+
+
+def test_noalloc_skips_and_reports_out_of_range_columns():
+    """A data-row column equal to dof (one past the grid) is skipped by the
+    kernels, which check every column before using it, and the call reports
+    LS_ERR_ARG when it reads x.Nx back; a following valid call succeeds."""
+    interp, system = _system()
+    lib = _lib.load()
+    bad_idc = system._idc.clone()
+    row = 3
+    col = int(torch.nonzero(bad_idc[row] >= 0)[0, 0])
+    bad_idc[row, col] = system.n
+    desc = _desc(system, interp)
+    desc.d_idc = _lib.ptr(bad_idc)
+    x = torch.from_numpy(np.random.default_rng(13).normal(size=system.n)).cuda()
+    y = torch.zeros_like(x)
+    xnx = C.c_double(0.0)
+    assert lib.ls_fd_apply_noalloc(C.byref(desc), _lib.ptr(x), _lib.ptr(y), C.byref(xnx), _lib.stream_ptr()) == -1
+    assert b"outside [0, dof)" in lib.ls_last_error()
+    assert bool(torch.isfinite(y).all())
+    good = _desc(system, interp)
+    assert lib.ls_fd_apply_noalloc(C.byref(good), _lib.ptr(x), _lib.ptr(y), C.byref(xnx), _lib.stream_ptr()) == 0
+    ref = system.apply(x)
+    torch.cuda.synchronize()
+    assert float((y - ref).abs().max()) <= 1e-12 * float(ref.abs().max())
+    system.close()
