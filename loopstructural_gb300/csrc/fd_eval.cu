@@ -2,9 +2,11 @@
 // G:295-391 (StructuredGrid.evaluate_value / evaluate_gradient) with the
 // interpolator-level conventions of DI:1342-1379.  Sums follow numpy's
 // pairwise order for 8 terms, so results agree with the reference to ~1 ulp.
-// Compiled with -fmad=false (value parity, not speed, decides here: the
-// kernel is bound by the 8 coefficient gathers per point).
+// Compiled with -fmad=false: the point kernel keeps numpy's evaluation order
+// for value parity; the lattice kernel writes its FMAs explicitly.
 #include <math.h>
+
+#include <algorithm>
 
 #include "ls_common.cuh"
 
@@ -158,83 +160,149 @@ __device__ __forceinline__ AxisLoc locate_axis(const EvalGrid &g, int d, double 
   return a;
 }
 
-// Lattice evaluation: block (256) covers a run of lattice x-indices of one
-// (j, k) lattice row, so the y / z location is computed once per block.
-__global__ void __launch_bounds__(256) eval_lattice_kernel(EvalGrid g, const double *__restrict__ c, double ox,
-                                                           double oy, double oz, double hx, double hy, double hz,
-                                                           int64_t n0, int64_t n1, int64_t n2,
-                                                           double *__restrict__ value, double *__restrict__ grad) {
-  __shared__ AxisLoc ly, lz;
-  const int64_t b = blockIdx.y, kk = blockIdx.z;
-  if (threadIdx.x == 0) {
-    ly = locate_axis(g, 1, oy + hy * (double)b);
-    lz = locate_axis(g, 2, oz + hz * (double)kk);
+// ---------------------------------------------------------------------------
+// Lattice evaluation.  GB300 runs FP64 arithmetic at a small fraction of its
+// FP32 rate, so this kernel is built to spend as few FP64 operations per
+// lattice point as possible (the point kernel above keeps the reference's
+// operation order for parity; here sums are regrouped, agreeing to a few ulp):
+//  * the trilinear weight factorises as w_x(a) * w_yz(b, k): the x location of
+//    every lattice x index is computed once per block (each thread keeps its
+//    own), the y / z part once per lattice row (RowCoef, one lane per row);
+//  * row collapse: along one lattice row the y / z interpolation is done once
+//    per grid node, E(i) = sum w_yz c(i, ., .), and likewise its y / z
+//    derivatives, into shared memory; each lattice point is then a lerp of two
+//    neighbouring entries (value, d/dy, d/dz: 2 FP64 ops each; d/dx: 1).
+//    This needs the chunk's node span to fit the buffer, i.e. a lattice at
+//    least about as dense as the grid in x; otherwise (sparse lattices) each
+//    point gathers its 8 coefficients and reuses the row weights (~24 ops).
+// Block: 256 threads = one chunk of 256 consecutive lattice x indices; the
+// block walks a strided set of lattice rows (b, k) for that chunk.
+constexpr int kLatThreads = 256;
+constexpr int kLatRowBatch = 32;
+constexpr int kLatMaxSpan = 2 * kLatThreads + 2;
+
+struct RowCoef {
+  double w[4];    // value weights of the 4 x-lines (by + 2 bz): wy(by) * wz(bz)
+  double gy[2];   // d/dy weights of the z = cz / cz + 1 line pairs: (1 - lz) / hy, lz / hy
+  double gz[2];   // d/dz weights of the y = cy / cy + 1 line pairs: (1 - ly) / hz, ly / hz
+  int64_t base;   // node index of (0, cy, cz)
+  int inside;
+};
+
+__device__ RowCoef row_coef(const EvalGrid &g, double py, double pz) {
+  const AxisLoc ly = locate_axis(g, 1, py), lz = locate_axis(g, 2, pz);
+  RowCoef r;
+  const double y = ly.l, z = lz.l;
+  r.w[0] = (1 - y) * (1 - z);
+  r.w[1] = y * (1 - z);
+  r.w[2] = (1 - y) * z;
+  r.w[3] = y * z;
+  r.gy[0] = (1 - z) / g.step[1];
+  r.gy[1] = z / g.step[1];
+  r.gz[0] = (1 - y) / g.step[2];
+  r.gz[1] = y / g.step[2];
+  r.base = g.n[0] * (ly.cell + g.n[1] * lz.cell);
+  r.inside = ly.inside & lz.inside;
+  return r;
+}
+
+__global__ void __launch_bounds__(kLatThreads) eval_lattice_kernel(EvalGrid g, const double *__restrict__ c,
+                                                                   double ox, double oy, double oz, double hx,
+                                                                   double hy, double hz, int64_t n0, int64_t n1,
+                                                                   int64_t n2, double *__restrict__ value,
+                                                                   double *__restrict__ grad) {
+  __shared__ RowCoef rc[kLatRowBatch];
+  __shared__ double buf[2][3][kLatMaxSpan];  // E, dE/dy, dE/dz per node, double-buffered over rows
+  __shared__ int span_lo, span_hi;
+  const int tid = threadIdx.x;
+  const int64_t a = blockIdx.y * (int64_t)kLatThreads + tid;
+  const bool active = a < n0;
+  // x location of this thread's lattice index, once for every row
+  AxisLoc lx = {0.0, 0, false};
+  if (active) lx = locate_axis(g, 0, ox + hx * (double)a);
+  if (tid == 0) {
+    span_lo = 0x7fffffff;
+    span_hi = -1;
   }
   __syncthreads();
-  const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (a >= n0) return;
-  const AxisLoc lx = locate_axis(g, 0, ox + hx * (double)a);
-  const int64_t i = a + n0 * (b + n1 * kk);
-  if (!(lx.inside & ly.inside & lz.inside)) {
-    if (value) value[i] = __longlong_as_double(0x7ff8000000000000LL);
-    if (grad) grad[3 * i] = grad[3 * i + 1] = grad[3 * i + 2] = 0.0;
-    return;
+  if (active) {
+    atomicMin(&span_lo, (int)lx.cell);
+    atomicMax(&span_hi, (int)lx.cell + 1);
   }
+  __syncthreads();
+  const int lo = span_lo, span = span_hi - span_lo + 1;
+  const bool collapse = span <= kLatMaxSpan;
+  const double inv_hx = 1.0 / g.step[0];
   const int64_t nx = g.n[0], nxy = g.n[0] * g.n[1];
-  const int64_t g0 = lx.cell + nx * ly.cell + nxy * lz.cell;
-  double cv[8];
-  cv[0] = __ldg(c + g0);
-  cv[1] = __ldg(c + g0 + 1);
-  cv[2] = __ldg(c + g0 + nx);
-  cv[3] = __ldg(c + g0 + nx + 1);
-  cv[4] = __ldg(c + g0 + nxy);
-  cv[5] = __ldg(c + g0 + nxy + 1);
-  cv[6] = __ldg(c + g0 + nxy + nx);
-  cv[7] = __ldg(c + g0 + nxy + nx + 1);
-  const double x = lx.l, y = ly.l, z = lz.l;
-  if (value) {
-    double w[8];
-    w[0] = (1 - x) * (1 - y) * (1 - z);
-    w[1] = x * (1 - y) * (1 - z);
-    w[2] = (1 - x) * y * (1 - z);
-    w[4] = (1 - x) * (1 - y) * z;
-    w[5] = x * (1 - y) * z;
-    w[6] = (1 - x) * y * z;
-    w[3] = x * y * (1 - z);
-    w[7] = x * y * z;
+  const int64_t rows = n1 * n2;
+  int parity = 0;
+  for (int64_t t0 = blockIdx.x; t0 < rows; t0 += (int64_t)gridDim.x * kLatRowBatch) {
+    __syncthreads();  // the previous batch's coefficients are no longer read
+    if (tid < kLatRowBatch) {
+      const int64_t r = t0 + (int64_t)tid * gridDim.x;
+      if (r < rows) rc[tid] = row_coef(g, oy + hy * (double)(r % n1), oz + hz * (double)(r / n1));
+    }
+    __syncthreads();
+    for (int q = 0; q < kLatRowBatch; ++q) {
+      const int64_t r = t0 + (int64_t)q * gridDim.x;
+      if (r >= rows) break;  // uniform across the block
+      const RowCoef &R = rc[q];
+      const int64_t out = a + n0 * r;
+      if (collapse) {
+        if (R.inside) {
+          for (int m = tid; m < span; m += kLatThreads) {
+            const double *p = c + R.base + lo + m;
+            const double c00 = __ldg(p), c10 = __ldg(p + nx), c01 = __ldg(p + nxy), c11 = __ldg(p + nxy + nx);
+            buf[parity][0][m] = fma(R.w[3], c11, fma(R.w[2], c01, fma(R.w[1], c10, R.w[0] * c00)));
+            buf[parity][1][m] = fma(R.gy[1], c11 - c01, R.gy[0] * (c10 - c00));
+            buf[parity][2][m] = fma(R.gz[1], c11 - c10, R.gz[0] * (c01 - c00));
+          }
+        }
+        __syncthreads();
+        if (!active) {
+          parity ^= 1;
+          continue;
+        }
+        if (!(R.inside & lx.inside)) {
+          if (value) value[out] = __longlong_as_double(0x7ff8000000000000LL);
+          if (grad) grad[3 * out] = grad[3 * out + 1] = grad[3 * out + 2] = 0.0;
+          parity ^= 1;
+          continue;
+        }
+        const int m = (int)lx.cell - lo;
+        const double e0 = buf[parity][0][m], de = buf[parity][0][m + 1] - e0;
+        if (value) value[out] = fma(lx.l, de, e0);
+        if (grad) {
+          const double y0 = buf[parity][1][m], z0 = buf[parity][2][m];
+          grad[3 * out] = de * inv_hx;
+          grad[3 * out + 1] = fma(lx.l, buf[parity][1][m + 1] - y0, y0);
+          grad[3 * out + 2] = fma(lx.l, buf[parity][2][m + 1] - z0, z0);
+        }
+        parity ^= 1;
+      } else {
+        if (!active) continue;
+        if (!(R.inside & lx.inside)) {
+          if (value) value[out] = __longlong_as_double(0x7ff8000000000000LL);
+          if (grad) grad[3 * out] = grad[3 * out + 1] = grad[3 * out + 2] = 0.0;
+          continue;
+        }
+        const double *p = c + R.base + lx.cell;
+        double e[4], d[4];
+        const int64_t off[4] = {0, nx, nxy, nxy + nx};
 #pragma unroll
-    for (int k = 0; k < 8; ++k) w[k] = w[k] * cv[k];
-    value[i] = sum8(w);
-  }
-  if (grad) {
-    double T[8];
-    T[0] = (1 - z) * (y - 1) * cv[0];
-    T[1] = (1 - y) * (1 - z) * cv[1];
-    T[2] = -y * (1 - z) * cv[2];
-    T[4] = -(1 - y) * z * cv[4];
-    T[5] = (1 - y) * z * cv[5];
-    T[6] = -y * z * cv[6];
-    T[3] = y * (1 - z) * cv[3];
-    T[7] = y * z * cv[7];
-    grad[3 * i] = sum8(T) / g.step[0];
-    T[0] = (x - 1) * (1 - z) * cv[0];
-    T[1] = -x * (1 - z) * cv[1];
-    T[2] = (1 - x) * (1 - z) * cv[2];
-    T[4] = -(1 - x) * z * cv[4];
-    T[5] = -x * z * cv[5];
-    T[6] = (1 - x) * z * cv[6];
-    T[3] = x * (1 - z) * cv[3];
-    T[7] = x * z * cv[7];
-    grad[3 * i + 1] = sum8(T) / g.step[1];
-    T[0] = -(1 - x) * (1 - y) * cv[0];
-    T[1] = -x * (1 - y) * cv[1];
-    T[2] = -(1 - x) * y * cv[2];
-    T[4] = (1 - x) * (1 - y) * cv[4];
-    T[5] = x * (1 - y) * cv[5];
-    T[6] = (1 - x) * y * cv[6];
-    T[3] = -x * y * cv[3];
-    T[7] = x * y * cv[7];
-    grad[3 * i + 2] = sum8(T) / g.step[2];
+        for (int j = 0; j < 4; ++j) {
+          const double c0 = __ldg(p + off[j]);
+          d[j] = __ldg(p + off[j] + 1) - c0;
+          e[j] = fma(lx.l, d[j], c0);
+        }
+        if (value) value[out] = fma(R.w[3], e[3], fma(R.w[2], e[2], fma(R.w[1], e[1], R.w[0] * e[0])));
+        if (grad) {
+          grad[3 * out] = fma(R.w[3], d[3], fma(R.w[2], d[2], fma(R.w[1], d[1], R.w[0] * d[0]))) * inv_hx;
+          grad[3 * out + 1] = fma(R.gy[1], e[3] - e[2], R.gy[0] * (e[1] - e[0]));
+          grad[3 * out + 2] = fma(R.gz[1], e[3] - e[1], R.gz[0] * (e[2] - e[0]));
+        }
+      }
+    }
   }
 }
 
@@ -312,11 +380,18 @@ extern "C" int ls_fd_eval_lattice(const ls_grid3 *grid, const double *d_c, const
   if (total == 0 || (!d_value && !d_grad)) return LS_OK;
   EvalGrid g = make_eval_grid(*grid);
   cudaStream_t s = as_stream(stream);
-  LS_ARG_CHECK(lat_n[1] <= 65535 && lat_n[2] <= 65535, "lattice y / z extent above 65535");
-  const dim3 lgrid((unsigned)((lat_n[0] + 255) / 256), (unsigned)lat_n[1], (unsigned)lat_n[2]);
-  eval_lattice_kernel<<<lgrid, 256, 0, s>>>(g, d_c, lat_origin[0], lat_origin[1], lat_origin[2],
-                                                              lat_step[0], lat_step[1], lat_step[2], lat_n[0],
-                                                              lat_n[1], lat_n[2], d_value, d_grad);
+  const int64_t chunks = (lat_n[0] + kLatThreads - 1) / kLatThreads;
+  LS_ARG_CHECK(chunks <= 65535, "lattice x extent above 16.7 M");
+  LS_ARG_CHECK(g.n[0] < (int64_t)0x7fffffff, "grid x extent too large");
+  // enough blocks to fill every SM several times over; each walks a strided
+  // set of lattice rows of its x chunk
+  const int64_t rows = lat_n[1] * lat_n[2];
+  const int64_t want = (int64_t)sm_count() * 8;
+  const int64_t per_chunk = std::max<int64_t>(1, std::min<int64_t>(rows, (want + chunks - 1) / chunks));
+  const dim3 lgrid((unsigned)per_chunk, (unsigned)chunks, 1);
+  eval_lattice_kernel<<<lgrid, kLatThreads, 0, s>>>(g, d_c, lat_origin[0], lat_origin[1], lat_origin[2], lat_step[0],
+                                                    lat_step[1], lat_step[2], lat_n[0], lat_n[1], lat_n[2], d_value,
+                                                    d_grad);
   LS_CUDA_TRY(cudaGetLastError());
   return LS_OK;
 }

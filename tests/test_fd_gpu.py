@@ -241,6 +241,30 @@ def test_lattice_evaluation_matches_oracle():
     np.testing.assert_allclose(g.cpu().numpy(), fdo.evaluate_gradient_local(ref, pts, c), rtol=1e-12, atol=1e-12)
 
 
+@pytest.mark.parametrize("cells, origin, step, counts", [
+    # a lattice far coarser than the grid in x: the chunk's node span exceeds the
+    # row-collapse buffer, so every point gathers its 8 coefficients
+    ((700, 3, 4), (-0.01, 0.05, 0.1), (0.0251, 0.3, 0.2), (41, 4, 5)),
+    # a reversed lattice (negative steps), partly outside the grid
+    ((13, 9, 6), (1.02, 0.97, 0.99), (-0.0173, -0.0211, -0.0197), (70, 50, 53)),
+])
+def test_lattice_evaluation_paths(cells, origin, step, counts):
+    cells = np.array(cells)
+    grid = _grid(cells)
+    ref = fdo.Grid(np.zeros(3), cells, 1.0 / cells)
+    c = np.random.default_rng(4).normal(size=grid.n_nodes)
+    v, g = fd.eval_lattice(grid, torch.from_numpy(c).cuda(), origin, step, counts)
+    i, j, k = np.meshgrid(*[np.arange(n) for n in counts], indexing="ij")
+    pts = np.stack([origin[0] + step[0] * i.ravel(order="F"), origin[1] + step[1] * j.ravel(order="F"),
+                    origin[2] + step[2] * k.ravel(order="F")], axis=1)
+    vr = fdo.evaluate_value_local(ref, pts, c)
+    gr = fdo.evaluate_gradient_local(ref, pts, c)
+    assert np.isnan(vr).any() and np.isfinite(vr).any()
+    np.testing.assert_allclose(v.cpu().numpy(), vr, rtol=1e-13, atol=1e-13, equal_nan=True)
+    scale = np.abs(gr).max()
+    np.testing.assert_allclose(g.cpu().numpy(), gr, rtol=1e-12, atol=1e-12 * scale)
+
+
 def test_mixed_solve_is_deterministic(golden):
     a = _interp(golden, "fd_cfg1_20")
     a.solve_system("cg", solver_kwargs={"rtol": 1e-12, "atol": 0.0})
