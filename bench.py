@@ -271,16 +271,25 @@ def gpu_arm(args, rank, world):
     prof = fd.profile_iteration(system, "mixed", reps=50)
     peak, peak_kind = measured_peaks()
     it_gbs = prof["iteration_bytes"] / (prof["iteration_ms"] * 1e-3) / 1e9
-    # dominant kernel: the staged deep-box operator apply with the Chebyshev
-    # epilogue on the finest multigrid level (6 of the 8 finest-level applies
-    # of every iteration), timed with CUDA events on the solver's stream
+    # dominant kernel: the finest-level operator apply with the Chebyshev
+    # epilogue (6 of the 8 finest-level applies of every iteration), timed
+    # alone with CUDA events on the solver's stream.  With TMA staging it is
+    # one kernel over every node; otherwise the staged deep-box kernel over
+    # [3, n-4]^3 (the boundary shell runs in a second kernel).
     mgp = fd.profile_mg(system, reps=50)
-    nd = int(np.prod([c + 1 - 6 for c in cells]))  # deep-box nodes [3, n-4]^3
-    dom_bytes = 28.0 * nd  # p read; x, r read + written; D^-1 read; next direction written (FP32)
-    dom_ms = mgp[0]["cheb_deep_ms"]
+    if system.staged_apply:
+        units = int(np.prod([c + 1 for c in cells]))
+        dom_name = "fd_tma_apply_kernel<EPI_CHEB> (finest level, every node)"
+        tname = "fd_tma_apply_cheb_200cubed.json"
+    else:
+        units = int(np.prod([c + 1 - 6 for c in cells]))  # deep-box nodes [3, n-4]^3
+        dom_name = "fd_apply_kernel<float, EPI_CHEB, MODE_DEEP> (finest level, deep box)"
+        tname = "fd_apply_cheb_deep_200cubed.json"
+    dom_bytes = 28.0 * units  # p read; x, r read + written; D^-1 read; next direction written (FP32)
+    dom_ms = mgp[0]["cheb_main_ms"]
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "fd_apply_cheb_deep_200cubed.json")
+    tpath = os.path.join(ROOT, "profiles", tname)
     if os.path.exists(tpath):
         with open(tpath) as fh:
             traffic = json.load(fh).get("dram_bytes_per_launch")
@@ -344,7 +353,7 @@ def gpu_arm(args, rank, world):
                      "field_rel_error_64cubed": field_err, "coef_rel_error": coef_err},
         "jacobi_cg_iteration": {"iteration_ms": prof["iteration_ms"], "iteration_GBps": round(it_gbs, 1)},
         "kernels_ms": {k: prof[k] for k in ("stencil_ms", "data_ms", "update_ms", "iteration_ms")},
-        "roofline": {"kernel": "fd_apply_kernel<float, EPI_CHEB, MODE_DEEP> (finest level, deep box)",
+        "roofline": {"kernel": dom_name,
                      "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind + " (burst copy)",
                      "algorithmic_bytes": dom_bytes, "launch_ms": dom_ms, "traffic": traffic},

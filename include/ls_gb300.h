@@ -259,6 +259,13 @@ int ls_fd_prepare(ls_fd_handle *h, const ls_solve_opts *opts);
 /* Device the handle was created on. */
 int ls_fd_device(const ls_fd_handle *h);
 
+/* 1 when the handle's finest-level FP32 applies run the TMA-staged kernel
+ * (grids whose x extent is a multiple of 4 nodes and every axis >= 8 nodes,
+ * unless the environment variable LS_GB300_STAGED_APPLY=tiles was set when
+ * the handle was created), 0 when they run the cp.async tile kernels.  No
+ * counterpart in the reference. */
+int ls_fd_staged_apply(const ls_fd_handle *h);
+
 /* Solves `count` independent systems (a model ensemble) with up to
  * `concurrency` (<= 0: 8) solves in flight, each on its handle's stream:
  * model i solves with opts[i] into d_x[i], filling stats[i] and statuses[i]
@@ -289,8 +296,9 @@ int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps, ls_fd_prof
  * (plain), 2 apply with the Chebyshev epilogue, 3 apply with the residual
  * epilogue, 4 restriction to level l+1, 5 prolongation from level l+1,
  * 6 data rows (row form), 7 the coarsest dense solve (last level only),
- * 8 / 9 the Chebyshev apply's staged interior kernel / boundary kernel alone
- * (levels whose operator is split into the two; 0 otherwise).
+ * 8 / 9 the Chebyshev apply's kernels alone: on a finest level run by the
+ * TMA-staged kernel, that kernel / the data-totals kernel before it; on levels
+ * split into a staged interior and a boundary kernel, those two (0 otherwise).
  * Returns 0 with *levels = 0 when the grid does not coarsen.  The solver
  * vectors are overwritten.  No counterpart in the reference. */
 #define LS_MG_PROFILE_FIELDS 10
@@ -301,6 +309,12 @@ int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps, ls_fd_prof
  * query it).  A diagnostic of the preconditioner; no reference counterpart. */
 int ls_fd_mg_apply_level(ls_fd_handle *h, int level, const float *d_x, float *d_y, int64_t *h_nodes, void *stream);
 int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_levels, int *levels, void *stream);
+
+/* z = V(r): one application of the multigrid preconditioner of the mixed
+ * solve (FP32, dof entries each), building the hierarchy if needed.  A
+ * diagnostic of the preconditioner (symmetric positive definite by
+ * construction); overwrites the solver's vectors.  No reference counterpart. */
+int ls_fd_mg_vcycle(ls_fd_handle *h, const float *d_r, float *d_z, void *stream);
 
 /* ------------------------------------------------------------------ */
 /* FD evaluation (K7)                                                   */

@@ -1,0 +1,136 @@
+// Host side of the TMA-staged finest-level apply (fd_apply_tma.cuh): tensor-map
+// encoding through the driver entry point, eligibility, launch geometry.
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "fd_apply_tma.cuh"
+
+namespace ls {
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+std::once_flag g_encode_once;
+
+void resolve_encoder() {
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q{};
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+      q == cudaDriverEntryPointSuccess && fn != nullptr)
+    g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  cudaGetLastError();  // a failed lookup leaves no sticky error behind
+}
+
+bool encode(CUtensorMap *out, const float *base, int nx, int ny, int nz, int kind) {
+  if (g_encode == nullptr || (reinterpret_cast<uintptr_t>(base) & 15u) != 0) return false;
+  const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  const cuuint64_t strides[2] = {(cuuint64_t)nx * sizeof(float), (cuuint64_t)nx * ny * sizeof(float)};
+  const cuuint32_t box[3] = {kind == 0 ? (cuuint32_t)kTmPX : (cuuint32_t)kTmX,
+                             kind == 0 ? (cuuint32_t)kTmPY : (cuuint32_t)kTmY, 1u};
+  const cuuint32_t estride[3] = {1u, 1u, 1u};
+  const CUresult r = g_encode(out, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box,
+                              estride, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+const CUtensorMap *lookup(TmCache &cache, const float *ptr, int kind) {
+  for (const auto &en : cache.entries)
+    if (en.ptr == ptr && en.kind == kind) return &en.map;
+  TmCache::Entry en;
+  en.ptr = ptr;
+  en.kind = kind;
+  if (!encode(&en.map, ptr, cache.nx, cache.ny, cache.nz, kind)) return nullptr;
+  cache.entries.push_back(en);
+  return &cache.entries.back().map;
+}
+
+template <int EPI>
+void set_attributes() {
+  cudaFuncSetAttribute(fd_tma_apply_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, tm_smem_bytes<EPI>());
+  cudaFuncSetAttribute(fd_tma_apply_kernel<EPI>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+}
+
+}  // namespace
+
+void tm_setup(TmCache &cache, int nx, int ny, int nz, bool allow) {
+  cache.entries.clear();
+  cache.nx = nx;
+  cache.ny = ny;
+  cache.nz = nz;
+  std::call_once(g_encode_once, resolve_encoder);
+  // rows of a multiple of 16 bytes; every axis long enough for the 5-plane
+  // window; extents the launch geometry can address
+  cache.enabled = allow && g_encode != nullptr && nx % 4 == 0 && nx >= 8 && ny >= 8 && nz >= 8 &&
+                  (int64_t)nx * ny * nz < (int64_t)2000000000;
+  if (cache.enabled) {
+    set_attributes<EPI_STORE>();
+    set_attributes<EPI_CHEB>();
+    set_attributes<EPI_RESID>();
+    cudaGetLastError();
+  }
+}
+
+template <int EPI>
+int tm_launch(TmCache &cache, const CoefT<float> &c, const float *p, DataView<float> dv, const EpiArgs<float> &e,
+              const int *done, int64_t ntouched, const int64_t *inc_ptr, const int32_t *inc_row, const float *inc_a,
+              int width, const int32_t *cols, const float *a, const float *w2, float *qd, double *partials,
+              unsigned int *ticket, double *dot, double *dot_clear, int *fault, int max_blocks, cudaStream_t st,
+              int parts) {
+  if (!cache.enabled || c.nx != cache.nx || c.ny != cache.ny || c.nz != cache.nz) return 0;
+  TmMaps maps;
+  const CUtensorMap *mp = lookup(cache, p, 0);
+  if (mp == nullptr) return 0;
+  maps.p = *mp;
+  const float *opnd[3] = {nullptr, nullptr, nullptr};
+  if (EPI == EPI_CHEB) {
+    opnd[0] = e.x;
+    opnd[1] = e.r;
+    opnd[2] = e.dinv;
+  } else if (EPI == EPI_RESID) {
+    opnd[0] = e.b;
+    opnd[1] = e.dinv;
+  }
+  for (int k = 0; k < TmOps<EPI>::n; ++k) {
+    const CUtensorMap *m = lookup(cache, opnd[k], 1);
+    if (m == nullptr) return 0;
+    maps.op[k] = *m;
+  }
+  const int ntx = (c.nx + kTmX - 1) / kTmX, nty = (c.ny + kTmY - 1) / kTmY;
+  const int64_t ntiles = (int64_t)ntx * nty;
+  const int64_t slots = (int64_t)kTmBlocksPerSm * sm_count();
+  int64_t nseg = std::max<int64_t>(1, slots / std::max<int64_t>(1, ntiles));
+  const int zlen = (int)((c.nz + nseg - 1) / nseg);
+  nseg = (c.nz + zlen - 1) / zlen;
+  if (ntiles > 0x7fffffff || (dot != nullptr && ntiles * nseg > max_blocks)) return 0;
+  int launched = 0;
+  if (dv.enabled) {
+    if (parts & TM_TOTALS) {
+      data_node_totals_kernel<float><<<stream_grid(ntouched, 256), 256, 0, st>>>(ntouched, inc_ptr, inc_row, inc_a,
+                                                                                 width, cols, a, w2, p, qd, done);
+      ++launched;
+    }
+    dv.qd = qd;
+  }
+  if (parts & TM_APPLY) {
+    fd_tma_apply_kernel<EPI><<<dim3((unsigned)ntiles, (unsigned)nseg), kTmThreads, tm_smem_bytes<EPI>(), st>>>(
+        maps, c, dv, e, done, ntx, zlen, partials, ticket, dot, dot_clear, fault);
+    ++launched;
+  }
+  LS_CUDA_TRY(cudaGetLastError());
+  return launched;
+}
+
+#define LS_TM_INST(EPI)                                                                                              \
+  template int tm_launch<EPI>(TmCache &, const CoefT<float> &, const float *, DataView<float>,                      \
+                              const EpiArgs<float> &, const int *, int64_t, const int64_t *, const int32_t *,       \
+                              const float *, int, const int32_t *, const float *, const float *, float *, double *, \
+                              unsigned int *, double *, double *, int *, int, cudaStream_t, int);
+LS_TM_INST(EPI_STORE)
+LS_TM_INST(EPI_CHEB)
+LS_TM_INST(EPI_RESID)
+#undef LS_TM_INST
+
+}  // namespace ls

@@ -14,12 +14,15 @@
 // explicit scaling: identical iterates x_k = S y_k and identical stopping test
 // ||S r|| < max(atol, rtol ||S rhs||).
 #include <math.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include <algorithm>
 #include <chrono>
 #include <vector>
 
 #include "fd_apply.cuh"
+#include "fd_apply_tma.cuh"
 #include "fd_directional.cuh"
 #include "fd_mg.cuh"
 #include "fd_mg_cells.cuh"
@@ -51,6 +54,7 @@ struct CgScalars {
   int done;        // DONE_* stop code
   int pending;     // stop code raised mid-iteration; becomes `done` once p is updated
   int profile;     // timing mode: never stop, never flag a breakdown
+  int fault;       // a staged (TMA) apply gave up waiting for a copy
 };
 
 struct DataTerm {
@@ -108,6 +112,10 @@ struct ls_fd_handle {
   // directional regularisation weights (6 x n, family-major; null without)
   double *dir64 = nullptr;
   float *dir32 = nullptr;
+  // TMA-staged finest-level FP32 apply (fd_apply_tma.cuh): tensor maps of the
+  // grid's vectors, and the per-touched-node data totals it reads
+  ls::TmCache tm;
+  float *qd32 = nullptr;
   std::vector<int64_t> h_idc;           // host copy of the data rows (Galerkin coarsening)
   std::vector<double> h_a, h_w2;
   int h_width = 0;
@@ -357,15 +365,26 @@ void launch_apply(ls_fd_handle *h, const T *p, T *q, T *s, const T *a, const T *
                   cudaStream_t st) {
   const DataTerm &d = h->data;
   const int *done = check_done ? &h->sc->done : nullptr;
-  if (d.nrows > 0) {
-    rows_kernel<T><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, a, w2, p, s, done);
-    ++h->launches;
-  }
   EpiArgs<T> e{};
   e.q = q;
-  h->launches += launch_operator<T, EPI_STORE>(coef_as<T>(h->coef), p, data_view<T>(h, s, ia), e, done, h->partials,
-                                               h->tickets + T_STENCIL, &h->sc->pq_s, h->tickets + T_SHELL,
-                                               &h->sc->pq_d, h->red_blocks, st);
+  int staged = 0;
+  if constexpr (sizeof(T) == 4) {
+    staged = tm_launch<EPI_STORE>(h->tm, coef_as<float>(h->coef), p, data_view<float>(h, s, ia), e, done, d.ntouched,
+                                  d.inc_ptr, d.inc_row, ia, d.width, d.cols, a, w2, h->qd32, h->partials,
+                                  h->tickets + T_STENCIL, &h->sc->pq_s, &h->sc->pq_d, &h->sc->fault, h->red_blocks,
+                                  st);
+  }
+  if (staged > 0) {
+    h->launches += staged;
+  } else {
+    if (d.nrows > 0) {
+      rows_kernel<T><<<grid_for(h, d.nrows), kBlock, 0, st>>>(d.nrows, d.width, d.cols, a, w2, p, s, done);
+      ++h->launches;
+    }
+    h->launches += launch_operator<T, EPI_STORE>(coef_as<T>(h->coef), p, data_view<T>(h, s, ia), e, done,
+                                                 h->partials, h->tickets + T_STENCIL, &h->sc->pq_s,
+                                                 h->tickets + T_SHELL, &h->sc->pq_d, h->red_blocks, st);
+  }
   if (h->dir64) {  // q += D^T W D p in place; its share of p.q lands in pq_x
     const DirView<T> dv{(int)h->grid.nsteps[0], (int)h->grid.nsteps[1], (int)h->grid.nsteps[2], dir_weights<T>(h)};
     dir_apply_kernel<T, EPI_STORE><<<grid_for(h, h->n), 256, 0, st>>>(dv, p, q, e, done, h->partials,
@@ -417,6 +436,10 @@ int build_graph(ls_fd_handle *h, int batch, cudaGraphExec_t *out, int64_t *kerne
 int read_scalars(ls_fd_handle *h) {
   LS_CUDA_TRY(cudaMemcpyAsync(h->sc_h, h->sc, sizeof(CgScalars), cudaMemcpyDeviceToHost, h->stream));
   LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (h->sc_h->fault) {  // sticky: the handle's results can no longer be trusted
+    set_error("a TMA-staged operator apply gave up waiting for a tensor copy");
+    return LS_ERR_CUDA;
+  }
   return LS_OK;
 }
 
@@ -759,6 +782,30 @@ DirCoarse dir_coarse(const MgLevel &lv) {
 template <int EPI>
 void mg_apply(ls_fd_handle *h, const MgLevel &lv, const float *p, const EpiArgs<float> &e, const int *done,
               cudaStream_t st) {
+  if (&lv == &h->mg.levels[0] && h->tm.enabled) {
+    // finest level: the TMA-staged kernel (isotropic + data; with directional
+    // terms it stores to dq and the directional kernel completes the epilogue)
+    const DataTerm &d = h->data;
+    EpiArgs<float> es{};
+    es.q = lv.dq;
+    const int staged =
+        lv.dir ? tm_launch<EPI_STORE>(h->tm, lv.coef, p, mg_view(lv), es, done, d.ntouched, d.inc_ptr, d.inc_row,
+                                      d.inc_a32, d.width, d.cols, d.a32, d.w2_32, h->qd32, nullptr, nullptr, nullptr,
+                                      nullptr, &h->sc->fault, h->red_blocks, st)
+               : tm_launch<EPI>(h->tm, lv.coef, p, mg_view(lv), e, done, d.ntouched, d.inc_ptr, d.inc_row,
+                                d.inc_a32, d.width, d.cols, d.a32, d.w2_32, h->qd32, nullptr, nullptr, nullptr,
+                                nullptr, &h->sc->fault, h->red_blocks, st);
+    if (staged > 0) {
+      h->launches += staged;
+      if (lv.dir) {
+        const DirView<float> dv{lv.nx, lv.ny, lv.nz, lv.dir};
+        dir_apply_kernel<float, EPI><<<grid_for(h, lv.n), 256, 0, st>>>(dv, p, lv.dq, e, done, nullptr, nullptr,
+                                                                       nullptr);
+        ++h->launches;
+      }
+      return;
+    }
+  }
   if (lv.nrows > 0) {
     rows_kernel<float><<<grid_for(h, lv.nrows), kBlock, 0, st>>>(lv.nrows, lv.width, lv.cols, lv.a, lv.w2, p, lv.s, done);
     ++h->launches;
@@ -1810,6 +1857,14 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
     return fail(LS_ERR_CUDA);
   }
   h->rhs_norm2 = h->sc_h->scratch;
+  if (d.ntouched > 0 && (st = dev_alloc(&h->qd32, d.ntouched)) < 0) return fail(st);
+  {
+    // the TMA-staged FP32 apply unless LS_GB300_STAGED_APPLY=tiles asks for
+    // the cp.async tile kernels (same operator, for comparison)
+    const char *mode = getenv("LS_GB300_STAGED_APPLY");
+    const bool allow = !(mode && strcmp(mode, "tiles") == 0);
+    tm_setup(h->tm, (int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], allow);
+  }
   cudaEventCreate(&h->ev0);
   cudaEventCreate(&h->ev1);
   *out = h;
@@ -1827,7 +1882,7 @@ extern "C" int ls_fd_destroy(ls_fd_handle *h) {
   void *ptrs[] = {h->rhs, h->diag, h->dinv64, h->dinv32, h->x64, h->r64, h->p64, h->q64, h->s64, h->x32, h->r32,
                   h->p32, h->q32, h->s32, h->sc, h->partials, h->tickets, h->data.cols, h->data.a64, h->data.a32,
                   h->data.w2_64, h->data.w2_32, h->data.b, h->data.touched, h->data.inc_ptr, h->data.inc_row,
-                  h->data.inc_a64, h->data.inc_a32, h->data.mask, h->data.word_rank, h->dir64, h->dir32};
+                  h->data.inc_a64, h->data.inc_a32, h->data.mask, h->data.word_rank, h->dir64, h->dir32, h->qd32};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->sc_h) cudaFreeHost(h->sc_h);
@@ -1840,6 +1895,7 @@ extern "C" int ls_fd_destroy(ls_fd_handle *h) {
 
 extern "C" int64_t ls_fd_dof(const ls_fd_handle *h) { return h ? h->n : -1; }
 extern "C" int ls_fd_device(const ls_fd_handle *h) { return h ? h->device : -1; }
+extern "C" int ls_fd_staged_apply(const ls_fd_handle *h) { return h && h->tm.enabled ? 1 : 0; }
 
 extern "C" int ls_fd_rhs(ls_fd_handle *h, double *d_rhs, void *stream) {
   LS_ARG_CHECK(h && d_rhs, "NULL argument");
@@ -1897,8 +1953,7 @@ extern "C" int ls_fd_apply_f32(ls_fd_handle *h, const float *d_x, float *d_y, vo
   LS_CUDA_TRY(cudaStreamSynchronize(cs));
   launch_apply32(h, d_x, d_y, false, h->stream);
   LS_CUDA_TRY(cudaGetLastError());
-  LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
-  return LS_OK;
+  return read_scalars(h);  // synchronises; reports a staged-apply fault
 }
 
 extern "C" int ls_fd_setup_profile(const ls_fd_handle *h, double *h_out, int n) {
@@ -2178,6 +2233,20 @@ extern "C" int ls_fd_mg_apply_level(ls_fd_handle *h, int level, const float *d_x
   return LS_OK;
 }
 
+extern "C" int ls_fd_mg_vcycle(ls_fd_handle *h, const float *d_r, float *d_z, void *stream) {
+  LS_ARG_CHECK(h && d_r && d_z, "NULL argument");
+  LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+  LS_TRY(mg_build(h, kMgDefaultDegree));
+  LS_ARG_CHECK(h->mg.built, "the grid does not coarsen");
+  cudaStream_t st = h->stream;
+  // levels[0].b aliases r32 and levels[0].x aliases z32
+  LS_CUDA_TRY(cudaMemcpyAsync(h->r32, d_r, h->n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  mg_vcycle(h, nullptr, st);
+  LS_CUDA_TRY(cudaMemcpyAsync(d_z, h->z32, h->n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+  LS_CUDA_TRY(cudaGetLastError());
+  return read_scalars(h);  // synchronises; reports a staged-apply fault
+}
+
 extern "C" int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_levels, int *levels, void *stream) {
   LS_ARG_CHECK(h && out && levels && reps > 0 && max_levels > 0, "bad argument");
   LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
@@ -2228,7 +2297,19 @@ extern "C" int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_
     ec.c1 = 0.5f;
     ec.c2 = 1e-3f;
     LS_TRY(timed([&] { mg_apply<EPI_CHEB>(h, lv, lv.d0, ec, nullptr, st); }, &o[2]));
-    if (lv.g1) {
+    if (l == 0 && h->tm.enabled && !lv.dir) {
+      // the TMA-staged kernel alone (data totals computed once before), then
+      // the data-totals kernel alone
+      const DataTerm &d = h->data;
+      auto part = [&](int parts) {
+        return tm_launch<EPI_CHEB>(h->tm, lv.coef, lv.d0, mg_view(lv), ec, nullptr, d.ntouched, d.inc_ptr, d.inc_row,
+                                   d.inc_a32, d.width, d.cols, d.a32, d.w2_32, h->qd32, nullptr, nullptr, nullptr,
+                                   nullptr, &h->sc->fault, h->red_blocks, st, parts);
+      };
+      h->launches += part(TM_TOTALS);
+      LS_TRY(timed([&] { h->launches += part(TM_APPLY); }, &o[8]));
+      if (d.ntouched > 0) LS_TRY(timed([&] { h->launches += part(TM_TOTALS); }, &o[9]));
+    } else if (lv.g1) {
       const DataView<float> dv = mg_view(lv);
       LS_TRY(timed([&] { h->launches += launch_g1<EPI_CHEB>(lv.g1op, lv.d0, dv, ec, nullptr, h->red_blocks / 8, st, 1); },
                    &o[8]));

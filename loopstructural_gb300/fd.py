@@ -169,6 +169,11 @@ class FdSystem:
         except Exception:
             pass
 
+    @property
+    def staged_apply(self) -> bool:
+        """True when the finest-level FP32 applies run the TMA-staged kernel."""
+        return bool(self.lib.ls_fd_staged_apply(self.handle))
+
     def apply(self, x):
         torch = _torch()
         x = x.to(self.dev).contiguous()
@@ -250,7 +255,17 @@ def solve_batched(systems, concurrency=8, atol=0.0, rtol=1e-5, maxiter=None, pre
 
 
 MG_PROFILE_FIELDS = ("nodes", "apply_ms", "cheb_apply_ms", "resid_apply_ms", "restrict_ms", "prolong_ms",
-                     "rows_ms", "coarse_solve_ms", "cheb_deep_ms", "cheb_shell_ms")
+                     "rows_ms", "coarse_solve_ms", "cheb_main_ms", "cheb_aux_ms")
+
+
+def mg_vcycle(system: "FdSystem", r):
+    """z = V(r): one application of the multigrid preconditioner (FP32
+    device tensors)."""
+    torch = _torch()
+    r = r.to(device=system.dev, dtype=torch.float32).contiguous()
+    z = torch.empty_like(r)
+    _lib.check(system.lib.ls_fd_mg_vcycle(system.handle, _lib.ptr(r), _lib.ptr(z), _lib.stream_ptr()))
+    return z
 
 
 def profile_mg(system: "FdSystem", reps=20, max_levels=16):
