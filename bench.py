@@ -72,11 +72,11 @@ def field_gradient(p):
     return g
 
 
-def make_workload(n_nodes=N_NODES, n_value=N_VALUE, n_normal=N_NORMAL, sigma=NORMAL_SIGMA, seed=0):
+def make_workload(n_nodes=N_NODES, n_value=N_VALUE, n_normal=N_NORMAL, sigma=NORMAL_SIGMA, seed=0, fault=True):
     rng = np.random.default_rng(seed)
     noise = np.random.default_rng(seed + 1)
     vp = rng.uniform(0, 1, size=(n_value, 3))
-    val = np.column_stack([vp, field(vp), np.ones(n_value)])
+    val = np.column_stack([vp, field(vp, fault), np.ones(n_value)])
     npnt = rng.uniform(0, 1, size=(n_normal, 3))
     g = field_gradient(npnt)
     g /= np.linalg.norm(g, axis=1)[:, None]
@@ -84,6 +84,15 @@ def make_workload(n_nodes=N_NODES, n_value=N_VALUE, n_normal=N_NORMAL, sigma=NOR
     nrm = np.column_stack([npnt, g, np.ones(n_normal)])
     cells = np.array([n_nodes - 1] * 3)
     return cells, val, nrm
+
+
+# the CPU-runnable configuration: 50^3 nodes, 200 values, 50 normals of the
+# unfaulted field, CG tol 1e-10, evaluation on a 100^3 lattice
+CFG1_NODES, CFG1_VALUE, CFG1_NORMAL, CFG1_LATTICE = 50, 200, 50, 100
+
+
+def cfg1_workload():
+    return make_workload(CFG1_NODES, CFG1_VALUE, CFG1_NORMAL, NORMAL_SIGMA, seed=0, fault=False)
 
 
 def lattice_points(n=LATTICE):

@@ -25,3 +25,44 @@ def dgolden():
     import numpy as np
 
     return np.load(os.path.join(ROOT, "tests", "golden", "directional_golden.npz"), allow_pickle=False)
+
+
+@pytest.fixture(scope="session")
+def cgolden():
+    """Fixtures at the benchmark configurations' sizes (make_golden.py --configs)."""
+    import numpy as np
+
+    return np.load(os.path.join(ROOT, "tests", "golden", "config_golden.npz"), allow_pickle=False)
+
+
+class AffineBox:
+    """A stand-in for the reference's BoundingBox built from its recorded
+    affine maps: project / project_vectors / reproject / reproject_vectors."""
+
+    def __init__(self, world_to_local, local_to_world, local_rotation):
+        import numpy as np
+
+        self.w2l = np.asarray(world_to_local, dtype=float)
+        self.l2w = np.asarray(local_to_world, dtype=float)
+        self.rot = np.asarray(local_rotation, dtype=float)
+
+    @staticmethod
+    def _affine(m, xyz):
+        import numpy as np
+
+        xyz = np.asarray(xyz, dtype=float)
+        hom = np.ones((xyz.shape[0], 4))
+        hom[:, :3] = xyz
+        return (m @ hom.T).T[:, :3]
+
+    def project(self, xyz):
+        return self._affine(self.w2l, xyz)
+
+    def reproject(self, xyz):
+        return self._affine(self.l2w, xyz)
+
+    def project_vectors(self, v):
+        return (self.rot @ v.T).T
+
+    def reproject_vectors(self, v):
+        return (self.l2w[:3, :3] @ v.T).T

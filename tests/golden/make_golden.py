@@ -4,6 +4,7 @@ Run in a container where the reference source tree is available:
 
     python tests/golden/make_golden.py /path/to/LoopStructural
     python tests/golden/make_golden.py /path/to/LoopStructural --directional
+    python tests/golden/make_golden.py /path/to/LoopStructural --configs
 
 It imports the reference's ``loop_interpolation`` / ``loop_common`` packages
 (``pyvista`` and ``yaml`` are stubbed: they are only used for VTK/YAML export)
@@ -367,6 +368,225 @@ def fd_fold_case(li, StructuredGrid, name, cells, seed, out):
         cls.add_constraints_to_least_squares = orig
 
 
+# ---------------------------------------------------------------------------
+# cases at the benchmark configurations' sizes (--configs)
+# ---------------------------------------------------------------------------
+def _repo_bench():
+    """The benchmark's seeded workload generator (same data for the fixtures,
+    the GPU tests and bench.py)."""
+    root = os.path.dirname(os.path.dirname(HERE))
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    import bench
+
+    return bench
+
+
+def _point_families(interp, calls, prefix, out, keep=("value", "norm")):
+    """Full rows of the point families (value / norm_k): raw idc plus the
+    stored coefficients; and the names and row counts of every family."""
+    names = []
+    for name, idc in calls:
+        if not name.startswith(keep):
+            continue
+        c = interp.constraints[name]
+        m = c["matrix"].tocsr()
+        m.sort_indices()
+        names.append(name)
+        out[f"{prefix}fam_{name}_idc"] = idc
+        out[f"{prefix}fam_{name}_indptr"] = m.indptr.astype(np.int64)
+        out[f"{prefix}fam_{name}_indices"] = m.indices.astype(np.int64)
+        out[f"{prefix}fam_{name}_data"] = m.data
+        out[f"{prefix}fam_{name}_b"] = np.asarray(c["b"], dtype=float)
+        out[f"{prefix}fam_{name}_w"] = np.asarray(c["w"], dtype=float)
+    out[f"{prefix}point_family_names"] = np.array(names)
+    out[f"{prefix}all_family_names"] = np.array(list(interp.constraints.keys()))
+    out[f"{prefix}all_family_rows"] = np.array([interp.constraints[k]["matrix"].shape[0] for k in interp.constraints])
+
+
+def cfg1_case(li, StructuredGrid, out):
+    """Configuration 1 exactly: 50^3 nodes in the unit box, 200 value points,
+    50 noisy normals (sigma 0.02) of the unfaulted layered field,
+    regularisation 0.1.  The reference's own CG to rtol 1e-12 (atol 1e-10,
+    its `tol`), and value / gradient of that solution on 4096 points of the
+    100^3 evaluation lattice."""
+    bench = _repo_bench()
+    cells, val, nrm = bench.cfg1_workload()
+    calls, (cls, orig) = _hook(li)
+    try:
+        grid = StructuredGrid(origin=np.zeros(3), nsteps=cells, step_vector=1.0 / cells.astype(float))
+        interp = li.FiniteDifferenceInterpolator(grid)
+        interp.set_value_constraints(val)
+        interp.set_normal_constraints(nrm)
+        interp.setup_interpolator(regularisation=bench.REGULARISATION, cpw=1.0, npw=1.0)
+        _point_families(interp, calls, "cfg1_", out)
+        interp.solve_system("cg", tol=1e-10, solver_kwargs={"rtol": 1e-12, "maxiter": 400000})
+        out["cfg1_c_tight"] = np.array(interp.c)
+        ax = np.linspace(0.0, 1.0, bench.CFG1_LATTICE)
+        pick = np.random.default_rng(2).choice(bench.CFG1_LATTICE ** 3, 4096, replace=False)
+        i, j, k = np.unravel_index(pick, (bench.CFG1_LATTICE,) * 3, order="F")
+        q = np.column_stack([ax[i], ax[j], ax[k]])
+        out["cfg1_lattice_pick"] = pick.astype(np.int64)
+        out["cfg1_eval_value"] = interp.evaluate_value(q)
+        out["cfg1_eval_gradient"] = interp.evaluate_gradient(q)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
+def factory_case(li, out):
+    """An FD interpolator built by the reference's own factory from a
+    BoundingBox with a non-zero origin and an anisotropic extent
+    (InterpolatorFactory.create_interpolator("FDI", boundingbox, nelements)):
+    the support lives in the box's local frame with non-unit cells, the
+    setters project world points, evaluation projects query points and
+    reprojects gradients."""
+    from loop_common.geometry import BoundingBox
+
+    calls, (cls, orig) = _hook(li)
+    try:
+        origin = np.array([100.0, -50.0, 20.0])
+        maximum = np.array([600.0, 250.0, 120.0])
+        bb = BoundingBox(origin=origin, maximum=maximum)
+        interp = li.InterpolatorFactory.create_interpolator("FDI", boundingbox=bb, nelements=3000)
+        sup = interp.support
+        rng = np.random.default_rng(9)
+        ext = maximum - origin
+
+        def f(p):
+            u = (p - origin) / ext
+            return u[:, 2] + 0.1 * np.sin(2 * np.pi * u[:, 0]) + 0.05 * np.cos(2 * np.pi * u[:, 1])
+
+        def grad(p):
+            u = (p - origin) / ext
+            g = np.column_stack([0.2 * np.pi * np.cos(2 * np.pi * u[:, 0]),
+                                 -0.1 * np.pi * np.sin(2 * np.pi * u[:, 1]), np.ones(len(u))])
+            return g / ext
+
+        vp = origin + ext * rng.uniform(0, 1, size=(300, 3))
+        val = np.column_stack([vp, f(vp), np.ones(300)])
+        npnt = origin + ext * rng.uniform(0, 1, size=(60, 3))
+        g = grad(npnt)
+        g /= np.linalg.norm(g, axis=1)[:, None]
+        g += rng.normal(0, 0.02, size=g.shape)
+        nrm = np.column_stack([npnt, g, np.ones(60)])
+        interp.set_value_constraints(val)
+        interp.set_normal_constraints(nrm)
+        interp.setup_interpolator(regularisation=0.1, cpw=1.0, npw=1.0)
+        out["fac_value_in"] = val
+        out["fac_normal_in"] = nrm
+        out["fac_origin"] = np.asarray(sup.origin, dtype=float)
+        out["fac_step"] = np.asarray(sup.step_vector, dtype=float)
+        out["fac_nsteps"] = np.asarray(sup.nsteps, dtype=np.int64)  # nodes per axis
+        out["fac_world_to_local"] = np.asarray(bb.world_to_local_matrix, dtype=float)
+        out["fac_local_to_world"] = np.asarray(bb.local_to_world_matrix, dtype=float)
+        out["fac_local_rotation"] = np.asarray(bb.local_rotation, dtype=float)
+        out["fac_data_value"] = np.asarray(interp.data["value"], dtype=float)
+        out["fac_data_normal"] = np.asarray(interp.data["normal"], dtype=float)
+        _point_families(interp, calls, "fac_", out)
+        interp.solve_system("cg", tol=1e-12, solver_kwargs={"rtol": 1e-13, "maxiter": 400000})
+        out["fac_c_tight"] = np.array(interp.c)
+        q = origin + ext * rng.uniform(-0.05, 1.05, size=(500, 3))
+        out["fac_query"] = q
+        out["fac_eval_value"] = interp.evaluate_value(q)
+        out["fac_eval_gradient"] = interp.evaluate_gradient(q)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
+def anisotropic_case(li, StructuredGrid, out):
+    """A StructuredGrid with a shifted origin and a different cell size per
+    axis (0.07 / 0.13 / 0.21): 250 values, 50 normals, regularisation 0.1."""
+    calls, (cls, orig) = _hook(li)
+    try:
+        origin = np.array([-1.5, 2.0, 0.25])
+        cells = np.array([22, 15, 11])
+        step = np.array([0.07, 0.13, 0.21])
+        ext = cells * step
+        rng = np.random.default_rng(13)
+        grid = StructuredGrid(origin=origin, nsteps=cells, step_vector=step)
+        interp = li.FiniteDifferenceInterpolator(grid)
+        vp = origin + ext * rng.uniform(0, 1, size=(250, 3))
+        u = (vp - origin) / ext
+        val = np.column_stack([vp, _field(u), np.ones(250)])
+        npnt = origin + ext * rng.uniform(0, 1, size=(50, 3))
+        g = _grad((npnt - origin) / ext) / ext
+        g /= np.linalg.norm(g, axis=1)[:, None]
+        nrm = np.column_stack([npnt, g + rng.normal(0, 0.02, size=g.shape), np.ones(50)])
+        interp.set_value_constraints(val)
+        interp.set_normal_constraints(nrm)
+        interp.setup_interpolator(regularisation=0.1, cpw=1.0, npw=1.0)
+        out["ani_origin"], out["ani_cells"], out["ani_step"] = origin, cells, step
+        out["ani_value_in"], out["ani_normal_in"] = val, nrm
+        _point_families(interp, calls, "ani_", out)
+        interp.solve_system("cg", solver_kwargs={"rtol": 1e-13, "atol": 0.0, "maxiter": 400000})
+        out["ani_c_tight"] = np.array(interp.c)
+        q = origin + ext * rng.uniform(-0.05, 1.05, size=(400, 3))
+        out["ani_query"] = q
+        out["ani_eval_value"] = interp.evaluate_value(q)
+        out["ani_eval_gradient"] = interp.evaluate_gradient(q)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
+def p1_config_case(li, TetMesh, out):
+    """P1 at 16^3 cells (20,480 tetrahedra): 600 noisy values of the faulted
+    field and 120 normals, cgw 0.1.  Face rows are recorded as their count, an
+    order-sensitive checksum over all rows' indices and every 37th row in
+    full (coefficients summed per column, as the stored matrix holds them)."""
+    calls, (cls, orig) = _hook(li)
+    try:
+        cells = np.array([16, 16, 16])
+        rng = np.random.default_rng(11)
+        mesh = TetMesh(origin=np.zeros(3), nsteps_cells=cells, step_vector=1.0 / cells.astype(float))
+        interp = li.P1Interpolator(mesh)
+        vp = rng.uniform(0, 1, size=(600, 3))
+        val = np.column_stack([vp, _field(vp, fault=True) + rng.normal(0, 0.01, 600), np.ones(600)])
+        npnt = rng.uniform(0, 1, size=(120, 3))
+        nrm = np.column_stack([npnt, _grad(npnt), np.ones(120)])
+        interp.set_value_constraints(val)
+        interp.set_normal_constraints(nrm)
+        interp.setup_interpolator(cgw=0.1, cpw=1.0, npw=1.0)
+        out["p1c_value_in"] = val
+        out["p1c_normal_in"] = nrm
+        out["p1c_cells"] = cells
+        _point_families(interp, calls, "p1c_", out)
+        for name, idc in calls:
+            if name != "edge jump":
+                continue
+            m = interp.constraints[name]["matrix"].tocsr()
+            m.sort_indices()
+            nrow = idc.shape[0]
+            rw = (np.arange(nrow, dtype=np.int64) % 1009) + 1
+            out["p1c_face_rows"] = np.array(nrow)
+            out["p1c_face_idc_checksum"] = np.array(np.sum(idc * (np.arange(idc.shape[1]) + 1)[None, :] * rw[:, None]))
+            sub = np.arange(0, nrow, 37)
+            dense = m[sub].toarray()
+            out["p1c_face_sub_rows"] = sub
+            out["p1c_face_sub_idc"] = idc[sub]
+            out["p1c_face_sub_vals"] = np.take_along_axis(dense, idc[sub], axis=1)
+            out["p1c_face_w"] = np.asarray(interp.constraints[name]["w"], dtype=float)[sub]
+        interp.solve_system("cg", solver_kwargs={"rtol": 1e-13, "atol": 0.0, "maxiter": 400000})
+        out["p1c_c_tight"] = np.array(interp.c)
+        q = _queries(rng, 0.0, 1.0, n=400)
+        out["p1c_query"] = q
+        out["p1c_eval_value"] = interp.evaluate_value(q)
+        out["p1c_eval_gradient"] = interp.evaluate_gradient(q)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
+def main_configs(root):
+    li, StructuredGrid, TetMesh = _import_reference(root)
+    out = {}
+    cfg1_case(li, StructuredGrid, out)
+    factory_case(li, out)
+    anisotropic_case(li, StructuredGrid, out)
+    p1_config_case(li, TetMesh, out)
+    path = os.path.join(HERE, "config_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")
+
+
 def main_directional(root):
     li, StructuredGrid, TetMesh = _import_reference(root)
     out = {}
@@ -395,7 +615,7 @@ def main(root):
 
 
 if __name__ == "__main__":
-    # usage: make_golden.py <reference source root> [--directional]
+    # usage: make_golden.py <reference source root> [--directional | --configs]
     # (or the root in the LOOPSTRUCTURAL_REFERENCE environment variable)
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else os.environ.get("LOOPSTRUCTURAL_REFERENCE")
@@ -403,5 +623,7 @@ if __name__ == "__main__":
         sys.exit("make_golden.py: pass the LoopStructural source root (or set LOOPSTRUCTURAL_REFERENCE)")
     if "--directional" in sys.argv:
         main_directional(root)
+    elif "--configs" in sys.argv:
+        main_configs(root)
     else:
         main(root)
