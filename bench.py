@@ -321,11 +321,10 @@ def gpu_arm(args, rank, world):
         it.setup_interpolator(regularisation=REGULARISATION, cpw=1.0, npw=1.0)
         it.solve_system("cg", solver_kwargs=dict(rtol=args.rtol, atol=0.0, precision="mixed",
                                                  maxiter=args.maxiter))
-        vv = it.evaluate_value(q_host)
-        gg = it.evaluate_gradient(q_host)
+        vv, gg = it.evaluate_value_and_gradient(q_host)
         torch.cuda.synchronize()
         t_e2e.append(time.perf_counter() - t0)
-        h2d = val.nbytes + nrm.nbytes + 2 * q_host.nbytes
+        h2d = val.nbytes + nrm.nbytes + q_host.nbytes
         d2h = it.c.nbytes + vv.nbytes + gg.nbytes
         del it
     e2e_s = float(np.mean(t_e2e)) if t_e2e else None
@@ -343,13 +342,7 @@ def gpu_arm(args, rank, world):
         "vs_baseline": None,
         "dtype": "f32+f64",
         "data": "synthetic (seeded faulted layered field; no dataset)",
-        "config": {
-            "workload": "FD 200^3 nodes (8M DOF), 20000 value + 5000 normal pts, reg 0.1; mixed FP32 CG + FP64 "
-                        "reliable updates to rtol %g; value+gradient on a 256^3 lattice" % args.rtol,
-            "dof": system.n, "data_rows": system.nrows, "rtol": args.rtol,
-            "cache": "inputs larger than L2 (working set ~0.6 GB of 8M-DOF vectors)",
-            "parallelism": "replicas" if world > 1 else "single GPU",
-        },
+        "config": headline_config(args, world),
         "solve": {"iterations": iters, "reliable_updates": int(np.mean([s["reliable_updates"] for s in stats])),
                   "preconditioner": stats[-1]["preconditioner"], "solve_ms": float(np.mean([s["device_ms"] for s in stats])),
                   "residual": stats[-1]["residual"], "threshold": stats[-1]["threshold"],
@@ -387,95 +380,228 @@ def gpu_arm(args, rank, world):
 # ---------------------------------------------------------------------------
 # CPU reference (oracle port of the reference's default path)
 # ---------------------------------------------------------------------------
-def cpu_reference_sample(rtol, sample_nodes=60, iters_for_rate=30):
-    """Time the reference default path (explicit assembly + column-scaled
-    scipy CG + evaluation) on a bounded sample and extrapolate to 200^3."""
-    from oracle import fd_oracle as fdo
-
-    cells, val, nrm = make_workload(n_nodes=sample_nodes,
-                                    n_value=int(N_VALUE * (sample_nodes / N_NODES) ** 3) + 1,
-                                    n_normal=int(N_NORMAL * (sample_nodes / N_NODES) ** 3) + 1)
-    grid = fdo.Grid(np.zeros(3), cells, 1.0 / cells)
-    w = fdo.resolve_weights(regularisation=REGULARISATION, cpw=1.0, npw=1.0)
-    t0 = time.perf_counter()
-    cs = fdo.assemble(grid, {"value": val, "normal": nrm}, w)
-    A, b = cs.matrix()
-    t_asm = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    _, _, it = fdo.solve_reference_cg(A, b, tol=0.0, rtol=1e-30, maxiter=iters_for_rate)
-    t_it = (time.perf_counter() - t0) / max(it, 1)
-    c = np.random.default_rng(0).normal(size=grid.n_nodes)
-    q = np.random.default_rng(1).uniform(0, 1, size=(200_000, 3))
-    t0 = time.perf_counter()
-    grid.evaluate_value(q, c)
-    grid.evaluate_gradient(q, c)
-    t_eval_pt = (time.perf_counter() - t0) / q.shape[0]
-    scale = (N_NODES / sample_nodes) ** 3
-    return {"assembly_s": t_asm * scale, "s_per_iteration": t_it * scale, "eval_s": t_eval_pt * LATTICE ** 3,
-            "sample": f"{sample_nodes}^3 nodes: assembly + {iters_for_rate} scipy-cg iterations of the "
-                      f"column-scaled explicit system, eval of 200k points; scaled x{scale:.1f} (DOF) and x"
-                      f"{LATTICE ** 3 / 2e5:.1f} (points)"}
+def headline_config(args, world):
+    """The workload both arms print (the same object in the GPU and the
+    reference line)."""
+    return {
+        "workload": "FD 200^3 nodes (8M DOF), 20000 value + 5000 normal pts of the faulted layered field, "
+                    "reg 0.1; CG on the normal equations to rtol %g (the reference's stopping test); "
+                    "value + gradient on a 256^3 lattice" % args.rtol,
+        "dof": N_NODES ** 3, "data_rows": N_VALUE + 3 * N_NORMAL, "rtol": args.rtol,
+        "cache": "inputs larger than L2 (working set ~0.6 GB of 8M-DOF vectors)",
+        "parallelism": "replicas" if world > 1 else "single GPU",
+    }
 
 
-def cpu_baseline(gpu_iters, rtol):
-    r = cpu_reference_sample(rtol)
-    total = r["s_per_iteration"] * gpu_iters + r["eval_s"]
-    return {"value": round(total, 3), "unit": "s", "cores": 1, "kind": "port",
-            "sample": r["sample"] + f"; x {gpu_iters} iterations (extrapolated: the FP64 Jacobi-CG count on the GPU "
-                                    f"at rtol {rtol:g}, the reference's iteration)"}
+class ReferenceSystem:
+    """The reference's default `solve_system('cg')` path on one system,
+    restated by the oracle (port): explicit assembly, then ridge rows, column
+    scaling and the normal matrix (AS)^T(AS), then scipy CG iterations, then
+    evaluation.  Wall times of each phase on this host (one core: scipy's
+    sparse products are single-threaded)."""
+
+    def __init__(self, cells, val, nrm):
+        from oracle import fd_oracle as fdo
+
+        t0 = time.perf_counter()
+        self.grid = fdo.Grid(np.zeros(3), cells, 1.0 / cells)
+        cs = fdo.assemble(self.grid, {"value": val, "normal": nrm},
+                          fdo.resolve_weights(regularisation=REGULARISATION, cpw=1.0, npw=1.0))
+        A, b = cs.matrix()
+        t1 = time.perf_counter()
+        self.N, self.rhs, self.s = fdo.reference_cg_system(A, b)
+        del A, b, cs
+        self.setup_s = {"assembly": t1 - t0, "normal_matrix": time.perf_counter() - t1}
+
+    def s_per_iteration(self, k):
+        """Wall time per scipy CG iteration, over k iterations from zero."""
+        from scipy.sparse import linalg as spla
+
+        t0 = time.perf_counter()
+        spla.cg(self.N, self.rhs, rtol=1e-300, atol=0.0, maxiter=k)
+        return (time.perf_counter() - t0) / k
+
+    def solve(self, tol, rtol=None):
+        """The stock stopping test: atol = tol, scipy's default rtol unless given."""
+        from scipy.sparse import linalg as spla
+
+        kw = {"atol": tol}
+        if rtol is not None:
+            kw["rtol"] = rtol
+        y, _ = spla.cg(self.N, self.rhs, **kw)
+        return self.s * y
+
+    def eval_seconds(self, pts, c=None):
+        c = np.zeros(self.grid.n_nodes) if c is None else c
+        t0 = time.perf_counter()
+        self.grid.evaluate_value(pts, c)
+        self.grid.evaluate_gradient(pts, c)
+        return time.perf_counter() - t0
 
 
-# Iterations of the reference's column-scaled CG (= Jacobi-preconditioned CG)
-# on the headline system, as counted by this bench's FP64 Jacobi-CG GPU leg
-# (same system, same stopping test): 8,757 to rtol 1e-10.
+def lattice_sample(n=LATTICE, planes=16):
+    """The first `planes` z-planes of the n^3 evaluation lattice (i fastest)."""
+    ax = np.linspace(0.0, 1.0, n)
+    zz, yy, xx = np.meshgrid(ax[:planes], ax, ax, indexing="ij")
+    return np.stack([xx.ravel(), yy.ravel(), zz.ravel()], axis=1)
+
+
+# Iterations of the reference's column-scaled CG (= Jacobi-preconditioned CG,
+# the same iteration in exact arithmetic; the GPU's FP64 count stays within 5%
+# of scipy's on the oracle systems the tests solve) on the headline system, as
+# counted by this bench's FP64 Jacobi-CG GPU leg: 8,757 to rtol 1e-10.
 REFERENCE_CG_ITERATIONS = {1e-10: 8757}
 
 
+def cpu_baseline(gpu_iters, rtol, sample_nodes=100):
+    """A bounded sample of the headline workload for the GPU line: the
+    reference path's setup and per-iteration cost on the 100^3-node system of
+    the same field and point densities, scaled to 200^3 by its DOF, times the
+    reference's iteration count; evaluation of 2^20 lattice points scaled."""
+    cells, val, nrm = make_workload(n_nodes=sample_nodes,
+                                    n_value=int(N_VALUE * (sample_nodes / N_NODES) ** 3) + 1,
+                                    n_normal=int(N_NORMAL * (sample_nodes / N_NODES) ** 3) + 1)
+    ref = ReferenceSystem(cells, val, nrm)
+    scale = (N_NODES / sample_nodes) ** 3
+    s_it = ref.s_per_iteration(20) * scale
+    setup = sum(ref.setup_s.values()) * scale
+    q = lattice_sample()
+    t_eval = ref.eval_seconds(q) * (LATTICE ** 3 / len(q))
+    total = setup + s_it * gpu_iters + t_eval
+    return {"value": round(total, 3), "unit": "s", "cores": 1, "kind": "port",
+            "sample": f"{sample_nodes}^3-node system of the same field and densities: setup and 20 scipy-cg "
+                      f"iterations of the column-scaled normal matrix, scaled x{scale:.0f} (DOF); evaluation of "
+                      f"{len(q)} lattice points scaled x{LATTICE ** 3 / len(q):.0f}; x {gpu_iters} iterations "
+                      f"(extrapolated: the FP64 Jacobi-CG count on the GPU at rtol {rtol:g}, the reference's "
+                      f"iteration)"}
+
+
 def reference_arm(args, rank, world):
+    """The reference's default path (oracle port, one host core) on the REAL
+    200^3 system: its setup (assembly, ridge, column scaling, normal matrix)
+    timed once; each timed step runs a fixed number of scipy CG iterations on
+    it (>= 200 over the timed steps); evaluation of 2^20 lattice points.  Step
+    value = setup + s/iteration x the reference's iteration count (an
+    extrapolation: running ~8,800 iterations would take the better part of an
+    hour) + the evaluation scaled to the 256^3 lattice."""
     if rank != 0:
         return None
-    from oracle import fd_oracle as fdo
-
-    if args.rtol in REFERENCE_CG_ITERATIONS:
-        iters = REFERENCE_CG_ITERATIONS[args.rtol]
-        how = "the FP64 Jacobi-CG count of the same system on the GPU (the reference's iteration)"
-        times = []
-        r = None
-        for _ in range(args.warmup + args.steps):
-            r = cpu_reference_sample(args.rtol)
-            times.append(r["s_per_iteration"] * iters + r["eval_s"])
-        v = float(np.mean(times[args.warmup:]))
-        return _reference_line(args, world, v, r["sample"] + f"; x {iters} iterations ({how})")
-    # other tolerances: calibrate the iteration count at n = 24, scaled linearly in n
-    n_cal = 24
-    cells, val, nrm = make_workload(n_nodes=n_cal, n_value=max(2, int(N_VALUE * (n_cal / N_NODES) ** 3)),
-                                    n_normal=max(2, int(N_NORMAL * (n_cal / N_NODES) ** 3)))
-    grid = fdo.Grid(np.zeros(3), cells, 1.0 / cells)
-    cs = fdo.assemble(grid, {"value": val, "normal": nrm}, fdo.resolve_weights(regularisation=REGULARISATION,
-                                                                                 cpw=1.0, npw=1.0))
-    A, b = cs.matrix()
-    _, _, it_cal = fdo.solve_reference_cg(A, b, tol=0.0, rtol=args.rtol, maxiter=200000)
-    iters = int(it_cal * N_NODES / n_cal)
-    times = []
-    r = None
-    for _ in range(args.warmup + args.steps):
-        r = cpu_reference_sample(args.rtol)
-        times.append(r["s_per_iteration"] * iters + r["eval_s"])
-    v = float(np.mean(times[args.warmup:]))
-    sample = r["sample"] + f"; x {iters} iterations (reference cg at {n_cal}^3 took {it_cal}, scaled linearly in n)"
-    return _reference_line(args, world, v, sample)
-
-
-def _reference_line(args, world, v, sample):
+    if args.rtol not in REFERENCE_CG_ITERATIONS:
+        return {"impl": "reference", "unavailable": f"no reference iteration count recorded for rtol {args.rtol:g}"}
+    iters = REFERENCE_CG_ITERATIONS[args.rtol]
+    cells, val, nrm = make_workload()
+    ref = ReferenceSystem(cells, val, nrm)
+    setup = sum(ref.setup_s.values())
+    q = lattice_sample()
+    t_eval = ref.eval_seconds(q) * (LATTICE ** 3 / len(q))
+    per_step = max(5, -(-200 // max(1, args.steps)))
+    for _ in range(args.warmup):
+        ref.s_per_iteration(5)
+    rates = [ref.s_per_iteration(per_step) for _ in range(args.steps)]
+    s_it = float(np.mean(rates))
+    v = setup + s_it * iters + t_eval
+    sample = (f"the 200^3 system itself: setup {setup:.1f} s (assembly {ref.setup_s['assembly']:.1f}, normal matrix "
+              f"{ref.setup_s['normal_matrix']:.1f}); {per_step} scipy-cg iterations per timed step "
+              f"({per_step * args.steps} in all), {s_it:.3f} s/iteration; x {iters} iterations (extrapolated: the "
+              f"FP64 Jacobi-CG count on the GPU at rtol {args.rtol:g}, the reference's iteration); evaluation of "
+              f"{len(q)} lattice points, {t_eval:.1f} s scaled to 256^3")
     return {
         "metric": METRIC, "impl": "reference", "value": round(v, 3), "unit": "s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(v * 1e3, 1), "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": "FD 200^3 nodes, 20000 value + 5000 normal pts, reg 0.1; reference default path "
-                               "(column-scaled scipy CG) to rtol %g; eval on 256^3" % args.rtol},
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded faulted layered field; no dataset)",
+        "config": headline_config(args, world),
         "cpu_baseline": {"value": round(v, 3), "unit": "s", "cores": 1, "kind": "port", "sample": sample},
         "e2e": {"value": round(v, 3), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "extrapolated": {"iterations": iters, "measured_iterations": per_step * args.steps,
+                         "s_per_iteration": s_it, "setup_s": setup, "eval_s": t_eval},
     }
+
+
+# ---------------------------------------------------------------------------
+# configuration 1 (50^3, CPU-runnable): both arms fully measured
+# ---------------------------------------------------------------------------
+CFG1_METRIC = "FD 50^3 setup + solve(tol 1e-10) + value/gradient on a 100^3 lattice, s (configuration 1)"
+
+
+def cfg1_config():
+    return {"workload": "FD 50^3 nodes (125k DOF), 200 value + 50 normal pts of the layered field, reg 0.1; "
+                        "solve_system('cg', tol=1e-10) with the reference's stopping test (atol 1e-10, scipy's "
+                        "default rtol 1e-5); value + gradient on a 100^3 lattice from host arrays",
+            "dof": CFG1_NODES ** 3, "data_rows": CFG1_VALUE + 3 * CFG1_NORMAL, "tol": 1e-10,
+            "parallelism": "single GPU"}
+
+
+def cfg1_lattice():
+    ax = np.linspace(0.0, 1.0, CFG1_LATTICE)
+    zz, yy, xx = np.meshgrid(ax, ax, ax, indexing="ij")
+    return np.stack([xx.ravel(), yy.ravel(), zz.ravel()], axis=1)
+
+
+def cfg1_arm(args, rank=0, world=1):
+    """Configuration 1 end to end, every step measured: the public API from
+    host arrays (GPU arm) or the reference path's oracle port on one host core
+    (reference arm)."""
+    if rank != 0:
+        return None
+    cells, val, nrm = cfg1_workload()
+    q = cfg1_lattice()
+    line = {"metric": CFG1_METRIC, "unit": "s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "data": "synthetic (seeded)",
+            "config": cfg1_config()}
+    if args.impl == "reference":
+        def step():
+            t0 = time.perf_counter()
+            ref = ReferenceSystem(cells, val, nrm)
+            c = ref.solve(1e-10)
+            ref.grid.evaluate_value(q, c)
+            ref.grid.evaluate_gradient(q, c)
+            return time.perf_counter() - t0
+
+        for _ in range(args.warmup):
+            step()
+        t = float(np.mean([step() for _ in range(args.steps)]))
+        line.update({"impl": "reference", "value": round(t, 4), "ms_per_step": round(t * 1e3, 1), "dtype": "f64",
+                     "cpu_baseline": {"value": round(t, 4), "unit": "s", "cores": 1, "kind": "port",
+                                      "sample": "the whole workload, every step"},
+                     "e2e": {"value": round(t, 4), "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        return line
+    import torch
+
+    import loopstructural_gb300 as L
+
+    torch.cuda.set_device(0)
+    L.build()
+    grid = L.StructuredGrid(origin=np.zeros(3), nsteps=cells, step_vector=1.0 / cells.astype(float))
+    io = {}
+    stats = {}
+
+    def step():
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        it = L.FiniteDifferenceInterpolator(grid)
+        it.set_value_constraints(val)
+        it.set_normal_constraints(nrm)
+        it.setup_interpolator(regularisation=REGULARISATION, cpw=1.0, npw=1.0)
+        it.solve_system("cg", tol=1e-10)
+        v = it.evaluate_value(q)
+        g = it.evaluate_gradient(q)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        io["h2d"] = val.nbytes + nrm.nbytes + 2 * q.nbytes
+        io["d2h"] = it.c.nbytes + v.nbytes + g.nbytes
+        stats.update(it.get_last_solve_timing())
+        return dt
+
+    for _ in range(args.warmup):
+        step()
+    t = float(np.mean([step() for _ in range(args.steps)]))
+    line.update({"impl": "gb300", "value": round(t, 4), "ms_per_step": round(t * 1e3, 2), "dtype": "f32+f64",
+                 "solve": {k: stats.get(k) for k in ("iterations", "preconditioner", "status", "solve_seconds")},
+                 "e2e": {"value": round(t, 4), "unit": "s", "h2d_bytes_per_step": int(io["h2d"]),
+                         "d2h_bytes_per_step": int(io["d2h"])},
+                 "note": "value is the wall time of the public-API call sequence from host arrays (= e2e)"})
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -831,7 +957,7 @@ def main():
     ap.add_argument("--skip-legs", action="store_true",
                     help="profiling runs: skip the FP64 leg, the e2e leg and the CPU baseline")
     ap.add_argument("--workload", default="headline", choices=["headline", "ensemble", "adjoint", "p1", "directional", "fold", "isosurface",
-                             "mgprofile"],
+                             "mgprofile", "cfg1"],
                     help="secondary workloads print their own line (ensembles, adjoint gradient, per-level "
                          "multigrid kernel times)")
     ap.add_argument("--models", type=int, default=256)
@@ -848,7 +974,8 @@ def main():
             out = ensemble_arm(args, rank, world)
         else:
             arms = {"adjoint": adjoint_arm, "p1": p1_arm, "directional": directional_arm,
-                    "fold": fold_arm, "isosurface": isosurface_arm, "mgprofile": mgprofile_arm}
+                    "fold": fold_arm, "isosurface": isosurface_arm, "mgprofile": mgprofile_arm,
+                    "cfg1": lambda a: cfg1_arm(a, rank, world)}
             out = arms[args.workload](args) if rank == 0 else None
         if rank == 0:
             print(json.dumps(out))

@@ -502,6 +502,21 @@ class _DiscreteInterpolatorBase:
             g = self.bounding_box.reproject_vectors(g)
         return g
 
+    def evaluate_value_and_gradient(self, locations):
+        """``(evaluate_value(locations), evaluate_gradient(locations))`` from
+        one upload of the points and one kernel launch (no reference
+        counterpart: the reference evaluates the two separately)."""
+        loc = np.asarray(locations, dtype=float)
+        if self.bounding_box is not None:
+            loc = self.bounding_box.project(loc)
+        self.update()
+        if loc.shape[0] == 0:
+            return np.zeros(0), np.zeros((0, 3))
+        v, g = self._eval_points(loc)
+        if self.bounding_box is not None:
+            g = self.bounding_box.reproject_vectors(g)
+        return v, g
+
 
 class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
     """FD interpolator on a StructuredGrid (FD:91-224)."""
@@ -746,6 +761,9 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
         for r, _t, op in self.directional_families.values():
             nnz += r * (4 if op in ("dxy", "dyz", "dxz") else 3)
         return nnz
+
+    def _eval_points(self, loc, value=True, gradient=True):
+        return fd.eval_points(self.support, self._c_device(), loc, value=value, gradient=gradient)
 
     def _evaluate_value_local(self, locations):
         self.update()

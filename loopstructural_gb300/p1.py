@@ -205,6 +205,9 @@ class P1Interpolator(_DiscreteInterpolatorBase):
     def _matrix_nnz(self):
         return sum(f.n_rows * f.idc.shape[1] for f in self.constraints.values())
 
+    def _eval_points(self, loc, value=True, gradient=True):
+        return eval_points(self.support, self._c_device(), loc, value=value, gradient=gradient)
+
     def _evaluate_value_local(self, locations):
         self.update()
         loc = np.asarray(locations, dtype=float)

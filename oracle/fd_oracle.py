@@ -552,16 +552,25 @@ def solve_direct(A, b, ridge=RIDGE):
     return spla.spsolve(N.tocsc(), rhs)
 
 
-def solve_reference_cg(A, b, tol=None, rtol=1e-5, maxiter=None, ridge=RIDGE, x0=None):
-    """The reference default path verbatim in scipy: ridge rows, column
-    scaling, cg on (AS)ᵀ(AS), scale back (SP:86-124, SS:48-72, DI:1312)."""
+def reference_cg_system(A, b, ridge=RIDGE):
+    """Everything the reference's default solve does before scipy's CG
+    iterations (SP:86-124, DI:815-833, SS:48-72): ridge rows, column scaling
+    S = 1/|col|, the normal matrix (AS)ᵀ(AS) and its right-hand side.
+    Returns (N, rhs, s) with s the diagonal of S."""
     Af = sparse.vstack([A, sparse.eye(A.shape[1]) * ridge]).tocsr()
     bf = np.hstack([b, np.zeros(A.shape[1])])
     cn = sparse.linalg.norm(Af, axis=0)
     s = np.ones(Af.shape[1])
     s[cn > 0] = 1.0 / cn[cn > 0]
+    As = (Af @ sparse.diags(s)).tocsr()
+    return (As.T @ As).tocsr(), As.T @ bf, s
+
+
+def solve_reference_cg(A, b, tol=None, rtol=1e-5, maxiter=None, ridge=RIDGE, x0=None):
+    """The reference default path verbatim in scipy: ridge rows, column
+    scaling, cg on (AS)ᵀ(AS), scale back (SP:86-124, SS:48-72, DI:1312)."""
+    N, rhs, s = reference_cg_system(A, b, ridge)
     S = sparse.diags(s)
-    As = (Af @ S).tocsr()
     kw = {"rtol": rtol}
     if tol is not None:
         kw["atol"] = tol
@@ -574,7 +583,7 @@ def solve_reference_cg(A, b, tol=None, rtol=1e-5, maxiter=None, ridge=RIDGE, x0=
     def cb(_):
         info["it"] = info.get("it", 0) + 1
 
-    y, flag = spla.cg((As.T @ As).tocsr(), As.T @ bf, callback=cb, **kw)
+    y, flag = spla.cg(N, rhs, callback=cb, **kw)
     return S @ y, flag, info.get("it", 0)
 
 

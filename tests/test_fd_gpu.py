@@ -418,3 +418,27 @@ def test_build_matrix_and_custom_solver_match_reference(golden, name):
     assert np.linalg.norm(interp.c - ref) <= 1e-8 * np.linalg.norm(ref)
     res = interp.calculate_residual_for_constraints()
     assert set(res) == set(cs.families)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_non_finite_rows_give_nan_status(caplog, precision):
+    """A data row with a NaN coefficient that reaches ls_fd_create (the
+    interpolator's own checks drop such families, as the reference does, so
+    the row is planted in the device tensor after setup): the solve stops with
+    LS_NAN instead of iterating to maxiter, and solve_system warns."""
+    import logging
+
+    rng = np.random.default_rng(31)
+    grid = _grid((12, 10, 9))
+    interp = L.FiniteDifferenceInterpolator(grid)
+    vp = rng.uniform(0, 1, size=(50, 3))
+    interp.set_value_constraints(np.column_stack([vp, vp[:, 2], np.ones(50)]))
+    interp.setup_interpolator(regularisation=0.1, cpw=1.0)
+    interp.constraints["value"].a[3, 2] = float("nan")
+    with caplog.at_level(logging.WARNING):
+        assert interp.solve_system("cg", solver_kwargs={"precision": precision, "maxiter": 5000,
+                                                        "preconditioner": "jacobi"})
+    t = interp.get_last_solve_timing()
+    assert t["status"] == _lib.LS_NAN, t
+    assert t["iterations"] < 5000
+    assert "nan" in caplog.text
