@@ -336,6 +336,15 @@ int ls_fd_eval_points(const ls_grid3 *grid, const double *d_c, const double *d_p
 int ls_fd_eval_adjoint(const ls_grid3 *grid, const double *d_pts, int64_t npts, int64_t ld, const double *d_gvalue,
                        const double *d_ggrad, double *d_out, void *stream);
 
+/* Jets of the trilinear field c at points (npts x ld, x y z first): d_out
+ * (npts x 11 FP64) = u, du/dx, du/dy, du/dz, d2u/dxdy, d2u/dxdz, d2u/dydz,
+ * the local coordinates lx, ly, lz in the cell (G:126-146, clipped to [0, 1])
+ * and 1 for points inside the support; all 0 outside.  The quantities the
+ * adjoint with respect to point positions and normal vectors needs; no
+ * counterpart in the reference. */
+int ls_fd_eval_jets(const ls_grid3 *grid, const double *d_c, const double *d_pts, int64_t npts, int64_t ld,
+                    double *d_out, void *stream);
+
 /* The same on a regular lattice of points origin + step * (i, j, k),
  * i < n[0] fastest; output index i + n0*j + n0*n1*k. */
 int ls_fd_eval_lattice(const ls_grid3 *grid, const double *d_c, const double lat_origin[3],

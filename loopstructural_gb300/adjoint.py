@@ -126,3 +126,188 @@ class ValueFieldAdjoint:
 
     def close(self):
         self.system.close()
+
+
+class ConstraintAdjoint:
+    """u(theta) = E_q c(theta): the field at `query` points as a differentiable
+    function of an FD interpolator's data -- the value constraints' values
+    and positions, the normal constraints' vectors and positions -- and of the
+    isotropic regularisation weight.
+
+        f = ConstraintAdjoint(grid, query, value_weights, normal_weights, cpw=1.0, npw=1.0)
+        u = f(values, value_points, normals, normal_points, reg)   # FP64 CUDA tensors
+        loss(u).backward()                                        # .grad on every input
+
+    Each forward call assembles the rows (ls_fd_point_rows) and solves the
+    normal equations N c = A^T W b; backward runs one adjoint solve
+    N lam = E_q^T dL/du with the same handle and then, per data row r with
+    a = row coefficients, b = target, w = weight (rows normalised as the
+    reference does, DI:361-366):
+
+        dL/db_r = w^2 (lam . a),   dL/da_r = w^2 ((b - a.c) lam - (lam . a) c),
+
+    chained through a = t/|t|, b = v/|t| (value rows, t the trilinear weights)
+    and a = T_d/|T_d|, b = n_d/|T_d| (normal rows, T_d the shape-function
+    derivatives along axis d), using the jets (value, gradient, mixed second
+    derivatives) of c and lam at the points (ls_fd_eval_jets).  The
+    regularisation weight scales every interior family's row weight, so
+    dL/dreg = -(2/reg) lam^T N_int c with N_int the interior regularisation
+    operator (a second handle without data rows, borders or ridge).
+    Positions move rows inside their cell; a point crossing a cell face changes
+    the row's columns, where the field is continuous but its derivative is not.
+    The reference has no gradient path; iterates are not stored (the backward
+    solve recomputes what it needs)."""
+
+    def __init__(self, support, query, value_weights, normal_weights, cpw=1.0, npw=1.0, precision="fp64",
+                 rtol=1e-13, maxiter=None):
+        import torch
+
+        self.support = support
+        self.dev = _lib.device()
+        self.qpts = torch.as_tensor(np.ascontiguousarray(np.asarray(query, dtype=float)[:, :3])).to(self.dev)
+        self.value_w = np.asarray(value_weights, dtype=float)
+        self.normal_w = np.asarray(normal_weights, dtype=float)
+        self.cpw, self.npw = float(cpw), float(npw)
+        self.precision, self.rtol, self.maxiter = precision, rtol, maxiter
+        self.step = torch.as_tensor(np.asarray(support.step_vector, dtype=float)).to(self.dev)
+        self.last_stats = {}
+
+    # -- device helpers ---------------------------------------------------------
+    def _jets(self, pts, c):
+        import torch
+
+        out = torch.empty((pts.shape[0], 11), dtype=torch.float64, device=self.dev)
+        if pts.shape[0]:
+            grid = self.support.grid3()
+            _lib.check(_lib.load().ls_fd_eval_jets(C.byref(grid), _lib.ptr(c.contiguous()), _lib.ptr(pts.contiguous()),
+                                                   pts.shape[0], 3, _lib.ptr(out), _lib.stream_ptr()))
+        return out
+
+    def _spread(self, pts, g):
+        import torch
+
+        out = torch.zeros(self.support.n_nodes, dtype=torch.float64, device=self.dev)
+        grid = self.support.grid3()
+        _lib.check(_lib.load().ls_fd_eval_adjoint(C.byref(grid), _lib.ptr(pts), pts.shape[0], 3,
+                                                  _lib.ptr(g.contiguous()), None, _lib.ptr(out), _lib.stream_ptr()))
+        return out
+
+    def _interp(self, values, vpts, normals, npts, reg):
+        from .interpolators import FiniteDifferenceInterpolator
+
+        it = FiniteDifferenceInterpolator(self.support)
+        if values.shape[0]:
+            it.set_value_constraints(np.column_stack([vpts, values, self.value_w]))
+        if normals.shape[0]:
+            it.set_normal_constraints(np.column_stack([npts, normals, self.normal_w]))
+        it.setup_interpolator(regularisation=reg, cpw=self.cpw, npw=self.npw)
+        return it
+
+    def solve(self, values, vpts, normals, npts, reg):
+        """(c, u, system) for the given data (host or device tensors; no autograd)."""
+        cpu = [np.asarray(t.detach().cpu().numpy() if hasattr(t, "detach") else t, dtype=float)
+               for t in (values, vpts, normals, npts)]
+        it = self._interp(*cpu, float(reg))
+        system = it._build_system()
+        c, st = system.solve(atol=0.0, rtol=self.rtol, precision=self.precision, maxiter=self.maxiter)
+        self.last_stats["forward"] = st
+        u = self._jets(self.qpts, c)[:, 0]
+        return c, u, system, it
+
+    # -- gradients ---------------------------------------------------------------
+    def gradients(self, system, interp, c, grad_u, values, vpts, normals, npts, reg):
+        """dL/d(values, value points, normals, normal points, reg) for
+        dL/du = grad_u, at the solution c of `system`."""
+        import torch
+
+        _lib.check(_lib.load().ls_fd_set_rhs(system.handle, _lib.ptr(self._spread(self.qpts, grad_u)),
+                                             _lib.stream_ptr()))
+        lam, st = system.solve(atol=0.0, rtol=self.rtol, precision=self.precision, maxiter=self.maxiter)
+        self.last_stats["adjoint"] = st
+        h = self.step
+
+        def axis_terms(J):
+            loc = J[:, 7:10]
+            s = loc * loc + (1.0 - loc) ** 2            # per-axis |weights|^2
+            ds = 2.0 * (2.0 * loc - 1.0) / h            # d s / d p (per axis)
+            return s, ds
+
+        # value rows ------------------------------------------------------------
+        v = values.to(torch.float64)
+        gv = torch.zeros_like(v)
+        gvp = torch.zeros((v.shape[0], 3), dtype=torch.float64, device=self.dev)
+        if v.shape[0]:
+            Jc, Jl = self._jets(vpts, c), self._jets(vpts, lam)
+            inside = Jc[:, 10] > 0
+            s, ds = axis_terms(Jc)
+            n2 = s.prod(dim=1)
+            w2 = (self.cpw * torch.as_tensor(self.value_w, device=self.dev)) ** 2
+            U, gU, L0, gL = Jc[:, 0], Jc[:, 1:4], Jl[:, 0], Jl[:, 1:4]
+            safe = torch.where(inside, n2, torch.ones_like(n2))
+            f = torch.where(inside, w2 / safe, torch.zeros_like(n2))
+            gv = f * L0
+            res = v - U
+            gn_over_n = 0.5 * ds / s                   # (d|t|/dp) / |t|
+            gvp = f[:, None] * (res[:, None] * gL - L0[:, None] * gU - 2.0 * (res * L0)[:, None] * gn_over_n)
+        # normal rows -----------------------------------------------------------
+        nv = normals.to(torch.float64)
+        gn = torch.zeros_like(nv)
+        gnp = torch.zeros((nv.shape[0], 3), dtype=torch.float64, device=self.dev)
+        if nv.shape[0]:
+            Jc, Jl = self._jets(npts, c), self._jets(npts, lam)
+            inside = Jc[:, 10] > 0
+            s, ds = axis_terms(Jc)
+            w2 = (self.npw / 3.0 * torch.as_tensor(self.normal_w, device=self.dev)) ** 2
+            # mixed second derivatives, symmetric: index (d, e) -> column
+            mix = {(0, 1): 4, (1, 0): 4, (0, 2): 5, (2, 0): 5, (1, 2): 6, (2, 1): 6}
+            for d in range(3):
+                others = [e for e in range(3) if e != d]
+                m2 = 2.0 * s[:, others[0]] * s[:, others[1]] / (h[d] * h[d])   # |T_d|^2
+                safe = torch.where(inside, m2, torch.ones_like(m2))
+                f = torch.where(inside, w2 / safe, torch.zeros_like(m2))
+                dU, dL = Jc[:, 1 + d], Jl[:, 1 + d]
+                gn[:, d] = f * dL
+                res = nv[:, d] - dU
+                for e in others:
+                    gm_over_m = 0.5 * ds[:, e] / s[:, e]  # (d|T_d|/dp_e) / |T_d|
+                    gnp[:, e] += f * (res * Jl[:, mix[(d, e)]] - dL * Jc[:, mix[(d, e)]] - 2.0 * res * dL * gm_over_m)
+        # regularisation weight ------------------------------------------------------
+        greg = torch.zeros((), dtype=torch.float64, device=self.dev)
+        if reg != 0.0:
+            from .fd import FdSystem
+
+            wint = {k: float(val) for k, val in interp._reg_weights().items()}
+            for k in ("dx", "dy", "dz"):
+                wint[k] = 0.0
+            interior = FdSystem(self.support, wint, [], 0.0)
+            try:
+                greg = -(2.0 / float(reg)) * torch.dot(lam, interior.apply(c))
+            finally:
+                interior.close()
+        return gv, gvp, gn, gnp, greg
+
+    def __call__(self, values, value_points, normals, normal_points, reg):
+        import torch
+
+        outer = self
+
+        class _Fn(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, v, vp, n, np_, r):
+                c, u, system, it = outer.solve(v, vp, n, np_, float(r))
+                ctx.saved = (c, system, it, v.detach().to(torch.float64), vp.detach().to(torch.float64).contiguous(),
+                             n.detach().to(torch.float64), np_.detach().to(torch.float64).contiguous(), float(r))
+                return u
+
+            @staticmethod
+            def backward(ctx, grad_u):
+                c, system, it, v, vp, n, np_, r = ctx.saved
+                try:
+                    gv, gvp, gn, gnp, greg = outer.gradients(system, it, c, grad_u.detach().to(torch.float64).contiguous(),
+                                                             v, vp, n, np_, r)
+                finally:
+                    system.close()
+                return gv, gvp, gn, gnp, greg
+
+        return _Fn.apply(values, value_points, normals, normal_points, torch.as_tensor(reg, dtype=torch.float64,
+                                                                                       device=self.dev))

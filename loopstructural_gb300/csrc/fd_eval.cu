@@ -340,10 +340,77 @@ __global__ void eval_adjoint_kernel(EvalGrid g, const double *__restrict__ pts, 
   }
 }
 
+// Field jets at points: out[11 i ..] = (u, du/dx, du/dy, du/dz, d2u/dxdy,
+// d2u/dxdz, d2u/dydz, lx, ly, lz, inside) of the trilinear interpolant of c
+// (second derivatives along one axis vanish); local coordinates in [0, 1];
+// all 0 outside the support.  The inputs of the adjoint with respect to point
+// positions and normal vectors.
+__global__ void eval_jets_kernel(EvalGrid g, const double *__restrict__ c, const double *__restrict__ pts, int64_t n,
+                                 int64_t ld, double *__restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double *p = pts + i * ld;
+    AxisLoc l[3];
+    bool inside = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      l[d] = locate_axis(g, d, p[d]);
+      inside &= l[d].inside;
+    }
+    double *o = out + 11 * i;
+    if (!inside) {
+#pragma unroll
+      for (int k = 0; k < 11; ++k) o[k] = 0.0;
+      continue;
+    }
+    const int64_t nx = g.n[0], nxy = g.n[0] * g.n[1];
+    const int64_t g0 = l[0].cell + nx * l[1].cell + nxy * l[2].cell;
+    double u = 0, ux = 0, uy = 0, uz = 0, uxy = 0, uxz = 0, uyz = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int bx = k & 1, by = (k >> 1) & 1, bz = (k >> 2) & 1;
+      const double cv = c[g0 + bx + nx * by + nxy * bz];
+      const double wx = bx ? l[0].l : 1 - l[0].l, wy = by ? l[1].l : 1 - l[1].l, wz = bz ? l[2].l : 1 - l[2].l;
+      const double dx = (bx ? 1.0 : -1.0) / g.step[0], dy = (by ? 1.0 : -1.0) / g.step[1],
+                   dz = (bz ? 1.0 : -1.0) / g.step[2];
+      u += wx * wy * wz * cv;
+      ux += dx * wy * wz * cv;
+      uy += wx * dy * wz * cv;
+      uz += wx * wy * dz * cv;
+      uxy += dx * dy * wz * cv;
+      uxz += dx * wy * dz * cv;
+      uyz += wx * dy * dz * cv;
+    }
+    o[0] = u;
+    o[1] = ux;
+    o[2] = uy;
+    o[3] = uz;
+    o[4] = uxy;
+    o[5] = uxz;
+    o[6] = uyz;
+    o[7] = l[0].l;
+    o[8] = l[1].l;
+    o[9] = l[2].l;
+    o[10] = 1.0;
+  }
+}
+
 }  // namespace
 }  // namespace ls
 
 using namespace ls;
+
+extern "C" int ls_fd_eval_jets(const ls_grid3 *grid, const double *d_c, const double *d_pts, int64_t npts, int64_t ld,
+                               double *d_out, void *stream) {
+  LS_ARG_CHECK(grid && d_c && d_out, "NULL argument");
+  LS_ARG_CHECK(npts >= 0 && ld >= 3, "bad npts / ld");
+  if (npts == 0) return LS_OK;
+  LS_ARG_CHECK(d_pts != nullptr, "NULL points");
+  EvalGrid g = make_eval_grid(*grid);
+  cudaStream_t s = as_stream(stream);
+  eval_jets_kernel<<<stream_grid(npts, 256), 256, 0, s>>>(g, d_c, d_pts, npts, ld, d_out);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
 
 extern "C" int ls_fd_eval_adjoint(const ls_grid3 *grid, const double *d_pts, int64_t npts, int64_t ld,
                                   const double *d_gvalue, const double *d_ggrad, double *d_out, void *stream) {
