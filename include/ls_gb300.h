@@ -352,6 +352,72 @@ int ls_fd_eval_lattice(const ls_grid3 *grid, const double *d_c, const double lat
                        void *stream);
 
 /* ------------------------------------------------------------------ */
+/* Fault displacement: evaluation of a faulted feature (the caller of K7) */
+/* ------------------------------------------------------------------ */
+
+/* A fault profile function of one fault-frame coordinate (the reference's
+ * LoopStructural/modelling/features/fault/_fault_function.py, FF below):
+ * ONES / ZEROS (FF:252-307), SMOOTH_PEAK x^4 - 2 x^2 + 1 on [-1, 1] else 0
+ * (FF:12-16), CUBIC w0 v^3 + w1 v^2 + w2 v + w3 held at its value at lim[0] /
+ * lim[1] outside them, then clamped to [min_v, max_v] (FF:40-150, the
+ * coefficients already fitted), COMPOSITE: the cubic [0] for v > 0, the cubic
+ * [1] for v < 0, 0 at 0 (FF:197-230). */
+typedef enum ls_profile_kind {
+  LS_PROFILE_ONES = 0, LS_PROFILE_ZEROS = 1, LS_PROFILE_SMOOTH_PEAK = 2, LS_PROFILE_CUBIC = 3,
+  LS_PROFILE_COMPOSITE = 4
+} ls_profile_kind;
+
+typedef struct ls_fault_profile {
+  int32_t kind;
+  int32_t pad;
+  double w[2][4];     /* cubic coefficients ([1] only for COMPOSITE, its negative side) */
+  double lim[2][2];   /* [lower, upper] x limits of each cubic */
+  double clamp[2][2]; /* [min_v, max_v] of each cubic */
+} ls_fault_profile;
+
+/* One fault-frame coordinate field: a solved FD field (node values d_c on
+ * `grid`, device) and the affine maps of its interpolator's bounding box:
+ * local = to_local[0..2][0..2] world + to_local[.][3], gradients back to the
+ * world frame by the 3x3 rotation to_world. */
+typedef struct ls_fault_field {
+  ls_grid3 grid;
+  const double *d_c;
+  double to_local[3][4];
+  double to_world[3][3];
+} ls_fault_field;
+
+/* A fault slip event (the reference's FaultSegment, LoopStructural/modelling/
+ * features/fault/_fault_segment.py FS:25-60): the three frame fields
+ * (gx normal to the fault, gy along slip, gz along extent), the displacement
+ * magnitude, the number of integration steps, and the displacement function
+ * scale * gx(gx) * gy(gy) * gz(gz) (FF:310-361); has_function = 0 gives unit
+ * displacement on the hanging wall (gx > 0) instead. */
+typedef struct ls_fault {
+  ls_fault_field frame[3];
+  double displacement;
+  int32_t steps;
+  int32_t has_function;
+  double scale;
+  ls_fault_profile profile[3];
+} ls_fault;
+
+/* Restores points through one fault in place (FS:315-423 apply_to_points):
+ * per point, the frame coordinates and the displacement d at the point; points
+ * with d = 0 (or a frame coordinate NaN: outside a frame field) stay put; the
+ * others move `steps` times by d / steps along the unit gradient of the gy
+ * field, re-evaluating the frame at every step.  As in the reference, the
+ * `reverse` sign of apply_to_points does not reach the integration (its
+ * displacement is recomputed each step), so there is no reverse flag here.
+ * d_pts: npts x ld FP64 (x y z first), device. */
+int ls_fault_apply(const ls_fault *fault, double *d_pts, int64_t npts, int64_t ld, void *stream);
+
+/* Gradient of a linear field over tetrahedra (LoopStructural/utils/maths.py
+ * gradient_from_tetrahedron): d_tetra (n x 4 x 3 vertex coordinates),
+ * d_values (n x 4 vertex values) -> d_grad (n x 3) solving
+ * (v_k - v_0) . g = f_k - f_0, k = 1..3.  Degenerate tetrahedra give NaN. */
+int ls_tetra_gradient(const double *d_tetra, const double *d_values, int64_t n, double *d_grad, void *stream);
+
+/* ------------------------------------------------------------------ */
 /* P1 on a structured TetMesh (5 tetrahedra per cell) (K3)              */
 /* ------------------------------------------------------------------ */
 

@@ -38,7 +38,7 @@ EXPORTS = (
     "ls_fd_create", "ls_fd_destroy", "ls_fd_dof", "ls_fd_apply", "ls_fd_apply_f32", "ls_fd_apply_noalloc", "ls_fd_rhs",
     "ls_fd_diagonal", "ls_fd_solve", "ls_fd_profile_iteration", "ls_fd_profile_mg", "ls_fd_eval_points", "ls_fd_eval_lattice",
     "ls_fd_eval_adjoint", "ls_fd_set_rhs", "ls_fd_data_rows_apply", "ls_fd_device", "ls_fd_prepare", "ls_fd_solve_batched",
-    "ls_fd_mg_apply_level", "ls_fd_setup_profile", "ls_fd_staged_apply", "ls_fd_mg_vcycle", "ls_fd_eval_jets",
+    "ls_fd_mg_apply_level", "ls_fd_setup_profile", "ls_fd_staged_apply", "ls_fd_mg_vcycle", "ls_fd_eval_jets", "ls_fault_apply", "ls_tetra_gradient",
     "ls_p1_face_count", "ls_p1_face_rows", "ls_p1_face_rows_directional", "ls_p1_locate", "ls_p1_point_rows",
     "ls_p1_eval_points", "ls_iso_extract", "ls_iso_copy", "ls_iso_destroy",
 )
@@ -96,6 +96,25 @@ class SolveStats(C.Structure):
     ]
 
 
+# fault displacement (ls_fault_*): profile kinds and structures
+PROFILE_ONES, PROFILE_ZEROS, PROFILE_SMOOTH_PEAK, PROFILE_CUBIC, PROFILE_COMPOSITE = 0, 1, 2, 3, 4
+
+
+class FaultProfile(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("pad", C.c_int32), ("w", (C.c_double * 4) * 2),
+                ("lim", (C.c_double * 2) * 2), ("clamp", (C.c_double * 2) * 2)]
+
+
+class FaultField(C.Structure):
+    _fields_ = [("grid", Grid3), ("d_c", C.c_void_p), ("to_local", (C.c_double * 4) * 3),
+                ("to_world", (C.c_double * 3) * 3)]
+
+
+class Fault(C.Structure):
+    _fields_ = [("frame", FaultField * 3), ("displacement", C.c_double), ("steps", C.c_int32),
+                ("has_function", C.c_int32), ("scale", C.c_double), ("profile", FaultProfile * 3)]
+
+
 class FdProfile(C.Structure):
     _fields_ = [("stencil_ms", C.c_double), ("data_ms", C.c_double), ("update_ms", C.c_double),
                 ("iteration_ms", C.c_double), ("stencil_bytes", C.c_double), ("iteration_bytes", C.c_double)]
@@ -133,6 +152,8 @@ _SIGS = {
     "ls_fd_staged_apply": (C.c_int, [_P]),
     "ls_fd_mg_vcycle": (C.c_int, [_P, _P, _P, _P]),
     "ls_fd_eval_jets": (C.c_int, [C.POINTER(Grid3), _P, _P, C.c_int64, C.c_int64, _P, _P]),
+    "ls_fault_apply": (C.c_int, [C.POINTER(Fault), _P, C.c_int64, C.c_int64, _P]),
+    "ls_tetra_gradient": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "ls_fd_prepare": (C.c_int, [_P, C.POINTER(SolveOpts)]),
     "ls_fd_mg_apply_level": (C.c_int, [_P, C.c_int, _P, _P, C.POINTER(C.c_int64), _P]),
     "ls_fd_solve_batched": (C.c_int, [C.POINTER(_P), C.POINTER(SolveOpts), C.POINTER(_P), C.POINTER(SolveStats),

@@ -394,10 +394,173 @@ __global__ void eval_jets_kernel(EvalGrid g, const double *__restrict__ c, const
   }
 }
 
+// ---------------------------------------------------------------------------
+// Fault displacement (the caller of K7 for faulted features).
+struct FaultDev {
+  EvalGrid grid[3];
+  const double *c[3];
+  double to_local[3][3][4];
+  double to_world[3][3][3];
+  double displacement, scale;
+  int steps, has_function;
+  ls_fault_profile prof[3];
+};
+
+__device__ __forceinline__ double cubic_at(const double *w, double v) {
+  return w[0] * pow(v, 3.0) + w[1] * pow(v, 2.0) + w[2] * v + w[3];
+}
+
+// one cubic with its limits and clamp (FF:123-140)
+__device__ double cubic_profile(const ls_fault_profile &p, int k, double v) {
+  double e = cubic_at(p.w[k], v);
+  if (v > p.lim[k][1]) e = cubic_at(p.w[k], p.lim[k][1]);
+  if (v < p.lim[k][0]) e = cubic_at(p.w[k], p.lim[k][0]);
+  if (e > p.clamp[k][1]) e = p.clamp[k][1];
+  if (e < p.clamp[k][0]) e = p.clamp[k][0];
+  return e;
+}
+
+__device__ double profile_at(const ls_fault_profile &p, double v) {
+  switch (p.kind) {
+    case LS_PROFILE_ZEROS: return 0.0;
+    case LS_PROFILE_SMOOTH_PEAK: return (v >= -1.0 && v <= 1.0) ? pow(v, 4.0) - 2.0 * pow(v, 2.0) + 1.0 : 0.0;
+    case LS_PROFILE_CUBIC: return cubic_profile(p, 0, v);
+    case LS_PROFILE_COMPOSITE: return v > 0.0 ? cubic_profile(p, 0, v) : (v < 0.0 ? cubic_profile(p, 1, v) : 0.0);
+    default: return 1.0;
+  }
+}
+
+// frame coordinate k at world point w (NaN outside its support); with grad,
+// also its world-frame gradient (0 outside)
+__device__ double frame_value(const FaultDev &f, int k, const double w[3], double *grad) {
+  double l[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+    l[a] = f.to_local[k][a][0] * w[0] + f.to_local[k][a][1] * w[1] + f.to_local[k][a][2] * w[2] +
+           f.to_local[k][a][3];
+  double v, gl[3];
+  eval_one(f.grid[k], f.c[k], l[0], l[1], l[2], &v, grad ? gl : nullptr);
+  if (grad) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+      grad[a] = f.to_world[k][a][0] * gl[0] + f.to_world[k][a][1] * gl[1] + f.to_world[k][a][2] * gl[2];
+  }
+  return v;
+}
+
+// displacement of FS:352-362 / FS:399-410 for frame coordinates (gx, gy, gz)
+__device__ double fault_d(const FaultDev &f, double gx, double gy, double gz) {
+  const bool ok = !isnan(gx) && !isnan(gy) && !isnan(gz);
+  if (!ok) return 0.0;
+  if (f.has_function)
+    return f.scale * profile_at(f.prof[0], gx) * profile_at(f.prof[1], gy) * profile_at(f.prof[2], gz);
+  return gx > 0.0 ? 1.0 : 0.0;
+}
+
+__global__ void fault_apply_kernel(FaultDev f, double *__restrict__ pts, int64_t n, int64_t ld) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double *p = pts + i * ld;
+    double w[3] = {p[0], p[1], p[2]};
+    double gx = frame_value(f, 0, w, nullptr), gy = frame_value(f, 1, w, nullptr), gz = frame_value(f, 2, w, nullptr);
+    if (!(fabs(fault_d(f, gx, gy, gz)) > 0.0)) continue;  // unaffected by this fault
+    const double inv_steps = 1.0 / (double)f.steps;
+    for (int s = 0; s < f.steps; ++s) {
+      double g[3];
+      if (s > 0) {
+        gx = frame_value(f, 0, w, nullptr);
+        gz = frame_value(f, 2, w, nullptr);
+      }
+      gy = frame_value(f, 1, w, g);
+      const double d = fault_d(f, gx, gy, gz) * f.displacement;
+      const bool ok = !isnan(gx) && !isnan(gy) && !isnan(gz);
+      const double mag = ok ? sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]) : 0.0;
+      const double scale = inv_steps * d;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const double ga = mag > 0.0 ? g[a] / mag : g[a];
+        w[a] += ga * scale;
+      }
+    }
+    p[0] = w[0];
+    p[1] = w[1];
+    p[2] = w[2];
+  }
+}
+
+// gradient of the linear interpolant over one tetrahedron: M g = df with
+// M rows v_k - v_0, df_k = f_k - f_0 (k = 1..3), by cofactors
+__global__ void tetra_gradient_kernel(const double *__restrict__ tet, const double *__restrict__ val, int64_t n,
+                                      double *__restrict__ grad) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double *t = tet + 12 * i;
+    const double *f = val + 4 * i;
+    double m[3][3], r[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+#pragma unroll
+      for (int a = 0; a < 3; ++a) m[k][a] = t[3 * (k + 1) + a] - t[a];
+      r[k] = f[k + 1] - f[0];
+    }
+    // cofactor matrix C, det = row 0 . C row 0; inverse = C^T / det
+    const double c00 = m[1][1] * m[2][2] - m[1][2] * m[2][1], c01 = m[1][2] * m[2][0] - m[1][0] * m[2][2],
+                 c02 = m[1][0] * m[2][1] - m[1][1] * m[2][0];
+    const double c10 = m[0][2] * m[2][1] - m[0][1] * m[2][2], c11 = m[0][0] * m[2][2] - m[0][2] * m[2][0],
+                 c12 = m[0][1] * m[2][0] - m[0][0] * m[2][1];
+    const double c20 = m[0][1] * m[1][2] - m[0][2] * m[1][1], c21 = m[0][2] * m[1][0] - m[0][0] * m[1][2],
+                 c22 = m[0][0] * m[1][1] - m[0][1] * m[1][0];
+    const double det = m[0][0] * c00 + m[0][1] * c01 + m[0][2] * c02;
+    const double inv = det != 0.0 ? 1.0 / det : __longlong_as_double(0x7ff8000000000000LL);
+    double *o = grad + 3 * i;
+    o[0] = (c00 * r[0] + c10 * r[1] + c20 * r[2]) * inv;
+    o[1] = (c01 * r[0] + c11 * r[1] + c21 * r[2]) * inv;
+    o[2] = (c02 * r[0] + c12 * r[1] + c22 * r[2]) * inv;
+  }
+}
+
 }  // namespace
 }  // namespace ls
 
 using namespace ls;
+
+extern "C" int ls_fault_apply(const ls_fault *fault, double *d_pts, int64_t npts, int64_t ld, void *stream) {
+  LS_ARG_CHECK(fault != nullptr, "NULL fault");
+  LS_ARG_CHECK(npts >= 0 && ld >= 3, "bad npts / ld");
+  LS_ARG_CHECK(fault->steps >= 1, "steps must be >= 1");
+  if (npts == 0) return LS_OK;
+  LS_ARG_CHECK(d_pts != nullptr, "NULL points");
+  FaultDev f;
+  for (int k = 0; k < 3; ++k) {
+    const ls_fault_field &fr = fault->frame[k];
+    LS_ARG_CHECK(fr.d_c != nullptr, "NULL frame field");
+    for (int d = 0; d < 3; ++d) LS_ARG_CHECK(fr.grid.nsteps[d] >= 2 && fr.grid.step[d] > 0.0, "bad frame grid");
+    f.grid[k] = make_eval_grid(fr.grid);
+    f.c[k] = fr.d_c;
+    for (int a = 0; a < 3; ++a) {
+      for (int b = 0; b < 4; ++b) f.to_local[k][a][b] = fr.to_local[a][b];
+      for (int b = 0; b < 3; ++b) f.to_world[k][a][b] = fr.to_world[a][b];
+    }
+    f.prof[k] = fault->profile[k];
+    LS_ARG_CHECK(f.prof[k].kind >= LS_PROFILE_ONES && f.prof[k].kind <= LS_PROFILE_COMPOSITE, "unknown profile kind");
+  }
+  f.displacement = fault->displacement;
+  f.scale = fault->scale;
+  f.steps = fault->steps;
+  f.has_function = fault->has_function;
+  cudaStream_t s = as_stream(stream);
+  fault_apply_kernel<<<stream_grid(npts, 128), 128, 0, s>>>(f, d_pts, npts, ld);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
+
+extern "C" int ls_tetra_gradient(const double *d_tetra, const double *d_values, int64_t n, double *d_grad,
+                                 void *stream) {
+  LS_ARG_CHECK(n >= 0, "n < 0");
+  if (n == 0) return LS_OK;
+  LS_ARG_CHECK(d_tetra && d_values && d_grad, "NULL argument");
+  tetra_gradient_kernel<<<stream_grid(n, 256), 256, 0, as_stream(stream)>>>(d_tetra, d_values, n, d_grad);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
 
 extern "C" int ls_fd_eval_jets(const ls_grid3 *grid, const double *d_c, const double *d_pts, int64_t npts, int64_t ld,
                                double *d_out, void *stream) {

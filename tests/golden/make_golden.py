@@ -5,6 +5,7 @@ Run in a container where the reference source tree is available:
     python tests/golden/make_golden.py /path/to/LoopStructural
     python tests/golden/make_golden.py /path/to/LoopStructural --directional
     python tests/golden/make_golden.py /path/to/LoopStructural --configs
+    python tests/golden/make_golden.py /path/to/LoopStructural --faults
 
 It imports the reference's ``loop_interpolation`` / ``loop_common`` packages
 (``pyvista`` and ``yaml`` are stubbed: they are only used for VTK/YAML export)
@@ -587,6 +588,150 @@ def main_configs(root):
     print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")
 
 
+# ---------------------------------------------------------------------------
+# faulted features (--faults)
+# ---------------------------------------------------------------------------
+def _import_reference_modelling(root):
+    """The reference's modelling package (fault segments, geological
+    features).  Its top-level import needs pandas, scikit-image and its own
+    installed metadata, none of which the fault path uses: they are stubbed
+    (only here, for recording fixtures)."""
+    import importlib.metadata as md
+
+    _version = md.version
+    md.version = lambda name: "1.8.0" if name.lower() == "loopstructural" else _version(name)
+    for name in ("pyvista", "yaml", "pandas", "skimage", "skimage.measure"):
+        if name in sys.modules:
+            continue
+        try:
+            __import__(name)
+        except Exception:
+            m = types.ModuleType(name)
+            if name == "pandas":
+                m.DataFrame = type("DataFrame", (), {})
+                m.Series = type("Series", (), {})
+            if name == "skimage.measure":
+                m.marching_cubes = m.marching_cubes_lewiner = lambda *a, **k: None
+            sys.modules[name] = m
+    if "skimage.measure" in sys.modules and isinstance(sys.modules.get("skimage"), types.ModuleType):
+        sys.modules["skimage"].measure = sys.modules["skimage.measure"]
+    li, StructuredGrid, _ = _import_reference(root)
+    sys.path.insert(0, root)
+    from LoopStructural.modelling.features import GeologicalFeature
+    from LoopStructural.modelling.features.fault._fault_function import CubicFunction, FaultDisplacement, Ones
+    from LoopStructural.modelling.features.fault._fault_segment import FaultSegment
+
+    return li, StructuredGrid, GeologicalFeature, FaultSegment, (CubicFunction, FaultDisplacement, Ones)
+
+
+def _frame_fields(p, variant):
+    """Analytic fault-frame coordinates: gx across a dipping fault surface,
+    gy along slip (a curved direction), gz along the fault's extent."""
+    if variant == 0:
+        gx = (p[:, 0] - 0.5 - 0.1 * (p[:, 2] - 0.5)) / 0.4
+        gy = (0.1 * p[:, 0] + p[:, 2] + 0.05 * np.sin(2 * np.pi * p[:, 1]) - 0.55) / 0.6
+        gz = (p[:, 1] - 0.5) / 0.45
+    else:
+        gx = (p[:, 1] - 0.45 + 0.15 * (p[:, 0] - 0.5)) / 0.35
+        gy = (p[:, 2] - 0.5 + 0.2 * p[:, 1] + 0.03 * np.cos(2 * np.pi * p[:, 0])) / 0.5
+        gz = (p[:, 0] - 0.5) / 0.5
+    return gx, gy, gz
+
+
+def main_faults(root):
+    li, StructuredGrid, GeologicalFeature, FaultSegment, (CubicFunction, FaultDisplacement, Ones) = \
+        _import_reference_modelling(root)
+    out = {}
+
+    def fd_field(cells, origin, step, values_fn, name):
+        grid = StructuredGrid(origin=np.asarray(origin, dtype=float), nsteps=np.asarray(cells),
+                              step_vector=np.asarray(step, dtype=float))
+        interp = li.FiniteDifferenceInterpolator(grid)
+        interp.c = values_fn(grid.nodes)
+        interp.up_to_date = True
+        out[f"{name}_cells"] = np.asarray(cells)
+        out[f"{name}_origin"] = np.asarray(origin, dtype=float)
+        out[f"{name}_step"] = np.asarray(step, dtype=float)
+        out[f"{name}_c"] = np.asarray(interp.c, dtype=float)
+        return interp
+
+    faults = []
+    for k, (cells, disp) in enumerate((((14, 13, 12), 0.2), ((12, 14, 13), -0.15))):
+        frame = []
+        for j, nm in enumerate(("gx", "gy", "gz")):
+            interp = fd_field(cells, (-0.05, -0.05, -0.05), 1.1 / np.asarray(cells, dtype=float),
+                              lambda p, j=j, k=k: _frame_fields(p, k)[j], f"f{k}_{nm}")
+            frame.append(GeologicalFeature(f"fault{k}_{nm}", builder=None, interpolator=interp))
+        fault = FaultSegment(f"fault{k}", frame, displacement=disp)
+        out[f"f{k}_displacement"] = np.array(disp)
+        faults.append(fault)
+    strat = fd_field((16, 15, 17), (0.0, 0.0, 0.0), 1.0 / np.array([16.0, 15.0, 17.0]),
+                     lambda p: p[:, 2] + 0.1 * np.sin(2 * np.pi * p[:, 0]) + 0.05 * np.cos(2 * np.pi * p[:, 1]),
+                     "strat")
+    rng = np.random.default_rng(21)
+    pts = rng.uniform(0.05, 0.95, size=(400, 3))
+    out["points"] = pts
+    # restoration through each fault with the default profile, BaseFault3D,
+    # and a custom displacement with a cubic slip profile
+    for k, f in enumerate(faults):
+        out[f"restored_f{k}_base"] = f.apply_to_points(pts)
+    faults[0].faultfunction = "BaseFault3D"
+    out["restored_f0_base3d"] = faults[0].apply_to_points(pts)
+    gyf = CubicFunction()
+    gyf.add_cstr(-1, 0)
+    gyf.add_cstr(1, 0)
+    gyf.add_cstr(0, 1)
+    gyf.add_grad(0, 0)
+    gyf.add_min(-1)
+    gyf.add_max(1)
+    hw = CubicFunction()
+    hw.add_cstr(0, 1)
+    hw.add_grad(0, 0)
+    hw.add_cstr(1, 0)
+    hw.add_grad(1, 0)
+    hw.set_lim(0, 1)
+    fw = CubicFunction()
+    fw.add_cstr(0, -1)
+    fw.add_grad(0, 0)
+    fw.add_cstr(-1, 0)
+    fw.add_grad(-1, 0)
+    fw.set_lim(-1, 0)
+    faults[0].faultfunction = FaultDisplacement(hw=hw, fw=fw, gy=gyf, gz=Ones(), scale=0.7)
+    out["restored_f0_custom"] = faults[0].apply_to_points(pts)
+    faults[0].faultfunction = "BaseFault"
+    feature = GeologicalFeature("strat", builder=None, interpolator=strat, faults=faults)
+    out["faulted_value"] = feature.evaluate_value(pts)
+    try:
+        out["faulted_gradient"] = feature.evaluate_gradient(pts, element_scale_parameter=0.01)
+        out["faulted_gradient_error"] = np.array("")
+    except Exception as exc:  # recorded: the reference's faulted gradient path
+        out["faulted_gradient_error"] = np.array(f"{type(exc).__name__}: {exc}")
+    # the same steps with the reference's own functions and the result stored
+    # in an (N, 3) array (GF:187-226 with the straddle-check values kept apart)
+    from LoopStructural.utils.maths import gradient_from_tetrahedron, regular_tetraherdron_for_points
+
+    esp = 0.01
+    tet = regular_tetraherdron_for_points(pts, esp)
+    resolved = False
+    while not resolved:
+        resolved = True
+        for f in faults:
+            gxv = f[0].evaluate_value(tet.reshape(-1, 3), fillnan="nearest").reshape(tet.shape[0], 4)
+            if np.any(~(np.all(gxv > 0, axis=1) | np.all(gxv < 0, axis=1))):
+                esp *= 0.5
+                tet = regular_tetraherdron_for_points(pts, esp)
+                resolved = False
+    moved = feature._apply_faults(np.array(tet.reshape(-1, 3))).reshape(tet.shape)
+    vals = strat.evaluate_value(moved.reshape(-1, 3)).reshape(-1, 4)
+    out["faulted_gradient_reference_steps"] = gradient_from_tetrahedron(tet, vals)
+    out["faulted_gradient_scale"] = np.array(esp)
+    plain = GeologicalFeature("strat", builder=None, interpolator=strat)
+    out["plain_gradient"] = plain.evaluate_gradient(pts)
+    path = os.path.join(HERE, "fault_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, sum(v.nbytes for v in out.values()), "bytes;", str(out["faulted_gradient_error"]))
+
+
 def main_directional(root):
     li, StructuredGrid, TetMesh = _import_reference(root)
     out = {}
@@ -615,7 +760,7 @@ def main(root):
 
 
 if __name__ == "__main__":
-    # usage: make_golden.py <reference source root> [--directional | --configs]
+    # usage: make_golden.py <reference source root> [--directional | --configs | --faults]
     # (or the root in the LOOPSTRUCTURAL_REFERENCE environment variable)
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else os.environ.get("LOOPSTRUCTURAL_REFERENCE")
@@ -625,5 +770,7 @@ if __name__ == "__main__":
         main_directional(root)
     elif "--configs" in sys.argv:
         main_configs(root)
+    elif "--faults" in sys.argv:
+        main_faults(root)
     else:
         main(root)
