@@ -2,6 +2,8 @@
 // encoding through the driver entry point, eligibility, launch geometry.
 #include <cudaTypedefs.h>
 
+#include <stdlib.h>
+
 #include <algorithm>
 #include <mutex>
 #include <vector>
@@ -47,10 +49,17 @@ const CUtensorMap *lookup(TmCache &cache, const float *ptr, int kind) {
   return &cache.entries.back().map;
 }
 
+template <int EPI, int ZU>
+void set_attributes_zu() {
+  cudaFuncSetAttribute(fd_tma_apply_kernel<EPI, ZU>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       tm_smem_bytes<EPI>());
+  cudaFuncSetAttribute(fd_tma_apply_kernel<EPI, ZU>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+}
+
 template <int EPI>
 void set_attributes() {
-  cudaFuncSetAttribute(fd_tma_apply_kernel<EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize, tm_smem_bytes<EPI>());
-  cudaFuncSetAttribute(fd_tma_apply_kernel<EPI>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  set_attributes_zu<EPI, 1>();
+  set_attributes_zu<EPI, 2>();
 }
 
 }  // namespace
@@ -65,6 +74,11 @@ void tm_setup(TmCache &cache, int nx, int ny, int nz, bool allow) {
   // window; extents the launch geometry can address
   cache.enabled = allow && g_encode != nullptr && nx % 4 == 0 && nx >= 8 && ny >= 8 && nz >= 8 &&
                   (int64_t)nx * ny * nz < (int64_t)2000000000;
+  // segments per column tile: LS_GB300_TMA_SEGMENTS overrides the one-wave default
+  const char *seg = getenv("LS_GB300_TMA_SEGMENTS");
+  cache.segments = seg ? std::max(0, atoi(seg)) : 0;
+  const char *step = getenv("LS_GB300_TMA_STEP");
+  cache.zu = (step && (atoi(step) == 1 || atoi(step) == 2)) ? atoi(step) : 0;
   if (cache.enabled) {
     set_attributes<EPI_STORE>();
     set_attributes<EPI_CHEB>();
@@ -101,7 +115,12 @@ int tm_launch(TmCache &cache, const CoefT<float> &c, const float *p, DataView<fl
   const int ntx = (c.nx + kTmX - 1) / kTmX, nty = (c.ny + kTmY - 1) / kTmY;
   const int64_t ntiles = (int64_t)ntx * nty;
   const int64_t slots = (int64_t)kTmBlocksPerSm * sm_count();
-  int64_t nseg = std::max<int64_t>(1, slots / std::max<int64_t>(1, ntiles));
+  // segments of ~16 planes (several waves of blocks, so that the tiles with
+  // boundary columns, which cost more per plane, do not set the makespan), at
+  // least enough to fill every SM once
+  int64_t nseg = cache.segments > 0
+                     ? cache.segments
+                     : std::max<int64_t>((c.nz + 15) / 16, std::max<int64_t>(1, slots / std::max<int64_t>(1, ntiles)));
   const int zlen = (int)((c.nz + nseg - 1) / nseg);
   nseg = (c.nz + zlen - 1) / zlen;
   if (ntiles > 0x7fffffff || (dot != nullptr && ntiles * nseg > max_blocks)) return 0;
@@ -115,12 +134,53 @@ int tm_launch(TmCache &cache, const CoefT<float> &c, const float *p, DataView<fl
     dv.qd = qd;
   }
   if (parts & TM_APPLY) {
-    fd_tma_apply_kernel<EPI><<<dim3((unsigned)ntiles, (unsigned)nseg), kTmThreads, tm_smem_bytes<EPI>(), st>>>(
-        maps, c, dv, e, done, ntx, zlen, partials, ticket, dot, dot_clear, fault);
+    const dim3 grid((unsigned)ntiles, (unsigned)nseg);
+    if (cache.zu == 2)
+      fd_tma_apply_kernel<EPI, 2><<<grid, kTmThreads, tm_smem_bytes<EPI>(), st>>>(
+          maps, c, dv, e, done, ntx, zlen, partials, ticket, dot, dot_clear, fault);
+    else
+      fd_tma_apply_kernel<EPI, 1><<<grid, kTmThreads, tm_smem_bytes<EPI>(), st>>>(
+          maps, c, dv, e, done, ntx, zlen, partials, ticket, dot, dot_clear, fault);
     ++launched;
   }
   LS_CUDA_TRY(cudaGetLastError());
   return launched;
+}
+
+int tm_autotune(TmCache &cache, const CoefT<float> &c, const float *p, float *q, int *fault, cudaStream_t st) {
+  if (!cache.enabled || cache.zu != 0) return LS_OK;
+  DataView<float> dv{};
+  dv.enabled = 0;
+  EpiArgs<float> e{};
+  e.q = q;
+  cudaEvent_t a, b;
+  LS_CUDA_TRY(cudaEventCreate(&a));
+  LS_CUDA_TRY(cudaEventCreate(&b));
+  float best = 0.f;
+  int pick = 1;
+  for (int zu = 1; zu <= 2; ++zu) {
+    cache.zu = zu;
+    int st1 = tm_launch<EPI_STORE>(cache, c, p, dv, e, nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr,
+                                   nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, fault, 0, st, TM_APPLY);
+    if (st1 <= 0) break;  // the maps could not be encoded: the launch path stays off
+    cudaEventRecord(a, st);
+    for (int r = 0; r < 5; ++r)
+      tm_launch<EPI_STORE>(cache, c, p, dv, e, nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr,
+                           nullptr, nullptr, nullptr, nullptr, nullptr, fault, 0, st, TM_APPLY);
+    cudaEventRecord(b, st);
+    LS_CUDA_TRY(cudaEventSynchronize(b));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (zu == 1 || ms < best) {
+      best = ms;
+      pick = zu;
+    }
+  }
+  cache.zu = pick;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
 }
 
 #define LS_TM_INST(EPI)                                                                                              \

@@ -135,7 +135,9 @@ __global__ void data_node_totals_kernel(int64_t ntouched, const int64_t *__restr
   }
 }
 
-template <int EPI>
+// ZU: output planes per barrier step (1 or 2; the launcher picks the faster
+// for the grid at first use).
+template <int EPI, int ZU = 1>
 __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
     fd_tma_apply_kernel(const __grid_constant__ TmMaps maps, CoefT<float> c, DataView<float> dv, EpiArgs<float> e,
                         const int *done, int ntx, int zlen, double *partials, unsigned int *ticket, double *dot_out,
@@ -143,8 +145,10 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
   if (done && *done) return;
   constexpr int NOP = TmOps<EPI>::n;
   constexpr int SLOT = tm_slot_floats<EPI>();
-  extern __shared__ __align__(128) unsigned char tm_raw[];
-  float *const tm_smem = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(tm_raw) + 127) & ~(uintptr_t)127);
+  // staged planes: float offsets into the shared array itself (so every read
+  // stays a shared-memory access), the base rounded up to 128 bytes
+  extern __shared__ __align__(128) float tm_smem[];
+  const int sbase = (int)(((128u - (smem_u32(tm_smem) & 127u)) & 127u) >> 2);
   __shared__ __align__(8) uint64_t bars[kTmSlots];
   const int tid = threadIdx.x, tx = tid & (kTmX - 1), ty = tid / kTmX;
   const int x0 = (int)(blockIdx.x % ntx) * kTmX, y0 = (int)(blockIdx.x / ntx) * kTmY;
@@ -158,13 +162,14 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
   const int hx = tx + 4, hy = ty + 2;         // the column's position in a staged plane
   const int own = hy * kTmPX + hx;
 
-  auto slot_of = [&](int t) -> float * { return tm_smem + ((t - tfirst) % kTmSlots) * SLOT; };
-  auto bar_of = [&](int t) -> uint64_t * { return &bars[(t - tfirst) % kTmSlots]; };
-  auto parity_of = [&](int t) -> uint32_t { return (uint32_t)(((t - tfirst) / kTmSlots) & 1); };
+  auto slot_of = [&](int t) -> int { return sbase + ((t - tfirst) & (kTmSlots - 1)) * SLOT; };
+  auto bar_of = [&](int t) -> uint64_t * { return &bars[(t - tfirst) & (kTmSlots - 1)]; };
+  auto parity_of = [&](int t) -> uint32_t { return (uint32_t)(((t - tfirst) >> 3) & 1); };
+  static_assert(kTmSlots == 8, "slot arithmetic assumes 8 slots");
   // one elected thread: plane t of p and, when t - 2 is an output plane, the
   // epilogue operands of plane t - 2, all on the slot's barrier
   auto issue = [&](int t) {
-    float *s = slot_of(t);
+    float *s = tm_smem + slot_of(t);
     uint64_t *b = bar_of(t);
     const bool ops = NOP > 0 && t - 2 >= z0;
     tm_expect(b, (uint32_t)((kTmPlane + (ops ? NOP * kTmOp : 0)) * sizeof(float)));
@@ -184,19 +189,27 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
   if (tid == 0)
     for (int t = tfirst; t <= min(tlast, tfirst + kTmSlots - 1); ++t) issue(t);
 
+  // which formula a warp uses is decided for the whole warp (no divergence):
+  // the deep composite stencil, the exact sum specialised to nodes deep in y
+  // and z (warps holding x-boundary columns), or the general exact sum
+  // (boundary rows in y, boundary planes in z).  A warp is one tile row.
+  const bool ydeep = (j >= 3) & (j <= ny - 4);
+  const bool xshell_warp = __any_sync(0xffffffffu, col_in & !((i >= 3) & (i <= nx - 4))) != 0;
+
   // register windows over planes z-2 .. z+2: p, C_x p, C_y p at the column
   float P0 = 0.f, P1 = 0.f, P2 = 0.f, P3 = 0.f, P4 = 0.f;
   float X0 = 0.f, X1 = 0.f, X2 = 0.f, X3 = 0.f, X4 = 0.f;
   float Y0 = 0.f, Y1 = 0.f, Y2 = 0.f, Y3 = 0.f, Y4 = 0.f;
-  auto inplane = [&](const float *pl, float &P, float &X, float &Y) {
-    const float p0 = pl[own];
+  auto inplane = [&](int pl, float &P, float &X, float &Y) {
+    const float *q = tm_smem + pl + own;
+    const float p0 = q[0];
     P = p0;
-    X = (pl[own - 2] + pl[own + 2]) - 2.f * p0;
-    Y = (pl[own - 2 * kTmPX] + pl[own + 2 * kTmPX]) - 2.f * p0;
+    X = (q[-2] + q[2]) - 2.f * p0;
+    Y = (q[-2 * kTmPX] + q[2 * kTmPX]) - 2.f * p0;
   };
   bool ok = true;
   {
-    float *pls[4];
+    int pls[4];
     for (int t = z0 - 2; t <= z0 + 1; ++t) {
       ok &= tm_wait(bar_of(t), parity_of(t));
       pls[t - z0 + 2] = slot_of(t);
@@ -208,95 +221,99 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
   }
   ok = __syncthreads_and(ok);
 
-  // data term pipeline: mask word + word rank of plane z+1 / z+2, total of plane z / z+1
+  // data term pipeline: mask word of plane z+1 (loaded one step ahead), the
+  // total of plane z+1 requested one step ahead of its use; the word rank is
+  // read only for touched nodes
   const bool data_on = dv.enabled && col_in;
-  auto word_of = [&](int z, uint32_t &w, int32_t &r) {
-    w = 0u;
-    r = 0;
-    if (data_on && z < z1) {
-      const int g = z * sxy + gcol;
-      w = __ldg(dv.mask + (g >> 5));
-      r = __ldg(dv.word_rank + (g >> 5));
-    }
+  auto word_of = [&](int z) -> uint32_t {
+    return (data_on && z < z1) ? __ldg(dv.mask + ((z * sxy + gcol) >> 5)) : 0u;
   };
-  auto total_of = [&](int z, uint32_t w, int32_t r) -> float {
-    if (!data_on || z >= z1) return 0.f;
+  auto total_of = [&](int z, uint32_t w) -> float {
     const int g = z * sxy + gcol;
     const uint32_t bit = 1u << (g & 31);
-    return (w & bit) ? __ldg(dv.qd + r + __popc(w & (bit - 1u))) : 0.f;
+    if (!(w & bit)) return 0.f;
+    return __ldg(dv.qd + __ldg(dv.word_rank + (g >> 5)) + __popc(w & (bit - 1u)));
   };
-  uint32_t mw1 = 0u, mw2 = 0u;
-  int32_t wr1 = 0, wr2 = 0;
-  float qd0 = 0.f, qd1 = 0.f;
-  {
-    uint32_t mw0;
-    int32_t wr0;
-    word_of(z0, mw0, wr0);
-    word_of(z0 + 1, mw1, wr1);
-    qd0 = total_of(z0, mw0, wr0);
-  }
+  uint32_t mw1 = word_of(z0 + 1);
+  float qd0 = total_of(z0, word_of(z0)), qd1 = 0.f;
 
   float local = 0.f;
   int z = z0;
   int zfail = z0 - 3;  // the step whose wait gave up (prologue: z0 - 3)
-  for (; ok && z < z1; ++z) {
-    ok = tm_wait(bar_of(z + 2), parity_of(z + 2));
-    const float *pl2 = slot_of(z + 2);
+  int pm2 = slot_of(z0 - 2), pm1 = slot_of(z0 - 1), po = slot_of(z0), pp1 = slot_of(z0 + 1);
+  for (; ok && z < z1; z += ZU) {
+#pragma unroll
+   for (int u = 0; u < ZU; ++u) {
+    const int zz = z + u;
+    if (ZU > 1 && zz >= z1) break;  // uniform across the block
+    ok = tm_wait(bar_of(zz + 2), parity_of(zz + 2)) && ok;
+    const int pl2 = slot_of(zz + 2);
     inplane(pl2, P4, X4, Y4);
-    // data pipeline: total of plane z+1 requested, words of plane z+2 requested
-    qd1 = total_of(z + 1, mw1, wr1);
-    word_of(z + 2, mw2, wr2);
-    if (col_in) {
-      const float *po = slot_of(z);
-      float q;
-      const bool deep = (i >= 3) & (i <= nx - 4) & (j >= 3) & (j <= ny - 4) & (z >= 3) & (z <= nz - 4);
-      if (deep) {
+    // data pipeline: total of plane zz+1 requested, word of plane zz+2 requested
+    qd1 = total_of(zz + 1, mw1);
+    const uint32_t mw2 = word_of(zz + 2);
+    float q;
+    const bool zdeep = (zz >= 3) & (zz <= nz - 4);
+    if (ydeep & zdeep) {
+      if (!xshell_warp) {
         const float q0 = P2;
-        const float ex = po[own - 2] + po[own + 2], ey = po[own - 2 * kTmPX] + po[own + 2 * kTmPX];
-        const float d4x = ex - 4.f * (po[own - 1] + po[own + 1]) + 6.f * q0;
-        const float d4y = ey - 4.f * (po[own - kTmPX] + po[own + kTmPX]) + 6.f * q0;
-        const float corners = (po[own - 2 * kTmPX - 2] + po[own - 2 * kTmPX + 2]) +
-                              (po[own + 2 * kTmPX - 2] + po[own + 2 * kTmPX + 2]);
+        const float *o = tm_smem + po + own;
+        const float ex = o[-2] + o[2], ey = o[-2 * kTmPX] + o[2 * kTmPX];
+        const float d4x = ex - 4.f * (o[-1] + o[1]) + 6.f * q0;
+        const float d4y = ey - 4.f * (o[-kTmPX] + o[kTmPX]) + 6.f * q0;
+        const float corners = (o[-2 * kTmPX - 2] + o[-2 * kTmPX + 2]) + (o[2 * kTmPX - 2] + o[2 * kTmPX + 2]);
         const float d4z = (P0 + P4) - 4.f * (P1 + P3) + 6.f * q0;
         q = c.ridge2 * q0 + c.xx_int * d4x + c.yy_int * d4y + c.zz_int * d4z +
             c.xy * (corners - 2.f * (ex + ey) + 4.f * q0) + c.xz * ((X0 + X4) - 2.f * X2) +
             c.yz * ((Y0 + Y4) - 2.f * Y2);
       } else {
-        const float *pm2 = slot_of(z - 2), *pm1 = slot_of(z - 1), *pp1 = slot_of(z + 1);
         auto pr = [&](int dz, int dy, int dx) -> float {
-          const float *pl = dz == -2 ? pm2 : dz == -1 ? pm1 : dz == 0 ? po : dz == 1 ? pp1 : pl2;
-          return pl[own + dy * kTmPX + dx];
+          const int pl = dz == -2 ? pm2 : dz == -1 ? pm1 : dz == 0 ? po : dz == 1 ? pp1 : pl2;
+          return tm_smem[pl + own + dy * kTmPX + dx];
         };
-        q = shell_node<float>(c, pr, i, j, z);
+        q = shell_node<float, decltype(pr), false, false>(c, pr, i, j, zz);
       }
-      q += qd0;
-      const int g = z * sxy + gcol;
-      const float *ops = pl2 + kTmPlane + ty * kTmX + tx;
+    } else {
+      auto pr = [&](int dz, int dy, int dx) -> float {
+        const int pl = dz == -2 ? pm2 : dz == -1 ? pm1 : dz == 0 ? po : dz == 1 ? pp1 : pl2;
+        return tm_smem[pl + own + dy * kTmPX + dx];
+      };
+      q = shell_node<float>(c, pr, i, j, zz);
+    }
+    // epilogue of one node: q (data term added), its p, operands in the slot
+    auto emit = [&](int g, int opi, float qn, float pn) {
+      const float *ops = tm_smem + pl2 + kTmPlane + opi;
       if (EPI == EPI_STORE) {
-        e.q[g] = q;
-        local += P2 * q;
+        e.q[g] = qn;
+        local += pn * qn;
       } else if (EPI == EPI_CHEB) {
         const float xv = ops[0], rv = ops[kTmOp], dinv = ops[2 * kTmOp];
-        e.x[g] = xv + P2;
-        const float rn = rv - q;
+        e.x[g] = xv + pn;
+        const float rn = rv - qn;
         e.r[g] = rn;
-        e.d_out[g] = e.c1 * P2 + e.c2 * dinv * rn;
+        e.d_out[g] = e.c1 * pn + e.c2 * dinv * rn;
       } else {
         const float bv = ops[0], dinv = ops[kTmOp];
-        const float rn = bv - q;
+        const float rn = bv - qn;
         e.r[g] = rn;
         e.d_out[g] = e.c2 * dinv * rn;
       }
-    }
+    };
+    if (col_in) emit(zz * sxy + gcol, ty * kTmX + tx, q + qd0, P2);
     P0 = P1; P1 = P2; P2 = P3; P3 = P4;
     X0 = X1; X1 = X2; X2 = X3; X3 = X4;
     Y0 = Y1; Y1 = Y2; Y2 = Y3; Y3 = Y4;
+    pm2 = pm1; pm1 = po; po = pp1; pp1 = pl2;
     qd0 = qd1;
     mw1 = mw2;
-    wr1 = wr2;
-    ok = __syncthreads_and(ok);  // plane z - 2 is free in every thread
+   }
+    ok = __syncthreads_and(ok);  // planes z - 2 .. z + ZU - 3 are free in every thread
     if (!ok) zfail = z;
-    if (ok && tid == 0 && z + kTmSlots - 2 <= tlast) issue(z + kTmSlots - 2);
+    if (ok && tid == 0) {
+#pragma unroll
+      for (int u = 0; u < ZU; ++u)
+        if (z + u < z1 && z + u + kTmSlots - 2 <= tlast) issue(z + u + kTmSlots - 2);
+    }
   }
   if (!ok) {
     // a copy never arrived: record it, give every copy this block issued a
@@ -335,6 +352,8 @@ struct TmCache {
   std::vector<Entry> entries;
   int nx = 0, ny = 0, nz = 0;
   bool enabled = false;  // the grid qualifies and the encoder is available
+  int segments = 0;      // z segments per column tile (0: ~16 planes each)
+  int zu = 0;            // output planes per barrier step (0: not chosen yet)
 };
 
 // Sets up the cache for an nx x ny x nz FP32 grid: TMA staging needs rows of a
@@ -342,6 +361,11 @@ struct TmCache {
 // kernel attributes are set here (outside any capture).  `allow` = false
 // keeps the staged-tile kernels of fd_apply.cuh.
 void tm_setup(TmCache &cache, int nx, int ny, int nz, bool allow);
+
+// Picks the planes-per-step variant of the kernel for this grid by timing
+// both on the handle's own vectors (p -> q, STORE epilogue, no data term);
+// LS_GB300_TMA_STEP=1|2 forces one.  Outside any stream capture.
+int tm_autotune(TmCache &cache, const CoefT<float> &c, const float *p, float *q, int *fault, cudaStream_t st);
 
 // q = N p with the epilogue through fd_tma_apply_kernel (plus the data-node
 // totals kernel when the grid has touched nodes; `qd` receives them).  With

@@ -1864,6 +1864,7 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
     const char *mode = getenv("LS_GB300_STAGED_APPLY");
     const bool allow = !(mode && strcmp(mode, "tiles") == 0);
     tm_setup(h->tm, (int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], allow);
+    if ((st = tm_autotune(h->tm, coef_as<float>(h->coef), h->p32, h->q32, &h->sc->fault, h->stream)) < 0) return fail(st);
   }
   cudaEventCreate(&h->ev0);
   cudaEventCreate(&h->ev1);

@@ -87,8 +87,10 @@ def test_cfg1_families_and_evaluation(cgolden):
     for nm in names:
         got = interp.constraints[nm].n_rows if nm in interp.constraints else interp.regularisation_families[nm][0]
         assert got == rows[nm], nm
-    # evaluation of the reference's solution on the 100^3 lattice sample
+    # evaluation of the reference's solution on the 100^3 lattice sample (the
+    # interpolator is marked solved, so that evaluate does not re-solve)
     interp.c = cgolden["cfg1_c_tight"]
+    interp.up_to_date = True
     q = _cfg1_points(cgolden)
     np.testing.assert_allclose(interp.evaluate_value(q), cgolden["cfg1_eval_value"], rtol=1e-12, atol=1e-12)
     np.testing.assert_allclose(interp.evaluate_gradient(q), cgolden["cfg1_eval_gradient"], rtol=1e-12, atol=1e-12)

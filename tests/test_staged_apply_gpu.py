@@ -31,7 +31,7 @@ def _data(rng, npts, nnrm):
     return val, nrm
 
 
-def _interp(cells, val, nrm, setup, tiles=False, directional=None):
+def _interp(cells, val, nrm, setup, tiles=False, directional=None, step=None):
     cells = np.asarray(cells)
     grid = L.StructuredGrid(origin=np.zeros(3), nsteps=cells, step_vector=1.0 / cells.astype(float))
     it = L.FiniteDifferenceInterpolator(grid)
@@ -41,27 +41,34 @@ def _interp(cells, val, nrm, setup, tiles=False, directional=None):
     if directional is not None:
         kw["regularisation"] = {"isotropic": kw.pop("regularisation", 0.1), "directional": directional}
     it.setup_interpolator(**kw)
-    old = os.environ.get("LS_GB300_STAGED_APPLY")
+    env = {"LS_GB300_STAGED_APPLY": "tiles" if tiles else None,
+           "LS_GB300_TMA_STEP": None if step is None else str(step)}
+    old = {k: os.environ.get(k) for k in env}
     try:
-        if tiles:
-            os.environ["LS_GB300_STAGED_APPLY"] = "tiles"
+        for k, v in env.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
         system = it._build_system()
     finally:
-        if old is None:
-            os.environ.pop("LS_GB300_STAGED_APPLY", None)
-        else:
-            os.environ["LS_GB300_STAGED_APPLY"] = old
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     return it, system
 
 
-@pytest.mark.parametrize("cells", [(71, 69, 65), (75, 68, 64)])
-def test_staged_apply_matches_explicit_operator(cells):
+@pytest.mark.parametrize("cells, step", [((71, 69, 65), 1), ((75, 68, 64), 2), ((71, 69, 62), 2)])
+def test_staged_apply_matches_explicit_operator(cells, step):
     """x extent a multiple of 4 (72 / 76 nodes), y / z not multiples of the
-    8-row tile; data rows near every face."""
+    8-row tile; data rows near every face; one and two planes per step (an odd
+    segment length for the two-plane variant)."""
     rng = np.random.default_rng(21)
     val, nrm = _data(rng, 3000, 600)
     setup = dict(cpw=1.0, npw=1.0, **KW)
-    it, system = _interp(cells, val, nrm, setup)
+    it, system = _interp(cells, val, nrm, setup, step=step)
     assert system.staged_apply and (cells[0] + 1) % 4 == 0
     grid = fdo.Grid(np.zeros(3), np.asarray(cells), 1.0 / np.asarray(cells, dtype=float))
     cs = fdo.assemble(grid, {"value": val, "normal": nrm}, fdo.resolve_weights(**setup))
@@ -95,8 +102,8 @@ def test_staged_apply_matches_tile_kernels():
     s_tile.close()
 
 
-@pytest.mark.parametrize("directional", [False, True])
-def test_multigrid_solve_with_staged_apply(directional):
+@pytest.mark.parametrize("directional, step", [(False, 1), (True, 2), (False, 2)])
+def test_multigrid_solve_with_staged_apply(directional, step):
     """Whole mixed multigrid solves (every level-0 epilogue through the TMA
     kernel) reach the same solution as with the tile kernels and as the FP64
     Jacobi solve, at 1e-8."""
@@ -113,7 +120,7 @@ def test_multigrid_solve_with_staged_apply(directional):
         terms = [L.DirectionalRegularisation(0.05, across, "fold regularisation 1")]
     sols = {}
     for mode in ("tiles", "tma", "fp64"):
-        it, system = _interp(cells, val, nrm, setup, tiles=(mode == "tiles"), directional=terms)
+        it, system = _interp(cells, val, nrm, setup, tiles=(mode == "tiles"), directional=terms, step=step)
         assert system.staged_apply == (mode != "tiles")
         if mode == "fp64":
             x, st = system.solve(rtol=1e-12, precision="fp64", preconditioner="jacobi", maxiter=400000)
@@ -130,7 +137,8 @@ def test_multigrid_solve_with_staged_apply(directional):
     assert abs(sols["tma"][1] - sols["tiles"][1]) <= max(2, sols["tiles"][1] // 20), {k: v[1] for k, v in sols.items()}
 
 
-def test_vcycle_with_staged_apply_matches_tile_kernels():
+@pytest.mark.parametrize("step", [1, 2])
+def test_vcycle_with_staged_apply_matches_tile_kernels(step):
     """One multigrid V-cycle (the CHEB and RESID epilogues of every level-0
     smoothing step) through the TMA kernel and through the tile kernels; the
     preconditioner stays symmetric and positive."""
@@ -140,7 +148,7 @@ def test_vcycle_with_staged_apply_matches_tile_kernels():
     rng = np.random.default_rng(24)
     val, nrm = _data(rng, 3000, 600)
     setup = dict(regularisation=0.1, cpw=1.0, npw=1.0)
-    _, s_tma = _interp(cells, val, nrm, setup)
+    _, s_tma = _interp(cells, val, nrm, setup, step=step)
     _, s_tile = _interp(cells, val, nrm, setup, tiles=True)
     assert s_tma.staged_apply and not s_tile.staged_apply
     r = torch.from_numpy(rng.normal(size=s_tma.n)).float()
