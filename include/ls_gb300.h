@@ -201,6 +201,20 @@ int ls_fd_set_rhs(ls_fd_handle *h, const double *d_rhs, void *stream);
  * with x = lambda, the gradient of the loss with respect to the rows'
  * right-hand sides b_r.  No counterpart in the reference. */
 int ls_fd_data_rows_apply(ls_fd_handle *h, const double *d_x, double *d_s, void *stream);
+/* One ADMM projection step over the data rows [row0, row0 + m), which hold
+ * the inequality rows q'_r with weight rho (replaces the update of
+ * loopsolver/admm_solver.py:380-404 admm_solve with
+ * admm_method.py:12-25 ADMM.admm_method_iterate_admm_array, for exact inner
+ * solves of the normal equations): qx = q'_r . x (x = d_x, the current
+ * solution), arg = qx + u, z = arg when lo <= arg <= hi, else the bound it
+ * passed (unchanged when arg is NaN), u = u + qx - z, and the row's
+ * right-hand side becomes z - u; the handle's A^T W b is then recomputed, so
+ * that the next ls_fd_solve minimises |A x - b|^2 + rho^2 |Q' x - (z - u)|^2.
+ * d_lo, d_hi, d_z, d_u: m FP64 each (z and u updated in place).  h_sums (5
+ * host doubles): sum (qx - z)^2, sum (z - z_prev)^2, sum qx^2, sum z^2,
+ * sum u^2 of this step.  Synchronises the handle's stream. */
+int ls_fd_admm_step(ls_fd_handle *h, int64_t row0, int64_t m, const double *d_lo, const double *d_hi, double *d_z,
+                    double *d_u, const double *d_x, double *h_sums, void *stream);
 /* diag(A^T W A + ridge^2 I): the squared column norms of the reference's
  * column scaling (DI:815-833) */
 int ls_fd_diagonal(ls_fd_handle *h, double *d_diag, void *stream);

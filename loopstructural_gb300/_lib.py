@@ -37,7 +37,7 @@ EXPORTS = (
     "ls_fd_point_rows", "ls_fd_pair_rows", "ls_fd_reg_shape", "ls_fd_reg_rows", "ls_fd_directional_weights",
     "ls_fd_create", "ls_fd_destroy", "ls_fd_dof", "ls_fd_apply", "ls_fd_apply_f32", "ls_fd_apply_noalloc", "ls_fd_rhs",
     "ls_fd_diagonal", "ls_fd_solve", "ls_fd_profile_iteration", "ls_fd_profile_mg", "ls_fd_eval_points", "ls_fd_eval_lattice",
-    "ls_fd_eval_adjoint", "ls_fd_set_rhs", "ls_fd_data_rows_apply", "ls_fd_device", "ls_fd_prepare", "ls_fd_solve_batched",
+    "ls_fd_eval_adjoint", "ls_fd_set_rhs", "ls_fd_data_rows_apply", "ls_fd_admm_step", "ls_fd_device", "ls_fd_prepare", "ls_fd_solve_batched",
     "ls_fd_mg_apply_level", "ls_fd_setup_profile", "ls_fd_staged_apply", "ls_fd_mg_vcycle", "ls_fd_eval_jets", "ls_fault_apply", "ls_tetra_gradient",
     "ls_p1_face_count", "ls_p1_face_rows", "ls_p1_face_rows_directional", "ls_p1_locate", "ls_p1_point_rows",
     "ls_p1_eval_points", "ls_iso_extract", "ls_iso_copy", "ls_iso_destroy",
@@ -159,6 +159,7 @@ _SIGS = {
     "ls_fd_solve_batched": (C.c_int, [C.POINTER(_P), C.POINTER(SolveOpts), C.POINTER(_P), C.POINTER(SolveStats),
                                       C.c_int64, C.c_int, C.POINTER(C.c_int)]),
     "ls_fd_data_rows_apply": (C.c_int, [_P, _P, _P, _P]),
+    "ls_fd_admm_step": (C.c_int, [_P, C.c_int64, C.c_int64, _P, _P, _P, _P, _P, C.POINTER(C.c_double), _P]),
     "ls_fd_eval_lattice": (C.c_int, [C.POINTER(Grid3), _P, C.POINTER(C.c_double * 3), C.POINTER(C.c_double * 3),
                                      C.POINTER(C.c_int64 * 3), _P, _P, _P]),
     "ls_p1_face_count": (C.c_int, [C.POINTER(Grid3), C.POINTER(C.c_int64)]),

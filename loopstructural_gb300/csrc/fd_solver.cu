@@ -34,6 +34,7 @@ namespace ls {
 namespace {
 
 constexpr int kBlock = 256;
+constexpr int kAuxDoubles = 8;
 
 // Device-resident CG scalars.  All reductions land here so that a whole batch
 // of iterations runs without host round trips.
@@ -116,6 +117,7 @@ struct ls_fd_handle {
   // grid's vectors, and the per-touched-node data totals it reads
   ls::TmCache tm;
   float *qd32 = nullptr;
+  double *aux = nullptr;                // kAuxDoubles of scratch (ADMM step sums)
   std::vector<int64_t> h_idc;           // host copy of the data rows (Galerkin coarsening)
   std::vector<double> h_a, h_w2;
   int h_width = 0;
@@ -293,6 +295,80 @@ __global__ void data_node_setup_kernel(int64_t ntouched, const int64_t *__restri
     const int64_t g = touched[t];
     diag[g] += dd;
     rhs[g] = rr;
+  }
+}
+
+// touched nodes: rhs = sum a w2 b (the right-hand side after the rows' b
+// changed; same summation order as data_node_setup_kernel)
+__global__ void data_node_rhs_kernel(int64_t ntouched, const int64_t *__restrict__ touched,
+                                     const int64_t *__restrict__ ptr, const int32_t *__restrict__ row,
+                                     const double *__restrict__ ia, const double *__restrict__ w2,
+                                     const double *__restrict__ b, double *__restrict__ rhs) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntouched;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    double rr = 0.0;
+    for (int64_t e = ptr[t]; e < ptr[t + 1]; ++e) rr += ia[e] * w2[row[e]] * b[row[e]];
+    rhs[touched[t]] = rr;
+  }
+}
+
+// ADMM projection over inequality rows (loopsolver/admm_method.py:12-25 and
+// the per-iteration update of loopsolver/admm_solver.py:380-404): for row r,
+// qx = a_r . x, arg = qx + u, z = arg inside [lo, hi], else the bound it
+// passed (z unchanged when arg is NaN), u += qx - z, and the row's new
+// right-hand side b = z - u.  Five sums per block, in this order:
+// (qx - z)^2, (z - z_prev)^2, qx^2, z^2, u^2.
+constexpr int kAdmmSums = 5;
+
+__global__ void __launch_bounds__(kBlock) admm_rows_kernel(int64_t m, int width, const int32_t *__restrict__ cols,
+                                                           const double *__restrict__ a, const double *__restrict__ x,
+                                                           const double *__restrict__ lo, const double *__restrict__ hi,
+                                                           double *__restrict__ z, double *__restrict__ u,
+                                                           double *__restrict__ b, double *__restrict__ partials) {
+  __shared__ double red[kBlock / 32];
+  double s[kAdmmSums] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < m; r += (int64_t)gridDim.x * blockDim.x) {
+    double qx = 0.0;
+    for (int k = 0; k < width; ++k) {
+      const int32_t c = cols[r * width + k];
+      if (c >= 0) qx += a[r * width + k] * x[c];
+    }
+    const double zo = z[r], uo = u[r], l = lo[r], h = hi[r];
+    const double arg = qx + uo;
+    double zn = zo;
+    if (arg >= l && arg <= h)
+      zn = arg;
+    else if (arg < l)
+      zn = l;
+    else if (arg > h)
+      zn = h;
+    const double un = (uo + qx) - zn;
+    z[r] = zn;
+    u[r] = un;
+    b[r] = zn - un;
+    s[0] += (qx - zn) * (qx - zn);
+    s[1] += (zn - zo) * (zn - zo);
+    s[2] += qx * qx;
+    s[3] += zn * zn;
+    s[4] += un * un;
+  }
+#pragma unroll
+  for (int k = 0; k < kAdmmSums; ++k) {
+    const double t = block_sum<kBlock, double>(s[k], red);
+    if (threadIdx.x == 0) partials[kAdmmSums * blockIdx.x + k] = t;
+  }
+}
+
+// fixed-order sum of the per-block partials of admm_rows_kernel (one block)
+__global__ void __launch_bounds__(kBlock) admm_sum_kernel(int nblocks, const double *__restrict__ partials,
+                                                          double *__restrict__ out) {
+  __shared__ double red[kBlock / 32];
+#pragma unroll
+  for (int k = 0; k < kAdmmSums; ++k) {
+    double v = 0.0;
+    for (int i = threadIdx.x; i < nblocks; i += kBlock) v += partials[kAdmmSums * i + k];
+    v = block_sum<kBlock, double>(v, red);
+    if (threadIdx.x == 0) out[k] = v;
   }
 }
 
@@ -1799,6 +1875,7 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
     if ((st = dev_alloc(&h->partials, 4 * nb)) < 0) return fail(st);
   }
   if ((st = dev_alloc(&h->tickets, T_COUNT)) < 0) return fail(st);
+  if ((st = dev_alloc(&h->aux, kAuxDoubles)) < 0) return fail(st);
   if ((st = dev_alloc(&h->sc, 1)) < 0) return fail(st);
   if (cudaMallocHost((void **)&h->sc_h, sizeof(CgScalars)) != cudaSuccess) {
     set_error("cudaMallocHost failed");
@@ -1883,7 +1960,8 @@ extern "C" int ls_fd_destroy(ls_fd_handle *h) {
   void *ptrs[] = {h->rhs, h->diag, h->dinv64, h->dinv32, h->x64, h->r64, h->p64, h->q64, h->s64, h->x32, h->r32,
                   h->p32, h->q32, h->s32, h->sc, h->partials, h->tickets, h->data.cols, h->data.a64, h->data.a32,
                   h->data.w2_64, h->data.w2_32, h->data.b, h->data.touched, h->data.inc_ptr, h->data.inc_row,
-                  h->data.inc_a64, h->data.inc_a32, h->data.mask, h->data.word_rank, h->dir64, h->dir32, h->qd32};
+                  h->data.inc_a64, h->data.inc_a32, h->data.mask, h->data.word_rank, h->dir64, h->dir32, h->qd32,
+                  h->aux};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->sc_h) cudaFreeHost(h->sc_h);
@@ -1928,6 +2006,33 @@ extern "C" int ls_fd_data_rows_apply(ls_fd_handle *h, const double *d_x, double 
     ++h->launches;
   }
   LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return LS_OK;
+}
+
+extern "C" int ls_fd_admm_step(ls_fd_handle *h, int64_t row0, int64_t m, const double *d_lo, const double *d_hi,
+                               double *d_z, double *d_u, const double *d_x, double *h_sums, void *stream) {
+  LS_ARG_CHECK(h && d_lo && d_hi && d_z && d_u && d_x && h_sums, "NULL argument");
+  const DataTerm &d = h->data;
+  LS_ARG_CHECK(row0 >= 0 && m >= 1 && row0 + m <= d.nrows, "rows [row0, row0 + m) outside the data rows");
+  LS_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+  cudaStream_t hs = h->stream;
+  // partials hold 4 * max(red_blocks, ...) doubles: kAdmmSums per block fit
+  const int nb = (int)std::max<int64_t>(1, std::min<int64_t>((m + kBlock - 1) / kBlock, h->red_blocks / 2));
+  admm_rows_kernel<<<nb, kBlock, 0, hs>>>(m, d.width, d.cols + row0 * d.width, d.a64 + row0 * d.width, d_x, d_lo,
+                                          d_hi, d_z, d_u, d.b + row0, h->partials);
+  admm_sum_kernel<<<1, kBlock, 0, hs>>>(nb, h->partials, h->aux);
+  h->launches += 2;
+  if (d.ntouched > 0) {
+    data_node_rhs_kernel<<<grid_for(h, d.ntouched), kBlock, 0, hs>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row,
+                                                                     d.inc_a64, d.w2_64, d.b, h->rhs);
+    ++h->launches;
+  }
+  norm2_kernel<<<grid_for(h, h->n), kBlock, 0, hs>>>(h->n, h->rhs, h->dinv64, h->sc, h->partials, h->tickets + T_MISC);
+  ++h->launches;
+  LS_CUDA_TRY(cudaGetLastError());
+  LS_CUDA_TRY(cudaMemcpyAsync(h_sums, h->aux, kAdmmSums * sizeof(double), cudaMemcpyDeviceToHost, hs));
+  LS_TRY(read_scalars(h));  // synchronises
+  h->rhs_norm2 = h->sc_h->scratch;
   return LS_OK;
 }
 

@@ -194,6 +194,16 @@ class FdSystem:
         _lib.check(self.lib.ls_fd_diagonal(self.handle, _lib.ptr(y), _lib.stream_ptr()))
         return y
 
+    def admm_step(self, row0: int, lo, hi, z, u, x):
+        """One ADMM projection over the data rows [row0, row0 + len(z)) (the
+        inequality rows; ls_fd_admm_step): updates z, u and the rows'
+        right-hand sides in place and returns the five sums
+        (|qx - z|^2, |z - z_prev|^2, |qx|^2, |z|^2, |u|^2)."""
+        out = (C.c_double * 5)()
+        _lib.check(self.lib.ls_fd_admm_step(self.handle, int(row0), int(z.shape[0]), _lib.ptr(lo), _lib.ptr(hi),
+                                            _lib.ptr(z), _lib.ptr(u), _lib.ptr(x), out, _lib.stream_ptr()))
+        return np.array(out[:], dtype=float)
+
     def solve(self, x=None, atol=0.0, rtol=1e-5, maxiter=None, precision="mixed", reliable_delta=0.1,
               check_every=64, preconditioner="mg", mg_degree=0):
         """Returns (x device tensor, stats dict)."""

@@ -16,7 +16,7 @@ from time import perf_counter
 
 import numpy as np
 
-from . import _lib, constraints, fd
+from . import _lib, admm, constraints, fd
 from . import regularisation as regcfg
 
 logger = logging.getLogger(__name__)
@@ -38,6 +38,19 @@ class ConstraintFamily:
     def numpy(self):
         return {"idc": self.idc.cpu().numpy(), "A": self.a.cpu().numpy(), "B": self.b.cpu().numpy(),
                 "w": self.w.cpu().numpy()}
+
+
+class InequalityFamily:
+    """One inequality family as the reference stores it
+    (DI:467-507 add_inequality_constraints_to_matrix): raw rows over columns
+    idc (m x k, device) with per-row bounds (m x 2: lower, upper)."""
+
+    def __init__(self, idc, a, bounds):
+        self.idc, self.a, self.bounds = idc, a, bounds
+
+    @property
+    def rows(self):
+        return int(self.idc.shape[0])
 
 
 def _row_weights(w, nrows):
@@ -105,6 +118,8 @@ class _DiscreteInterpolatorBase:
         self.interpolation_weights = {}
         self.latest_solve_timing = {}
         self.constraints: dict[str, ConstraintFamily] = {}
+        self.ineq_constraints: dict[str, InequalityFamily] = {}
+        self.solver_history = None
         self.family_order: list[str] = []
         self.up_to_date = False
         self._c = np.zeros(self.support.n_nodes)
@@ -167,6 +182,28 @@ class _DiscreteInterpolatorBase:
         except constraints.ValidationError as e:
             raise constraints.ValidationError(f"Failed to set interface constraints: {e}") from e
         self.up_to_date = False
+
+    def set_value_inequality_constraints(self, points):
+        """[x, y, z, lower, upper, (w)] (GI:464-493); lower < upper on every row."""
+        try:
+            self.data["inequality"] = self._project(constraints.inequality_array(points)).copy()
+        except constraints.ValidationError as e:
+            raise constraints.ValidationError(f"Failed to set inequality value constraints: {e}") from e
+        self.up_to_date = False
+
+    def set_inequality_pairs_constraints(self, points):
+        """[x, y, z, pair_id, (w)] (GI:495-522)."""
+        try:
+            self.data["inequality_pairs"] = self._project(constraints.inequality_pair_array(points)).copy()
+        except constraints.ValidationError as e:
+            raise constraints.ValidationError(f"Failed to set inequality pairs constraints: {e}") from e
+        self.up_to_date = False
+
+    def get_inequality_value_constraints(self):
+        return self.data["inequality"]
+
+    def get_inequality_pairs_constraints(self):
+        return self.data["inequality_pairs"]
 
     def get_value_constraints(self):
         return self.data["value"]
@@ -263,9 +300,54 @@ class _DiscreteInterpolatorBase:
                          torch.from_numpy(B).to(dev), torch.from_numpy(w).to(dev))
         self.up_to_date = False
 
+    def add_inequality_constraints_to_matrix(self, A, bounds, idc, name="undefined"):
+        """Inequality rows lower <= A c <= upper over columns idc
+        (DI:467-507); bounds is n x 2 (lower, upper) or n x 3 (the third
+        column is not used).  Raises ValueError on the reference's shape and
+        range checks; a family of the same name is replaced."""
+        import torch
+
+        A = np.asarray(A, dtype=float)
+        idc = np.asarray(idc, dtype=int)
+        bounds = np.asarray(bounds, dtype=float)
+        if A.ndim != 2 or idc.ndim != 2:
+            raise ValueError("A and idc must be 2D arrays")
+        if A.shape != idc.shape:
+            raise ValueError("A and idc must have the same shape")
+        if bounds.ndim != 2 or bounds.shape[0] != A.shape[0] or bounds.shape[1] not in (2, 3):
+            raise ValueError("bounds must have shape (n_rows, 2) or (n_rows, 3)")
+        if np.any(idc < 0) or np.any(idc >= self.dof):
+            raise ValueError("Inequality constraint indices are out of range")
+        dev = _lib.device()
+        self._add_inequality_family(name, torch.from_numpy(idc.astype(np.int64)).to(dev), torch.from_numpy(A).to(dev),
+                                    torch.from_numpy(np.ascontiguousarray(bounds[:, :2])).to(dev))
+
+    def _add_inequality_family(self, name, idc, a, bounds):
+        self.ineq_constraints[name] = InequalityFamily(idc.contiguous(), a.contiguous(), bounds.contiguous())
+        self.up_to_date = False
+
+    def build_inequality_matrix(self):
+        """(Q, bounds) of every inequality family, stacked in insertion order
+        (DI:874-884): Q a CSR matrix over the dof, bounds n x 2."""
+        from scipy import sparse
+
+        mats, bounds = [], []
+        for f in self.ineq_constraints.values():
+            idc, a = f.idc.cpu().numpy(), f.a.cpu().numpy()
+            n, k = idc.shape
+            keep = idc.reshape(-1) >= 0
+            rows = np.repeat(np.arange(n), k)[keep]
+            mats.append(sparse.coo_matrix((a.reshape(-1)[keep], (rows, idc.reshape(-1)[keep])),
+                                          shape=(n, self.dof)).tocsr())
+            bounds.append(f.bounds.cpu().numpy())
+        if not mats:
+            return sparse.csr_matrix((0, self.dof), dtype=float), np.zeros((0, 3))
+        return sparse.vstack(mats).tocsr(), np.vstack(bounds)
+
     def clear_constraints(self):
         """Drops every constraint family (DI:297-304)."""
         self.constraints = {}
+        self.ineq_constraints = {}
         if hasattr(self, "regularisation_families"):
             self.regularisation_families = {}
         if hasattr(self, "_reset_directional"):
@@ -410,7 +492,7 @@ class _DiscreteInterpolatorBase:
             solver = "cg"
         solver = "cg" if solver is None else solver
         if solver == "admm":
-            raise NotImplementedError("the ADMM inequality solver is not part of the GPU path")
+            return solver, admm.admm_options(solver_kwargs)
         kw = dict(solver_kwargs or {})
         kw.pop("backend", None)
         if solver == "lsmr":  # same least-squares solution; lsmr's btol maps to the relative tolerance
@@ -453,6 +535,9 @@ class _DiscreteInterpolatorBase:
         self._c_dev = None
         solver, opts = self._solver_options(solver, tol, solver_kwargs)
         timing = {"solver": solver, "backend": "gb300"}
+        self.solver_history = None
+        if solver == "admm":
+            return self._solve_admm(opts, timing, solve_started)
         t0 = perf_counter()
         self._release_system()
         self._system = self._build_system()
@@ -485,6 +570,25 @@ class _DiscreteInterpolatorBase:
         timing["up_to_date"] = True
         self.latest_solve_timing = timing
         return True
+
+    def _solve_admm(self, opts, timing, solve_started):
+        """solver='admm' (DI:1171-1219, loopsolver/admm_solver.py): see
+        admm.solve_admm."""
+        import torch
+
+        o, inner = opts
+        self._release_system()
+        t0 = perf_counter()
+        ok = admm.solve_admm(self, o, inner, timing)
+        torch.cuda.synchronize()
+        timing["solve_seconds"] = perf_counter() - t0
+        timing["matrix_rows"] = int(self._matrix_rows())
+        timing["matrix_cols"] = int(self.dof)
+        self.up_to_date = bool(ok)
+        timing["total_seconds"] = perf_counter() - solve_started
+        timing["up_to_date"] = bool(ok)
+        self.latest_solve_timing = timing
+        return bool(ok)
 
     # -- evaluation (GI:723-742, DI:1342-1379) ---------------------------------
     def evaluate_value(self, locations):
@@ -573,6 +677,11 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
         self._add_point_rows(_lib.ROWS_VALUE, self.get_value_constraints(), w["cpw"], ["value"])
         self._add_point_rows(_lib.ROWS_TANGENT, self.get_tangent_constraints(), w["tpw"], ["gradient orthogonal"])
         self._add_interface_rows(w["ipw"])
+        self.add_value_inequality_constraints()  # FD:214-219
+        self.add_inequality_pairs_constraints(pairs=kwargs.get("inequality_pairs", None),
+                                              upper_bound=kwargs.get("inequality_pair_upper_bound",
+                                                                     np.finfo(float).eps),
+                                              lower_bound=kwargs.get("inequality_pair_lower_bound", -np.inf))
         self._add_regularisation_families(interior=True, borders=False)
         self.add_directional_regularisation(cfg.directional)  # FD:222, between interior and border families
         self._add_regularisation_families(interior=False, borders=True)
@@ -583,6 +692,8 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
             report[name] = rows
         for name, (rows, _t, _f) in self.directional_families.items():
             report[name] = rows
+        for name, f in self.ineq_constraints.items():
+            report[name] = f.rows
         return report
 
     # -- directional regularisation (FD:1207-1348) ----------------------------
@@ -744,11 +855,107 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
             out[k] = fam[k + "_lower"][1] if (k + "_lower") in fam else 0.0
         return out
 
-    def _build_system(self):
-        rows = [(f.idc, f.a, f.b, f.w) for f in self.constraints.values()]
+    def _data_rows(self):
+        return [(f.idc, f.a, f.b, f.w) for f in self.constraints.values()]
+
+    def _make_system(self, rows):
         ridge = self.ridge_factor if self.add_ridge_regulatisation else 0.0
         omega = self._dir_omega if self.directional_families else None
         return fd.FdSystem(self.support, self._reg_weights(), rows, ridge, directional=omega)
+
+    def _build_system(self):
+        return self._make_system(self._data_rows())
+
+    # -- inequality rows (DI:509-630) -----------------------------------------
+    def _trilinear_rows(self, points):
+        """(idc, raw trilinear weights) of the points inside the grid, in
+        order (device), and the host mask of those points."""
+        import torch
+
+        inside = np.asarray(self.support.inside(points[:, :3]), dtype=bool)
+        if not inside.any():
+            return None, None, inside
+        pts = np.ascontiguousarray(np.column_stack([points[:, :3], np.zeros(points.shape[0]),
+                                                    np.ones(points.shape[0])]))
+        n, fams, _nan = fd.point_rows(self.support, _lib.ROWS_VALUE, pts, 1.0)
+        if n != int(inside.sum()):
+            raise RuntimeError("inside test of the row kernel and the support disagree")
+        idc, a = fams[0][0], fams[0][1]
+        # the rows come normalised (a / |a|); the trilinear weights sum to 1
+        a = a / a.sum(dim=1, keepdim=True)
+        return idc, a, inside
+
+    def add_value_inequality_constraints(self, w=1.0):
+        """lower <= f(x) <= upper at the inequality points inside the grid
+        (DI:509-518); w is not used, as in the reference."""
+        import torch
+
+        points = self.get_inequality_value_constraints()
+        if points.shape[0] == 0:
+            return
+        idc, a, inside = self._trilinear_rows(points)
+        if idc is None:
+            return
+        bounds = torch.from_numpy(np.ascontiguousarray(points[inside, 3:5])).to(_lib.device())
+        self._add_inequality_family("inequality_value", idc, a, bounds)
+
+    def add_inequality_pairs_constraints(self, w=1.0, upper_bound=1.0, lower_bound=-np.inf, pairs=None):
+        """lower_bound <= f(p) - f(q) <= upper_bound for every point p of the
+        group pair[0] and q of pair[1] (inside points only); without
+        ``pairs``, every pair of distinct group ids (i < j) (DI:520-593)."""
+        import torch
+
+        points = self.get_inequality_pairs_constraints()
+        if points.shape[0] == 0:
+            return
+        ids = points[:, 3]
+        if not pairs:
+            u = np.unique(ids)
+            pairs = [(u[i], u[j]) for i in range(len(u)) for j in range(i + 1, len(u))]
+        dev = _lib.device()
+        for pair in pairs:
+            upper = points[ids == pair[0]]
+            lower = points[ids == pair[1]]
+            in_u = np.asarray(self.support.inside(upper[:, :3]), dtype=bool)
+            in_l = np.asarray(self.support.inside(lower[:, :3]), dtype=bool)
+            if (~in_u).sum() > 0:
+                logger.warning(f"Upper points not in mesh {upper[~in_u]}")
+            if (~in_l).sum() > 0:
+                logger.warning(f"Lower points not in mesh {lower[~in_l]}")
+            nu, nl = int(in_u.sum()), int(in_l.sum())
+            if nu == 0 or nl == 0:
+                continue
+            both = np.ascontiguousarray(np.vstack([upper[in_u, :3], lower[in_l, :3]]))
+            # rows ordered as the reference's meshgrid: upper index fastest
+            iu, il = np.meshgrid(np.arange(nu), np.arange(nl))
+            pr = np.ascontiguousarray(np.column_stack([iu.ravel(), nu + il.ravel()]).astype(np.int64))
+            idc, a, _b, _w = fd.pair_rows(self.support, both, pr, 1.0)
+            a = a / a[:, :8].sum(dim=1, keepdim=True)
+            bounds = torch.empty((pr.shape[0], 2), dtype=torch.float64, device=dev)
+            bounds[:, 0] = float(lower_bound)
+            bounds[:, 1] = float(upper_bound)
+            self._add_inequality_family(f"inequality_pairs_{pair[0]}_{pair[1]}", idc, a, bounds)
+
+    def add_inequality_feature(self, feature, lower=True, mask=None):
+        """f >= feature (lower) or f <= feature at the grid nodes where the
+        feature is not NaN and the mask holds (DI:595-632)."""
+        import torch
+
+        value = np.asarray(feature(self.support.nodes), dtype=float)
+        if mask is None:
+            mask = np.ones(value.shape[0], dtype=bool)
+        lo = np.full(value.shape[0], -np.inf)
+        hi = np.full(value.shape[0], np.inf)
+        mask = np.logical_and(mask, ~np.isnan(value))
+        if lower:
+            lo[mask] = value[mask]
+        else:
+            hi[mask] = value[mask]
+        dev = _lib.device()
+        n = self.dof
+        self._add_inequality_family("inequality_feature", torch.arange(n, dtype=torch.int64, device=dev)[:, None],
+                                    torch.ones((n, 1), dtype=torch.float64, device=dev),
+                                    torch.from_numpy(np.column_stack([lo, hi])).to(dev))
 
     def _matrix_rows(self):
         return (sum(f.n_rows for f in self.constraints.values()) + sum(r for r, _ in self.regularisation_families.values())

@@ -35,6 +35,32 @@ def cgolden():
     return np.load(os.path.join(ROOT, "tests", "golden", "config_golden.npz"), allow_pickle=False)
 
 
+@pytest.fixture(scope="session")
+def agolden():
+    """ADMM fixtures (make_golden.py --admm)."""
+    import numpy as np
+
+    return np.load(os.path.join(ROOT, "tests", "golden", "admm_golden.npz"), allow_pickle=False)
+
+
+ADMM_CASES = ("admm_const", "admm_sched", "admm_adapt", "admm_loose")
+
+
+def admm_kwargs(g, name):
+    """The solver kwargs an ADMM fixture case was recorded with (besides the
+    exact inner solver); x0 as the name of its start vector."""
+    import ast
+
+    out = {}
+    for k, v in zip(g[f"{name}_kwargs_keys"], g[f"{name}_kwargs_vals"]):
+        k, v = str(k), str(v)
+        try:
+            out[k] = ast.literal_eval(v)
+        except (ValueError, SyntaxError):
+            out[k] = v
+    return out
+
+
 class AffineBox:
     """A stand-in for the reference's BoundingBox built from its recorded
     affine maps: project / project_vectors / reproject / reproject_vectors."""

@@ -6,6 +6,7 @@ Run in a container where the reference source tree is available:
     python tests/golden/make_golden.py /path/to/LoopStructural --directional
     python tests/golden/make_golden.py /path/to/LoopStructural --configs
     python tests/golden/make_golden.py /path/to/LoopStructural --faults
+    python tests/golden/make_golden.py /path/to/LoopStructural --admm
 
 It imports the reference's ``loop_interpolation`` / ``loop_common`` packages
 (``pyvista`` and ``yaml`` are stubbed: they are only used for VTK/YAML export)
@@ -732,6 +733,112 @@ def main_faults(root):
     print("wrote", path, sum(v.nbytes for v in out.values()), "bytes;", str(out["faulted_gradient_error"]))
 
 
+def _exact_lsq(matrix, rhs, x0=None, **_kw):
+    """Exact inner least-squares solve for the reference's ADMM (a callable
+    ``linsys_solver``): the normal equations by sparse LU."""
+    from scipy.sparse.linalg import splu
+
+    m = matrix.tocsr()
+    return splu((m.T @ m).tocsc()).solve(np.asarray(m.T @ rhs).reshape(-1))
+
+
+ADMM_CASES = {
+    # name: (cells, seed, solver kwargs besides linsys_solver, feature bound, bound spread)
+    "admm_const": ((10, 9, 12), 11, dict(admm_weight=1.0, nmajor=80), None, 1.0),
+    "admm_sched": ((9, 8, 10), 12, dict(admm_weight=0.05, admm_weight_final=2.0, nmajor=25,
+                                         admm_weight_schedule="geometric"), None, 1.0),
+    "admm_adapt": ((8, 9, 10), 13, dict(admm_weight=0.1, adaptive_rho=True, nmajor=60, min_iterations=3),
+                   0.25, 1.0),
+    # loose bounds and a start from x0: stops on the primal/dual test
+    "admm_loose": ((9, 9, 9), 14, dict(admm_weight=0.5, nmajor=200, x0="nodes_z"), None, 20.0),
+}
+
+ADMM_X0 = {"nodes_z": lambda support: support.nodes[:, 2].copy()}
+
+
+def admm_case(li, StructuredGrid, name, out):
+    """Value + normal constraints with value inequalities and inequality pairs
+    that the unconstrained field violates; ``solve_system('admm')`` with an
+    exact inner solver; optionally a lower-bound inequality feature."""
+    cells, seed, kwargs, feature, spread = ADMM_CASES[name]
+    rng = np.random.default_rng(seed)
+    grid = StructuredGrid(origin=np.zeros(3), nsteps=np.array(cells), step_vector=1.0 / np.array(cells, dtype=float))
+    interp = li.FiniteDifferenceInterpolator(grid)
+    vp = rng.uniform(0.05, 0.95, size=(30, 3))
+    val = np.column_stack([vp, _field(vp), np.ones(30)])
+    npnt = rng.uniform(0.05, 0.95, size=(8, 3))
+    g = _grad(npnt)
+    g /= np.linalg.norm(g, axis=1)[:, None]
+    nrm = np.column_stack([npnt, g, np.ones(8)])
+    ip = rng.uniform(0.1, 0.9, size=(12, 3))
+    f0 = _field(ip)
+    lo = f0 + rng.uniform(0.02, 0.1, 12)  # above the unconstrained field: active
+    hi = lo + rng.uniform(0.05, 0.2, 12)
+    lo[8:] = -10.0  # upper-bound-only rows below the field: active from above
+    hi[8:] = f0[8:] - 0.05
+    if spread > 1.0:  # wide bounds around the field: inactive at the solution
+        lo, hi = f0 - spread, f0 + spread
+    ineq = np.column_stack([ip, lo, hi, np.ones(12)])
+    ineq = np.vstack([ineq, [[1.2, 0.5, 0.5, 0.0, 1.0, 1.0]]])  # outside: dropped
+    pp = np.vstack([rng.uniform(0.1, 0.9, size=(5, 3)), rng.uniform(0.1, 0.9, size=(4, 3))])
+    pp[:5, 2] = rng.uniform(0.6, 0.9, 5)  # group 0 above group 1: f(0) <= f(1) is violated
+    pp[5:, 2] = rng.uniform(0.1, 0.4, 4)
+    if spread > 1.0:
+        pp[:, 2] = pp[::-1, 2]  # group 0 below group 1: satisfied
+    pairs = np.column_stack([pp, np.r_[np.zeros(5), np.ones(4)], np.ones(9)])
+    interp.set_value_constraints(val)
+    interp.set_normal_constraints(nrm)
+    interp.set_value_inequality_constraints(ineq)
+    interp.set_inequality_pairs_constraints(pairs)
+    setup = dict(regularisation=0.1, cpw=1.0, npw=1.0)
+    interp.setup_interpolator(**setup)
+    if feature is not None:
+        interp.add_inequality_feature(lambda p: p[:, 2] - feature, lower=True,
+                                      mask=grid.nodes[:, 0] > 0.5)
+    Q, bounds = interp.build_inequality_matrix()
+    Q = Q.tocoo()
+    out[f"{name}_cells"] = np.array(cells)
+    out[f"{name}_value"] = val
+    out[f"{name}_normal"] = nrm
+    out[f"{name}_ineq"] = ineq
+    out[f"{name}_pairs"] = pairs
+    out[f"{name}_feature"] = np.array([np.nan if feature is None else feature])
+    out[f"{name}_Q_row"] = Q.row.astype(np.int64)
+    out[f"{name}_Q_col"] = Q.col.astype(np.int64)
+    out[f"{name}_Q_val"] = Q.data
+    out[f"{name}_bounds"] = np.asarray(bounds, dtype=float)
+    out[f"{name}_ineq_names"] = np.array(list(interp.ineq_constraints.keys()))
+    out[f"{name}_kwargs_keys"] = np.array(list(kwargs.keys()))
+    out[f"{name}_kwargs_vals"] = np.array([str(v) for v in kwargs.values()])
+    run = dict(kwargs, linsys_solver=_exact_lsq, return_history=True)
+    if "x0" in run:
+        run["x0"] = ADMM_X0[run["x0"]]
+    ok = interp.solve_system("admm", solver_kwargs=run)
+    assert ok
+    hist = interp.solver_history
+    out[f"{name}_c"] = np.array(interp.c)
+    out[f"{name}_iterations"] = np.array(len(hist))
+    for k in ("primal_norm", "dual_norm", "eps_pri", "eps_dual", "rho"):
+        out[f"{name}_hist_{k}"] = np.array([h[k] for h in hist], dtype=float)
+    A, b = interp.build_matrix()
+    A = A.tocsr()
+    from scipy import sparse
+    from scipy.sparse.linalg import spsolve
+
+    N = (A.T @ A).tocsc() + sparse.eye(A.shape[1], format="csc") * (interp.ridge_factor ** 2)
+    out[f"{name}_c_unconstrained"] = spsolve(N, A.T @ b)
+
+
+def main_admm(root):
+    li, StructuredGrid, _TetMesh = _import_reference(root)
+    out = {}
+    for name in ADMM_CASES:
+        admm_case(li, StructuredGrid, name, out)
+    path = os.path.join(HERE, "admm_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")
+
+
 def main_directional(root):
     li, StructuredGrid, TetMesh = _import_reference(root)
     out = {}
@@ -772,5 +879,7 @@ if __name__ == "__main__":
         main_configs(root)
     elif "--faults" in sys.argv:
         main_faults(root)
+    elif "--admm" in sys.argv:
+        main_admm(root)
     else:
         main(root)

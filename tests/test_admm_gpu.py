@@ -1,0 +1,109 @@
+"""GPU ADMM (``solve_system('admm')``) through the interpolator API against
+the fixtures recorded from the reference with an exact inner solver
+(make_golden.py --admm): the inequality rows the GPU assembles, the solution,
+and the primal/dual history.  The GPU inner solves stop at a relative
+residual of 1e-11 (FP64 CG), so the iterates follow the exact ones to about
+1e-7 of the field's range after 200 major iterations.  At 64^3 nodes, a
+size-independent property: after the iteration stops on the primal/dual
+test, every inequality row holds its bounds to the stopping tolerance."""
+import logging
+
+import numpy as np
+import pytest
+from scipy import sparse
+
+from conftest import ADMM_CASES, admm_kwargs
+
+torch = pytest.importorskip("torch")
+
+import loopstructural_gb300 as L  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+INNER = dict(rtol=1e-11, precision="fp64")
+
+
+def _interp(g, name):
+    cells = g[f"{name}_cells"]
+    grid = L.StructuredGrid(origin=np.zeros(3), nsteps=cells, step_vector=1.0 / cells.astype(float))
+    it = L.FiniteDifferenceInterpolator(grid)
+    it.set_value_constraints(g[f"{name}_value"])
+    it.set_normal_constraints(g[f"{name}_normal"])
+    it.set_value_inequality_constraints(g[f"{name}_ineq"])
+    it.set_inequality_pairs_constraints(g[f"{name}_pairs"])
+    it.setup_interpolator(regularisation=0.1, cpw=1.0, npw=1.0)
+    feat = float(g[f"{name}_feature"][0])
+    if not np.isnan(feat):
+        it.add_inequality_feature(lambda p: p[:, 2] - feat, lower=True, mask=grid.nodes[:, 0] > 0.5)
+    return grid, it
+
+
+@pytest.mark.parametrize("name", ADMM_CASES)
+def test_inequality_rows_match_reference(agolden, name):
+    grid, it = _interp(agolden, name)
+    assert list(it.ineq_constraints) == [str(s) for s in agolden[f"{name}_ineq_names"]]
+    Q, bounds = it.build_inequality_matrix()
+    ref = sparse.coo_matrix((agolden[f"{name}_Q_val"], (agolden[f"{name}_Q_row"], agolden[f"{name}_Q_col"])),
+                            shape=Q.shape).tocsr()
+    assert abs(Q - ref).max() <= 1e-15
+    np.testing.assert_array_equal(bounds, agolden[f"{name}_bounds"])
+
+
+@pytest.mark.parametrize("name", ADMM_CASES)
+def test_admm_matches_reference(agolden, name):
+    grid, it = _interp(agolden, name)
+    kw = admm_kwargs(agolden, name)
+    if kw.get("x0") == "nodes_z":
+        kw["x0"] = lambda support: support.nodes[:, 2].copy()
+    assert it.solve_system("admm", solver_kwargs=dict(kw, return_history=True, **INNER))
+    hist = it.solver_history
+    t = it.get_last_solve_timing()
+    assert t["solver"] == "admm" and t["admm_iterations"] == len(hist)
+    assert len(hist) == int(agolden[f"{name}_iterations"])
+    ref = agolden[f"{name}_c"]
+    scale = np.abs(ref).max()
+    np.testing.assert_allclose(it.c, ref, rtol=0, atol=1e-7 * scale)
+    for k in ("primal_norm", "dual_norm", "eps_pri", "eps_dual", "rho"):
+        got = np.array([h[k] for h in hist])
+        exp = agolden[f"{name}_hist_{k}"]
+        np.testing.assert_allclose(got, exp, rtol=1e-5, atol=1e-7 * np.abs(exp).max(), err_msg=k)
+    # evaluation reads the ADMM solution, no re-solve
+    v = it.evaluate_value(agolden[f"{name}_value"][:, :3])
+    assert np.all(np.isfinite(v))
+
+
+def test_admm_without_inequalities_logs_and_returns_false(agolden, caplog):
+    cells = agolden["admm_const_cells"]
+    grid = L.StructuredGrid(origin=np.zeros(3), nsteps=cells, step_vector=1.0 / cells.astype(float))
+    it = L.FiniteDifferenceInterpolator(grid)
+    it.set_value_constraints(agolden["admm_const_value"])
+    it.setup_interpolator(regularisation=0.1)
+    with caplog.at_level(logging.ERROR):
+        assert it.solve_system("admm") is False
+    assert "ADMM solver failed" in caplog.text
+    assert it.up_to_date is False
+
+
+def test_admm_bounds_hold_at_64():
+    """64^3 nodes: a dome-shaped value set capped by upper bounds at 400
+    points and ordered by 2 x 60 inequality pairs; the stopped iterate's
+    inequality rows (in the reference's scaled variable) sit inside their
+    bounds to the primal tolerance."""
+    rng = np.random.default_rng(3)
+    n = 63
+    grid = L.StructuredGrid(origin=np.zeros(3), nsteps=np.array([n, n, n]), step_vector=np.full(3, 1.0 / n))
+    it = L.FiniteDifferenceInterpolator(grid)
+    vp = rng.uniform(0.05, 0.95, size=(2000, 3))
+    it.set_value_constraints(np.column_stack([vp, vp[:, 2] + 0.2 * np.exp(-8 * ((vp[:, 0] - 0.5) ** 2)),
+                                              np.ones(2000)]))
+    ip = rng.uniform(0.1, 0.9, size=(400, 3))
+    it.set_value_inequality_constraints(np.column_stack([ip, ip[:, 2] - 5.0, ip[:, 2] + 0.05]))
+    pp = rng.uniform(0.1, 0.9, size=(120, 3))
+    it.set_inequality_pairs_constraints(np.column_stack([pp, (pp[:, 2] < 0.5).astype(float)]))
+    it.setup_interpolator(regularisation=0.1, cpw=1.0)
+    ok = it.solve_system("admm", solver_kwargs=dict(admm_weight=1.0, nmajor=400, return_history=True,
+                                                    rtol=1e-10))
+    assert ok
+    h = it.solver_history[-1]
+    assert len(it.solver_history) < 400, "did not stop on the primal/dual test"
+    assert h["primal_norm"] <= h["eps_pri"] and h["dual_norm"] <= h["eps_dual"]

@@ -85,5 +85,5 @@ def test_solver_option_mapping():
     assert s == "cg"
     s, o = interp._solver_options("lsmr", 1e-8, None)
     assert s == "lsmr" and o["rtol"] == 1e-8
-    with pytest.raises(NotImplementedError):
-        interp._solver_options("admm", None, None)
+    s, (o, inner) = interp._solver_options("admm", None, {"admm_weight": 0.2, "nmajor": 7})
+    assert s == "admm" and o["rho"] == 0.2 and o["nmajor"] == 7 and inner["preconditioner"] == "mg"
