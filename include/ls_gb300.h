@@ -311,7 +311,7 @@ int ls_fd_profile_iteration(ls_fd_handle *h, int precision, int reps, ls_fd_prof
  * epilogue, 4 restriction to level l+1, 5 prolongation from level l+1,
  * 6 data rows (row form), 7 the coarsest dense solve (last level only),
  * 8 / 9 the Chebyshev apply's kernels alone: on a finest level run by the
- * TMA-staged kernel, that kernel / the data-totals kernel before it; on levels
+ * TMA-staged kernel, that kernel / the data term after it (rows + fix-up); on levels
  * split into a staged interior and a boundary kernel, those two (0 otherwise).
  * Returns 0 with *levels = 0 when the grid does not coarsen.  The solver
  * vectors are overwritten.  No counterpart in the reference. */

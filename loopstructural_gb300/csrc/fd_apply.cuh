@@ -161,16 +161,17 @@ __device__ __forceinline__ T ind_b(int a, int n) { return (T)((a == 1) + (a == n
 // planes z-2 .. z+2, in-plane halo 2).  Branch-free: every row centre's weight
 // is a product of per-axis factors, so the boundary shell costs the same as
 // the interior and needs no global loads.
-// Template flags BY / BZ = false declare the node deep along y / z (index in
-// [3, n-4]: every row centre around it interior, none on a border layer), so
-// that those factors are compile-time constants; the result is the same.
-template <typename T, typename PR, bool BY = true, bool BZ = true>
+// Template flags BY / BZ / BX = false declare the node deep along y / z / x
+// (index in [3, n-4]: every row centre around it interior, none on a border
+// layer), so that those factors are compile-time constants; the result is the
+// same.
+template <typename T, typename PR, bool BY = true, bool BZ = true, bool BX = true>
 __device__ __forceinline__ T shell_node(const CoefT<T> &c, const PR &pr, int i, int j, int k) {
   T ix[3], bx[3], iy[3], by[3], iz[3], bz[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    ix[d] = ind_i<T>(i + d - 1, c.nx);
-    bx[d] = ind_b<T>(i + d - 1, c.nx);
+    ix[d] = BX ? ind_i<T>(i + d - 1, c.nx) : (T)1;
+    bx[d] = BX ? ind_b<T>(i + d - 1, c.nx) : (T)0;
     iy[d] = BY ? ind_i<T>(j + d - 1, c.ny) : (T)1;
     by[d] = BY ? ind_b<T>(j + d - 1, c.ny) : (T)0;
     iz[d] = BZ ? ind_i<T>(k + d - 1, c.nz) : (T)1;

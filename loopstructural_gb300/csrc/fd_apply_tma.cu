@@ -88,11 +88,9 @@ void tm_setup(TmCache &cache, int nx, int ny, int nz, bool allow) {
 }
 
 template <int EPI>
-int tm_launch(TmCache &cache, const CoefT<float> &c, const float *p, DataView<float> dv, const EpiArgs<float> &e,
-              const int *done, int64_t ntouched, const int64_t *inc_ptr, const int32_t *inc_row, const float *inc_a,
-              int width, const int32_t *cols, const float *a, const float *w2, float *qd, double *partials,
-              unsigned int *ticket, double *dot, double *dot_clear, int *fault, int max_blocks, cudaStream_t st,
-              int parts) {
+int tm_launch(TmCache &cache, const CoefT<float> &c, const float *p, const TmData &d, const EpiArgs<float> &e,
+              const int *done, double *partials, unsigned int *ticket, double *dot, double *dot_clear, int *fault,
+              int max_blocks, cudaStream_t st, int parts) {
   if (!cache.enabled || c.nx != cache.nx || c.ny != cache.ny || c.nz != cache.nz) return 0;
   TmMaps maps;
   const CUtensorMap *mp = lookup(cache, p, 0);
@@ -125,23 +123,25 @@ int tm_launch(TmCache &cache, const CoefT<float> &c, const float *p, DataView<fl
   nseg = (c.nz + zlen - 1) / zlen;
   if (ntiles > 0x7fffffff || (dot != nullptr && ntiles * nseg > max_blocks)) return 0;
   int launched = 0;
-  if (dv.enabled) {
-    if (parts & TM_TOTALS) {
-      data_node_totals_kernel<float><<<stream_grid(ntouched, 256), 256, 0, st>>>(ntouched, inc_ptr, inc_row, inc_a,
-                                                                                 width, cols, a, w2, p, qd, done);
-      ++launched;
-    }
-    dv.qd = qd;
-  }
   if (parts & TM_APPLY) {
     const dim3 grid((unsigned)ntiles, (unsigned)nseg);
     if (cache.zu == 2)
-      fd_tma_apply_kernel<EPI, 2><<<grid, kTmThreads, tm_smem_bytes<EPI>(), st>>>(
-          maps, c, dv, e, done, ntx, zlen, partials, ticket, dot, dot_clear, fault);
+      fd_tma_apply_kernel<EPI, 2><<<grid, kTmThreads, tm_smem_bytes<EPI>(), st>>>(maps, c, e, done, ntx, zlen,
+                                                                                   partials, ticket, dot, dot_clear,
+                                                                                   fault);
     else
-      fd_tma_apply_kernel<EPI, 1><<<grid, kTmThreads, tm_smem_bytes<EPI>(), st>>>(
-          maps, c, dv, e, done, ntx, zlen, partials, ticket, dot, dot_clear, fault);
+      fd_tma_apply_kernel<EPI, 1><<<grid, kTmThreads, tm_smem_bytes<EPI>(), st>>>(maps, c, e, done, ntx, zlen,
+                                                                                   partials, ticket, dot, dot_clear,
+                                                                                   fault);
     ++launched;
+  }
+  if ((parts & TM_DATA) && d.ntouched > 0) {
+    rows_kernel<float><<<stream_grid(d.nrows, 256), 256, 0, st>>>(d.nrows, d.width, d.cols, d.a, d.w2, p, d.s, done);
+    // the fix-up's dot partials reuse the apply's (it runs after the apply)
+    data_fixup_kernel<EPI><<<(int)std::min<int64_t>(stream_grid(d.ntouched, 256), max_blocks > 0 ? max_blocks : 1024),
+                             256, 0, st>>>(d.ntouched, d.touched, d.inc_ptr, d.inc_row, d.inc_a, d.s, p, e, done,
+                                           partials, ticket, dot);
+    launched += 2;
   }
   LS_CUDA_TRY(cudaGetLastError());
   return launched;
@@ -149,8 +149,7 @@ int tm_launch(TmCache &cache, const CoefT<float> &c, const float *p, DataView<fl
 
 int tm_autotune(TmCache &cache, const CoefT<float> &c, const float *p, float *q, int *fault, cudaStream_t st) {
   if (!cache.enabled || cache.zu != 0) return LS_OK;
-  DataView<float> dv{};
-  dv.enabled = 0;
+  const TmData none{};
   EpiArgs<float> e{};
   e.q = q;
   cudaEvent_t a, b;
@@ -160,13 +159,12 @@ int tm_autotune(TmCache &cache, const CoefT<float> &c, const float *p, float *q,
   int pick = 1;
   for (int zu = 1; zu <= 2; ++zu) {
     cache.zu = zu;
-    int st1 = tm_launch<EPI_STORE>(cache, c, p, dv, e, nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr,
-                                   nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, fault, 0, st, TM_APPLY);
+    int st1 = tm_launch<EPI_STORE>(cache, c, p, none, e, nullptr, nullptr, nullptr, nullptr, nullptr, fault, 0, st,
+                                   TM_APPLY);
     if (st1 <= 0) break;  // the maps could not be encoded: the launch path stays off
     cudaEventRecord(a, st);
     for (int r = 0; r < 5; ++r)
-      tm_launch<EPI_STORE>(cache, c, p, dv, e, nullptr, 0, nullptr, nullptr, nullptr, 0, nullptr, nullptr, nullptr,
-                           nullptr, nullptr, nullptr, nullptr, nullptr, fault, 0, st, TM_APPLY);
+      tm_launch<EPI_STORE>(cache, c, p, none, e, nullptr, nullptr, nullptr, nullptr, nullptr, fault, 0, st, TM_APPLY);
     cudaEventRecord(b, st);
     LS_CUDA_TRY(cudaEventSynchronize(b));
     float ms = 0.f;
@@ -183,11 +181,10 @@ int tm_autotune(TmCache &cache, const CoefT<float> &c, const float *p, float *q,
   return LS_OK;
 }
 
-#define LS_TM_INST(EPI)                                                                                              \
-  template int tm_launch<EPI>(TmCache &, const CoefT<float> &, const float *, DataView<float>,                      \
-                              const EpiArgs<float> &, const int *, int64_t, const int64_t *, const int32_t *,       \
-                              const float *, int, const int32_t *, const float *, const float *, float *, double *, \
-                              unsigned int *, double *, double *, int *, int, cudaStream_t, int);
+#define LS_TM_INST(EPI)                                                                                           \
+  template int tm_launch<EPI>(TmCache &, const CoefT<float> &, const float *, const TmData &,                    \
+                              const EpiArgs<float> &, const int *, double *, unsigned int *, double *, double *, \
+                              int *, int, cudaStream_t, int);
 LS_TM_INST(EPI_STORE)
 LS_TM_INST(EPI_CHEB)
 LS_TM_INST(EPI_RESID)

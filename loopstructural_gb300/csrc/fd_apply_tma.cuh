@@ -16,9 +16,13 @@
 //
 // Deep nodes ([3, n-4]^3) use the constant composite stencil with register
 // windows over z (as fd_apply.cuh); shell nodes use the exact branch-free sum
-// shell_node() on the staged neighbourhood.  The data term at touched nodes
-// is a per-node total qd[rank] produced just before by data_node_totals_kernel,
-// prefetched one plane ahead.
+// shell_node() on the staged neighbourhood, specialised per warp to the axes
+// along which the warp's nodes are near a face.
+//
+// The data term does not enter this kernel: the kernel leaves p unchanged, so
+// the term A_d^T W A_d p of the few touched nodes is added afterwards, with its
+// share of the epilogue, by rows_kernel + data_fixup_kernel (q += qd, or
+// r -= qd and d -= c2 D^-1 qd).
 //
 // Every mbarrier wait is bounded (kTmSpin polls with a 1 us suspend hint); a
 // timeout raises *fault, ends the block's march (after a bounded wait for its
@@ -108,40 +112,60 @@ __device__ __forceinline__ bool tm_wait(uint64_t *bar, uint32_t parity) {
   return false;
 }
 
-// qd[t] = sum over the incidences e of touched node t of a_e w_r^2 (a_r . p),
-// r = row(e): the data term of every touched node, each row's dot product
-// recomputed per incidence in the order of rows_kernel + data_term.
-template <typename T>
-__global__ void data_node_totals_kernel(int64_t ntouched, const int64_t *__restrict__ inc_ptr,
-                                        const int32_t *__restrict__ inc_row, const T *__restrict__ inc_a, int width,
-                                        const int32_t *__restrict__ cols, const T *__restrict__ a,
-                                        const T *__restrict__ w2, const T *__restrict__ p, T *__restrict__ qd,
-                                        const int *done) {
+// The data term of the finest level, after fd_tma_apply_kernel: for touched
+// node t (rank order, node touched[t]) qd = sum_e a_e s[row(e)] over its
+// incidences, s = w^2 (a_row . p) from rows_kernel, and the epilogue the main
+// kernel ran without it corrected: STORE q += qd (p . qd added to *dot);
+// CHEB / RESID r -= qd, d -= c2 D^-1 qd (both epilogues are linear in q).
+template <int EPI>
+__global__ void __launch_bounds__(256) data_fixup_kernel(int64_t ntouched, const int64_t *__restrict__ touched,
+                                                         const int64_t *__restrict__ inc_ptr,
+                                                         const int32_t *__restrict__ inc_row,
+                                                         const float *__restrict__ inc_a, const float *__restrict__ s,
+                                                         const float *__restrict__ p, EpiArgs<float> e,
+                                                         const int *done, double *partials, unsigned int *ticket,
+                                                         double *dot) {
   if (done && *done) return;
+  float local = 0.f;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntouched;
        t += (int64_t)gridDim.x * blockDim.x) {
-    T acc = 0;
+    float qd = 0.f;
     const int64_t e1 = inc_ptr[t + 1];
-    for (int64_t e = inc_ptr[t]; e < e1; ++e) {
-      const int64_t r = inc_row[e];
-      T dot = 0;
-      for (int k = 0; k < width; ++k) {
-        const int32_t col = cols[r * width + k];
-        if (col >= 0) dot += a[r * width + k] * p[col];
-      }
-      acc += inc_a[e] * (w2[r] * dot);
+    for (int64_t k = inc_ptr[t]; k < e1; ++k) qd += inc_a[k] * s[inc_row[k]];
+    const int64_t g = touched[t];
+    if (EPI == EPI_STORE) {
+      e.q[g] += qd;
+      local += p[g] * qd;
+    } else {
+      e.r[g] -= qd;
+      e.d_out[g] -= e.c2 * e.dinv[g] * qd;
     }
-    qd[t] = acc;
+  }
+  if (dot) {
+    double tot;
+    if (grid_sum<256, float>(local, partials, ticket, &tot)) *dot += tot;
   }
 }
+
+// Data rows of the finest level as the TMA launcher needs them (FP32).
+struct TmData {
+  int64_t nrows = 0, ntouched = 0;
+  int width = 0;
+  const int32_t *cols = nullptr;
+  const float *a = nullptr, *w2 = nullptr;  // nrows x width, nrows
+  const int64_t *touched = nullptr, *inc_ptr = nullptr;
+  const int32_t *inc_row = nullptr;
+  const float *inc_a = nullptr;
+  float *s = nullptr;  // nrows: w^2 (a_row . p) of the current p
+};
 
 // ZU: output planes per barrier step (1 or 2; the launcher picks the faster
 // for the grid at first use).
 template <int EPI, int ZU = 1>
 __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
-    fd_tma_apply_kernel(const __grid_constant__ TmMaps maps, CoefT<float> c, DataView<float> dv, EpiArgs<float> e,
-                        const int *done, int ntx, int zlen, double *partials, unsigned int *ticket, double *dot_out,
-                        double *dot_clear, int *fault) {
+    fd_tma_apply_kernel(const __grid_constant__ TmMaps maps, CoefT<float> c, EpiArgs<float> e, const int *done,
+                        int ntx, int zlen, double *partials, unsigned int *ticket, double *dot_out, double *dot_clear,
+                        int *fault) {
   if (done && *done) return;
   constexpr int NOP = TmOps<EPI>::n;
   constexpr int SLOT = tm_slot_floats<EPI>();
@@ -190,9 +214,9 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
     for (int t = tfirst; t <= min(tlast, tfirst + kTmSlots - 1); ++t) issue(t);
 
   // which formula a warp uses is decided for the whole warp (no divergence):
-  // the deep composite stencil, the exact sum specialised to nodes deep in y
-  // and z (warps holding x-boundary columns), or the general exact sum
-  // (boundary rows in y, boundary planes in z).  A warp is one tile row.
+  // the deep composite stencil, or the exact sum specialised to the axes along
+  // which the warp is near a face (x: the warp holds a column within 3 of an
+  // x face; y: its row is; z: the plane is).  A warp is one tile row.
   const bool ydeep = (j >= 3) & (j <= ny - 4);
   const bool xshell_warp = __any_sync(0xffffffffu, col_in & !((i >= 3) & (i <= nx - 4))) != 0;
 
@@ -221,22 +245,6 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
   }
   ok = __syncthreads_and(ok);
 
-  // data term pipeline: mask word of plane z+1 (loaded one step ahead), the
-  // total of plane z+1 requested one step ahead of its use; the word rank is
-  // read only for touched nodes
-  const bool data_on = dv.enabled && col_in;
-  auto word_of = [&](int z) -> uint32_t {
-    return (data_on && z < z1) ? __ldg(dv.mask + ((z * sxy + gcol) >> 5)) : 0u;
-  };
-  auto total_of = [&](int z, uint32_t w) -> float {
-    const int g = z * sxy + gcol;
-    const uint32_t bit = 1u << (g & 31);
-    if (!(w & bit)) return 0.f;
-    return __ldg(dv.qd + __ldg(dv.word_rank + (g >> 5)) + __popc(w & (bit - 1u)));
-  };
-  uint32_t mw1 = word_of(z0 + 1);
-  float qd0 = total_of(z0, word_of(z0)), qd1 = 0.f;
-
   float local = 0.f;
   int z = z0;
   int zfail = z0 - 3;  // the step whose wait gave up (prologue: z0 - 3)
@@ -249,11 +257,12 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
     ok = tm_wait(bar_of(zz + 2), parity_of(zz + 2)) && ok;
     const int pl2 = slot_of(zz + 2);
     inplane(pl2, P4, X4, Y4);
-    // data pipeline: total of plane zz+1 requested, word of plane zz+2 requested
-    qd1 = total_of(zz + 1, mw1);
-    const uint32_t mw2 = word_of(zz + 2);
     float q;
     const bool zdeep = (zz >= 3) & (zz <= nz - 4);
+    auto pr = [&](int dz, int dy, int dx) -> float {
+      const int pl = dz == -2 ? pm2 : dz == -1 ? pm1 : dz == 0 ? po : dz == 1 ? pp1 : pl2;
+      return tm_smem[pl + own + dy * kTmPX + dx];
+    };
     if (ydeep & zdeep) {
       if (!xshell_warp) {
         const float q0 = P2;
@@ -267,17 +276,13 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
             c.xy * (corners - 2.f * (ex + ey) + 4.f * q0) + c.xz * ((X0 + X4) - 2.f * X2) +
             c.yz * ((Y0 + Y4) - 2.f * Y2);
       } else {
-        auto pr = [&](int dz, int dy, int dx) -> float {
-          const int pl = dz == -2 ? pm2 : dz == -1 ? pm1 : dz == 0 ? po : dz == 1 ? pp1 : pl2;
-          return tm_smem[pl + own + dy * kTmPX + dx];
-        };
-        q = shell_node<float, decltype(pr), false, false>(c, pr, i, j, zz);
+        q = shell_node<float, decltype(pr), false, false, true>(c, pr, i, j, zz);
       }
+    } else if (!xshell_warp & ydeep) {  // a plane near a z face
+      q = shell_node<float, decltype(pr), false, true, false>(c, pr, i, j, zz);
+    } else if (!xshell_warp) {  // a row near a y face
+      q = shell_node<float, decltype(pr), true, true, false>(c, pr, i, j, zz);
     } else {
-      auto pr = [&](int dz, int dy, int dx) -> float {
-        const int pl = dz == -2 ? pm2 : dz == -1 ? pm1 : dz == 0 ? po : dz == 1 ? pp1 : pl2;
-        return tm_smem[pl + own + dy * kTmPX + dx];
-      };
       q = shell_node<float>(c, pr, i, j, zz);
     }
     // epilogue of one node: q (data term added), its p, operands in the slot
@@ -299,13 +304,11 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
         e.d_out[g] = e.c2 * dinv * rn;
       }
     };
-    if (col_in) emit(zz * sxy + gcol, ty * kTmX + tx, q + qd0, P2);
+    if (col_in) emit(zz * sxy + gcol, ty * kTmX + tx, q, P2);
     P0 = P1; P1 = P2; P2 = P3; P3 = P4;
     X0 = X1; X1 = X2; X2 = X3; X3 = X4;
     Y0 = Y1; Y1 = Y2; Y2 = Y3; Y3 = Y4;
     pm2 = pm1; pm1 = po; po = pp1; pp1 = pl2;
-    qd0 = qd1;
-    mw1 = mw2;
    }
     ok = __syncthreads_and(ok);  // planes z - 2 .. z + ZU - 3 are free in every thread
     if (!ok) zfail = z;
@@ -367,19 +370,17 @@ void tm_setup(TmCache &cache, int nx, int ny, int nz, bool allow);
 // LS_GB300_TMA_STEP=1|2 forces one.  Outside any stream capture.
 int tm_autotune(TmCache &cache, const CoefT<float> &c, const float *p, float *q, int *fault, cudaStream_t st);
 
-// q = N p with the epilogue through fd_tma_apply_kernel (plus the data-node
-// totals kernel when the grid has touched nodes; `qd` receives them).  With
+// q = N p with the epilogue: fd_tma_apply_kernel, then, when the grid has
+// touched nodes, rows_kernel + data_fixup_kernel for the data term.  With
 // `dot`, sum p.q lands there and `dot_clear` (may be NULL) is zeroed.
-// `parts` selects what is launched: TM_TOTALS | TM_APPLY (both by default;
-// the profiler times them one at a time).  Returns the number of kernels
+// `parts` selects what is launched: TM_APPLY | TM_DATA (both by default; the
+// profiler times them one at a time).  Returns the number of kernels
 // launched, 0 when the cache is not enabled or a map could not be encoded
 // (the caller then uses launch_operator), or a negative status.
-enum { TM_TOTALS = 1, TM_APPLY = 2 };
+enum { TM_DATA = 1, TM_APPLY = 2 };
 template <int EPI>
-int tm_launch(TmCache &cache, const CoefT<float> &c, const float *p, DataView<float> dv, const EpiArgs<float> &e,
-              const int *done, int64_t ntouched, const int64_t *inc_ptr, const int32_t *inc_row, const float *inc_a,
-              int width, const int32_t *cols, const float *a, const float *w2, float *qd, double *partials,
-              unsigned int *ticket, double *dot, double *dot_clear, int *fault, int max_blocks, cudaStream_t st,
-              int parts = TM_TOTALS | TM_APPLY);
+int tm_launch(TmCache &cache, const CoefT<float> &c, const float *p, const TmData &d, const EpiArgs<float> &e,
+              const int *done, double *partials, unsigned int *ticket, double *dot, double *dot_clear, int *fault,
+              int max_blocks, cudaStream_t st, int parts = TM_DATA | TM_APPLY);
 
 }  // namespace ls

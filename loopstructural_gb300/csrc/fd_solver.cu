@@ -114,9 +114,8 @@ struct ls_fd_handle {
   double *dir64 = nullptr;
   float *dir32 = nullptr;
   // TMA-staged finest-level FP32 apply (fd_apply_tma.cuh): tensor maps of the
-  // grid's vectors, and the per-touched-node data totals it reads
+  // grid's vectors
   ls::TmCache tm;
-  float *qd32 = nullptr;
   double *aux = nullptr;                // kAuxDoubles of scratch (ADMM step sums)
   std::vector<int64_t> h_idc;           // host copy of the data rows (Galerkin coarsening)
   std::vector<double> h_a, h_w2;
@@ -434,6 +433,24 @@ DataView<T> data_view(const ls_fd_handle *h, const T *s_rows, const T *inc_a) {
   return dv;
 }
 
+// the finest level's data rows for the TMA launcher (FP32; s = rows' w^2 a.p)
+TmData tm_data(const ls_fd_handle *h, float *s) {
+  const DataTerm &d = h->data;
+  TmData t;
+  t.nrows = d.nrows;
+  t.ntouched = d.ntouched;
+  t.width = d.width;
+  t.cols = d.cols;
+  t.a = d.a32;
+  t.w2 = d.w2_32;
+  t.touched = d.touched;
+  t.inc_ptr = d.inc_ptr;
+  t.inc_row = d.inc_row;
+  t.inc_a = d.inc_a32;
+  t.s = s;
+  return t;
+}
+
 // q = N p (rows kernel + fused apply); p.q lands in sc->pq_s (deep box or full
 // grid) and sc->pq_d (boundary shell of a split grid; stays 0 otherwise)
 template <typename T>
@@ -445,8 +462,7 @@ void launch_apply(ls_fd_handle *h, const T *p, T *q, T *s, const T *a, const T *
   e.q = q;
   int staged = 0;
   if constexpr (sizeof(T) == 4) {
-    staged = tm_launch<EPI_STORE>(h->tm, coef_as<float>(h->coef), p, data_view<float>(h, s, ia), e, done, d.ntouched,
-                                  d.inc_ptr, d.inc_row, ia, d.width, d.cols, a, w2, h->qd32, h->partials,
+    staged = tm_launch<EPI_STORE>(h->tm, coef_as<float>(h->coef), p, tm_data(h, s), e, done, h->partials,
                                   h->tickets + T_STENCIL, &h->sc->pq_s, &h->sc->pq_d, &h->sc->fault, h->red_blocks,
                                   st);
   }
@@ -861,16 +877,14 @@ void mg_apply(ls_fd_handle *h, const MgLevel &lv, const float *p, const EpiArgs<
   if (&lv == &h->mg.levels[0] && h->tm.enabled) {
     // finest level: the TMA-staged kernel (isotropic + data; with directional
     // terms it stores to dq and the directional kernel completes the epilogue)
-    const DataTerm &d = h->data;
     EpiArgs<float> es{};
     es.q = lv.dq;
+    const TmData td = tm_data(h, lv.s);
     const int staged =
-        lv.dir ? tm_launch<EPI_STORE>(h->tm, lv.coef, p, mg_view(lv), es, done, d.ntouched, d.inc_ptr, d.inc_row,
-                                      d.inc_a32, d.width, d.cols, d.a32, d.w2_32, h->qd32, nullptr, nullptr, nullptr,
-                                      nullptr, &h->sc->fault, h->red_blocks, st)
-               : tm_launch<EPI>(h->tm, lv.coef, p, mg_view(lv), e, done, d.ntouched, d.inc_ptr, d.inc_row,
-                                d.inc_a32, d.width, d.cols, d.a32, d.w2_32, h->qd32, nullptr, nullptr, nullptr,
-                                nullptr, &h->sc->fault, h->red_blocks, st);
+        lv.dir ? tm_launch<EPI_STORE>(h->tm, lv.coef, p, td, es, done, nullptr, nullptr, nullptr, nullptr,
+                                      &h->sc->fault, h->red_blocks, st)
+               : tm_launch<EPI>(h->tm, lv.coef, p, td, e, done, nullptr, nullptr, nullptr, nullptr, &h->sc->fault,
+                                h->red_blocks, st);
     if (staged > 0) {
       h->launches += staged;
       if (lv.dir) {
@@ -1934,7 +1948,6 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
     return fail(LS_ERR_CUDA);
   }
   h->rhs_norm2 = h->sc_h->scratch;
-  if (d.ntouched > 0 && (st = dev_alloc(&h->qd32, d.ntouched)) < 0) return fail(st);
   {
     // the TMA-staged FP32 apply unless LS_GB300_STAGED_APPLY=tiles asks for
     // the cp.async tile kernels (same operator, for comparison)
@@ -1960,8 +1973,7 @@ extern "C" int ls_fd_destroy(ls_fd_handle *h) {
   void *ptrs[] = {h->rhs, h->diag, h->dinv64, h->dinv32, h->x64, h->r64, h->p64, h->q64, h->s64, h->x32, h->r32,
                   h->p32, h->q32, h->s32, h->sc, h->partials, h->tickets, h->data.cols, h->data.a64, h->data.a32,
                   h->data.w2_64, h->data.w2_32, h->data.b, h->data.touched, h->data.inc_ptr, h->data.inc_row,
-                  h->data.inc_a64, h->data.inc_a32, h->data.mask, h->data.word_rank, h->dir64, h->dir32, h->qd32,
-                  h->aux};
+                  h->data.inc_a64, h->data.inc_a32, h->data.mask, h->data.word_rank, h->dir64, h->dir32, h->aux};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h->sc_h) cudaFreeHost(h->sc_h);
@@ -2404,17 +2416,14 @@ extern "C" int ls_fd_profile_mg(ls_fd_handle *h, int reps, double *out, int max_
     ec.c2 = 1e-3f;
     LS_TRY(timed([&] { mg_apply<EPI_CHEB>(h, lv, lv.d0, ec, nullptr, st); }, &o[2]));
     if (l == 0 && h->tm.enabled && !lv.dir) {
-      // the TMA-staged kernel alone (data totals computed once before), then
-      // the data-totals kernel alone
-      const DataTerm &d = h->data;
+      // the TMA-staged kernel alone, then the data term (rows + fix-up) alone
+      const TmData td = tm_data(h, lv.s);
       auto part = [&](int parts) {
-        return tm_launch<EPI_CHEB>(h->tm, lv.coef, lv.d0, mg_view(lv), ec, nullptr, d.ntouched, d.inc_ptr, d.inc_row,
-                                   d.inc_a32, d.width, d.cols, d.a32, d.w2_32, h->qd32, nullptr, nullptr, nullptr,
-                                   nullptr, &h->sc->fault, h->red_blocks, st, parts);
+        return tm_launch<EPI_CHEB>(h->tm, lv.coef, lv.d0, td, ec, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                   &h->sc->fault, h->red_blocks, st, parts);
       };
-      h->launches += part(TM_TOTALS);
       LS_TRY(timed([&] { h->launches += part(TM_APPLY); }, &o[8]));
-      if (d.ntouched > 0) LS_TRY(timed([&] { h->launches += part(TM_TOTALS); }, &o[9]));
+      if (td.ntouched > 0) LS_TRY(timed([&] { h->launches += part(TM_DATA); }, &o[9]));
     } else if (lv.g1) {
       const DataView<float> dv = mg_view(lv);
       LS_TRY(timed([&] { h->launches += launch_g1<EPI_CHEB>(lv.g1op, lv.d0, dv, ec, nullptr, h->red_blocks / 8, st, 1); },

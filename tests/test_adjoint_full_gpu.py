@@ -53,7 +53,7 @@ def _gpu_grads(cells, vals, nrm, q, target, reg, precision="fp64"):
     t = torch.tensor(target, device=dev, dtype=torch.float64)
     loss = ((f(*args, r) - t) ** 2).mean()
     loss.backward()
-    return float(loss), [a.grad.cpu().numpy() for a in args] + [float(r.grad)]
+    return float(loss.detach()), [a.grad.cpu().numpy() for a in args] + [float(r.grad)]
 
 
 def _oracle_loss(cells, vals, nrm, q, target, reg):
