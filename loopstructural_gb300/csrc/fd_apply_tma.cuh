@@ -3,8 +3,9 @@
 //     q = (sum_f w_f^2 R_f^T R_f + A_d^T W A_d + ridge^2 I) p,  then an epilogue
 //
 // One kernel covers every node of the grid (deep interior and the 3-node
-// boundary shell).  A block owns a 32 x 8 column tile and marches along z
-// through a segment of planes.  The planes of p it needs (the tile plus a
+// boundary shell).  A block of 128 threads owns a 32 x 8 column tile (two
+// x-adjacent columns per thread) and marches along z through a segment of
+// planes.  The planes of p it needs (the tile plus a
 // 2-node halo, 40 x 12 nodes: x starts 4 nodes left of the tile so that the
 // copy starts on a 16-byte boundary) arrive by cp.async.bulk.tensor into a
 // ring of kTmSlots shared-memory slots, each tracked by one mbarrier; the
@@ -37,13 +38,14 @@
 
 namespace ls {
 
-constexpr int kTmX = 32, kTmY = 8, kTmThreads = kTmX * kTmY;
+constexpr int kTmX = 32, kTmY = 8;
+constexpr int kTmThreads = kTmX * kTmY / 2;  // 16 x 8 threads, two x-adjacent nodes each
 constexpr int kTmPX = kTmX + 8;             // staged plane: x0 - 4 .. x0 + 35
 constexpr int kTmPY = kTmY + 4;             // y0 - 2 .. y0 + 9
 constexpr int kTmPlane = kTmPX * kTmPY;     // 480 floats (1920 B)
 constexpr int kTmOp = kTmX * kTmY;          // 256 floats (1 KB)
 constexpr int kTmSlots = 8;
-constexpr int kTmBlocksPerSm = 4;
+constexpr int kTmBlocksPerSm = 5;
 constexpr int kTmSpin = 1 << 20;            // polls of one mbarrier before giving up
 constexpr int kTmSuspendNs = 1000;          // suspend-time hint of one poll (~1 s in all)
 
@@ -161,6 +163,12 @@ struct TmData {
 
 // ZU: output planes per barrier step (1 or 2; the launcher picks the faster
 // for the grid at first use).
+//
+// Thread (tx, ty) of the 16 x 8 block owns the node pair (x0 + 2 tx, y0 + ty)
+// and its right neighbour: every staged row is read as aligned float pairs
+// (ld.shared.v2), so one load serves both nodes, and the epilogue moves pairs
+// (nx is a multiple of 4, so a pair never straddles a row end).  A warp holds
+// two tile rows.
 template <int EPI, int ZU = 1>
 __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
     fd_tma_apply_kernel(const __grid_constant__ TmMaps maps, CoefT<float> c, EpiArgs<float> e, const int *done,
@@ -169,27 +177,34 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
   if (done && *done) return;
   constexpr int NOP = TmOps<EPI>::n;
   constexpr int SLOT = tm_slot_floats<EPI>();
-  // staged planes: float offsets into the shared array itself (so every read
-  // stays a shared-memory access), the base rounded up to 128 bytes
+  // staged planes: float offsets into the shared array, the base rounded up
+  // to 128 bytes; pairs are read through the array's shared-window address
   extern __shared__ __align__(128) float tm_smem[];
-  const int sbase = (int)(((128u - (smem_u32(tm_smem) & 127u)) & 127u) >> 2);
+  const uint32_t sm0 = smem_u32(tm_smem);
+  const int sbase = (int)(((128u - (sm0 & 127u)) & 127u) >> 2);
   __shared__ __align__(8) uint64_t bars[kTmSlots];
-  const int tid = threadIdx.x, tx = tid & (kTmX - 1), ty = tid / kTmX;
+  const int tid = threadIdx.x, tx = tid & (kTmX / 2 - 1), ty = tid / (kTmX / 2);
   const int x0 = (int)(blockIdx.x % ntx) * kTmX, y0 = (int)(blockIdx.x / ntx) * kTmY;
   const int nx = c.nx, ny = c.ny, nz = c.nz;
   const int z0 = blockIdx.y * zlen, z1 = min(nz, z0 + zlen);
-  const int i = x0 + tx, j = y0 + ty;
-  const bool col_in = (i < nx) & (j < ny);
+  const int i = x0 + 2 * tx, j = y0 + ty;     // the pair: (i, j) and (i + 1, j)
+  const bool col_in = (i < nx) & (j < ny);  // nx even: i < nx implies i + 1 < nx
   const int sxy = nx * ny;
   const int gcol = j * nx + i;
   const int tfirst = z0 - 2, tlast = z1 + 1;  // staged planes of p
-  const int hx = tx + 4, hy = ty + 2;         // the column's position in a staged plane
+  const int hx = 2 * tx + 4, hy = ty + 2;     // the pair's position in a staged plane (hx even)
   const int own = hy * kTmPX + hx;
 
   auto slot_of = [&](int t) -> int { return sbase + ((t - tfirst) & (kTmSlots - 1)) * SLOT; };
   auto bar_of = [&](int t) -> uint64_t * { return &bars[(t - tfirst) & (kTmSlots - 1)]; };
   auto parity_of = [&](int t) -> uint32_t { return (uint32_t)(((t - tfirst) >> 3) & 1); };
   static_assert(kTmSlots == 8, "slot arithmetic assumes 8 slots");
+  // a float pair at an even float offset of the shared array
+  auto ld2 = [&](int off) -> float2 {
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];\n" : "=f"(v.x), "=f"(v.y) : "r"(sm0 + 4u * (uint32_t)off));
+    return v;
+  };
   // one elected thread: plane t of p and, when t - 2 is an output plane, the
   // epilogue operands of plane t - 2, all on the slot's barrier
   auto issue = [&](int t) {
@@ -215,21 +230,22 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
 
   // which formula a warp uses is decided for the whole warp (no divergence):
   // the deep composite stencil, or the exact sum specialised to the axes along
-  // which the warp is near a face (x: the warp holds a column within 3 of an
-  // x face; y: its row is; z: the plane is).  A warp is one tile row.
-  const bool ydeep = (j >= 3) & (j <= ny - 4);
-  const bool xshell_warp = __any_sync(0xffffffffu, col_in & !((i >= 3) & (i <= nx - 4))) != 0;
+  // which the warp is near a face (x: it holds a column within 3 of an x face;
+  // y: one of its two rows is; z: the plane is)
+  const bool xshell_warp = __any_sync(0xffffffffu, col_in & !((i >= 3) & (i + 1 <= nx - 4))) != 0;
+  const bool ydeep_warp = __all_sync(0xffffffffu, !col_in | ((j >= 3) & (j <= ny - 4))) != 0;
 
-  // register windows over planes z-2 .. z+2: p, C_x p, C_y p at the column
-  float P0 = 0.f, P1 = 0.f, P2 = 0.f, P3 = 0.f, P4 = 0.f;
-  float X0 = 0.f, X1 = 0.f, X2 = 0.f, X3 = 0.f, X4 = 0.f;
-  float Y0 = 0.f, Y1 = 0.f, Y2 = 0.f, Y3 = 0.f, Y4 = 0.f;
-  auto inplane = [&](int pl, float &P, float &X, float &Y) {
-    const float *q = tm_smem + pl + own;
-    const float p0 = q[0];
-    P = p0;
-    X = (q[-2] + q[2]) - 2.f * p0;
-    Y = (q[-2 * kTmPX] + q[2 * kTmPX]) - 2.f * p0;
+  // register windows over planes z-2 .. z+2 for both nodes: p, C_x p, C_y p
+  float2 P0 = {0.f, 0.f}, P1 = P0, P2 = P0, P3 = P0, P4 = P0;
+  float2 X0 = P0, X1 = P0, X2 = P0, X3 = P0, X4 = P0;
+  float2 Y0 = P0, Y1 = P0, Y2 = P0, Y3 = P0, Y4 = P0;
+  auto inplane = [&](int pl, float2 &P, float2 &X, float2 &Y) {
+    const int q = pl + own;
+    const float2 cc = ld2(q), l = ld2(q - 2), r = ld2(q + 2);
+    const float2 u = ld2(q - 2 * kTmPX), d = ld2(q + 2 * kTmPX);
+    P = cc;
+    X = make_float2((l.x + r.x) - 2.f * cc.x, (l.y + r.y) - 2.f * cc.y);
+    Y = make_float2((u.x + d.x) - 2.f * cc.x, (u.y + d.y) - 2.f * cc.y);
   };
   bool ok = true;
   {
@@ -257,54 +273,77 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
     ok = tm_wait(bar_of(zz + 2), parity_of(zz + 2)) && ok;
     const int pl2 = slot_of(zz + 2);
     inplane(pl2, P4, X4, Y4);
-    float q;
+    float qa, qb;
     const bool zdeep = (zz >= 3) & (zz <= nz - 4);
     auto pr = [&](int dz, int dy, int dx) -> float {
       const int pl = dz == -2 ? pm2 : dz == -1 ? pm1 : dz == 0 ? po : dz == 1 ? pp1 : pl2;
       return tm_smem[pl + own + dy * kTmPX + dx];
     };
-    if (ydeep & zdeep) {
-      if (!xshell_warp) {
-        const float q0 = P2;
-        const float *o = tm_smem + po + own;
-        const float ex = o[-2] + o[2], ey = o[-2 * kTmPX] + o[2 * kTmPX];
-        const float d4x = ex - 4.f * (o[-1] + o[1]) + 6.f * q0;
-        const float d4y = ey - 4.f * (o[-kTmPX] + o[kTmPX]) + 6.f * q0;
-        const float corners = (o[-2 * kTmPX - 2] + o[-2 * kTmPX + 2]) + (o[2 * kTmPX - 2] + o[2 * kTmPX + 2]);
-        const float d4z = (P0 + P4) - 4.f * (P1 + P3) + 6.f * q0;
-        q = c.ridge2 * q0 + c.xx_int * d4x + c.yy_int * d4y + c.zz_int * d4z +
-            c.xy * (corners - 2.f * (ex + ey) + 4.f * q0) + c.xz * ((X0 + X4) - 2.f * X2) +
-            c.yz * ((Y0 + Y4) - 2.f * Y2);
-      } else {
-        q = shell_node<float, decltype(pr), false, false, true>(c, pr, i, j, zz);
+    auto prb = [&](int dz, int dy, int dx) -> float { return pr(dz, dy, dx + 1); };
+    if (ydeep_warp & zdeep & !xshell_warp) {
+      const int o = po + own;
+      // row y: columns hx-2 .. hx+3; rows y-/+1, y-/+2 at the pair; the
+      // corner columns of rows y-/+2
+      const float2 L = ld2(o - 2), R = ld2(o + 2);
+      const float2 U1 = ld2(o - kTmPX), D1 = ld2(o + kTmPX), U2 = ld2(o - 2 * kTmPX), D2 = ld2(o + 2 * kTmPX);
+      const float2 UL = ld2(o - 2 * kTmPX - 2), UR = ld2(o - 2 * kTmPX + 2);
+      const float2 DL = ld2(o + 2 * kTmPX - 2), DR = ld2(o + 2 * kTmPX + 2);
+      {
+        const float q0 = P2.x;
+        const float ex = L.x + R.x, ey = U2.x + D2.x;
+        const float d4x = ex - 4.f * (L.y + P2.y) + 6.f * q0;
+        const float d4y = ey - 4.f * (U1.x + D1.x) + 6.f * q0;
+        const float corners = (UL.x + UR.x) + (DL.x + DR.x);
+        const float d4z = (P0.x + P4.x) - 4.f * (P1.x + P3.x) + 6.f * q0;
+        qa = c.ridge2 * q0 + c.xx_int * d4x + c.yy_int * d4y + c.zz_int * d4z +
+             c.xy * (corners - 2.f * (ex + ey) + 4.f * q0) + c.xz * ((X0.x + X4.x) - 2.f * X2.x) +
+             c.yz * ((Y0.x + Y4.x) - 2.f * Y2.x);
       }
-    } else if (!xshell_warp & ydeep) {  // a plane near a z face
-      q = shell_node<float, decltype(pr), false, true, false>(c, pr, i, j, zz);
+      {
+        const float q0 = P2.y;
+        const float ex = L.y + R.y, ey = U2.y + D2.y;
+        const float d4x = ex - 4.f * (P2.x + R.x) + 6.f * q0;
+        const float d4y = ey - 4.f * (U1.y + D1.y) + 6.f * q0;
+        const float corners = (UL.y + UR.y) + (DL.y + DR.y);
+        const float d4z = (P0.y + P4.y) - 4.f * (P1.y + P3.y) + 6.f * q0;
+        qb = c.ridge2 * q0 + c.xx_int * d4x + c.yy_int * d4y + c.zz_int * d4z +
+             c.xy * (corners - 2.f * (ex + ey) + 4.f * q0) + c.xz * ((X0.y + X4.y) - 2.f * X2.y) +
+             c.yz * ((Y0.y + Y4.y) - 2.f * Y2.y);
+      }
+    } else if (ydeep_warp & zdeep) {  // columns near an x face
+      qa = shell_node<float, decltype(pr), false, false, true>(c, pr, i, j, zz);
+      qb = shell_node<float, decltype(prb), false, false, true>(c, prb, i + 1, j, zz);
+    } else if (!xshell_warp & ydeep_warp) {  // a plane near a z face
+      qa = shell_node<float, decltype(pr), false, true, false>(c, pr, i, j, zz);
+      qb = shell_node<float, decltype(prb), false, true, false>(c, prb, i + 1, j, zz);
     } else if (!xshell_warp) {  // a row near a y face
-      q = shell_node<float, decltype(pr), true, true, false>(c, pr, i, j, zz);
+      qa = shell_node<float, decltype(pr), true, true, false>(c, pr, i, j, zz);
+      qb = shell_node<float, decltype(prb), true, true, false>(c, prb, i + 1, j, zz);
     } else {
-      q = shell_node<float>(c, pr, i, j, zz);
+      qa = shell_node<float>(c, pr, i, j, zz);
+      qb = shell_node<float>(c, prb, i + 1, j, zz);
     }
-    // epilogue of one node: q (data term added), its p, operands in the slot
-    auto emit = [&](int g, int opi, float qn, float pn) {
-      const float *ops = tm_smem + pl2 + kTmPlane + opi;
+    // epilogue of the pair: q, its p, operands in the slot (pairs throughout)
+    if (col_in) {
+      const int g = zz * sxy + gcol;  // even
+      const int opo = pl2 + kTmPlane + ty * kTmX + 2 * tx;
       if (EPI == EPI_STORE) {
-        e.q[g] = qn;
-        local += pn * qn;
+        *reinterpret_cast<float2 *>(e.q + g) = make_float2(qa, qb);
+        local += P2.x * qa + P2.y * qb;
       } else if (EPI == EPI_CHEB) {
-        const float xv = ops[0], rv = ops[kTmOp], dinv = ops[2 * kTmOp];
-        e.x[g] = xv + pn;
-        const float rn = rv - qn;
-        e.r[g] = rn;
-        e.d_out[g] = e.c1 * pn + e.c2 * dinv * rn;
+        const float2 xv = ld2(opo), rv = ld2(opo + kTmOp), dv = ld2(opo + 2 * kTmOp);
+        *reinterpret_cast<float2 *>(e.x + g) = make_float2(xv.x + P2.x, xv.y + P2.y);
+        const float ra = rv.x - qa, rb = rv.y - qb;
+        *reinterpret_cast<float2 *>(e.r + g) = make_float2(ra, rb);
+        *reinterpret_cast<float2 *>(e.d_out + g) =
+            make_float2(e.c1 * P2.x + e.c2 * dv.x * ra, e.c1 * P2.y + e.c2 * dv.y * rb);
       } else {
-        const float bv = ops[0], dinv = ops[kTmOp];
-        const float rn = bv - qn;
-        e.r[g] = rn;
-        e.d_out[g] = e.c2 * dinv * rn;
+        const float2 bv = ld2(opo), dv = ld2(opo + kTmOp);
+        const float ra = bv.x - qa, rb = bv.y - qb;
+        *reinterpret_cast<float2 *>(e.r + g) = make_float2(ra, rb);
+        *reinterpret_cast<float2 *>(e.d_out + g) = make_float2(e.c2 * dv.x * ra, e.c2 * dv.y * rb);
       }
-    };
-    if (col_in) emit(zz * sxy + gcol, ty * kTmX + tx, q, P2);
+    }
     P0 = P1; P1 = P2; P2 = P3; P3 = P4;
     X0 = X1; X1 = X2; X2 = X3; X3 = X4;
     Y0 = Y1; Y1 = Y2; Y2 = Y3; Y3 = Y4;
