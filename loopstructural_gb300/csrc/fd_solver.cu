@@ -99,6 +99,7 @@ struct ls_fd_handle {
   double *partials = nullptr;      // 2 * max_blocks
   unsigned int *tickets = nullptr; // one per reduction site
   int red_blocks = 0;
+  int64_t partials_cap = 0;        // doubles in partials (one per block of a one-value grid reduction)
   // graphs of one batch of iterations
   cudaGraphExec_t g64 = nullptr, g32 = nullptr, gmg = nullptr;
   int g64_batch = 0, g32_batch = 0, gmg_batch = 0;
@@ -463,8 +464,8 @@ void launch_apply(ls_fd_handle *h, const T *p, T *q, T *s, const T *a, const T *
   int staged = 0;
   if constexpr (sizeof(T) == 4) {
     staged = tm_launch<EPI_STORE>(h->tm, coef_as<float>(h->coef), p, tm_data(h, s), e, done, h->partials,
-                                  h->tickets + T_STENCIL, &h->sc->pq_s, &h->sc->pq_d, &h->sc->fault, h->red_blocks,
-                                  st);
+                                  h->tickets + T_STENCIL, &h->sc->pq_s, &h->sc->pq_d, &h->sc->fault,
+                                  (int)std::min<int64_t>(h->partials_cap, 0x7fffffff), st);
   }
   if (staged > 0) {
     h->launches += staged;
@@ -1887,6 +1888,7 @@ extern "C" int ls_fd_create(const ls_fd_system *sys, ls_fd_handle **out, void *s
     const dim3 a8 = apply_grid<double, 8>((int)g.nsteps[0], (int)g.nsteps[1], (int)g.nsteps[2], MODE_FULL);
     const size_t nb = std::max<size_t>({(size_t)h->red_blocks, (size_t)a4.x * a4.y * a4.z, (size_t)a8.x * a8.y * a8.z});
     if ((st = dev_alloc(&h->partials, 4 * nb)) < 0) return fail(st);
+    h->partials_cap = (int64_t)(4 * nb);
   }
   if ((st = dev_alloc(&h->tickets, T_COUNT)) < 0) return fail(st);
   if ((st = dev_alloc(&h->aux, kAuxDoubles)) < 0) return fail(st);
