@@ -161,6 +161,34 @@ struct TmData {
   float *s = nullptr;  // nrows: w^2 (a_row . p) of the current p
 };
 
+// The exact sum at a node deep in y and z (index in [3, n-4]) but near an x
+// face: shell_node() with iy = iz = 1 and by = bz = 0 written out, from the
+// values the deep formula stages plus p at x -/+ 2 on planes z -/+ 2.  fi[0..2]
+// = I(i-1), I(i), I(i+1) and fb[0..2] = B(i-1), B(i), B(i+1) are the node's
+// x row-existence factors (interior row centre; border-layer rows).  Row and
+// plane values: r* row y (x-2 .. x+2), u* / d* rows y-2 / y+2 at x-2, x, x+2,
+// u1 / d1 rows y-1 / y+1 at x, m* / p* planes z-2 / z+2 at x-2, x, x+2, z1m /
+// z1p planes z-1 / z+1 at x, ycross = (C_y p)(z-2) + (C_y p)(z+2) -
+// 2 (C_y p)(z).  Cross terms use the one-sided differences
+// R(v) = v(x+2) - v(x), L(v) = v(x) - v(x-2):
+//   a_xy = I(i+1) (R(y+2) - 2 R(y) + R(y-2)) - I(i-1) (L(y+2) - 2 L(y) + L(y-2))
+// (and a_xz alike over planes), which at I = 1 is the deep corner sum.
+__device__ __forceinline__ float xshell_node(const CoefT<float> &c, const float fi[3], const float fb[3], float rm2,
+                                             float rm1, float r0, float rp1, float rp2, float um, float u0, float up,
+                                             float dm, float d0, float dp, float u1, float d1, float mm, float m0,
+                                             float mp, float pm, float p0, float pp, float z1m, float z1p,
+                                             float ycross) {
+  const float sxm = rm2 - 2.f * rm1 + r0, sx0 = rm1 - 2.f * r0 + rp1, sxp = r0 - 2.f * rp1 + rp2;
+  const float xpart = (c.xx_int * fi[0] + c.xx_bdr * fb[0]) * sxm - 2.f * (c.xx_int * fi[1] + c.xx_bdr * fb[1]) * sx0 +
+                      (c.xx_int * fi[2] + c.xx_bdr * fb[2]) * sxp;
+  const float R0 = rp2 - r0, L0 = r0 - rm2;
+  const float axy = fi[2] * ((dp - d0) - 2.f * R0 + (up - u0)) - fi[0] * ((d0 - dm) - 2.f * L0 + (u0 - um));
+  const float axz = fi[2] * ((pp - p0) - 2.f * R0 + (mp - m0)) - fi[0] * ((p0 - pm) - 2.f * L0 + (m0 - mm));
+  const float d4y = (u0 + d0) - 4.f * (u1 + d1) + 6.f * r0;
+  const float d4z = (m0 + p0) - 4.f * (z1m + z1p) + 6.f * r0;
+  return c.ridge2 * r0 + xpart + c.xy * axy + c.xz * axz + fi[1] * (c.yy_int * d4y + c.zz_int * d4z + c.yz * ycross);
+}
+
 // ZU: output planes per barrier step (1 or 2; the launcher picks the faster
 // for the grid at first use).
 //
@@ -235,6 +263,7 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
   const bool xshell_warp = __any_sync(0xffffffffu, col_in & !((i >= 3) & (i + 1 <= nx - 4))) != 0;
   const bool ydeep_warp = __all_sync(0xffffffffu, !col_in | ((j >= 3) & (j <= ny - 4))) != 0;
 
+
   // register windows over planes z-2 .. z+2 for both nodes: p, C_x p, C_y p
   float2 P0 = {0.f, 0.f}, P1 = P0, P2 = P0, P3 = P0, P4 = P0;
   float2 X0 = P0, X1 = P0, X2 = P0, X3 = P0, X4 = P0;
@@ -280,7 +309,7 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
       return tm_smem[pl + own + dy * kTmPX + dx];
     };
     auto prb = [&](int dz, int dy, int dx) -> float { return pr(dz, dy, dx + 1); };
-    if (ydeep_warp & zdeep & !xshell_warp) {
+    if (ydeep_warp & zdeep) {
       const int o = po + own;
       // row y: columns hx-2 .. hx+3; rows y-/+1, y-/+2 at the pair; the
       // corner columns of rows y-/+2
@@ -288,6 +317,18 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
       const float2 U1 = ld2(o - kTmPX), D1 = ld2(o + kTmPX), U2 = ld2(o - 2 * kTmPX), D2 = ld2(o + 2 * kTmPX);
       const float2 UL = ld2(o - 2 * kTmPX - 2), UR = ld2(o - 2 * kTmPX + 2);
       const float2 DL = ld2(o + 2 * kTmPX - 2), DR = ld2(o + 2 * kTmPX + 2);
+      if (xshell_warp) {  // columns near an x face: per-node x factors
+        const float2 ML = ld2(pm2 + own - 2), MR = ld2(pm2 + own + 2);
+        const float2 QL = ld2(pl2 + own - 2), QR = ld2(pl2 + own + 2);
+        auto fI = [&](int a) -> float { return (a >= 1 && a <= nx - 2) ? 1.f : 0.f; };
+        auto fB = [&](int a) -> float { return (float)((a == 1) + (a == nx - 2)) * ((a >= 0 && a < nx) ? 1.f : 0.f); };
+        const float fia[3] = {fI(i - 1), fI(i), fI(i + 1)}, fba[3] = {fB(i - 1), fB(i), fB(i + 1)};
+        const float fib[3] = {fI(i), fI(i + 1), fI(i + 2)}, fbb[3] = {fB(i), fB(i + 1), fB(i + 2)};
+        qa = xshell_node(c, fia, fba, L.x, L.y, P2.x, P2.y, R.x, UL.x, U2.x, UR.x, DL.x, D2.x, DR.x, U1.x, D1.x, ML.x,
+                         P0.x, MR.x, QL.x, P4.x, QR.x, P1.x, P3.x, (Y0.x + Y4.x) - 2.f * Y2.x);
+        qb = xshell_node(c, fib, fbb, L.y, P2.x, P2.y, R.x, R.y, UL.y, U2.y, UR.y, DL.y, D2.y, DR.y, U1.y, D1.y, ML.y,
+                         P0.y, MR.y, QL.y, P4.y, QR.y, P1.y, P3.y, (Y0.y + Y4.y) - 2.f * Y2.y);
+      } else {
       {
         const float q0 = P2.x;
         const float ex = L.x + R.x, ey = U2.x + D2.x;
@@ -310,9 +351,7 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
              c.xy * (corners - 2.f * (ex + ey) + 4.f * q0) + c.xz * ((X0.y + X4.y) - 2.f * X2.y) +
              c.yz * ((Y0.y + Y4.y) - 2.f * Y2.y);
       }
-    } else if (ydeep_warp & zdeep) {  // columns near an x face
-      qa = shell_node<float, decltype(pr), false, false, true>(c, pr, i, j, zz);
-      qb = shell_node<float, decltype(prb), false, false, true>(c, prb, i + 1, j, zz);
+      }
     } else if (!xshell_warp & ydeep_warp) {  // a plane near a z face
       qa = shell_node<float, decltype(pr), false, true, false>(c, pr, i, j, zz);
       qb = shell_node<float, decltype(prb), false, true, false>(c, prb, i + 1, j, zz);
