@@ -102,6 +102,27 @@ int ls_fd_point_rows(const ls_grid3 *grid, int kind, const double *d_pts, int64_
 int ls_fd_directional_weights(const ls_grid3 *grid, const double *d_vec, int64_t ld, double weight,
                               double *d_omega, int64_t *h_counts, void *stream);
 
+/* Regularisation weight scale of use_regularisation_weight_scale
+ * (FD:66-90 compute_weighting, called from FD:416-444 add_norm_constraints;
+ * P1:52-69): for every node m, d_scale[m] += 1 + alpha exp(-d^2 / (2 sigma^2)),
+ * d = the distance from the node (numpy linspace coordinates) to
+ * the nearest of the npts points (x y z = the first columns of d_pts, npts x
+ * ld FP64; pass the normal constraints inside the support).  The nearest
+ * point is exact (an FP32 screen, then FP64 distances).  The reference scale
+ * starts at 1 (DI:313), so d_scale starts as ones. */
+int ls_fd_weight_scale(const ls_grid3 *grid, const double *d_pts, int64_t npts, int64_t ld, double alpha,
+                       double sigma, double *d_scale, void *stream);
+
+/* The six interior regularisation families with the per-node scale
+ * (FD:668-672): for every interior node m (1 <= i, j, k <= n - 2) and family
+ * f in (dxx, dyy, dzz, dxy, dxz, dyz), d_omega[f * dof + m] += s_f^2
+ * (d_scale[m] h_w[f])^2 (s_f^2 = 1/6, 1/4), h_w = the families' row weights
+ * (cross families already divided by 4).  d_omega is the d_dir weight
+ * array of the system struct; it accumulates with ls_fd_directional_weights,
+ * and the system's isotropic interior weights are then 0. */
+int ls_fd_scaled_weights(const ls_grid3 *grid, const double *d_scale, const double h_w[6], double *d_omega,
+                         void *stream);
+
 /* Interface pair rows (FD:297-340 add_interface_constraints): row p is
  * [trilinear(i), -trilinear(j)] over 16 columns for d_pairs[p] = (i, j), both
  * indices into d_pts (all points must be inside), b = 0, w = weight. */

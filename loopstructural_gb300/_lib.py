@@ -34,7 +34,7 @@ REG_FAMILIES = (
 # every symbol include/ls_gb300.h declares
 EXPORTS = (
     "ls_last_error", "ls_abi_version",
-    "ls_fd_point_rows", "ls_fd_pair_rows", "ls_fd_reg_shape", "ls_fd_reg_rows", "ls_fd_directional_weights",
+    "ls_fd_point_rows", "ls_fd_pair_rows", "ls_fd_reg_shape", "ls_fd_reg_rows", "ls_fd_directional_weights", "ls_fd_weight_scale", "ls_fd_scaled_weights",
     "ls_fd_create", "ls_fd_destroy", "ls_fd_dof", "ls_fd_apply", "ls_fd_apply_f32", "ls_fd_apply_noalloc", "ls_fd_rhs",
     "ls_fd_diagonal", "ls_fd_solve", "ls_fd_profile_iteration", "ls_fd_profile_mg", "ls_fd_eval_points", "ls_fd_eval_lattice",
     "ls_fd_eval_adjoint", "ls_fd_set_rhs", "ls_fd_data_rows_apply", "ls_fd_admm_step", "ls_fd_device", "ls_fd_prepare", "ls_fd_solve_batched",
@@ -132,6 +132,8 @@ _SIGS = {
     "ls_fd_pair_rows": (C.c_int, [C.POINTER(Grid3), _P, C.c_int64, _P, C.c_int64, C.c_double, _P, _P, _P, _P, _P]),
     "ls_fd_reg_shape": (C.c_int, [C.POINTER(Grid3), C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]),
     "ls_fd_reg_rows": (C.c_int, [C.POINTER(Grid3), C.c_int, _P, _P]),
+    "ls_fd_weight_scale": (C.c_int, [C.POINTER(Grid3), _P, C.c_int64, C.c_int64, C.c_double, C.c_double, _P, _P]),
+    "ls_fd_scaled_weights": (C.c_int, [C.POINTER(Grid3), _P, C.POINTER(C.c_double * 6), _P, _P]),
     "ls_fd_directional_weights": (C.c_int, [C.POINTER(Grid3), _P, C.c_int64, C.c_double, _P,
                                             C.POINTER(C.c_int64), _P]),
     "ls_fd_create": (C.c_int, [C.POINTER(FdSystem), C.POINTER(_P), _P]),

@@ -433,6 +433,132 @@ __global__ void dir_weights_kernel(int nx, int ny, int nz, const double *__restr
       if (cnt[f]) atomicAdd(counts + f, cnt[f]);
 }
 
+// Node coordinate along one axis as numpy's linspace(o, max, n) makes it
+// (S:233-245 nodes): x_i = i * ((max - o) / (n - 1)) + o, the last node
+// exactly max = o + cells * h.  This translation unit is built without FMA
+// contraction, so each step rounds as numpy's does.
+struct LinAxis {
+  double o, step, mx;
+  int n;
+};
+
+__host__ LinAxis lin_axis(const ls_grid3 &g, int d) {
+  LinAxis a;
+  a.o = g.origin[d];
+  a.n = (int)g.nsteps[d];
+  a.mx = g.origin[d] + (double)(g.nsteps[d] - 1) * g.step[d];
+  a.step = (a.mx - a.o) / (double)(a.n - 1);
+  return a;
+}
+
+__device__ __forceinline__ double lin_at(const LinAxis &a, int i) {
+  return i == a.n - 1 ? a.mx : (double)i * a.step + a.o;
+}
+
+// Regularisation weight scale (FD:66-90 compute_weighting over the normal
+// constraints, FD:416-444 / P1:52-69): scale[m] += 1 + alpha exp(-d^2 /
+// (2 sigma^2)), d the distance from node m to the nearest point.  Brute force
+// over tiles of points in shared memory: an FP32 pass for the smallest
+// distance, then the exact FP64 distance (squared differences summed x, y,
+// z in turn, then the square root, as a KD-tree query reports it) of every
+// point within a margin of it, so the nearest point is found exactly.
+constexpr int kWsTile = 256;
+
+__global__ void __launch_bounds__(kWsTile) weight_scale_kernel(LinAxis ax, LinAxis ay, LinAxis az,
+                                                               const double *__restrict__ pts, int64_t npts,
+                                                               int64_t ld, double alpha, double sigma, double extent,
+                                                               double *__restrict__ scale) {
+  __shared__ float sf[3][kWsTile];
+  __shared__ double sd[3][kWsTile];
+  const int nx = ax.n, ny = ay.n;
+  const int64_t n = (int64_t)nx * ny * az.n;
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double px = 0.0, py = 0.0, pz = 0.0;
+  if (g < n) {
+    const int k = (int)(g / ((int64_t)nx * ny));
+    const int rem = (int)(g - (int64_t)k * nx * ny);
+    const int j = rem / nx, i = rem - j * nx;
+    px = lin_at(ax, i);
+    py = lin_at(ay, j);
+    pz = lin_at(az, k);
+  }
+  // FP32 coordinates relative to the grid origin
+  const float fx = (float)(px - ax.o), fy = (float)(py - ay.o), fz = (float)(pz - az.o);
+  float best32 = INFINITY;
+  for (int64_t t0 = 0; t0 < npts; t0 += kWsTile) {
+    __syncthreads();
+    const int64_t q = t0 + threadIdx.x;
+    if (q < npts) {
+      sf[0][threadIdx.x] = (float)(pts[q * ld] - ax.o);
+      sf[1][threadIdx.x] = (float)(pts[q * ld + 1] - ay.o);
+      sf[2][threadIdx.x] = (float)(pts[q * ld + 2] - az.o);
+    }
+    __syncthreads();
+    const int m = (int)(npts - t0 < kWsTile ? npts - t0 : kWsTile);
+    for (int u = 0; u < m; ++u) {
+      const float dx = fx - sf[0][u], dy = fy - sf[1][u], dz = fz - sf[2][u];
+      best32 = fminf(best32, dx * dx + dy * dy + dz * dz);
+    }
+  }
+  // candidates: FP32 distance within a margin of the smallest (rounding of
+  // coordinates of magnitude `extent` to FP32 and of the FP32 sums)
+  const double b = sqrt((double)best32);
+  const double lim = b + 1e-5 * (extent + b) + 1e-30;
+  const float lim2 = (float)(lim * lim);
+  double best = INFINITY;
+  for (int64_t t0 = 0; t0 < npts; t0 += kWsTile) {
+    __syncthreads();
+    const int64_t q = t0 + threadIdx.x;
+    if (q < npts) {
+      sd[0][threadIdx.x] = pts[q * ld];
+      sd[1][threadIdx.x] = pts[q * ld + 1];
+      sd[2][threadIdx.x] = pts[q * ld + 2];
+      sf[0][threadIdx.x] = (float)(sd[0][threadIdx.x] - ax.o);
+      sf[1][threadIdx.x] = (float)(sd[1][threadIdx.x] - ay.o);
+      sf[2][threadIdx.x] = (float)(sd[2][threadIdx.x] - az.o);
+    }
+    __syncthreads();
+    const int m = (int)(npts - t0 < kWsTile ? npts - t0 : kWsTile);
+    for (int u = 0; u < m; ++u) {
+      const float dx = fx - sf[0][u], dy = fy - sf[1][u], dz = fz - sf[2][u];
+      if (dx * dx + dy * dy + dz * dz <= lim2) {
+        const double ex = px - sd[0][u], ey = py - sd[1][u], ez = pz - sd[2][u];
+        double d2 = ex * ex;
+        d2 = d2 + ey * ey;
+        d2 = d2 + ez * ez;
+        best = fmin(best, d2);
+      }
+    }
+  }
+  if (g < n) {
+    const double d = sqrt(best);
+    scale[g] += 1.0 + alpha * exp(-(d * d) / (2.0 * (sigma * sigma)));
+  }
+}
+
+// Interior regularisation families with a per-node scale (FD:668-672 with
+// use_regularisation_weight_scale): the row centred at interior node m has
+// weight scale_m w_f, i.e. omega[f][m] += s_f^2 (scale_m w_f)^2 in the
+// directional-term weight planes (f = dxx, dyy, dzz, dxy, dxz, dyz; s_f^2 =
+// 1/6, 1/4: the squared row normalisation).
+__global__ void scaled_weights_kernel(int nx, int ny, int nz, const double *__restrict__ scale, double w0, double w1,
+                                      double w2, double w3, double w4, double w5, double *__restrict__ omega) {
+  const int64_t n = (int64_t)nx * ny * nz;
+  const double w[6] = {w0, w1, w2, w3, w4, w5};
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const int k = (int)(g / ((int64_t)nx * ny));
+    const int rem = (int)(g - (int64_t)k * nx * ny);
+    const int j = rem / nx, i = rem - j * nx;
+    if (i < 1 || i > nx - 2 || j < 1 || j > ny - 2 || k < 1 || k > nz - 2) continue;
+    const double sc = scale[g];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      const double rw = sc * w[f];
+      omega[f * n + g] += (f < 3 ? 1.0 / 6.0 : 0.25) * (rw * rw);
+    }
+  }
+}
+
 int check_grid(const ls_grid3 *g) {
   LS_ARG_CHECK(g != nullptr, "grid is NULL");
   for (int d = 0; d < 3; ++d) {
@@ -535,6 +661,41 @@ extern "C" int ls_fd_reg_rows(const ls_grid3 *grid, int family, int64_t *d_idc, 
   cudaStream_t s = as_stream(stream);
   reg_rows_kernel<<<stream_grid(sh.rows, 256), 256, 0, s>>>(grid->nsteps[0], grid->nsteps[1], grid->nsteps[2], family,
                                                           sh.rows, d_idc);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
+
+extern "C" int ls_fd_weight_scale(const ls_grid3 *grid, const double *d_pts, int64_t npts, int64_t ld, double alpha,
+                                  double sigma, double *d_scale, void *stream) {
+  LS_TRY(check_grid(grid));
+  LS_ARG_CHECK(ld >= 3, "ld < 3");
+  LS_ARG_CHECK(npts >= 0, "npts < 0");
+  LS_ARG_CHECK(d_scale != nullptr && (npts == 0 || d_pts != nullptr), "NULL device buffer");
+  LS_ARG_CHECK(sigma > 0.0, "sigma must be positive");
+  if (npts == 0) return LS_OK;
+  const int64_t n = grid->nsteps[0] * grid->nsteps[1] * grid->nsteps[2];
+  LS_ARG_CHECK(n < (int64_t)2000000000, "grid too large");
+  const LinAxis ax = lin_axis(*grid, 0), ay = lin_axis(*grid, 1), az = lin_axis(*grid, 2);
+  double extent = 1.0;
+  for (int d = 0; d < 3; ++d)
+    extent = fmax(extent, fabs(grid->origin[d]) + (double)(grid->nsteps[d] - 1) * grid->step[d]);
+  cudaStream_t s = as_stream(stream);
+  const int64_t blocks = (n + kWsTile - 1) / kWsTile;
+  weight_scale_kernel<<<(unsigned)blocks, kWsTile, 0, s>>>(ax, ay, az, d_pts, npts, ld, alpha, sigma, extent, d_scale);
+  LS_CUDA_TRY(cudaGetLastError());
+  return LS_OK;
+}
+
+extern "C" int ls_fd_scaled_weights(const ls_grid3 *grid, const double *d_scale, const double h_w[6], double *d_omega,
+                                    void *stream) {
+  LS_TRY(check_grid(grid));
+  LS_ARG_CHECK(d_scale != nullptr && d_omega != nullptr && h_w != nullptr, "NULL argument");
+  const int64_t n = grid->nsteps[0] * grid->nsteps[1] * grid->nsteps[2];
+  LS_ARG_CHECK(n < (int64_t)2000000000, "grid too large");
+  cudaStream_t s = as_stream(stream);
+  scaled_weights_kernel<<<stream_grid(n, 256), 256, 0, s>>>((int)grid->nsteps[0], (int)grid->nsteps[1],
+                                                            (int)grid->nsteps[2], d_scale, h_w[0], h_w[1], h_w[2],
+                                                            h_w[3], h_w[4], h_w[5], d_omega);
   LS_CUDA_TRY(cudaGetLastError());
   return LS_OK;
 }

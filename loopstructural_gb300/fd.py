@@ -55,6 +55,30 @@ def point_rows(support, kind: int, pts: np.ndarray, weight: float):
     return n, out, bool(nan.value)
 
 
+def weight_scale(support, pts: np.ndarray, alpha: float, sigma: float, scale):
+    """scale += 1 + alpha exp(-d^2 / 2 sigma^2), d = the distance from each node
+    to the nearest of the points (GPU, ls_fd_weight_scale); `scale` is a device
+    FP64 tensor of one entry per node, updated in place."""
+    torch = _torch()
+    pts = np.ascontiguousarray(pts[:, :3], dtype=np.float64)
+    d_pts = torch.from_numpy(pts).to(_lib.device())
+    g = support.grid3()
+    _lib.check(_lib.load().ls_fd_weight_scale(C.byref(g), _lib.ptr(d_pts), pts.shape[0], 3, float(alpha), float(sigma),
+                                              _lib.ptr(scale), _lib.stream_ptr()))
+    return scale
+
+
+def scaled_weights(support, scale, weights, omega):
+    """The interior regularisation families with a per-node scale added to the
+    directional weight planes `omega` (GPU, ls_fd_scaled_weights); `weights`
+    = the six row weights in (dxx, dyy, dzz, dxy, dxz, dyz) order."""
+    g = support.grid3()
+    w6 = (C.c_double * 6)(*[float(v) for v in weights])
+    _lib.check(_lib.load().ls_fd_scaled_weights(C.byref(g), _lib.ptr(scale), C.byref(w6), _lib.ptr(omega),
+                                                _lib.stream_ptr()))
+    return omega
+
+
 def pair_rows(support, pts: np.ndarray, pairs: np.ndarray, weight: float):
     """Interface pair rows (GPU): 16 columns per row."""
     torch = _torch()

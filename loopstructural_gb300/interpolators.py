@@ -120,6 +120,7 @@ class _DiscreteInterpolatorBase:
         self.constraints: dict[str, ConstraintFamily] = {}
         self.ineq_constraints: dict[str, InequalityFamily] = {}
         self.solver_history = None
+        self._reg_scale = None
         self.family_order: list[str] = []
         self.up_to_date = False
         self._c = np.zeros(self.support.n_nodes)
@@ -396,6 +397,34 @@ class _DiscreteInterpolatorBase:
             return sparse.csr_matrix((0, self.dof)), np.zeros(0)
         return sparse.vstack(mats).tocsr(), np.hstack(bs)
 
+    # -- regularisation weight scale (FD:66-90, 416-444; P1:52-69) -------------
+    def _regularisation_scale(self):
+        """Per-node scale of use_regularisation_weight_scale: 1, plus
+        1 + 10 exp(-d^2 / 2 sigma^2) with d the distance to the nearest normal
+        constraint inside the support (GPU); sigma defaults to 10 x the node
+        count along x."""
+        import torch
+
+        scale = torch.ones(int(self.support.n_nodes), dtype=torch.float64, device=_lib.device())
+        points = self.get_norm_constraints()
+        if points.shape[0] == 0:
+            return scale
+        inside = np.asarray(self.support.inside(points[:, :3]), dtype=bool)
+        if inside.any():
+            sigma = self.regularisation_weight_sigma
+            if sigma is None:
+                sigma = float(self.support.nsteps[0]) * 10
+            fd.weight_scale(self.support, points[inside, :3], 10.0, float(sigma), scale)
+        return scale
+
+    def regularisation_scale_array(self):
+        """The per-node regularisation weight scale as a host array (ones
+        without use_regularisation_weight_scale), as the reference's
+        ``regularisation_scale``."""
+        if self._reg_scale is None:
+            return np.ones(int(self.support.n_nodes))
+        return self._reg_scale.cpu().numpy()
+
     # -- directional regularisation (DI:395-451) ----------------------------
     def resolve_regularisation_config(self, regularisation=None, directional_regularisation=None):
         return regcfg.coerce_regularisation_config(regularisation=regularisation,
@@ -637,6 +666,8 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
         self.interface_pair_mode = "auto"
         self.interface_pair_threshold = 200
         self.interface_pair_fallback = "star"
+        self.use_regularisation_weight_scale = False
+        self.regularisation_weight_sigma = None
         self.regularisation_families = {}
         self._reset_directional()
 
@@ -646,6 +677,18 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
         self.directional_families = {}
         self._dir_terms = []
         self._dir_omega = None
+        # use_regularisation_weight_scale: the per-node scale (device), and
+        # whether the interior families went to the weight planes
+        self._reg_scale = None
+        self._scaled_interior = False
+
+    def _omega(self):
+        import torch
+
+        if self._dir_omega is None:
+            self._dir_omega = torch.zeros((len(_lib.DIRECTIONAL_FAMILIES), int(self.support.n_nodes)),
+                                          dtype=torch.float64, device=_lib.device())
+        return self._dir_omega
 
     def reset(self):
         super().reset()
@@ -665,14 +708,16 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
             if k in ("regularisation", "directional_regularisation"):
                 continue
             self.interpolation_weights[k] = v
-        if kwargs.get("use_regularisation_weight_scale", False):
-            raise NotImplementedError("use_regularisation_weight_scale is not part of the GPU path")
+        self.use_regularisation_weight_scale = bool(kwargs.get("use_regularisation_weight_scale", False))
+        self.regularisation_weight_sigma = kwargs.get("regularisation_weight_sigma", None)
         self.interface_pair_mode = kwargs.get("interface_pair_mode", self.interface_pair_mode)
         self.interface_pair_threshold = int(kwargs.get("interface_pair_threshold", self.interface_pair_threshold))
         self.interface_pair_fallback = kwargs.get("interface_pair_fallback", self.interface_pair_fallback)
         w = self.interpolation_weights
         t0 = perf_counter()
         self._add_point_rows(_lib.ROWS_NORM, self.get_norm_constraints(), w["npw"], ["norm_0", "norm_1", "norm_2"])
+        if self.use_regularisation_weight_scale:
+            self._reg_scale = self._regularisation_scale()
         self._add_point_rows(_lib.ROWS_GRADIENT, self.get_gradient_constraints(), w["gpw"], ["gradient", "gradient"])
         self._add_point_rows(_lib.ROWS_VALUE, self.get_value_constraints(), w["cpw"], ["value"])
         self._add_point_rows(_lib.ROWS_TANGENT, self.get_tangent_constraints(), w["tpw"], ["gradient orthogonal"])
@@ -721,10 +766,7 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
                            None if vector is None else np.shape(vector))
             return
         vector = np.asarray(vector, dtype=float)
-        if self._dir_omega is None:
-            self._dir_omega = torch.zeros((len(_lib.DIRECTIONAL_FAMILIES), n), dtype=torch.float64,
-                                          device=_lib.device())
-        counts = fd.directional_weights(self.support, vector, float(w), self._dir_omega)
+        counts = fd.directional_weights(self.support, vector, float(w), self._omega())
         self._dir_terms.append((float(w), vector))
         taken = set(self.constraints) | set(self.regularisation_families) | set(self.directional_families)
         for f, op in enumerate(_lib.DIRECTIONAL_FAMILIES):
@@ -821,6 +863,7 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
         """Matrix-free: record (rows, weight) per family in the reference order
         (G:489-510 interior families, FD:1052-1144 borders)."""
         w = self.interpolation_weights
+        scale = self._reg_scale
         if interior:
             self.regularisation_families = {}
             rw = {"dxy": w["dxy"] / 4, "dyz": w["dyz"] / 4, "dxz": w["dxz"] / 4, "dxx": w["dxx"], "dyy": w["dyy"],
@@ -830,13 +873,29 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
                 if rows > 0:
                     self.regularisation_families[name] = (rows, float(weight))
                     self.family_order.append(name)
+            if scale is not None and self.regularisation_families:
+                # rows of weight scale(centre) * w: the directional weight planes
+                fd.scaled_weights(self.support, scale,
+                                  [rw[f] if f in self.regularisation_families else 0.0
+                                   for f in _lib.DIRECTIONAL_FAMILIES], self._omega())
+                self._scaled_interior = True
         if borders:
             for name, key in (("dx_lower", "dx"), ("dx_upper", "dx"), ("dy_lower", "dy"), ("dy_upper", "dy"),
                               ("dz_lower", "dz"), ("dz_upper", "dz")):
                 rows, _ = fd.reg_shape(self.support, name)
                 if w[key] != 0 and rows > 0:
-                    self.regularisation_families[name] = (rows, float(w[key]))
-                    self.family_order.append(name)
+                    if scale is None:
+                        self.regularisation_families[name] = (rows, float(w[key]))
+                        self.family_order.append(name)
+                    else:
+                        # per-row weights scale(centre) * w: explicit data rows
+                        import torch
+
+                        idc = fd.reg_rows(self.support, name)
+                        dev = idc.device
+                        a = torch.from_numpy(np.tile(fd.REG_TAP_VALUES[name], (rows, 1))).to(dev)
+                        self._add_family(name, idc, a, torch.zeros(rows, dtype=torch.float64, device=dev),
+                                         (scale[idc[:, 1]] * float(w[key])).contiguous())
 
     def regularisation_rows(self, name):
         """Explicit (idc, A, B, w) of a matrix-free family, as the reference's
@@ -844,13 +903,20 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
         rows, weight = self.regularisation_families[name]
         idc = fd.reg_rows(self.support, name).cpu().numpy()
         vals = fd.REG_TAP_VALUES[name]
-        return {"idc": idc, "A": np.tile(vals, (rows, 1)), "B": np.zeros(rows), "w": np.full(rows, weight)}
+        w = np.full(rows, weight)
+        if self._scaled_interior:  # interior rows are centred on the interior nodes, ascending
+            nx, ny, nz = (int(v) for v in self.support.nsteps)
+            i, j, k = np.meshgrid(np.arange(1, nx - 1), np.arange(1, ny - 1), np.arange(1, nz - 1), indexing="ij")
+            centre = (i + nx * (j + ny * k)).transpose(2, 1, 0).ravel()
+            w = self.regularisation_scale_array()[centre] * weight
+        return {"idc": idc, "A": np.tile(vals, (rows, 1)), "B": np.zeros(rows), "w": w}
 
     def _reg_weights(self):
         fam = self.regularisation_families
         out = {}
         for k in ("dxx", "dyy", "dzz", "dxy", "dyz", "dxz"):
-            out[k] = fam[k][1] if k in fam else 0.0
+            # scaled interior families live in the weight planes instead
+            out[k] = fam[k][1] if (k in fam and not self._scaled_interior) else 0.0
         for k in ("dx", "dy", "dz"):
             out[k] = fam[k + "_lower"][1] if (k + "_lower") in fam else 0.0
         return out
@@ -860,7 +926,7 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
 
     def _make_system(self, rows):
         ridge = self.ridge_factor if self.add_ridge_regulatisation else 0.0
-        omega = self._dir_omega if self.directional_families else None
+        omega = self._dir_omega if (self.directional_families or self._scaled_interior) else None
         return fd.FdSystem(self.support, self._reg_weights(), rows, ridge, directional=omega)
 
     def _build_system(self):

@@ -145,8 +145,9 @@ class P1Interpolator(_DiscreteInterpolatorBase):
             if k in ("regularisation", "directional_regularisation"):
                 continue
             self.interpolation_weights[k] = v
-        if kwargs.get("use_regularisation_weight_scale", False):
-            raise NotImplementedError("use_regularisation_weight_scale is not part of the GPU path")
+        self.use_regularisation_weight_scale = bool(kwargs.get("use_regularisation_weight_scale", False))
+        self.regularisation_weight_sigma = kwargs.get("regularisation_weight_sigma", None)
+        self._reg_scale = self._regularisation_scale() if self.use_regularisation_weight_scale else None  # P1:212-214
         w = self.interpolation_weights
         if w["cgw"] > 0.0:
             self.minimise_edge_jumps(w["cgw"])
@@ -177,14 +178,29 @@ class P1Interpolator(_DiscreteInterpolatorBase):
 
     def minimise_edge_jumps(self, w=0.1, vector_func=None, vector=None, name="edge jump"):
         """Constant-gradient face rows (P1:115-166); ``vector`` (one row per
-        face) or ``vector_func`` (evaluated at the faces' mid-edge points,
-        P1:126-127) replaces the face normal."""
-        if vector_func is not None:
-            raise NotImplementedError("vector_func needs the reference's shared-edge points; pass vector=")
-        if vector is not None and np.shape(vector)[0] == self._regularisation_sample_shape()[0]:
+        face) or ``vector_func`` (evaluated at the midpoint of each shared
+        face's first two nodes, P1:126-127; ``vector`` wins when both are
+        given) replaces the face normal.  The shared nodes are taken in
+        ascending order; the reference's come from an unstable sort that keeps
+        that order on the meshes the fixtures record.  With use_regularisation_weight_scale
+        each row's weight is w times the mean of the two tetrahedra's mean
+        node scales (P1:150-155)."""
+        nfaces = self._regularisation_sample_shape()[0]
+        if vector is None or np.shape(vector)[0] != nfaces:
+            vector = None
+            if vector_func is not None:
+                shared = face_rows(self.support, 1.0, with_topology=True)[5].cpu().numpy()
+                nodes = self.support.nodes
+                vector = np.asarray(vector_func((nodes[shared[:, 0]] + nodes[shared[:, 1]]) / 2), dtype=float)
+        if vector is not None:
             idc, a, b, ww = face_rows_directional(self.support, w, np.asarray(vector, dtype=float))
         else:
             idc, a, b, ww = face_rows(self.support, w)
+        if self._reg_scale is not None:
+            s = self._reg_scale[idc]
+            m1 = (((s[:, 0] + s[:, 1]) + s[:, 2]) + s[:, 3]) / 4
+            m2 = (((s[:, 4] + s[:, 5]) + s[:, 6]) + s[:, 7]) / 4
+            ww = (0.5 * (m1 + m2) * float(w)).contiguous()
         self._add_family(name, idc, a, b, ww)
         self.up_to_date = False
 

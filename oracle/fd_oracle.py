@@ -387,10 +387,40 @@ def boundary_indexes(grid: Grid, axis, upper=False):  # FD:636-641
     return idx[idx[:, axis] == bi, :].T
 
 
-def add_regularisation(grid, cs, weights, directional=()):
+def compute_weighting(nodes, points, alpha=10.0, sigma=1.0):  # FD:66-90
+    """1 + alpha exp(-d^2 / 2 sigma^2), d = distance from each node to the
+    nearest point (a KD-tree query, as the reference)."""
+    from scipy.spatial import cKDTree
+
+    d, _ = cKDTree(points).query(nodes, k=1)
+    return 1 + alpha * np.exp(-(d**2) / (2 * sigma**2))
+
+
+def regularisation_scale(grid, normals, sigma=None):  # DI:313, FD:416-444
+    """The per-node scale ``use_regularisation_weight_scale`` puts on every
+    regularisation row's centre: 1 (reset), plus compute_weighting over the
+    normal constraints inside the grid (sigma defaults to 10 x the node count
+    along x)."""
+    scale = np.ones(grid.n_nodes)
+    if normals.shape[0] == 0:
+        return scale
+    _idc, inside = grid.position_to_cell_corners(normals[:, :3])
+    if inside.any():
+        s = grid.nsteps[0] * 10 if sigma is None else sigma
+        scale = scale + compute_weighting(grid.nodes, normals[inside, :3], sigma=s)
+    return scale
+
+
+def _row_centres(grid, indexes=None):
+    """Centre node of every row of a family (FD:662-667)."""
+    return grid.neighbour_global_indexes(np.zeros((3, 1), dtype=int), indexes)[0]
+
+
+def add_regularisation(grid, cs, weights, directional=(), scale=None):
     """Interior operators (G:489-510 order and /4 cross weights), the
     directional terms ((w, vector, name) triples, FD:222), then borders
-    (FD:1052-1144)."""
+    (FD:1052-1144).  ``scale`` (per node): every interior and border row's
+    weight times the scale at its centre (FD:668-672)."""
     ops = {
         "dxy": (DXY_MASK, weights["dxy"] / 4),
         "dyz": (DYZ_MASK, weights["dyz"] / 4),
@@ -403,6 +433,8 @@ def add_regularisation(grid, cs, weights, directional=()):
         idc, vals = family_rows(grid, mask)
         if idc.size == 0:
             continue
+        if scale is not None:
+            w = scale[_row_centres(grid)] * w
         cs.add(np.tile(vals, (idc.shape[0], 1)), np.zeros(idc.shape[0]), idc, w=w, name=name)
     for dw, vector, dname in directional:
         if dw != 0:
@@ -419,6 +451,8 @@ def add_regularisation(grid, cs, weights, directional=()):
         if w == 0 or indexes is None or indexes.shape[1] == 0:
             continue
         idc, vals = family_rows(grid, mask, indexes)
+        if scale is not None:
+            w = scale[_row_centres(grid, indexes)] * w
         cs.add(np.tile(vals, (idc.shape[0], 1)), np.zeros(idc.shape[0]), idc, w=w, name=name)
 
 
@@ -516,8 +550,10 @@ def resolve_weights(regularisation=None, **kwargs):
     return w
 
 
-def assemble(grid: Grid, data: dict, weights: dict, directional=()) -> ConstraintSet:
-    """FD:209-223 ``setup_interpolator`` family order."""
+def assemble(grid: Grid, data: dict, weights: dict, directional=(), weight_scale=False,
+             weight_sigma=None) -> ConstraintSet:
+    """FD:209-223 ``setup_interpolator`` family order; ``weight_scale`` =
+    ``use_regularisation_weight_scale`` (with ``regularisation_weight_sigma``)."""
     cs = ConstraintSet(grid.n_nodes)
     add_norm_constraints(grid, cs, data.get("normal", np.zeros((0, 7))), weights["npw"])
     add_gradient_constraints(grid, cs, data.get("gradient", np.zeros((0, 7))), weights["gpw"])
@@ -526,7 +562,8 @@ def assemble(grid: Grid, data: dict, weights: dict, directional=()) -> Constrain
     if tangent.shape[0] > 0:
         add_gradient_orthogonal_constraints(grid, cs, tangent[:, :3], tangent[:, 3:6], weights["tpw"])
     add_interface_constraints(grid, cs, data.get("interface", np.zeros((0, 5))), weights["ipw"])
-    add_regularisation(grid, cs, weights, directional)
+    scale = regularisation_scale(grid, data.get("normal", np.zeros((0, 7))), weight_sigma) if weight_scale else None
+    add_regularisation(grid, cs, weights, directional, scale=scale)
     return cs
 
 

@@ -226,9 +226,11 @@ class TetMesh(Grid):
         return vals
 
 
-def minimise_edge_jumps(mesh: TetMesh, cs: ConstraintSet, w, vector=None, name="edge jump"):  # P1:115-166
+def minimise_edge_jumps(mesh: TetMesh, cs: ConstraintSet, w, vector=None, name="edge jump", scale=None):  # P1:115-166
     """``vector`` (one row per face, P1:129-130) replaces the face normal:
-    the directional regularisation of P1:172-178."""
+    the directional regularisation of P1:172-178.  ``scale`` (per node,
+    ``use_regularisation_weight_scale``): each face row's weight times the
+    mean of the two tetrahedra's mean node scales (P1:150-155)."""
     rel, shared = mesh.face_table()
     norm = mesh.face_normals(shared)
     if vector is not None and np.asarray(vector).shape[0] == rel.shape[0]:
@@ -238,6 +240,8 @@ def minimise_edge_jumps(mesh: TetMesh, cs: ConstraintSet, w, vector=None, name="
     Dn = g[rel[:, 1]]
     const = np.hstack([np.einsum("ij,ijk->ik", norm, Dt), -np.einsum("ij,ijk->ik", norm, Dn)])
     idc = np.hstack([mesh.elements[rel[:, 0]], mesh.elements[rel[:, 1]]])
+    if scale is not None:
+        w = 0.5 * (scale[mesh.elements[rel[:, 0]]].mean(axis=1) + scale[mesh.elements[rel[:, 1]]].mean(axis=1)) * w
     cs.add(const, np.zeros(const.shape[0]), idc, w=w, name=name)
     return rel, shared
 
@@ -274,15 +278,32 @@ def resolve_weights(regularisation=None, **kwargs):  # P1:180-246
     return w
 
 
-def assemble(mesh: TetMesh, data: dict, weights: dict, directional=()) -> ConstraintSet:
+def regularisation_scale(mesh: TetMesh, normals, sigma=None):  # P1:52-69
+    """1 + compute_weighting over the normal constraints inside the mesh."""
+    from .fd_oracle import compute_weighting
+
+    scale = np.ones(mesh.n_nodes)
+    if normals.shape[0] == 0:
+        return scale
+    _, _, _tet, inside = mesh.element_for_location(normals[:, :3])
+    if inside.any():
+        s = mesh.nsteps[0] * 10 if sigma is None else sigma
+        scale = scale + compute_weighting(mesh.nodes, normals[inside, :3], sigma=s)
+    return scale
+
+
+def assemble(mesh: TetMesh, data: dict, weights: dict, directional=(), weight_scale=False,
+             weight_sigma=None) -> ConstraintSet:
     """P1:180-246 family order: edge jumps, directional terms ((w, vector,
-    name) triples, P1:229), (gradient: no-op), norm, value."""
+    name) triples, P1:229), (gradient: no-op), norm, value;
+    ``weight_scale`` = ``use_regularisation_weight_scale``."""
     cs = ConstraintSet(mesh.n_nodes)
+    scale = regularisation_scale(mesh, data.get("normal", np.zeros((0, 7))), weight_sigma) if weight_scale else None
     if weights["cgw"] > 0.0:
-        minimise_edge_jumps(mesh, cs, weights["cgw"])
+        minimise_edge_jumps(mesh, cs, weights["cgw"], scale=scale)
     for dw, vector, dname in directional:
         if dw != 0:
-            minimise_edge_jumps(mesh, cs, dw, vector=vector, name=dname)
+            minimise_edge_jumps(mesh, cs, dw, vector=vector, name=dname, scale=scale)
     add_norm_constraints(mesh, cs, data.get("normal", np.zeros((0, 7))), weights["npw"])
     add_value_constraints(mesh, cs, data.get("value", np.zeros((0, 5))), weights["cpw"])
     return cs

@@ -7,6 +7,7 @@ Run in a container where the reference source tree is available:
     python tests/golden/make_golden.py /path/to/LoopStructural --configs
     python tests/golden/make_golden.py /path/to/LoopStructural --faults
     python tests/golden/make_golden.py /path/to/LoopStructural --admm
+    python tests/golden/make_golden.py /path/to/LoopStructural --weight-scale
 
 It imports the reference's ``loop_interpolation`` / ``loop_common`` packages
 (``pyvista`` and ``yaml`` are stubbed: they are only used for VTK/YAML export)
@@ -829,6 +830,71 @@ def admm_case(li, StructuredGrid, name, out):
     out[f"{name}_c_unconstrained"] = spsolve(N, A.T @ b)
 
 
+def weight_scale_cases(li, StructuredGrid, TetMesh, out):
+    """``use_regularisation_weight_scale``: the per-node scale 1 + sum over the
+    normal-constraint calls of (1 + 10 exp(-d^2 / 2 sigma^2)), d the distance
+    to the nearest inside normal point, on every regularisation row's centre
+    (FD) or the mean over the face's two tetrahedra (P1).  The default sigma
+    (10 x the node count along x) and a small one."""
+    for name, cells, sigma in (("ws_fd_default", (9, 8, 10), None), ("ws_fd_sigma", (10, 9, 8), 0.15)):
+        calls, (cls, orig) = _hook(li)
+        try:
+            rng = np.random.default_rng(21 if sigma is None else 22)
+            grid = StructuredGrid(origin=np.zeros(3), nsteps=np.array(cells),
+                                  step_vector=1.0 / np.array(cells, dtype=float))
+            interp = li.FiniteDifferenceInterpolator(grid)
+            vp = rng.uniform(0.02, 0.98, size=(40, 3))
+            interp.set_value_constraints(np.column_stack([vp, _field(vp), np.ones(40)]))
+            npnt = rng.uniform(0.05, 0.95, size=(12, 3))
+            npnt[0] = [1.2, 0.5, 0.5]  # outside: not a distance target
+            g = _grad(npnt)
+            g /= np.linalg.norm(g, axis=1)[:, None]
+            interp.set_normal_constraints(np.column_stack([npnt, g, np.ones(12)]))
+            kw = dict(regularisation=0.1, cpw=1.0, npw=1.0, use_regularisation_weight_scale=True)
+            if sigma is not None:
+                kw["regularisation_weight_sigma"] = sigma
+            interp.setup_interpolator(**kw)
+            out[f"{name}_cells"] = np.array(cells)
+            out[f"{name}_sigma"] = np.array([np.nan if sigma is None else sigma])
+            out[f"{name}_value"] = np.asarray(interp.data["value"], dtype=float)
+            out[f"{name}_normal"] = np.asarray(interp.data["normal"], dtype=float)
+            out[f"{name}_scale"] = np.asarray(interp.regularisation_scale, dtype=float)
+            _families_to_arrays(interp, calls, f"{name}_", out)
+            out[f"{name}_c_direct"] = _solve_direct(interp)
+        finally:
+            cls.add_constraints_to_least_squares = orig
+    calls, (cls, orig) = _hook(li)
+    try:
+        name = "ws_p1"
+        cells = (3, 4, 3)
+        rng = np.random.default_rng(23)
+        mesh = TetMesh(origin=np.zeros(3), nsteps_cells=np.array(cells), step_vector=1.0 / np.array(cells, dtype=float))
+        interp = li.P1Interpolator(mesh)
+        vp = rng.uniform(0.02, 0.98, size=(30, 3))
+        interp.set_value_constraints(np.column_stack([vp, _field(vp), np.ones(30)]))
+        npnt = rng.uniform(0.05, 0.95, size=(8, 3))
+        interp.set_normal_constraints(np.column_stack([npnt, _grad(npnt), np.ones(8)]))
+        interp.setup_interpolator(cgw=0.1, cpw=1.0, npw=1.0, use_regularisation_weight_scale=True,
+                                  regularisation_weight_sigma=0.2)
+        out[f"{name}_cells"] = np.array(cells)
+        out[f"{name}_value"] = np.asarray(interp.data["value"], dtype=float)
+        out[f"{name}_normal"] = np.asarray(interp.data["normal"], dtype=float)
+        out[f"{name}_scale"] = np.asarray(interp.regularisation_scale, dtype=float)
+        _families_to_arrays(interp, calls, f"{name}_", out)
+        out[f"{name}_c_direct"] = _solve_direct(interp)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
+def main_weight_scale(root):
+    li, StructuredGrid, TetMesh = _import_reference(root)
+    out = {}
+    weight_scale_cases(li, StructuredGrid, TetMesh, out)
+    path = os.path.join(HERE, "weight_scale_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")
+
+
 def main_admm(root):
     li, StructuredGrid, _TetMesh = _import_reference(root)
     out = {}
@@ -881,5 +947,7 @@ if __name__ == "__main__":
         main_faults(root)
     elif "--admm" in sys.argv:
         main_admm(root)
+    elif "--weight-scale" in sys.argv:
+        main_weight_scale(root)
     else:
         main(root)
