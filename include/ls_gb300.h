@@ -480,9 +480,12 @@ int ls_p1_locate(const ls_grid3 *mesh, const double *d_pts, int64_t npts, int64_
                  void *stream);
 
 /* Value rows (kind LS_ROWS_VALUE, P1:98-113: barycentric, per-point weight
- * column ignored, w = weight) or normal rows (LS_ROWS_NORM, P1:73-96: 3
- * gradient rows per point, point-major, w = weight) of the inside points,
- * compacted in input order; 4 columns per row. */
+ * column ignored, w = weight), normal rows (LS_ROWS_NORM, P1:73-96: 3
+ * gradient rows per point, point-major, w = weight) or gradient-orthogonal
+ * rows (P1:248-296: v/|v| . grad phi, w = weight x the tetrahedron's volume;
+ * LS_ROWS_TANGENT: columns x y z vx vy vz, b = 0, the tangent rows of
+ * DI:668-682; LS_ROWS_ORTHOGONAL: a target b in column 6) of the inside
+ * points, compacted in input order; 4 columns per row. */
 int ls_p1_point_rows(const ls_grid3 *mesh, int kind, const double *d_pts, int64_t npts, int64_t ld, double weight,
                      int64_t *d_idc, double *d_a, double *d_b, double *d_w, int64_t *h_count, void *stream);
 

@@ -412,7 +412,30 @@ __global__ void locate_kernel(MeshArgs m, const double *__restrict__ pts, int64_
   }
 }
 
-// value (P1:98-113) or normal (P1:73-96) rows of the inside points at slot[i]
+// volume of a tetrahedron, |det(edges)| / 6 (T:81-95 element_size)
+__device__ __forceinline__ double tet_volume(const MeshArgs &m, const int64_t c[3], const int corners[4]) {
+  double p[4][3];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    const int k = corners[v];
+    p[v][0] = ix_coord(m, 0, c[0] + (k & 1));
+    p[v][1] = ix_coord(m, 1, c[1] + ((k >> 1) & 1));
+    p[v][2] = ix_coord(m, 2, c[2] + (k >> 2));
+  }
+  double e[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) e[r][d] = p[r + 1][d] - p[0][d];
+  const double det = e[0][0] * (e[1][1] * e[2][2] - e[1][2] * e[2][1]) -
+                     e[0][1] * (e[1][0] * e[2][2] - e[1][2] * e[2][0]) +
+                     e[0][2] * (e[1][0] * e[2][1] - e[1][1] * e[2][0]);
+  return fabs(det) / 6;
+}
+
+// value (P1:98-113), normal (P1:73-96) or gradient-orthogonal (P1:248-296;
+// KIND 2, b = 0, the tangent rows of DI:668-682; KIND 3, b = column 6) rows of
+// the inside points at slot[i]
 template <int KIND>
 __global__ void p1_point_rows_kernel(MeshArgs m, const double *__restrict__ pts, int64_t n, int64_t ld, double weight,
                                      const int32_t *__restrict__ flag, const int64_t *__restrict__ slot,
@@ -444,6 +467,28 @@ __global__ void p1_point_rows_kernel(MeshArgs m, const double *__restrict__ pts,
       }
       b[s] = bb;
       w[s] = weight;
+    } else if (KIND >= 2) {  // v/|v| . grad phi, weight w * volume of the tetrahedron
+      double g[3][4];
+      tet_gradient(m, cell, corners, g);
+      double v[3] = {p[3], p[4], p[5]};
+      const double vn = sqrt(((0.0 + v[0] * v[0]) + v[1] * v[1]) + v[2] * v[2]);
+      if (vn > 0)
+        for (int d = 0; d < 3; ++d) v[d] = v[d] / vn;
+      double row[4];
+      for (int k = 0; k < 4; ++k) row[k] = (v[0] * g[0][k] + v[1] * g[1][k]) + v[2] * g[2][k];
+      double bb = KIND == 3 ? p[6] : 0.0;
+      const double len =
+          sqrt(((((0.0 + row[0] * row[0]) + row[1] * row[1]) + row[2] * row[2]) + row[3] * row[3]));
+      if (len > 0) {
+        bb = bb / len;
+        for (int v2 = 0; v2 < 4; ++v2) row[v2] = row[v2] / len;
+      }
+      for (int v2 = 0; v2 < 4; ++v2) {
+        idc[4 * s + v2] = nodes[v2];
+        a[4 * s + v2] = row[v2];
+      }
+      b[s] = bb;
+      w[s] = weight * tet_volume(m, cell, corners);
     } else {  // normal: 3 gradient rows per point, point-major
       double g[3][4];
       tet_gradient(m, cell, corners, g);
@@ -571,8 +616,9 @@ extern "C" int ls_p1_point_rows(const ls_grid3 *mesh, int kind, const double *d_
                                 double weight, int64_t *d_idc, double *d_a, double *d_b, double *d_w,
                                 int64_t *h_count, void *stream) {
   LS_TRY(check_mesh(mesh));
-  LS_ARG_CHECK(kind == LS_ROWS_VALUE || kind == LS_ROWS_NORM, "P1 rows: kind must be VALUE or NORM");
-  LS_ARG_CHECK(ld >= (kind == LS_ROWS_VALUE ? 4 : 6), "ld too small for the row kind");
+  LS_ARG_CHECK(kind == LS_ROWS_VALUE || kind == LS_ROWS_NORM || kind == LS_ROWS_TANGENT || kind == LS_ROWS_ORTHOGONAL,
+               "P1 rows: kind must be VALUE, NORM, TANGENT or ORTHOGONAL");
+  LS_ARG_CHECK(ld >= (kind == LS_ROWS_VALUE ? 4 : kind == LS_ROWS_ORTHOGONAL ? 7 : 6), "ld too small for the row kind");
   LS_ARG_CHECK(h_count != nullptr, "h_count NULL");
   *h_count = 0;
   if (npts == 0) return LS_OK;
@@ -584,10 +630,15 @@ extern "C" int ls_p1_point_rows(const ls_grid3 *mesh, int kind, const double *d_
   LS_CUDA_TRY(cudaMallocAsync((void **)&slot, (npts + 1) * sizeof(int64_t), s));
   locate_kernel<<<stream_grid(npts, 128), 128, 0, s>>>(m, d_pts, npts, ld, nullptr, nullptr, flag);
   scan_counts_kernel<<<1, 1024, 0, s>>>(flag, npts, slot, slot + npts);
+  const int grd = stream_grid(npts, 128);
   if (kind == LS_ROWS_VALUE)
-    p1_point_rows_kernel<0><<<stream_grid(npts, 128), 128, 0, s>>>(m, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w);
+    p1_point_rows_kernel<0><<<grd, 128, 0, s>>>(m, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w);
+  else if (kind == LS_ROWS_NORM)
+    p1_point_rows_kernel<1><<<grd, 128, 0, s>>>(m, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w);
+  else if (kind == LS_ROWS_TANGENT)
+    p1_point_rows_kernel<2><<<grd, 128, 0, s>>>(m, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w);
   else
-    p1_point_rows_kernel<1><<<stream_grid(npts, 128), 128, 0, s>>>(m, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w);
+    p1_point_rows_kernel<3><<<grd, 128, 0, s>>>(m, d_pts, npts, ld, weight, flag, slot, d_idc, d_a, d_b, d_w);
   LS_CUDA_TRY(cudaGetLastError());
   int64_t cnt = 0;
   LS_CUDA_TRY(cudaMemcpyAsync(&cnt, slot + npts, sizeof(int64_t), cudaMemcpyDeviceToHost, s));

@@ -159,10 +159,32 @@ class P1Interpolator(_DiscreteInterpolatorBase):
         values = self.get_value_constraints()
         if values.shape[0] > 0:
             self._add_family("value", *point_rows(self.support, _lib.ROWS_VALUE, values, w["cpw"]))
-        if self.get_tangent_constraints().shape[0] > 0:
-            raise NotImplementedError("P1 tangent constraints are not part of the GPU path")
+        tangents = self.get_tangent_constraints()
+        if tangents.shape[0] > 0:  # DI:668-682 add_tangent_constraints
+            self.add_gradient_orthogonal_constraints(tangents[:, :3], tangents[:, 3:6], w["tpw"])
         self.up_to_date = False
         return SetupReport({name: f.n_rows for name, f in self.constraints.items()})
+
+    def add_gradient_orthogonal_constraints(self, points, vectors, w=1.0, b=0,
+                                            name="undefined gradient orthogonal constraint"):
+        """Rows grad(f) . v/|v| = b at the points inside the mesh, weight w
+        times the containing tetrahedron's volume (P1:248-296).  The reference
+        normalises the caller's ``vectors`` in place; here the caller's array
+        is left unchanged."""
+        points = np.asarray(points, dtype=float)
+        if points.shape[0] == 0:
+            return
+        vectors = np.asarray(vectors, dtype=float)
+        arr = np.empty((points.shape[0], 7))
+        arr[:, :3] = points[:, :3]
+        arr[:, 3:6] = vectors[:, :3]
+        arr[:, 6] = b
+        idc, a, bb, ww = point_rows(self.support, _lib.ROWS_ORTHOGONAL, arr, float(w))
+        if idc.shape[0] == 0:
+            logger.warning("%d gradient constraints not added: outside of model bounding box", points.shape[0])
+        else:
+            self._add_family(name, idc, a, bb, ww)
+        self.up_to_date = False
 
     # -- directional regularisation (P1:169-178) -----------------------------
     def get_regularisation_sample_points(self) -> np.ndarray:

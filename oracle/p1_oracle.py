@@ -270,6 +270,32 @@ def add_value_constraints(mesh: TetMesh, cs: ConstraintSet, points, w):  # P1:98
     cs.add(bc[inside], points[inside, 3], mesh.elements[tet[inside], :], w=wt, name="value")
 
 
+def element_size(mesh: TetMesh):  # T:81-95
+    """Volume of every tetrahedron, |det(edges)| / 6."""
+    nodes = mesh.nodes[mesh.elements]
+    vecs = nodes[:, 1:, :] - nodes[:, 0, None, :]
+    return np.abs(np.linalg.det(vecs)) / 6
+
+
+def add_gradient_orthogonal_constraints(mesh: TetMesh, cs: ConstraintSet, points, vectors, w=1.0, b=0.0,
+                                        name="undefined gradient orthogonal constraint"):  # P1:248-296
+    """grad(f) . v/|v| = b at the points inside, weight w x the tetrahedron's
+    volume (the tangent constraints of DI:668-682 with b = 0)."""
+    if points.shape[0] == 0:
+        return
+    _, _, tet, inside = mesh.element_for_location(points[:, :3])
+    grad = mesh.element_gradients(tet)
+    size = element_size(mesh)[tet[inside]]
+    wt = np.ones(size.shape[0])
+    wt *= w * size
+    v = np.array(vectors, dtype=float)
+    nrm = np.linalg.norm(v, axis=1)
+    v[nrm > 0, :] /= nrm[nrm > 0, None]
+    A = np.einsum("ij,ijk->ik", v[inside, :3], grad[inside, :, :])
+    B = np.zeros(int(inside.sum())) + b
+    cs.add(A, B, mesh.elements[tet[inside], :], w=wt, name=name)
+
+
 def resolve_weights(regularisation=None, **kwargs):  # P1:180-246
     w = dict(DEFAULT_P1_WEIGHTS)
     if regularisation is not None:
@@ -306,4 +332,7 @@ def assemble(mesh: TetMesh, data: dict, weights: dict, directional=(), weight_sc
             minimise_edge_jumps(mesh, cs, dw, vector=vector, name=dname, scale=scale)
     add_norm_constraints(mesh, cs, data.get("normal", np.zeros((0, 7))), weights["npw"])
     add_value_constraints(mesh, cs, data.get("value", np.zeros((0, 5))), weights["cpw"])
+    tangent = data.get("tangent", np.zeros((0, 7)))
+    if tangent.shape[0] > 0:  # DI:668-682
+        add_gradient_orthogonal_constraints(mesh, cs, tangent[:, :3], tangent[:, 3:6], weights["tpw"])
     return cs

@@ -886,10 +886,43 @@ def weight_scale_cases(li, StructuredGrid, TetMesh, out):
         cls.add_constraints_to_least_squares = orig
 
 
+def p1_orthogonal_case(li, TetMesh, out):
+    """P1 tangent constraints (DI:668-682) and gradient-orthogonal rows with a
+    target (P1:248-296) after setup: rows weighted by the tetrahedron volume,
+    one point outside the mesh."""
+    calls, (cls, orig) = _hook(li)
+    try:
+        name = "p1_orth"
+        cells = (4, 3, 3)
+        rng = np.random.default_rng(24)
+        mesh = TetMesh(origin=np.zeros(3), nsteps_cells=np.array(cells), step_vector=1.0 / np.array(cells, dtype=float))
+        interp = li.P1Interpolator(mesh)
+        vp = rng.uniform(0.02, 0.98, size=(25, 3))
+        interp.set_value_constraints(np.column_stack([vp, _field(vp), np.ones(25)]))
+        tp = rng.uniform(0.02, 0.98, size=(10, 3))
+        tp[0] = [1.5, 0.5, 0.5]
+        tv = rng.normal(size=(10, 3))
+        interp.set_tangent_constraints(np.column_stack([tp, tv, np.ones(10)]))
+        interp.setup_interpolator(cgw=0.1, cpw=1.0, tpw=2.0)
+        op = rng.uniform(0.02, 0.98, size=(6, 3))
+        ov = rng.normal(size=(6, 3))
+        out[f"{name}_orth_points"] = op
+        out[f"{name}_orth_vectors"] = ov.copy()
+        interp.add_gradient_orthogonal_constraints(op, ov, w=0.7, b=0.3, name="orth")
+        out[f"{name}_cells"] = np.array(cells)
+        out[f"{name}_value"] = np.asarray(interp.data["value"], dtype=float)
+        out[f"{name}_tangent"] = np.asarray(interp.data["tangent"], dtype=float)
+        _families_to_arrays(interp, calls, f"{name}_", out)
+        out[f"{name}_c_direct"] = _solve_direct(interp)
+    finally:
+        cls.add_constraints_to_least_squares = orig
+
+
 def main_weight_scale(root):
     li, StructuredGrid, TetMesh = _import_reference(root)
     out = {}
     weight_scale_cases(li, StructuredGrid, TetMesh, out)
+    p1_orthogonal_case(li, TetMesh, out)
     path = os.path.join(HERE, "weight_scale_golden.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")

@@ -58,3 +58,21 @@ def test_p1_weight_scale(wgolden):
     _check(g, "ws_p1", cs, mesh.n_nodes)
     np.testing.assert_allclose(fdo.solve_direct(*cs.matrix()), g["ws_p1_c_direct"], rtol=0,
                                atol=1e-9 * np.abs(g["ws_p1_c_direct"]).max())
+
+
+def test_p1_tangent_and_orthogonal_rows(wgolden):
+    """P1 tangent constraints and gradient-orthogonal rows with a target
+    (P1:248-296): weight = w x the tetrahedron's volume."""
+    g = wgolden
+    cells = g["p1_orth_cells"]
+    mesh = p1o.TetMesh(np.zeros(3), cells, 1.0 / cells.astype(float))
+    data = {"value": g["p1_orth_value"], "tangent": g["p1_orth_tangent"]}
+    cs = p1o.assemble(mesh, data, p1o.resolve_weights(cgw=0.1, cpw=1.0, tpw=2.0))
+    p1o.add_gradient_orthogonal_constraints(mesh, cs, g["p1_orth_orth_points"], g["p1_orth_orth_vectors"], w=0.7,
+                                            b=0.3, name="orth")
+    # the reference's family order: edge jumps, value, tangent, then "orth"
+    order = ["edge jump", "value", "undefined gradient orthogonal constraint", "orth"]
+    assert list(cs.families) == order == [str(s) for s in g["p1_orth_family_names"]]
+    _check(g, "p1_orth", cs, mesh.n_nodes)
+    np.testing.assert_allclose(fdo.solve_direct(*cs.matrix()), g["p1_orth_c_direct"], rtol=0,
+                               atol=1e-9 * np.abs(g["p1_orth_c_direct"]).max())

@@ -111,3 +111,35 @@ def test_fd_scale_at_96_cubed_nearest_point_exact():
     og = fdo.Grid(grid.origin, grid.nsteps_cells, grid.step_vector)
     ref = fdo.regularisation_scale(og, it.get_norm_constraints(), 2.0)
     np.testing.assert_allclose(it.regularisation_scale_array(), ref, rtol=1e-14, atol=0)
+
+
+def test_p1_tangent_and_orthogonal_rows(wgolden):
+    """P1 tangent constraints and gradient-orthogonal rows with a target
+    (LS_ROWS_TANGENT / LS_ROWS_ORTHOGONAL on the TetMesh): rows, volume
+    weights and the solution against the reference."""
+    from test_oracle_golden import _family_csr
+
+    g = wgolden
+    cells = g["p1_orth_cells"]
+    mesh = L.TetMesh(origin=np.zeros(3), nsteps_cells=cells, step_vector=1.0 / cells.astype(float))
+    it = L.P1Interpolator(mesh)
+    it.set_value_constraints(g["p1_orth_value"])
+    it.set_tangent_constraints(g["p1_orth_tangent"])
+    it.setup_interpolator(cgw=0.1, cpw=1.0, tpw=2.0)
+    vec = g["p1_orth_orth_vectors"].copy()
+    it.add_gradient_orthogonal_constraints(g["p1_orth_orth_points"], vec, w=0.7, b=0.3, name="orth")
+    np.testing.assert_array_equal(vec, g["p1_orth_orth_vectors"])  # the caller's array is left alone
+    assert list(it.constraints) == [str(s) for s in g["p1_orth_family_names"]]
+    for nm in it.constraints:
+        fam = it.constraints[nm].numpy()
+        np.testing.assert_array_equal(fam["idc"], g[f"p1_orth_fam_{nm}_idc"].reshape(fam["idc"].shape), err_msg=nm)
+        m = _family_csr(fam, it.dof)
+        ref = g[f"p1_orth_fam_{nm}_data"]
+        if nm == "edge jump":  # face rows agree up to the row sign (the shared-node order)
+            m.data, ref = np.abs(m.data), np.abs(ref)
+        np.testing.assert_allclose(m.data, ref, rtol=1e-13, atol=1e-13, err_msg=nm)
+        np.testing.assert_allclose(fam["B"], g[f"p1_orth_fam_{nm}_b"], rtol=1e-13, atol=1e-13, err_msg=nm)
+        np.testing.assert_allclose(fam["w"], g[f"p1_orth_fam_{nm}_w"], rtol=1e-13, atol=0, err_msg=nm)
+    assert it.solve_system("cg", solver_kwargs=dict(rtol=1e-13, atol=0.0, maxiter=200000, precision="fp64"))
+    c_ref = g["p1_orth_c_direct"]
+    assert np.abs(it.c - c_ref).max() <= 1e-6 * np.abs(c_ref).max()
