@@ -327,6 +327,27 @@ class _DiscreteInterpolatorBase:
         self.ineq_constraints[name] = InequalityFamily(idc.contiguous(), a.contiguous(), bounds.contiguous())
         self.up_to_date = False
 
+    def add_inequality_feature(self, feature, lower=True, mask=None):
+        """f >= feature (lower) or f <= feature at the support's nodes where
+        the feature is not NaN and the mask holds (DI:595-632)."""
+        import torch
+
+        value = np.asarray(feature(self.support.nodes), dtype=float)
+        if mask is None:
+            mask = np.ones(value.shape[0], dtype=bool)
+        lo = np.full(value.shape[0], -np.inf)
+        hi = np.full(value.shape[0], np.inf)
+        mask = np.logical_and(mask, ~np.isnan(value))
+        if lower:
+            lo[mask] = value[mask]
+        else:
+            hi[mask] = value[mask]
+        dev = _lib.device()
+        n = self.dof
+        self._add_inequality_family("inequality_feature", torch.arange(n, dtype=torch.int64, device=dev)[:, None],
+                                    torch.ones((n, 1), dtype=torch.float64, device=dev),
+                                    torch.from_numpy(np.column_stack([lo, hi])).to(dev))
+
     def build_inequality_matrix(self):
         """(Q, bounds) of every inequality family, stacked in insertion order
         (DI:874-884): Q a CSR matrix over the dof, bounds n x 2."""
@@ -1001,27 +1022,6 @@ class FiniteDifferenceInterpolator(_DiscreteInterpolatorBase):
             bounds[:, 0] = float(lower_bound)
             bounds[:, 1] = float(upper_bound)
             self._add_inequality_family(f"inequality_pairs_{pair[0]}_{pair[1]}", idc, a, bounds)
-
-    def add_inequality_feature(self, feature, lower=True, mask=None):
-        """f >= feature (lower) or f <= feature at the grid nodes where the
-        feature is not NaN and the mask holds (DI:595-632)."""
-        import torch
-
-        value = np.asarray(feature(self.support.nodes), dtype=float)
-        if mask is None:
-            mask = np.ones(value.shape[0], dtype=bool)
-        lo = np.full(value.shape[0], -np.inf)
-        hi = np.full(value.shape[0], np.inf)
-        mask = np.logical_and(mask, ~np.isnan(value))
-        if lower:
-            lo[mask] = value[mask]
-        else:
-            hi[mask] = value[mask]
-        dev = _lib.device()
-        n = self.dof
-        self._add_inequality_family("inequality_feature", torch.arange(n, dtype=torch.int64, device=dev)[:, None],
-                                    torch.ones((n, 1), dtype=torch.float64, device=dev),
-                                    torch.from_numpy(np.column_stack([lo, hi])).to(dev))
 
     def _matrix_rows(self):
         return (sum(f.n_rows for f in self.constraints.values()) + sum(r for r, _ in self.regularisation_families.values())

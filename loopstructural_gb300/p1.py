@@ -162,8 +162,72 @@ class P1Interpolator(_DiscreteInterpolatorBase):
         tangents = self.get_tangent_constraints()
         if tangents.shape[0] > 0:  # DI:668-682 add_tangent_constraints
             self.add_gradient_orthogonal_constraints(tangents[:, :3], tangents[:, 3:6], w["tpw"])
+        self.add_value_inequality_constraints()  # P1:243-244 (the DI defaults: upper bound 1.0)
+        self.add_inequality_pairs_constraints()
         self.up_to_date = False
         return SetupReport({name: f.n_rows for name, f in self.constraints.items()})
+
+    # -- inequality rows (DI:509-593 on the TetMesh) ---------------------------
+    def _barycentric_rows(self, points):
+        """(idc, raw barycentric weights) of the points inside the mesh, in
+        order (device), and the host mask of those points."""
+        tet, _bc = locate(self.support, np.ascontiguousarray(points[:, :3]))
+        inside = tet >= 0
+        if not inside.any():
+            return None, None, inside
+        pts = np.ascontiguousarray(np.column_stack([points[:, :3], np.zeros(points.shape[0])]))
+        idc, a, _b, _w = point_rows(self.support, _lib.ROWS_VALUE, pts, 1.0)
+        # the rows come normalised (bc / |bc|); barycentric weights sum to 1
+        return idc, a / a.sum(dim=1, keepdim=True), inside
+
+    def add_value_inequality_constraints(self, w=1.0):
+        """lower <= f(x) <= upper at the inequality points inside the mesh
+        (DI:509-518); w is not used, as in the reference."""
+        import torch
+
+        points = self.get_inequality_value_constraints()
+        if points.shape[0] == 0:
+            return
+        idc, a, inside = self._barycentric_rows(points)
+        if idc is None:
+            return
+        bounds = torch.from_numpy(np.ascontiguousarray(points[inside, 3:5])).to(_lib.device())
+        self._add_inequality_family("inequality_value", idc, a, bounds)
+
+    def add_inequality_pairs_constraints(self, w=1.0, upper_bound=1.0, lower_bound=-np.inf, pairs=None):
+        """lower_bound <= f(p) - f(q) <= upper_bound for every point p of the
+        group pair[0] and q of pair[1] inside the mesh; without ``pairs``,
+        every pair of distinct group ids (i < j) (DI:520-593)."""
+        import torch
+
+        points = self.get_inequality_pairs_constraints()
+        if points.shape[0] == 0:
+            return
+        ids = points[:, 3]
+        if not pairs:
+            u = np.unique(ids)
+            pairs = [(u[i], u[j]) for i in range(len(u)) for j in range(i + 1, len(u))]
+        dev = _lib.device()
+        for pair in pairs:
+            upper, lower = points[ids == pair[0]], points[ids == pair[1]]
+            iu_, au, in_u = self._barycentric_rows(upper)
+            il_, al, in_l = self._barycentric_rows(lower)
+            if (~in_u).sum() > 0:
+                logger.warning(f"Upper points not in mesh {upper[~in_u]}")
+            if (~in_l).sum() > 0:
+                logger.warning(f"Lower points not in mesh {lower[~in_l]}")
+            if iu_ is None or il_ is None:
+                continue
+            nu, nl = int(in_u.sum()), int(in_l.sum())
+            gu, gl = np.meshgrid(np.arange(nu), np.arange(nl))  # upper index fastest
+            su = torch.from_numpy(gu.ravel()).to(dev)
+            sl = torch.from_numpy(gl.ravel()).to(dev)
+            idc = torch.cat([iu_[su], il_[sl]], 1).contiguous()
+            a = torch.cat([au[su], -al[sl]], 1).contiguous()
+            bounds = torch.empty((idc.shape[0], 2), dtype=torch.float64, device=dev)
+            bounds[:, 0] = float(lower_bound)
+            bounds[:, 1] = float(upper_bound)
+            self._add_inequality_family(f"inequality_pairs_{pair[0]}_{pair[1]}", idc, a, bounds)
 
     def add_gradient_orthogonal_constraints(self, points, vectors, w=1.0, b=0,
                                             name="undefined gradient orthogonal constraint"):
@@ -226,15 +290,24 @@ class P1Interpolator(_DiscreteInterpolatorBase):
         self._add_family(name, idc, a, b, ww)
         self.up_to_date = False
 
-    def _build_system(self):
-        rows = [(f.idc, f.a, f.b, f.w) for f in self.constraints.values()]
+    def _data_rows(self):
+        return [(f.idc, f.a, f.b, f.w) for f in self.constraints.values()]
+
+    def _make_system(self, rows):
         ridge = self.ridge_factor if self.add_ridge_regulatisation else 0.0
         zero = {k: 0.0 for k in ("dxx", "dyy", "dzz", "dxy", "dyz", "dxz", "dx", "dy", "dz")}
         return fd.FdSystem(self.support, zero, rows, ridge)
 
+    def _build_system(self):
+        return self._make_system(self._data_rows())
+
     def _solver_options(self, solver, tol, solver_kwargs):
         solver, opts = super()._solver_options(solver, tol, solver_kwargs)
-        opts["preconditioner"] = "jacobi"  # the multigrid hierarchy is the FD stencil's
+        # the multigrid hierarchy is the FD stencil's: Jacobi-PCG for P1
+        if solver == "admm":
+            opts[1]["preconditioner"] = "jacobi"
+        else:
+            opts["preconditioner"] = "jacobi"
         return solver, opts
 
     def _matrix_rows(self):

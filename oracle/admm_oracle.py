@@ -61,6 +61,33 @@ def pair_rows(grid: Grid, points, pairs=None, upper_bound=np.finfo(float).eps, l
     return out
 
 
+def p1_value_inequality_rows(mesh, points):  # DI:509-518 on the TetMesh
+    """(idc, barycentric weights, bounds) of the points inside the mesh."""
+    _, bc, tet, inside = mesh.element_for_location(points[:, :3])
+    return mesh.elements[tet[inside]], bc[inside], points[inside, 3:5]
+
+
+def p1_pair_rows(mesh, points, pairs=None, upper_bound=1.0, lower_bound=-np.inf):  # DI:520-593 on the TetMesh
+    """[(name, idc, a, bounds)]: the P1 setup passes no bounds, so the DI
+    defaults [-inf, 1.0] apply (P1:244)."""
+    out = []
+    ids = points[:, 3]
+    if not pairs:
+        u = np.unique(ids)
+        pairs = [(u[i], u[j]) for i in range(len(u)) for j in range(i + 1, len(u))]
+    for p0, p1 in pairs:
+        up, lo = points[ids == p0], points[ids == p1]
+        _, bu, tu, in_u = mesh.element_for_location(up[:, :3])
+        _, bl, tl, in_l = mesh.element_for_location(lo[:, :3])
+        ju, jl = np.meshgrid(np.arange(int(in_u.sum())), np.arange(int(in_l.sum())))
+        ju, jl = ju.ravel(), jl.ravel()
+        a = np.hstack([bu[in_u][ju], -bl[in_l][jl]])
+        idc = np.hstack([mesh.elements[tu[in_u]][ju], mesh.elements[tl[in_l]][jl]])
+        bounds = np.column_stack([np.full(len(ju), lower_bound), np.full(len(ju), upper_bound)])
+        out.append((f"inequality_pairs_{p0}_{p1}", idc, a, bounds))
+    return out
+
+
 def feature_rows(grid: Grid, value, lower=True, mask=None):  # DI:595-632
     n = grid.n_nodes
     if mask is None:

@@ -928,11 +928,60 @@ def main_weight_scale(root):
     print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")
 
 
+def admm_p1_case(li, TetMesh, out):
+    """P1 with value inequalities and inequality pairs (P1:243-244: the
+    default pair bounds [-inf, 1.0]) under ``solve_system('admm')`` with an
+    exact inner solver."""
+    name = "admm_p1"
+    cells = (4, 4, 3)
+    rng = np.random.default_rng(31)
+    mesh = TetMesh(origin=np.zeros(3), nsteps_cells=np.array(cells), step_vector=1.0 / np.array(cells, dtype=float))
+    interp = li.P1Interpolator(mesh)
+    vp = rng.uniform(0.05, 0.95, size=(30, 3))
+    val = np.column_stack([vp, _field(vp), np.ones(30)])
+    npnt = rng.uniform(0.05, 0.95, size=(8, 3))
+    nrm = np.column_stack([npnt, _grad(npnt), np.ones(8)])
+    ip = rng.uniform(0.1, 0.9, size=(10, 3))
+    f0 = _field(ip)
+    lo = f0 + rng.uniform(0.05, 0.15, 10)
+    ineq = np.column_stack([ip, lo, lo + 0.1, np.ones(10)])
+    pp = rng.uniform(0.1, 0.9, size=(8, 3))
+    pp[:4, 2] = rng.uniform(0.6, 0.9, 4)
+    pp[4:, 2] = rng.uniform(0.1, 0.4, 4)
+    pairs = np.column_stack([pp, np.r_[np.zeros(4), np.ones(4)], np.ones(8)])
+    interp.set_value_constraints(val)
+    interp.set_normal_constraints(nrm)
+    interp.set_value_inequality_constraints(ineq)
+    interp.set_inequality_pairs_constraints(pairs)
+    interp.setup_interpolator(cgw=0.1, cpw=1.0, npw=1.0)
+    Q, bounds = interp.build_inequality_matrix()
+    Q = Q.tocoo()
+    out[f"{name}_cells"] = np.array(cells)
+    out[f"{name}_value"] = val
+    out[f"{name}_normal"] = nrm
+    out[f"{name}_ineq"] = ineq
+    out[f"{name}_pairs"] = pairs
+    out[f"{name}_Q_row"] = Q.row.astype(np.int64)
+    out[f"{name}_Q_col"] = Q.col.astype(np.int64)
+    out[f"{name}_Q_val"] = Q.data
+    out[f"{name}_bounds"] = np.asarray(bounds, dtype=float)
+    out[f"{name}_ineq_names"] = np.array(list(interp.ineq_constraints.keys()))
+    ok = interp.solve_system("admm", solver_kwargs=dict(admm_weight=1.0, nmajor=60, linsys_solver=_exact_lsq,
+                                                        return_history=True))
+    assert ok
+    hist = interp.solver_history
+    out[f"{name}_c"] = np.array(interp.c)
+    out[f"{name}_iterations"] = np.array(len(hist))
+    for k in ("primal_norm", "dual_norm", "eps_pri", "eps_dual", "rho"):
+        out[f"{name}_hist_{k}"] = np.array([h[k] for h in hist], dtype=float)
+
+
 def main_admm(root):
-    li, StructuredGrid, _TetMesh = _import_reference(root)
+    li, StructuredGrid, TetMesh = _import_reference(root)
     out = {}
     for name in ADMM_CASES:
         admm_case(li, StructuredGrid, name, out)
+    admm_p1_case(li, TetMesh, out)
     path = os.path.join(HERE, "admm_golden.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, sum(v.nbytes for v in out.values()), "bytes")

@@ -107,3 +107,27 @@ def test_admm_bounds_hold_at_64():
     h = it.solver_history[-1]
     assert len(it.solver_history) < 400, "did not stop on the primal/dual test"
     assert h["primal_norm"] <= h["eps_pri"] and h["dual_norm"] <= h["eps_dual"]
+
+
+def test_p1_admm_matches_reference(agolden):
+    """P1 with value inequalities and pairs (P1:243-244), Jacobi-PCG inner
+    solves."""
+    g = agolden
+    cells = g["admm_p1_cells"]
+    mesh = L.TetMesh(origin=np.zeros(3), nsteps_cells=cells, step_vector=1.0 / cells.astype(float))
+    it = L.P1Interpolator(mesh)
+    it.set_value_constraints(g["admm_p1_value"])
+    it.set_normal_constraints(g["admm_p1_normal"])
+    it.set_value_inequality_constraints(g["admm_p1_ineq"])
+    it.set_inequality_pairs_constraints(g["admm_p1_pairs"])
+    it.setup_interpolator(cgw=0.1, cpw=1.0, npw=1.0)
+    assert list(it.ineq_constraints) == [str(s) for s in g["admm_p1_ineq_names"]]
+    Q, bounds = it.build_inequality_matrix()
+    ref = sparse.coo_matrix((g["admm_p1_Q_val"], (g["admm_p1_Q_row"], g["admm_p1_Q_col"])), shape=Q.shape).tocsr()
+    assert abs(Q - ref).max() <= 1e-15
+    np.testing.assert_array_equal(bounds, g["admm_p1_bounds"])
+    assert it.solve_system("admm", solver_kwargs=dict(admm_weight=1.0, nmajor=60, return_history=True,
+                                                      rtol=1e-11, precision="fp64"))
+    assert len(it.solver_history) == int(g["admm_p1_iterations"])
+    c_ref = g["admm_p1_c"]
+    np.testing.assert_allclose(it.c, c_ref, rtol=0, atol=1e-7 * np.abs(c_ref).max())

@@ -63,3 +63,24 @@ def test_admm_solution_and_history_match_reference(agolden, name):
         np.testing.assert_allclose(got, exp, rtol=1e-7, atol=1e-9 * np.abs(exp).max(), err_msg=k)
     # the inequalities changed the solution: the case exercises them
     assert np.abs(ref - agolden[f"{name}_c_unconstrained"]).max() > 1e-3
+
+
+def test_p1_admm_rows_and_solution(agolden):
+    """P1 (P1:243-244): barycentric inequality rows, pair bounds [-inf, 1]."""
+    from oracle import p1_oracle as p1o
+
+    g = agolden
+    cells = g["admm_p1_cells"]
+    mesh = p1o.TetMesh(np.zeros(3), cells, 1.0 / cells.astype(float))
+    cs = p1o.assemble(mesh, {"value": g["admm_p1_value"], "normal": g["admm_p1_normal"]},
+                      p1o.resolve_weights(cgw=0.1, cpw=1.0, npw=1.0))
+    A, b = cs.matrix()
+    fams = [ao.p1_value_inequality_rows(mesh, g["admm_p1_ineq"])]
+    fams += [(i, a, bd) for _n, i, a, bd in ao.p1_pair_rows(mesh, g["admm_p1_pairs"])]
+    Q, bounds = ao.inequality_matrix(mesh.n_nodes, fams)
+    ref = _fixture_q(g, "admm_p1", mesh.n_nodes)
+    assert abs(Q - ref).max() <= 1e-15
+    np.testing.assert_array_equal(bounds, g["admm_p1_bounds"])
+    c, hist = ao.solve(A, b, Q, bounds, rho=1.0, nmajor=60)
+    assert len(hist) == int(g["admm_p1_iterations"])
+    np.testing.assert_allclose(c, g["admm_p1_c"], rtol=0, atol=1e-9 * np.abs(g["admm_p1_c"]).max())
