@@ -233,6 +233,8 @@ def solve_admm(interp, o, inner, timing) -> bool:
             inner_iterations += int(stats["iterations"])
             if stats["status"] == _lib.LS_NOT_CONVERGED:
                 logger.warning("ADMM inner solve %d reached its iteration limit", i)
+            elif stats["status"] in (_lib.LS_NAN, _lib.LS_BREAKDOWN):
+                logger.warning("ADMM inner solve %d stopped early (status %d)", i, int(stats["status"]))
             primal = math.sqrt(sums[0])
             dual = rho * math.sqrt(sums[1])
             qx_norm, z_norm, u_norm = math.sqrt(sums[2]), math.sqrt(sums[3]), rho * math.sqrt(sums[4])
