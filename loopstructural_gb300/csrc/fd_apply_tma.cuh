@@ -189,6 +189,33 @@ __device__ __forceinline__ float xshell_node(const CoefT<float> &c, const float 
   return c.ridge2 * r0 + xpart + c.xy * axy + c.xz * axz + fi[1] * (c.yy_int * d4y + c.zz_int * d4z + c.yz * ycross);
 }
 
+// The exact sum at a node deep in x and z but near a y face: shell_node()
+// with ix = iz = 1, bx = bz = 0 written out.  fi / fb = I, B of rows j-1, j,
+// j+1.  Values: r* row y (x-2 .. x+2) of plane z; u* / d* rows y-2 / y+2 at
+// x-2, x, x+2; u1 / d1 rows y-1 / y+1 at x; p0..p4 planes z-2 .. z+2 at the
+// node; zmu / zmd (zpu / zpd) plane z-2 (z+2) at rows y-2 / y+2; xcross =
+// (C_x p)(z-2) + (C_x p)(z+2) - 2 (C_x p)(z).  With the z second difference
+// G(r) of row y+r and the x second difference C(r) of row y+r:
+//   a_yz = I(j+1) (G(2) - G(0)) - I(j-1) (G(0) - G(-2)),
+//   a_xy = I(j+1) (C(2) - C(0)) - I(j-1) (C(0) - C(-2)).
+__device__ __forceinline__ float yshell_node(const CoefT<float> &c, const float fi[3], const float fb[3], float rm2,
+                                             float rm1, float r0, float rp1, float rp2, float um, float u0, float up,
+                                             float dm, float d0, float dp, float u1, float d1, float p0, float p1,
+                                             float p3, float p4, float zmu, float zmd, float zpu, float zpd,
+                                             float xcross) {
+  const float sym = u0 - 2.f * u1 + r0, sy0 = u1 - 2.f * r0 + d1, syp = r0 - 2.f * d1 + d0;
+  const float ypart = (c.yy_int * fi[0] + c.yy_bdr * fb[0]) * sym - 2.f * (c.yy_int * fi[1] + c.yy_bdr * fb[1]) * sy0 +
+                      (c.yy_int * fi[2] + c.yy_bdr * fb[2]) * syp;
+  const float Cm = (um + up) - 2.f * u0, C0 = (rm2 + rp2) - 2.f * r0, Cp = (dm + dp) - 2.f * d0;
+  const float axy = fi[2] * (Cp - C0) - fi[0] * (C0 - Cm);
+  const float Gm = (zpu + zmu) - 2.f * u0, G0 = (p4 + p0) - 2.f * r0, Gp = (zpd + zmd) - 2.f * d0;
+  const float ayz = fi[2] * (Gp - G0) - fi[0] * (G0 - Gm);
+  const float d4x = (rm2 + rp2) - 4.f * (rm1 + rp1) + 6.f * r0;
+  const float d4z = (p0 + p4) - 4.f * (p1 + p3) + 6.f * r0;
+  return c.ridge2 * r0 + fi[1] * (c.xx_int * d4x + c.zz_int * d4z + c.xz * xcross) + ypart + c.xy * axy +
+         c.yz * ayz;
+}
+
 // ZU: output planes per barrier step (1 or 2; the launcher picks the faster
 // for the grid at first use).
 //
@@ -309,7 +336,10 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
       return tm_smem[pl + own + dy * kTmPX + dx];
     };
     auto prb = [&](int dz, int dy, int dx) -> float { return pr(dz, dy, dx + 1); };
-    if (ydeep_warp & zdeep) {
+    // the general sum for warps near two faces (edges, corners); every other
+    // case from the pair loads below
+    const bool general = (xshell_warp & !(ydeep_warp & zdeep)) | (!ydeep_warp & !zdeep);
+    if (!general) {
       const int o = po + own;
       // row y: columns hx-2 .. hx+3; rows y-/+1, y-/+2 at the pair; the
       // corner columns of rows y-/+2
@@ -317,7 +347,53 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
       const float2 U1 = ld2(o - kTmPX), D1 = ld2(o + kTmPX), U2 = ld2(o - 2 * kTmPX), D2 = ld2(o + 2 * kTmPX);
       const float2 UL = ld2(o - 2 * kTmPX - 2), UR = ld2(o - 2 * kTmPX + 2);
       const float2 DL = ld2(o + 2 * kTmPX - 2), DR = ld2(o + 2 * kTmPX + 2);
-      if (xshell_warp) {  // columns near an x face: per-node x factors
+      if (!(ydeep_warp & zdeep)) {
+        if (ydeep_warp) {  // a plane near a z face: per-plane z factors, no further loads
+          auto fI = [&](int a) -> float { return (a >= 1 && a <= nz - 2) ? 1.f : 0.f; };
+          auto fB = [&](int a) -> float {
+            return (float)((a == 1) + (a == nz - 2)) * ((a >= 0 && a < nz) ? 1.f : 0.f);
+          };
+          const float iz0 = fI(zz - 1), iz1 = fI(zz), iz2 = fI(zz + 1);
+          const float w0 = c.zz_int * iz0 + c.zz_bdr * fB(zz - 1), w1 = c.zz_int * iz1 + c.zz_bdr * fB(zz),
+                      w2 = c.zz_int * iz2 + c.zz_bdr * fB(zz + 1);
+          {
+            const float q0 = P2.x;
+            const float ex = L.x + R.x, ey = U2.x + D2.x;
+            const float d4x = ex - 4.f * (L.y + P2.y) + 6.f * q0;
+            const float d4y = ey - 4.f * (U1.x + D1.x) + 6.f * q0;
+            const float corners = (UL.x + UR.x) + (DL.x + DR.x);
+            const float zpart = w0 * ((P0.x - 2.f * P1.x) + P2.x) - 2.f * w1 * ((P1.x - 2.f * P2.x) + P3.x) +
+                                w2 * ((P2.x - 2.f * P3.x) + P4.x);
+            qa = c.ridge2 * q0 + iz1 * (c.xx_int * d4x + c.yy_int * d4y + c.xy * (corners - 2.f * (ex + ey) + 4.f * q0)) +
+                 zpart + c.xz * (iz2 * (X4.x - X2.x) - iz0 * (X2.x - X0.x)) +
+                 c.yz * (iz2 * (Y4.x - Y2.x) - iz0 * (Y2.x - Y0.x));
+          }
+          {
+            const float q0 = P2.y;
+            const float ex = L.y + R.y, ey = U2.y + D2.y;
+            const float d4x = ex - 4.f * (P2.x + R.x) + 6.f * q0;
+            const float d4y = ey - 4.f * (U1.y + D1.y) + 6.f * q0;
+            const float corners = (UL.y + UR.y) + (DL.y + DR.y);
+            const float zpart = w0 * ((P0.y - 2.f * P1.y) + P2.y) - 2.f * w1 * ((P1.y - 2.f * P2.y) + P3.y) +
+                                w2 * ((P2.y - 2.f * P3.y) + P4.y);
+            qb = c.ridge2 * q0 + iz1 * (c.xx_int * d4x + c.yy_int * d4y + c.xy * (corners - 2.f * (ex + ey) + 4.f * q0)) +
+                 zpart + c.xz * (iz2 * (X4.y - X2.y) - iz0 * (X2.y - X0.y)) +
+                 c.yz * (iz2 * (Y4.y - Y2.y) - iz0 * (Y2.y - Y0.y));
+          }
+        } else {  // rows near a y face (deep in z): per-row y factors, p at rows y-/+2 of planes z-/+2
+          const float2 MU = ld2(pm2 + own - 2 * kTmPX), MD = ld2(pm2 + own + 2 * kTmPX);
+          const float2 QU = ld2(pl2 + own - 2 * kTmPX), QD = ld2(pl2 + own + 2 * kTmPX);
+          auto fI = [&](int a) -> float { return (a >= 1 && a <= ny - 2) ? 1.f : 0.f; };
+          auto fB = [&](int a) -> float {
+            return (float)((a == 1) + (a == ny - 2)) * ((a >= 0 && a < ny) ? 1.f : 0.f);
+          };
+          const float fi[3] = {fI(j - 1), fI(j), fI(j + 1)}, fb[3] = {fB(j - 1), fB(j), fB(j + 1)};
+          qa = yshell_node(c, fi, fb, L.x, L.y, P2.x, P2.y, R.x, UL.x, U2.x, UR.x, DL.x, D2.x, DR.x, U1.x, D1.x, P0.x,
+                           P1.x, P3.x, P4.x, MU.x, MD.x, QU.x, QD.x, (X0.x + X4.x) - 2.f * X2.x);
+          qb = yshell_node(c, fi, fb, L.y, P2.x, P2.y, R.x, R.y, UL.y, U2.y, UR.y, DL.y, D2.y, DR.y, U1.y, D1.y, P0.y,
+                           P1.y, P3.y, P4.y, MU.y, MD.y, QU.y, QD.y, (X0.y + X4.y) - 2.f * X2.y);
+        }
+      } else if (xshell_warp) {  // columns near an x face: per-node x factors
         const float2 ML = ld2(pm2 + own - 2), MR = ld2(pm2 + own + 2);
         const float2 QL = ld2(pl2 + own - 2), QR = ld2(pl2 + own + 2);
         auto fI = [&](int a) -> float { return (a >= 1 && a <= nx - 2) ? 1.f : 0.f; };
@@ -352,13 +428,7 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
              c.yz * ((Y0.y + Y4.y) - 2.f * Y2.y);
       }
       }
-    } else if (!xshell_warp & ydeep_warp) {  // a plane near a z face
-      qa = shell_node<float, decltype(pr), false, true, false>(c, pr, i, j, zz);
-      qb = shell_node<float, decltype(prb), false, true, false>(c, prb, i + 1, j, zz);
-    } else if (!xshell_warp) {  // a row near a y face
-      qa = shell_node<float, decltype(pr), true, true, false>(c, pr, i, j, zz);
-      qb = shell_node<float, decltype(prb), true, true, false>(c, prb, i + 1, j, zz);
-    } else {
+    } else {  // near two faces: the general sum
       qa = shell_node<float>(c, pr, i, j, zz);
       qb = shell_node<float>(c, prb, i + 1, j, zz);
     }

@@ -277,7 +277,10 @@ __global__ void diag_stencil_kernel(StencilCoef c, double *__restrict__ d) {
   }
 }
 
-// touched nodes: diag += sum w2 a^2 ; rhs = sum a w2 b
+// touched nodes: diag += sum over rows w2 (sum of the row's coefficients at
+// the node)^2 -- a row may hold a node twice (P1 face rows, pair rows within
+// one cell), and the node's incidences are sorted by row, so the entries of
+// one row are adjacent; rhs = sum a w2 b
 __global__ void data_node_setup_kernel(int64_t ntouched, const int64_t *__restrict__ touched,
                                        const int64_t *__restrict__ ptr, const int32_t *__restrict__ row,
                                        const double *__restrict__ ia, const double *__restrict__ w2,
@@ -285,13 +288,21 @@ __global__ void data_node_setup_kernel(int64_t ntouched, const int64_t *__restri
                                        double *__restrict__ rhs) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < ntouched;
        t += (int64_t)gridDim.x * blockDim.x) {
-    double dd = 0.0, rr = 0.0;
+    double dd = 0.0, rr = 0.0, run = 0.0;
+    int32_t prev = -1;
     for (int64_t e = ptr[t]; e < ptr[t + 1]; ++e) {
       const double a = ia[e];
       const int32_t r = row[e];
-      dd += w2[r] * a * a;
+      if (r != prev) {
+        if (prev >= 0) dd += w2[prev] * run * run;
+        prev = r;
+        run = a;
+      } else {
+        run += a;
+      }
       rr += a * w2[r] * b[r];
     }
+    if (prev >= 0) dd += w2[prev] * run * run;
     const int64_t g = touched[t];
     diag[g] += dd;
     rhs[g] = rr;

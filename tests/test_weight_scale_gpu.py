@@ -140,6 +140,15 @@ def test_p1_tangent_and_orthogonal_rows(wgolden):
         np.testing.assert_allclose(m.data, ref, rtol=1e-13, atol=1e-13, err_msg=nm)
         np.testing.assert_allclose(fam["B"], g[f"p1_orth_fam_{nm}_b"], rtol=1e-13, atol=1e-13, err_msg=nm)
         np.testing.assert_allclose(fam["w"], g[f"p1_orth_fam_{nm}_w"], rtol=1e-13, atol=0, err_msg=nm)
+    # the diagonal (the reference's column scaling): face rows hold the shared
+    # nodes twice, summed before squaring
+    A, b = it.build_matrix()
+    N, _rhs = fdo.normal_equations(A, b)
+    sys_ = it._build_system()
+    try:
+        np.testing.assert_allclose(sys_.diagonal().cpu().numpy(), N.diagonal(), rtol=1e-12, atol=0)
+    finally:
+        sys_.close()
     assert it.solve_system("cg", solver_kwargs=dict(rtol=1e-13, atol=0.0, maxiter=200000, precision="fp64"))
     c_ref = g["p1_orth_c_direct"]
     assert np.abs(it.c - c_ref).max() <= 1e-6 * np.abs(c_ref).max()
