@@ -216,6 +216,45 @@ __device__ __forceinline__ float yshell_node(const CoefT<float> &c, const float 
          c.yz * ayz;
 }
 
+// The exact sum at any node from the three axis planes through it: shell_node()
+// with all factors general, written out over the values the pair loads give
+// (for warps near two or three faces).  f* = {I(n-1), I(n), I(n+1), B(n-1),
+// B(n), B(n+1)} of the node's x, y, z indices.  Values: r* the x line (x-2 ..
+// x+2), u2 u1 d1 d2 the y line, p0 p1 p3 p4 the z line; corners of the xy
+// plane um up dm dp (y-2 / y+2 at x-2 / x+2), of the xz plane mm mp pm pp
+// (z-2 / z+2 at x-2 / x+2), of the yz plane zmu zmd zpu zpd (z-2 / z+2 at
+// y-2 / y+2).  Each cross family sums its four row centres (a, b) = (+-1,
+// +-1), e_ab = the difference of one-sided differences in the quadrant.
+__device__ __forceinline__ float general_node(const CoefT<float> &c, const float fx[6], const float fy[6],
+                                              const float fz[6], float rm2, float rm1, float r0, float rp1, float rp2,
+                                              float u2, float u1, float d1, float d2, float p0, float p1, float p3,
+                                              float p4, float um, float up, float dm, float dp, float mm, float mp,
+                                              float pm, float pp, float zmu, float zmd, float zpu, float zpd) {
+  auto axis = [&](float i_int, const float f[6], float wint, float wbdr, float a, float b, float cc, float d,
+                  float e) {  // a..e: the line at -2 .. +2
+    return (wint * f[0] * i_int + wbdr * f[3]) * ((a - 2.f * b) + cc) -
+           2.f * (wint * f[1] * i_int + wbdr * f[4]) * ((b - 2.f * cc) + d) +
+           (wint * f[2] * i_int + wbdr * f[5]) * ((cc - 2.f * d) + e);
+  };
+  float q = c.ridge2 * r0;
+  q += axis(fy[1] * fz[1], fx, c.xx_int, c.xx_bdr, rm2, rm1, r0, rp1, rp2);
+  q += axis(fx[1] * fz[1], fy, c.yy_int, c.yy_bdr, u2, u1, r0, d1, d2);
+  q += axis(fx[1] * fy[1], fz, c.zz_int, c.zz_bdr, p0, p1, r0, p3, p4);
+  // quadrant sums: (+,+), (-,+), (+,-), (-,-) of (first axis, second axis)
+  auto cross = [&](const float fa[6], const float fb[6], float lm, float lp, float bm, float bp, float cmm,
+                   float cmp, float cpm, float cpp) {
+    // lm / lp: the first axis at -2 / +2 on the second axis' 0 line; bm / bp:
+    // the second axis at -2 / +2 on the first axis' 0 line; c__: corners
+    const float epp = (cpp - bp) - (lp - r0), emp = (bp - cpm) - (r0 - lm);
+    const float epm = (lp - r0) - (cmp - bm), emm = (r0 - lm) - (bm - cmm);
+    return fa[2] * fb[2] * epp - fa[0] * fb[2] * emp - fa[2] * fb[0] * epm + fa[0] * fb[0] * emm;
+  };
+  q += c.xy * fz[1] * cross(fx, fy, rm2, rp2, u2, d2, um, up, dm, dp);
+  q += c.xz * fy[1] * cross(fx, fz, rm2, rp2, p0, p4, mm, mp, pm, pp);
+  q += c.yz * fx[1] * cross(fy, fz, u2, d2, p0, p4, zmu, zmd, zpu, zpd);
+  return q;
+}
+
 // ZU: output planes per barrier step (1 or 2; the launcher picks the faster
 // for the grid at first use).
 //
@@ -428,9 +467,31 @@ __global__ void __launch_bounds__(kTmThreads, kTmBlocksPerSm)
              c.yz * ((Y0.y + Y4.y) - 2.f * Y2.y);
       }
       }
-    } else {  // near two faces: the general sum
-      qa = shell_node<float>(c, pr, i, j, zz);
-      qb = shell_node<float>(c, prb, i + 1, j, zz);
+    } else {  // near two or three faces: the general sum from the three axis planes
+      const int o = po + own;
+      const float2 L = ld2(o - 2), R = ld2(o + 2);
+      const float2 U1 = ld2(o - kTmPX), D1 = ld2(o + kTmPX), U2 = ld2(o - 2 * kTmPX), D2 = ld2(o + 2 * kTmPX);
+      const float2 UL = ld2(o - 2 * kTmPX - 2), UR = ld2(o - 2 * kTmPX + 2);
+      const float2 DL = ld2(o + 2 * kTmPX - 2), DR = ld2(o + 2 * kTmPX + 2);
+      const float2 ML = ld2(pm2 + own - 2), MR = ld2(pm2 + own + 2), QL = ld2(pl2 + own - 2), QR = ld2(pl2 + own + 2);
+      const float2 MU = ld2(pm2 + own - 2 * kTmPX), MD = ld2(pm2 + own + 2 * kTmPX);
+      const float2 QU = ld2(pl2 + own - 2 * kTmPX), QD = ld2(pl2 + own + 2 * kTmPX);
+      auto fac = [](int a, int n, float f[6]) {
+        for (int d = 0; d < 3; ++d) {
+          const int v = a + d - 1;
+          f[d] = (v >= 1 && v <= n - 2) ? 1.f : 0.f;
+          f[3 + d] = (float)((v == 1) + (v == n - 2)) * ((v >= 0 && v < n) ? 1.f : 0.f);
+        }
+      };
+      float fxa[6], fxb[6], fy[6], fz[6];
+      fac(i, nx, fxa);
+      fac(i + 1, nx, fxb);
+      fac(j, ny, fy);
+      fac(zz, nz, fz);
+      qa = general_node(c, fxa, fy, fz, L.x, L.y, P2.x, P2.y, R.x, U2.x, U1.x, D1.x, D2.x, P0.x, P1.x, P3.x, P4.x,
+                        UL.x, UR.x, DL.x, DR.x, ML.x, MR.x, QL.x, QR.x, MU.x, MD.x, QU.x, QD.x);
+      qb = general_node(c, fxb, fy, fz, L.y, P2.x, P2.y, R.x, R.y, U2.y, U1.y, D1.y, D2.y, P0.y, P1.y, P3.y, P4.y,
+                        UL.y, UR.y, DL.y, DR.y, ML.y, MR.y, QL.y, QR.y, MU.y, MD.y, QU.y, QD.y);
     }
     // epilogue of the pair: q, its p, operands in the slot (pairs throughout)
     if (col_in) {
