@@ -267,7 +267,9 @@ def solve_admm(interp, o, inner, timing) -> bool:
     finally:
         system.close()
     interp._c_dev = c
-    interp._c = c.cpu().numpy()
+    from . import fd
+
+    interp._c = fd.to_host(c)
     interp.solver_history = history if o["return_history"] else None
     timing.update({"admm_iterations": len(history), "inner_iterations": inner_iterations, "rho": rho,
                    "inequality_rows": ineq.m, "system_builds": builds, "precision": inner["precision"],

@@ -13,6 +13,7 @@
 // column-scaled CG (SS:48-72 on A S, S = diag(N)^-1/2) written without the
 // explicit scaling: identical iterates x_k = S y_k and identical stopping test
 // ||S r|| < max(atol, rtol ||S rhs||).
+#include <cooperative_groups.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -962,6 +963,32 @@ __global__ void mg_gj_step_kernel(int nc, int c, double tiny, const double *__re
   }
 }
 
+// The whole Gauss-Jordan elimination in one cooperative launch on the same
+// ping-pong buffers, one grid-wide sync per pivot.  At step c only the columns
+// c .. nc+c change: the left columns before c are already unit vectors and the
+// right columns after nc+c are still the identity's, and neither is read again
+// before it enters that window, so both buffers start as [A | I] and the
+// window alone is written.  The cooperative launch guarantees that every
+// block is resident, so the sync cannot wait on a block that never runs.
+__global__ void mg_gj_coop_kernel(int nc, double tiny, double *b0, double *b1) {
+  cooperative_groups::grid_group grid = cooperative_groups::this_grid();
+  const int w = 2 * nc, span = nc + 1;
+  const int64_t total = (int64_t)nc * span;
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  for (int c = 0; c < nc; ++c) {
+    const double *in = (c & 1) ? b1 : b0;
+    double *out = (c & 1) ? b0 : b1;
+    double piv = in[(size_t)c * w + c];
+    if (fabs(piv) < tiny) piv = piv < 0.0 ? -tiny : tiny;
+    for (int64_t t = tid; t < total; t += stride) {
+      const int r = (int)(t / span), k = c + (int)(t - (int64_t)r * span);
+      const double rowc = in[(size_t)c * w + k] / piv;
+      out[(size_t)r * w + k] = (r == c) ? rowc : in[(size_t)r * w + k] - in[(size_t)r * w + c] * rowc;
+    }
+    grid.sync();
+  }
+}
+
 int mg_read_scalar(ls_fd_handle *h, double *dev, double *out) {
   LS_CUDA_TRY(cudaMemcpyAsync(out, dev, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   LS_CUDA_TRY(cudaStreamSynchronize(h->stream));
@@ -1066,9 +1093,8 @@ int mg_coarse_inverse(ls_fd_handle *h, MgLevel &lv) {
       const double m = 0.5 * (A[(size_t)i * nc + j] + A[(size_t)j * nc + i]);
       A[(size_t)i * nc + j] = A[(size_t)j * nc + i] = m;
     }
-  // Gauss-Jordan on the GPU: [A | I] -> [I | A^-1], one launch per pivot,
-  // ping-pong buffers (every element of step c reads row c and column c of
-  // the previous matrix).  No pivoting: the coarsest operator is symmetric
+  // Gauss-Jordan on the GPU: [A | I] -> [I | A^-1] (every element of step c
+  // reads row c and column c of the previous matrix).  No pivoting: the coarsest operator is symmetric
   // positive definite (Galerkin products of SPD operators plus the ridge); a
   // vanishing pivot is replaced by +-1e-14 max|diag| as a guard.
   double maxdiag = 0.0;
@@ -1083,14 +1109,33 @@ int mg_coarse_inverse(ls_fd_handle *h, MgLevel &lv) {
   LS_TRY(dev_alloc(&buf[0], (size_t)nc * w));
   LS_TRY(dev_alloc(&buf[1], (size_t)nc * w));
   LS_CUDA_TRY(cudaMemcpyAsync(buf[0], aug.data(), aug.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-  const int gs = (int)std::min<int64_t>(((int64_t)nc * w + 255) / 256, 8 * sm_count());
-  for (int c = 0; c < nc; ++c) {
-    mg_gj_step_kernel<<<gs, 256, 0, st>>>(nc, c, 1e-14 * maxdiag, buf[c & 1], buf[(c + 1) & 1]);
+  LS_CUDA_TRY(cudaMemcpyAsync(buf[1], buf[0], aug.size() * sizeof(double), cudaMemcpyDeviceToDevice, st));
+  // one cooperative launch sized to the resident capacity; if the device
+  // refuses it, one launch per pivot on ping-pong buffers
+  double tiny = 1e-14 * maxdiag;
+  int per_sm = 0, dev = 0, coop = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mg_gj_coop_kernel, 256, 0);
+  const int64_t want = ((int64_t)nc * w + 255) / 256;
+  const int cgs = (int)std::max<int64_t>(1, std::min<int64_t>(((int64_t)nc * (nc + 1) + 255) / 256,
+                                                              (int64_t)per_sm * sm_count()));
+  void *args[] = {(void *)&nc, (void *)&tiny, (void *)&buf[0], (void *)&buf[1]};
+  if (coop && per_sm > 0 &&
+      cudaLaunchCooperativeKernel((void *)mg_gj_coop_kernel, dim3(cgs), dim3(256), args, 0, st) == cudaSuccess) {
     ++h->launches;
+  } else {
+    cudaGetLastError();
+    const int gs = (int)std::min<int64_t>(want, 8 * sm_count());
+    for (int c = 0; c < nc; ++c) {
+      mg_gj_step_kernel<<<gs, 256, 0, st>>>(nc, c, tiny, buf[c & 1], buf[(c + 1) & 1]);
+      ++h->launches;
+    }
   }
   LS_CUDA_TRY(cudaGetLastError());
+  const int result = nc & 1;
   LS_TRY(mg_alloc(mg, &mg.coarse_inv64, (size_t)nc * nc));
-  LS_CUDA_TRY(cudaMemcpy2DAsync(mg.coarse_inv64, nc * sizeof(double), buf[nc & 1] + nc, w * sizeof(double),
+  LS_CUDA_TRY(cudaMemcpy2DAsync(mg.coarse_inv64, nc * sizeof(double), buf[result] + nc, w * sizeof(double),
                                 nc * sizeof(double), nc, cudaMemcpyDeviceToDevice, st));
   LS_CUDA_TRY(cudaStreamSynchronize(st));
   cudaFree(buf[0]);

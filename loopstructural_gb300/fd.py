@@ -363,7 +363,18 @@ def eval_points(support, c, pts: np.ndarray, value=True, gradient=True):
     g = support.grid3()
     _lib.check(lib.ls_fd_eval_points(C.byref(g), _lib.ptr(c_t), _lib.ptr(d_pts), n, pts.shape[1], _lib.ptr(v),
                                      _lib.ptr(gr), _lib.stream_ptr()))
-    return (v.cpu().numpy() if value else None, gr.cpu().numpy() if gradient else None)
+    return (to_host(v) if value else None, to_host(gr) if gradient else None)
+
+
+def to_host(t):
+    """Device tensor -> numpy array through page-locked host memory: the
+    device-to-host copy runs at the interconnect's rate instead of a pageable
+    copy's (the page-locked block comes from torch's caching host allocator,
+    reused once the returned array is released)."""
+    torch = _torch()
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    h.copy_(t)
+    return h.numpy()
 
 
 def eval_lattice(support, c_dev, origin, step, counts, value=True, gradient=True):

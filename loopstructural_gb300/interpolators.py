@@ -610,7 +610,7 @@ class _DiscreteInterpolatorBase:
         elif status in (_lib.LS_NAN, _lib.LS_BREAKDOWN):
             logger.warning("CG stopped early (status %d: %s)", status, "nan" if status == _lib.LS_NAN else "breakdown")
         self._c_dev = x
-        self._c = x.cpu().numpy()
+        self._c = fd.to_host(x)
         timing.update({"iterations": int(stats["iterations"]), "reliable_updates": int(stats["reliable_updates"]),
                        "residual": stats["residual"], "threshold": stats["threshold"],
                        "device_ms": stats["device_ms"], "precision": opts["precision"], "status": int(status),

@@ -122,7 +122,7 @@ def eval_points(mesh, c, pts: np.ndarray, value=True, gradient=True):
     g = mesh.grid3()
     _lib.check(lib.ls_p1_eval_points(C.byref(g), _lib.ptr(c_t), _lib.ptr(d_pts), n, pts.shape[1], _lib.ptr(v),
                                      _lib.ptr(gr), _lib.stream_ptr()))
-    return (v.cpu().numpy() if value else None, gr.cpu().numpy() if gradient else None)
+    return (fd.to_host(v) if value else None, fd.to_host(gr) if gradient else None)
 
 
 class P1Interpolator(_DiscreteInterpolatorBase):
