@@ -17,11 +17,13 @@
 // Coarsening keeps this form: each 1-D table becomes P^T T P (still
 // bandwidth 2).  Away from the faces every 1-D row equals the interior row, so
 // G is a constant, symmetric 125-point stencil there (staged-tile kernel); the
-// nodes near a face (two per side) evaluate the tensor-product sum from the
-// tables (node-per-thread kernel).  Levels of at most kG1ExplicitMax nodes
-// store every node's explicit 125-point stencil (evaluated from the tables at
-// setup) and run one node-per-thread kernel: one launch, no staging, which
-// is what small grids are bound by.  A rediscretised coarse operator would weight the border
+// nodes near a face (two per side) take precomputed face and edge stencils
+// (the stencil of a node with one or two axes in their bands depends only on
+// its band rows) and corners the tensor-product sum from the tables
+// (node-per-thread shell kernel).  Levels of at most kG1ExplicitMax nodes store
+// every node's explicit 125-point stencil (evaluated from the tables at setup)
+// and run one warp per node: one launch, no staging, which is what small
+// grids are bound by.  A rediscretised coarse operator would weight the border
 // layers much more than G does (P annihilates second differences centred on
 // odd fine nodes); at 200^3 the Galerkin hierarchy needs 137 instead of 213
 // iterations to rtol 1e-10.
@@ -33,7 +35,7 @@ namespace ls {
 
 enum G1Kind { G1_D2I = 0, G1_D1I = 1, G1_MI = 2, G1_D2B = 3, G1_M0 = 4, G1_KINDS = 5 };
 constexpr int kG1Families = 10;
-constexpr int64_t kG1ExplicitMax = 200000;
+constexpr int64_t kG1ExplicitMax = 50000;
 constexpr int kG1MaxBand = 6;  // face stencils kept for up to 3 band rows per side
 
 struct G1Op {
@@ -43,11 +45,25 @@ struct G1Op {
   float w[kG1Families];              // family weights
   float c[3][5][5];                  // interior stencil c(|dz|, dy, dx); c(-dz) = c(dz)
   const float *shell_coef;           // small levels: 125 x n explicit stencils of every node
+  const float *full_coef;            // small levels: shell_coef plus the folded 27-point data term
   // face nodes (one axis in its boundary band): the stencil depends only on
   // that axis' band row -- face_coef[(axis * kG1MaxBand + row) * 125 + o],
   // row = index (low side) or kG1MaxBand/2 + (n - 1 - index) (high side)
   const float *face_coef;
+  // edge nodes (two axes in their bands, the third interior): the stencil
+  // depends only on the two band rows -- edge_coef[((pair * kG1MaxBand + ra)
+  // * kG1MaxBand + rb) * 125 + o], pair 0 = (x, y), 1 = (x, z), 2 = (y, z),
+  // ra / rb the band rows of the lower / higher axis
+  const float *edge_coef;
 };
+
+// band row of coordinate x on axis a (see face_coef), or -1 when the node is
+// interior along a or its side's band is wider than the stored rows
+__host__ __device__ __forceinline__ int g1_band_row(const G1Op &g, int a, int x, int n) {
+  if (x < g.lo[a]) return g.lo[a] <= kG1MaxBand / 2 ? x : -1;
+  if (x > g.hi[a]) return n - 1 - g.hi[a] <= kG1MaxBand / 2 ? kG1MaxBand / 2 + (n - 1 - x) : -1;
+  return -1;
+}
 
 // 1-D kinds of family f along axis a
 __host__ __device__ __forceinline__ int g1_kind(int f, int a) {
@@ -268,22 +284,25 @@ __global__ void __launch_bounds__(256) g1_shell_kernel(G1Op g, const float *__re
       for (int o = 0; o < 125; ++o)
         q += __ldg(g.shell_coef + (size_t)o * ns + s) * pr(o / 25 - 2, (o / 5) % 5 - 2, o % 5 - 2);
     } else {
-      // axes in their boundary band and the band row of each
-      const int ax[3] = {i, j, k}, an[3] = {nx, ny, nz};
-      int nb = 0, axis = 0, row = 0;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const int x = ax[a];
-        if (x < g.lo[a] || x > g.hi[a]) {
-          ++nb;
-          axis = a;
-          row = x < g.lo[a] ? x : kG1MaxBand / 2 + (an[a] - 1 - x);
-        }
+      // axes in their boundary band and the band row of each: face nodes
+      // read their stencil from shared memory, edge nodes from edge_coef
+      // (one loop over generic addresses for both, so that a warp holding
+      // both kinds does not run it twice); corners and nodes of wider bands
+      // sum the tables.  Selects rather than an indexed array, which would
+      // sit in local memory.
+      int nb = 0, axis = 0, out = 0, r0 = 0, r1 = 0, r2 = 0;
+      bool ok = true;
+      if (i < g.lo[0] || i > g.hi[0]) { ++nb; axis = 0; r0 = g1_band_row(g, 0, i, nx); ok &= r0 >= 0; } else out = 0;
+      if (j < g.lo[1] || j > g.hi[1]) { ++nb; axis = 1; r1 = g1_band_row(g, 1, j, ny); ok &= r1 >= 0; } else out = 1;
+      if (k < g.lo[2] || k > g.hi[2]) { ++nb; axis = 2; r2 = g1_band_row(g, 2, k, nz); ok &= r2 >= 0; } else out = 2;
+      const float *c = nullptr;
+      if (ok && nb == 1) {
+        c = fc + (axis * kG1MaxBand + (axis == 0 ? r0 : axis == 1 ? r1 : r2)) * 125;
+      } else if (ok && nb == 2 && g.edge_coef) {
+        const int ra = out == 0 ? r1 : r0, rb = out == 2 ? r1 : r2;
+        c = g.edge_coef + (((2 - out) * kG1MaxBand + ra) * kG1MaxBand + rb) * 125;
       }
-      if (nb == 1 && (row % (kG1MaxBand / 2)) < kG1MaxBand / 2 &&
-          (row < kG1MaxBand / 2 ? row < g.lo[axis] : an[axis] - 1 - (row - kG1MaxBand / 2) > g.hi[axis]) &&
-          (row < kG1MaxBand / 2 ? g.lo[axis] <= kG1MaxBand / 2 : an[axis] - 1 - g.hi[axis] <= kG1MaxBand / 2)) {
-        const float *c = fc + (axis * kG1MaxBand + row) * 125;
+      if (c) {
 #pragma unroll
         for (int o = 0; o < 125; ++o) q += c[o] * pr(o / 25 - 2, (o / 5) % 5 - 2, o % 5 - 2);
       } else {
@@ -293,6 +312,63 @@ __global__ void __launch_bounds__(256) g1_shell_kernel(G1Op g, const float *__re
     if (dv.enabled) q += data_term<float>(dv, gi);
     if (K27) q += k27_term<float>(dv, gi, pr);
     epilogue<float, EPI>(e, gi, __ldg(p + gi), q);
+  }
+}
+
+// Explicit levels: the stencils node-major (kG1Row floats per node, the 125
+// offsets then zeros) with the 27-point data term of the marked nodes folded
+// in, so that one sum covers both.
+constexpr int kG1Row = 128;
+__global__ void g1_fold_k27_kernel(G1Op g, const uint32_t *__restrict__ kmask, const int32_t *__restrict__ krank,
+                                   const float *__restrict__ k27, int64_t knt, float *__restrict__ full) {
+  const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+    float *row = full + (size_t)s * kG1Row;
+    for (int o = 0; o < 125; ++o) row[o] = g.shell_coef[(size_t)o * n + s];
+    for (int o = 125; o < kG1Row; ++o) row[o] = 0.f;
+    if (!k27 || knt == 0) continue;
+    const uint32_t word = kmask[s >> 5], bit = 1u << (s & 31);
+    if (!(word & bit)) continue;
+    const int rank = krank[s >> 5] + __popc(word & (bit - 1u));
+    for (int o = 0; o < 27; ++o) {
+      const int dz = o / 9 - 1, dy = (o / 3) % 3 - 1, dx = o % 3 - 1;
+      row[25 * (dz + 2) + 5 * (dy + 2) + (dx + 2)] += k27[(size_t)o * knt + rank];
+    }
+  }
+}
+
+// Explicit levels (every node's stencil stored; small grids): one warp per
+// node, lane l < 25 sums stencil row (dz, dy) = (l / 5 - 2, l % 5 - 2) -- five
+// x-adjacent coefficients and values -- and the rows meet by shuffles.  One
+// thread per node cannot hide the latency of its 250 loads on grids this
+// small, and the node-major rows keep a warp's coefficient loads in one
+// 512-byte span.
+template <int EPI>
+__global__ void __launch_bounds__(256) g1_explicit_kernel(G1Op g, const float *__restrict__ p, DataView<float> dv,
+                                                          EpiArgs<float> e, const int *done) {
+  if (done && *done) return;
+  const int nx = g.nx, ny = g.ny, nz = g.nz, sxy = nx * ny;
+  const int n = sxy * nz;
+  const int lane = threadIdx.x & 31;
+  const int s = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  if (s >= n) return;  // uniform across the warp
+  const int k = s / sxy, rem = s - k * sxy, j = rem / nx, i = rem - j * nx;
+  float acc = 0.f;
+  if (lane < 25) {
+    const int dz = lane / 5 - 2, dy = lane % 5 - 2;
+    if ((k + dz >= 0) & (k + dz < nz) & (j + dy >= 0) & (j + dy < ny)) {
+      const float *c = g.full_coef + (size_t)s * kG1Row + 5 * lane;
+      const float *pp = p + (s + dz * sxy + dy * nx);
+#pragma unroll
+      for (int dx = -2; dx <= 2; ++dx)
+        if ((i + dx >= 0) & (i + dx < nx)) acc += __ldg(c + dx + 2) * __ldg(pp + dx);
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if (lane == 0) {
+    if (dv.enabled) acc += data_term<float>(dv, s);
+    epilogue<float, EPI>(e, s, __ldg(p + s), acc);
   }
 }
 
@@ -329,7 +405,10 @@ inline int launch_g1_k(const G1Op &g, const float *p, const DataView<float> &dv,
     ++launches;
   }
   const int64_t ns = box_shell_count(g);
-  if ((parts & 2) && ns > 0) {
+  if ((parts & 2) && ns > 0 && g.full_coef) {
+    g1_explicit_kernel<EPI><<<(int)((ns * 32 + 255) / 256), 256, 0, st>>>(g, p, dv, e, done);
+    ++launches;
+  } else if ((parts & 2) && ns > 0) {
     const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((ns + 255) / 256, 8 * (int64_t)sms));
     if (g.shell_coef)
       g1_shell_kernel<EPI, K27, true><<<gs, 256, 0, st>>>(g, p, dv, e, done);

@@ -1354,8 +1354,47 @@ int mg_build_g1(ls_fd_handle *h, MgHierarchy &mg, const MgLevel &f, MgLevel &c) 
     LS_CUDA_TRY(cudaMemcpyAsync(dfc, fcv.data(), fcv.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
     g.face_coef = dfc;
   }
+  // edge stencils: two axes in their bands, the third interior
+  {
+    const int half = kG1MaxBand / 2;
+    std::vector<float> ecv((size_t)3 * kG1MaxBand * kG1MaxBand * 125, 0.f);
+    auto band_idx = [&](int a, int row) -> int {  // node index of band row `row` on axis a, or -1
+      const int idx = row < half ? row : nc[a] - 1 - (row - half);
+      const bool band = row < half ? (idx < g.lo[a] && g.lo[a] <= half) : (idx > g.hi[a] && nc[a] - 1 - g.hi[a] <= half);
+      return (band && idx >= 0 && idx < nc[a]) ? idx : -1;
+    };
+    for (int out = 0; out < 3; ++out) {
+      const int pa = out == 0 ? 1 : 0, pb = out == 2 ? 1 : 2, pair = 2 - out;
+      for (int ra = 0; ra < kG1MaxBand; ++ra)
+        for (int rb = 0; rb < kG1MaxBand; ++rb) {
+          const int ia = band_idx(pa, ra), ib = band_idx(pb, rb);
+          if (ia < 0 || ib < 0) continue;
+          for (int o = 0; o < 125; ++o) {
+            const int d[3] = {o % 5, (o / 5) % 5, o / 25};  // dx, dy, dz (+2)
+            double acc = 0.0;
+            for (int fm = 0; fm < kG1Families; ++fm) {
+              double prod = w[fm];
+              for (int b = 0; b < 3; ++b) {
+                const int kind = g1_kind(fm, b);
+                const std::vector<double> &t = c.g1host[b];
+                prod *= b == pa   ? t[((size_t)kind * nc[b] + ia) * 5 + d[b]]
+                        : b == pb ? t[((size_t)kind * nc[b] + ib) * 5 + d[b]]
+                                  : irow[b][kind][d[b]];
+              }
+              acc += prod;
+            }
+            ecv[(((size_t)pair * kG1MaxBand + ra) * kG1MaxBand + rb) * 125 + o] = (float)acc;
+          }
+        }
+    }
+    float *dec = nullptr;
+    LS_TRY(mg_alloc(mg, &dec, ecv.size()));
+    LS_CUDA_TRY(cudaMemcpyAsync(dec, ecv.data(), ecv.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    g.edge_coef = dec;
+  }
   // small levels: every node's explicit stencil, one node-per-thread kernel
   g.shell_coef = nullptr;
+  g.full_coef = nullptr;
   if (c.n <= kG1ExplicitMax) {
     for (int a = 0; a < 3; ++a) {
       g.lo[a] = 1;
@@ -1513,6 +1552,15 @@ int mg_build(ls_fd_handle *h, int deg) {
     }
     c.knt = 0;
     if (cells.nrows > 0) LS_TRY(mg_cells_k27(h, c, cells));
+    if (c.g1op.shell_coef) {
+      // explicit level: stencil and 27-point data term in one coefficient set
+      float *full = nullptr;
+      LS_TRY(mg_alloc(mg, &full, (size_t)kG1Row * c.n));
+      g1_fold_k27_kernel<<<grid_for(h, c.n), kBlock, 0, h->stream>>>(c.g1op, c.kmask, c.krank,
+                                                                     c.knt > 0 ? c.k27 : nullptr, c.knt, full);
+      ++h->launches;
+      c.g1op.full_coef = full;
+    }
     LS_TRY(mg_upload_level(h, c, rows, touched, ddiag));
     LS_TRY(mark(3));
     // diagonal: regularisation, the row-form data term (touched / ddiag) and

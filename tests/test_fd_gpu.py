@@ -399,6 +399,56 @@ def test_coarse_levels_are_galerkin(cells):
     system.close()
 
 
+def _prolong_axes(x, ps, shape_c):
+    """P x for P = Pz (x) Py (x) Px applied axis by axis (x: coarse, z-major)."""
+    t = x.reshape(shape_c[::-1])
+    t = np.tensordot(t, ps[0].toarray(), axes=([2], [1]))
+    t = np.moveaxis(np.tensordot(t, ps[1].toarray(), axes=([1], [1])), 2, 1)
+    t = np.moveaxis(np.tensordot(t, ps[2].toarray(), axes=([0], [1])), 2, 0)
+    return t.ravel()
+
+
+def _restrict_axes(y, ps, shape_f):
+    """P^T y axis by axis (y: fine, z-major)."""
+    t = y.reshape(shape_f[::-1])
+    t = np.tensordot(t, ps[0].toarray(), axes=([2], [0]))
+    t = np.moveaxis(np.tensordot(t, ps[1].toarray(), axes=([1], [0])), 2, 1)
+    t = np.moveaxis(np.tensordot(t, ps[2].toarray(), axes=([0], [0])), 2, 0)
+    return t.ravel()
+
+
+def test_large_coarse_levels_are_galerkin_of_the_finer_level():
+    """Levels too large for explicit stencils (boundary faces, edges and
+    corners from their own tables) and the explicit level below them apply
+    P^T A_finer P, with A_finer the level above's own FP32 apply."""
+    cells = np.array([240, 80, 90])
+    assert int(np.prod(cells // 2 + 1)) > 200000  # level 1 holds no explicit stencils
+    rng = np.random.default_rng(11)
+    vp = rng.uniform(0, 1, size=(3000, 3))
+    val = np.column_stack([vp, vp[:, 2] + 0.1 * vp[:, 0], np.ones(3000)])
+    npnt = rng.uniform(0, 1, size=(600, 3))
+    nrm = np.column_stack([npnt, rng.normal(size=(600, 3)), np.ones(600)])
+    interp = L.FiniteDifferenceInterpolator(_grid(cells))
+    interp.set_value_constraints(val)
+    interp.set_normal_constraints(nrm)
+    interp.setup_interpolator(regularisation=0.1, cpw=1.0, npw=1.0)
+    system = interp._build_system()
+    nf = cells + 1
+    for level in (1, 2):
+        ps = [_prolong_1d(int(n)) for n in nf]
+        nc = np.array([p[1] for p in ps])
+        nodes, _ = fd.mg_apply_level(system, level)
+        assert nodes == int(np.prod(nc))
+        x = np.random.default_rng(level).normal(size=nodes)
+        fine = torch.from_numpy(_prolong_axes(x, [p[0] for p in ps], nc))
+        _, yf = fd.mg_apply_level(system, level - 1, fine)
+        ref = _restrict_axes(yf.cpu().numpy().astype(np.float64), [p[0] for p in ps], nf)
+        _, y = fd.mg_apply_level(system, level, torch.from_numpy(x))
+        assert np.max(np.abs(y.cpu().numpy() - ref)) <= 5e-5 * np.max(np.abs(ref)), level
+        nf = nc
+    system.close()
+
+
 @pytest.mark.parametrize("name", ["fd_small", "fd_cfg1_20"])
 def test_build_matrix_and_custom_solver_match_reference(golden, name):
     """The explicit system (DI:684-755) in the reference's family order, and a
