@@ -417,11 +417,13 @@ def _restrict_axes(y, ps, shape_f):
     return t.ravel()
 
 
-def test_large_coarse_levels_are_galerkin_of_the_finer_level():
+@pytest.mark.parametrize("cells", [(240, 80, 90), (200, 150, 120)])
+def test_large_coarse_levels_are_galerkin_of_the_finer_level(cells):
     """Levels too large for explicit stencils (boundary faces, edges and
-    corners from their own tables) and the explicit level below them apply
-    P^T A_finer P, with A_finer the level above's own FP32 apply."""
-    cells = np.array([240, 80, 90])
+    corners from their own tables: 121 x 41 x 46, 101 x 76 x 61 and
+    51 x 39 x 31) and an explicit level (61 x 21 x 24, one warp per node)
+    apply P^T A_finer P, with A_finer the level above's own FP32 apply."""
+    cells = np.array(cells)
     assert int(np.prod(cells // 2 + 1)) > 200000  # level 1 holds no explicit stencils
     rng = np.random.default_rng(11)
     vp = rng.uniform(0, 1, size=(3000, 3))
