@@ -69,3 +69,44 @@ def test_invalid_arguments_report_errors(lib):
     g = _lib.Grid3.make((5, 5, 5), np.zeros(3), (1.0, 0.0, 1.0))
     assert lib.ls_fd_reg_shape(C.byref(g), 0, C.byref(rows), None) == -1
     assert lib.ls_fd_create(None, None, None) == -1
+
+
+# Entry points whose first statement rejects a NULL handle, grid, mesh or
+# buffer: called with every pointer NULL and every number 0 they must return
+# LS_ERR_ARG with a message, before any CUDA call (so this runs without a GPU).
+NULL_CHECKED = [
+    "ls_fd_point_rows", "ls_fd_pair_rows", "ls_fd_reg_shape", "ls_fd_reg_rows", "ls_fd_weight_scale",
+    "ls_fd_scaled_weights", "ls_fd_directional_weights", "ls_fault_apply", "ls_fd_eval_jets", "ls_fd_eval_adjoint",
+    "ls_fd_eval_points", "ls_fd_eval_lattice", "ls_iso_extract", "ls_iso_copy", "ls_fd_apply_noalloc",
+    "ls_fd_create", "ls_fd_device", "ls_fd_set_rhs", "ls_fd_data_rows_apply", "ls_fd_admm_step",
+    "ls_fd_diagonal", "ls_fd_apply", "ls_fd_apply_f32", "ls_fd_setup_profile", "ls_fd_prepare", "ls_fd_solve",
+    "ls_fd_mg_apply_level", "ls_fd_mg_vcycle", "ls_fd_profile_mg", "ls_fd_profile_iteration",
+    "ls_p1_face_count", "ls_p1_face_rows", "ls_p1_face_rows_directional", "ls_p1_locate", "ls_p1_point_rows",
+    "ls_p1_eval_points",
+]
+
+
+def _null_args(fn):
+    out = []
+    for t in fn.argtypes:
+        if t in (C.c_double, C.c_float):
+            out.append(0.0)
+        elif t in (C.c_int, C.c_int32, C.c_int64, C.c_uint32, C.c_uint64, C.c_size_t):
+            out.append(0)
+        else:
+            out.append(None)
+    return out
+
+
+@pytest.mark.parametrize("name", NULL_CHECKED)
+def test_null_arguments_are_rejected_before_device_work(lib, name):
+    fn = getattr(lib, name)
+    assert fn(*_null_args(fn)) == -1, name
+    assert lib.ls_last_error(), name
+
+
+def test_tetra_gradient_and_destroy_accept_empty_input(lib):
+    assert lib.ls_tetra_gradient(None, None, 0, None, None) == 0
+    assert lib.ls_tetra_gradient(None, None, 1, None, None) == -1
+    assert lib.ls_fd_destroy(None) == 0
+    assert lib.ls_iso_destroy(None) == 0
